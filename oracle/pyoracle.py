@@ -1,0 +1,269 @@
+"""ctypes binding of the C oracle (oracle/spoa_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
+CPU-baseline leg of bench.py.  The product package never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_REF_DRIVER = os.path.join(_HERE, "_ref", "spoa_ref_driver")
+_lib = None
+
+TYPES = {"SW": 0, "NW": 1, "OV": 2}
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with the committed Makefile."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "spoa_oracle.c"))
+    ):
+        subprocess.run(["make", "-s", "-C", _HERE, "all"], check=True)
+    return _LIB_PATH
+
+
+def build_reference() -> str | None:
+    """Compile the reference driver (needs the reference source tree)."""
+    ref = os.environ.get("SPOA_REFERENCE_TREE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "src")):
+        return None
+    subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={ref}"], check=True,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    return _REF_DRIVER if os.path.exists(_REF_DRIVER) else None
+
+
+def reference_driver() -> str | None:
+    return _REF_DRIVER if os.path.exists(_REF_DRIVER) else None
+
+
+class WindowParams(C.Structure):
+    _fields_ = [("type", C.c_int32), ("m", C.c_int8), ("n", C.c_int8),
+                ("g", C.c_int8), ("e", C.c_int8), ("q", C.c_int8),
+                ("c", C.c_int8), ("strand_ambiguous", C.c_int8)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        P = C.c_void_p
+        L.oracle_graph_create.restype = P
+        L.oracle_graph_destroy.argtypes = [P]
+        L.oracle_graph_clear.argtypes = [P]
+        L.oracle_engine_create.restype = P
+        L.oracle_engine_create.argtypes = [C.c_int32] + [C.c_int8] * 6 + [C.POINTER(C.c_int32)]
+        L.oracle_engine_destroy.argtypes = [P]
+        L.oracle_engine_subtype.argtypes = [P]
+        L.oracle_align.argtypes = [P, C.c_char_p, C.c_uint32, P, C.POINTER(C.c_int32),
+                                   P, C.c_uint32, C.POINTER(C.c_uint32)]
+        L.oracle_add_alignment.argtypes = [P, P, C.c_uint32, C.c_char_p, C.c_uint32,
+                                           P, C.c_uint32]
+        L.oracle_consensus.argtypes = [P, C.c_char_p, C.c_uint32]
+        L.oracle_consensus.restype = C.c_uint32
+        L.oracle_msa.argtypes = [P, C.c_int32, C.c_char_p, C.c_uint64,
+                                 C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        for fn in ("num_nodes", "num_edges", "num_sequences", "consensus_len"):
+            f = getattr(L, f"oracle_graph_{fn}")
+            f.argtypes = [P]
+            f.restype = C.c_uint32
+        L.oracle_graph_export.argtypes = [P] * 8
+        L.oracle_graph_path.argtypes = [P, C.c_uint32, P, C.c_uint32]
+        L.oracle_graph_path.restype = C.c_uint32
+        L.oracle_window_run.argtypes = [C.POINTER(WindowParams), P, C.c_uint32, C.c_char_p,
+                                        P, C.c_char_p, P, P, P, C.c_uint64, P]
+        L.oracle_batch_run.argtypes = [C.POINTER(WindowParams), C.c_uint32, P, C.c_char_p,
+                                       P, C.c_char_p, C.c_int32, C.c_char_p, C.c_uint64,
+                                       P, P, P]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+@dataclass
+class WindowResult:
+    status: int
+    scores: list = field(default_factory=list)
+    reversed: list = field(default_factory=list)
+    alignments: list = field(default_factory=list)  # list of (n, 2) int32 arrays
+    consensus: str = ""
+    msa: list = field(default_factory=list)
+    graph: dict = field(default_factory=dict)
+
+
+def export_graph(g) -> dict:
+    """Node characters, rank order, out-edges in node-major order, sequence
+    paths and consensus ids of an oracle graph."""
+    L = lib()
+    nn = L.oracle_graph_num_nodes(g)
+    ne = L.oracle_graph_num_edges(g)
+    ns = L.oracle_graph_num_sequences(g)
+    nc = L.oracle_graph_consensus_len(g)
+    chars = np.zeros(max(nn, 1), np.uint8)
+    rank = np.zeros(max(nn, 1), np.uint32)
+    et = np.zeros(max(ne, 1), np.uint32)
+    eh = np.zeros(max(ne, 1), np.uint32)
+    ew = np.zeros(max(ne, 1), np.int64)
+    sb = np.zeros(max(ns, 1), np.uint32)
+    cons = np.zeros(max(nc, 1), np.uint32)
+    L.oracle_graph_export(g, _ptr(chars), _ptr(rank), _ptr(et), _ptr(eh), _ptr(ew),
+                          _ptr(sb), _ptr(cons))
+    paths = []
+    buf = np.zeros(max(nn, 1), np.uint32)
+    for s in range(ns):
+        k = L.oracle_graph_path(g, s, _ptr(buf), buf.size)
+        paths.append(buf[:k].copy())
+    return {"chars": chars[:nn].copy(), "rank_to_node": rank[:nn].copy(),
+            "edge_tail": et[:ne].copy(), "edge_head": eh[:ne].copy(),
+            "edge_weight": ew[:ne].copy(), "seq_begin": sb[:ns].copy(),
+            "consensus": cons[:nc].copy(), "paths": paths}
+
+
+def run_window(type_: int, m: int, n: int, g: int, e: int, q: int, c: int,
+               reads: list[bytes], quals: list[bytes] | None = None,
+               strand_ambiguous: bool = False, with_msa: bool = True,
+               with_graph: bool = False) -> WindowResult:
+    """One window the way spoa's CLI runs it: align/add per read in order,
+    then consensus and MSA."""
+    L = lib()
+    p = WindowParams(type_, m, n, g, e, q, c, 1 if strand_ambiguous else 0)
+    seqs = b"".join(reads)
+    off = np.zeros(len(reads) + 1, np.uint64)
+    off[1:] = np.cumsum([len(r) for r in reads])
+    qual_blob = b"".join(quals) if quals is not None else None
+    nr = len(reads)
+    scores = np.zeros(max(nr, 1), np.int32)
+    rev = np.zeros(max(nr, 1), np.uint8)
+    cap = int(sum(len(r) for r in reads) * 2 + 16) * (nr + 1) * 2
+    cap = min(cap, 1 << 31)
+    pairs = np.zeros(cap, np.int32)
+    aoff = np.zeros(nr + 1, np.uint64)
+    gr = L.oracle_graph_create()
+    try:
+        st = L.oracle_window_run(C.byref(p), gr, nr, seqs, _ptr(off), qual_blob,
+                                 _ptr(scores), _ptr(rev), _ptr(pairs), cap, _ptr(aoff))
+        res = WindowResult(status=st)
+        if st != 0:
+            return res
+        res.scores = scores[:nr].tolist()
+        res.reversed = rev[:nr].tolist()
+        res.alignments = [pairs[2 * int(aoff[r]):2 * int(aoff[r + 1])].reshape(-1, 2).copy()
+                          for r in range(nr)]
+        nn = L.oracle_graph_num_nodes(gr)
+        cbuf = C.create_string_buffer(nn + 1)
+        k = L.oracle_consensus(gr, cbuf, nn + 1)
+        res.consensus = cbuf.raw[:k].decode()
+        if with_msa:
+            rows = C.c_uint32()
+            rl = C.c_uint32()
+            mcap = (nr + 1) * (nn + 1)
+            mbuf = C.create_string_buffer(mcap)
+            st2 = L.oracle_msa(gr, 0, mbuf, mcap, C.byref(rows), C.byref(rl))
+            assert st2 == 0
+            raw = mbuf.raw
+            res.msa = [raw[i * rl.value:(i + 1) * rl.value].decode() for i in range(rows.value)]
+        if with_graph:
+            res.graph = export_graph(gr)
+        return res
+    finally:
+        L.oracle_graph_destroy(gr)
+
+
+def batch_run(type_: int, m: int, n: int, g: int, e: int, q: int, c: int,
+              windows: list[list[bytes]], strand_ambiguous: bool = False,
+              n_threads: int | None = None):
+    """Many windows on host threads (one window per task).  Returns
+    (consensus list, matrix cells)."""
+    L = lib()
+    p = WindowParams(type_, m, n, g, e, q, c, 1 if strand_ambiguous else 0)
+    reads = [r for w in windows for r in w]
+    wro = np.zeros(len(windows) + 1, np.uint32)
+    wro[1:] = np.cumsum([len(w) for w in windows])
+    off = np.zeros(len(reads) + 1, np.uint64)
+    off[1:] = np.cumsum([len(r) for r in reads])
+    seqs = b"".join(reads)
+    # consensus can exceed the longest read; give each window a generous slot
+    slot = np.array([4 * max(len(r) for r in w) + 64 if w else 64 for w in windows],
+                    np.uint64)
+    coff = np.zeros(len(windows) + 1, np.uint64)
+    coff[1:] = np.cumsum(slot)
+    cons = C.create_string_buffer(int(coff[-1]) + 1)
+    cells = C.c_uint64()
+    scores = np.zeros(max(len(reads), 1), np.int32)
+    st = L.oracle_batch_run(C.byref(p), len(windows), _ptr(wro), seqs, _ptr(off), None,
+                            n_threads or os.cpu_count() or 1, cons, int(coff[-1]),
+                            _ptr(coff), _ptr(scores), C.byref(cells))
+    if st != 0:
+        raise RuntimeError(f"oracle batch failed with status {st}")
+    raw = cons.raw
+    out = []
+    for w in range(len(windows)):
+        seg = raw[int(coff[w]):int(coff[w + 1])]
+        out.append(seg.split(b"\0", 1)[0].decode())
+    return out, cells.value
+
+
+def run_reference(windows_text: str, timing: bool = False) -> str:
+    """Feed the reference driver a window description (see ref_driver.cpp)."""
+    drv = reference_driver()
+    if drv is None:
+        raise FileNotFoundError("reference driver not built")
+    args = [drv] + (["--time"] if timing else [])
+    return subprocess.run(args, input=windows_text, capture_output=True, text=True,
+                          check=True).stdout
+
+
+def format_windows(specs) -> str:
+    """specs: iterable of (type, (m, n, g, e, q, c), reads, quals|None, strand)."""
+    out = []
+    for typ, (m, n, g, e, q, c), reads, quals, strand in specs:
+        hq = 1 if quals is not None else 0
+        out.append(f"W {typ} {m} {n} {g} {e} {q} {c} {1 if strand else 0} {hq} {len(reads)}\n")
+        for k, r in enumerate(reads):
+            out.append(r.decode() + "\n")
+            if hq:
+                out.append(quals[k].decode() + "\n")
+    return "".join(out)
+
+
+def parse_reference_output(text: str) -> list:
+    """Parse ref_driver output into a list of per-window dicts."""
+    wins = []
+    cur = None
+    for line in text.split("\n"):
+        if not line:
+            continue
+        tag, _, rest = line.partition(" ")
+        if tag == "W":
+            cur = {"scores": [], "reversed": [], "alignments": [], "consensus": "",
+                   "msa": [], "gfa": [], "error": None}
+        elif tag == "R":
+            parts = rest.split(" ")
+            cur["scores"].append(int(parts[1]))
+            cur["reversed"].append(int(parts[2]))
+            npairs = int(parts[3])
+            arr = np.array([[int(x) for x in p.split(",")] for p in parts[4:4 + npairs]],
+                           np.int32).reshape(-1, 2)
+            cur["alignments"].append(arr)
+        elif tag == "C":
+            cur["consensus"] = rest
+        elif tag == "M":
+            cur["msa"].append(rest)
+        elif tag == "G":
+            cur["gfa"].append(rest)
+        elif tag == "X":
+            cur["error"] = rest
+        elif tag == "E":
+            wins.append(cur)
+            cur = None
+    return wins

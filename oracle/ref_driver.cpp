@@ -1,0 +1,190 @@
+// ref_driver.cpp - runs POA windows through the UNMODIFIED reference library.
+//
+// TEST INFRASTRUCTURE ONLY.  Built by oracle/Makefile against the reference
+// sources (include/ and src/ of the spoa tree) into oracle/_ref/; used to pin
+// the C oracle and to generate the golden fixtures under tests/golden/.
+//
+// It replays the CLI's per-read loop (src/main.cpp:275-314: Align, optional
+// strand-ambiguous second strand, AddAlignment with or without qualities)
+// and prints, per window, every read's score and alignment, the consensus,
+// the MSA rows and the GFA text in the layout of PrintGfa
+// (src/main.cpp:119-199).
+//
+// Input (text, one or more windows):
+//   W <type> <m> <n> <g> <e> <q> <c> <strand_ambiguous> <has_quality> <reads>
+//   <sequence>            one line per read
+//   <quality>             one line per read when has_quality is 1
+// Output:
+//   W <index>
+//   R <read> <score> <reversed> <pairs> <node>,<pos> ...
+//   C <consensus>
+//   M <msa row>           one per read
+//   G <gfa line>          GFA with the consensus path
+//   E
+// A window that throws prints "X <message>" and continues with the next.
+#include <algorithm>
+#include <chrono>
+#include <cstdint>
+#include <iostream>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "spoa/spoa.hpp"
+
+namespace {
+
+char Complement(char ch) {
+  switch (ch) {
+    case 'A': return 'T';
+    case 'C': return 'G';
+    case 'G': return 'C';
+    case 'T': return 'A';
+    case 'U': return 'A';
+    case 'R': return 'Y';
+    case 'Y': return 'R';
+    case 'K': return 'M';
+    case 'M': return 'K';
+    case 'B': return 'V';
+    case 'D': return 'H';
+    case 'H': return 'D';
+    case 'V': return 'B';
+    case 'a': return 't';
+    case 'c': return 'g';
+    case 'g': return 'c';
+    case 't': return 'a';
+    case 'u': return 'a';
+    default: return ch;
+  }
+}
+
+void ReverseComplement(std::string* data, std::string* quality) {
+  for (auto& ch : *data) ch = Complement(ch);
+  std::reverse(data->begin(), data->end());
+  std::reverse(quality->begin(), quality->end());
+}
+
+void WriteGfa(const spoa::Graph& graph, const std::vector<bool>& is_reversed,
+              std::ostream& os) {
+  std::vector<bool> is_consensus_node(graph.nodes().size(), false);
+  for (const auto& it : graph.consensus()) is_consensus_node[it->id] = true;
+  os << "G H\tVN:Z:1.0\n";
+  for (const auto& it : graph.nodes()) {
+    os << "G S\t" << it->id + 1 << "\t"
+       << static_cast<char>(graph.decoder(it->code));
+    if (is_consensus_node[it->id]) os << "\tic:Z:true";
+    os << "\n";
+    for (const auto& jt : it->outedges) {
+      os << "G L\t" << it->id + 1 << "\t+\t" << jt->head->id + 1
+         << "\t+\tOM\tew:f:" << jt->weight;
+      if (is_consensus_node[it->id] && is_consensus_node[jt->head->id]) {
+        os << "\tic:Z:true";
+      }
+      os << "\n";
+    }
+  }
+  for (std::uint32_t i = 0; i < graph.sequences().size(); ++i) {
+    os << "G P\tread" << i << "\t";
+    std::vector<std::uint32_t> path;
+    auto curr = graph.sequences()[i];
+    while (curr) {
+      path.emplace_back(curr->id + 1);
+      curr = curr->Successor(i);
+    }
+    bool ir = !is_reversed.empty() && is_reversed[i];
+    if (ir) std::reverse(path.begin(), path.end());
+    for (std::uint32_t j = 0; j < path.size(); ++j) {
+      if (j != 0) os << ",";
+      os << path[j] << (ir ? "-" : "+");
+    }
+    os << "\t*\n";
+  }
+  os << "G P\tConsensus\t";
+  for (std::uint32_t i = 0; i < graph.consensus().size(); ++i) {
+    if (i != 0) os << ",";
+    os << graph.consensus()[i]->id + 1 << "+";
+  }
+  os << "\t*\n";
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  bool timing_only = argc > 1 && std::string(argv[1]) == "--time";
+  std::string tag;
+  std::uint64_t window = 0;
+  std::uint64_t cells = 0;
+  double seconds = 0;
+  while (std::cin >> tag) {
+    if (tag != "W") return 2;
+    int type, m, n, g, e, q, c, strand, has_quality;
+    std::uint32_t reads;
+    std::cin >> type >> m >> n >> g >> e >> q >> c >> strand >> has_quality >>
+        reads;
+    std::vector<std::string> data(reads), quality(reads);
+    for (std::uint32_t r = 0; r < reads; ++r) {
+      std::cin >> data[r];
+      if (has_quality) std::cin >> quality[r];
+    }
+    std::ostringstream os;
+    os << "W " << window++ << "\n";
+    auto t0 = std::chrono::steady_clock::now();
+    try {
+      auto engine = spoa::AlignmentEngine::Create(
+          static_cast<spoa::AlignmentType>(type), m, n, g, e, q, c);
+      spoa::Graph graph{};
+      std::vector<bool> is_reversed;
+      for (std::uint32_t r = 0; r < reads; ++r) {
+        cells += static_cast<std::uint64_t>(graph.nodes().size()) *
+                 data[r].size() * (strand ? 2 : 1);
+        std::int32_t score = 0;
+        auto alignment = engine->Align(data[r], graph, &score);
+        bool rev = false;
+        if (strand) {
+          ReverseComplement(&data[r], &quality[r]);
+          std::int32_t score_rev = 0;
+          auto alignment_rev = engine->Align(data[r], graph, &score_rev);
+          if (score >= score_rev) {
+            ReverseComplement(&data[r], &quality[r]);
+          } else {
+            alignment = alignment_rev;
+            score = score_rev;
+            rev = true;
+          }
+          is_reversed.push_back(rev);
+        }
+        if (quality[r].empty()) {
+          graph.AddAlignment(alignment, data[r]);
+        } else {
+          graph.AddAlignment(alignment, data[r], quality[r]);
+        }
+        if (!timing_only) {
+          os << "R " << r << " " << score << " " << (rev ? 1 : 0) << " "
+             << alignment.size();
+          for (const auto& it : alignment) {
+            os << " " << it.first << "," << it.second;
+          }
+          os << "\n";
+        }
+      }
+      auto consensus = graph.GenerateConsensus();
+      if (!timing_only) {
+        os << "C " << consensus << "\n";
+        auto msa = graph.GenerateMultipleSequenceAlignment();
+        for (const auto& row : msa) os << "M " << row << "\n";
+        WriteGfa(graph, is_reversed, os);
+      }
+    } catch (std::exception& ex) {
+      os << "X " << ex.what() << "\n";
+    }
+    seconds += std::chrono::duration<double>(
+        std::chrono::steady_clock::now() - t0).count();
+    os << "E\n";
+    if (!timing_only) std::cout << os.str();
+  }
+  if (timing_only) {
+    std::cout << "T " << window << " " << cells << " " << seconds << "\n";
+  }
+  return 0;
+}

@@ -1,0 +1,61 @@
+import gzip
+import hashlib
+import json
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def sha(text: str) -> str:
+    return hashlib.sha256(text.encode()).hexdigest()
+
+
+def canon_alignment(arr) -> str:
+    return " ".join(f"{int(a)},{int(b)}" for a, b in arr)
+
+
+@pytest.fixture(scope="session")
+def sample_reads():
+    with gzip.open(os.path.join(GOLDEN, "sample_reads.tsv.gz"), "rt") as fh:
+        rows = [ln.rstrip("\n").split("\t") for ln in fh if ln.strip()]
+    return [(s.encode(), q.encode()) for s, q in rows]
+
+
+@pytest.fixture(scope="session")
+def spoa_test_cases():
+    with open(os.path.join(GOLDEN, "spoa_test_cases.json")) as fh:
+        return json.load(fh)
+
+
+@pytest.fixture(scope="session")
+def spoa_test_outputs():
+    with open(os.path.join(GOLDEN, "spoa_test_outputs.json")) as fh:
+        return json.load(fh)
+
+
+@pytest.fixture(scope="session")
+def ref_windows():
+    with gzip.open(os.path.join(GOLDEN, "ref_windows.json.gz"), "rt") as fh:
+        return json.load(fh)
+
+
+def check_against_expect(expect, scores, reversed_, alignments, consensus, msa, gfa):
+    """Compare one window's outputs against a recorded reference run."""
+    assert list(scores) == expect["scores"]
+    assert [int(x) for x in reversed_] == expect["reversed"]
+    assert [len(a) for a in alignments] == expect["n_pairs"]
+    assert [sha(canon_alignment(a)) for a in alignments] == expect["aln_sha"]
+    assert consensus == expect["consensus"]
+    assert sha("\n".join(msa)) == expect["msa_sha"]
+    if gfa is not None:
+        assert sha("\n".join(gfa)) == expect["gfa_sha"]

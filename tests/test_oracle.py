@@ -1,0 +1,106 @@
+"""The C oracle against the reference's own golden vectors and against
+recorded outputs of the compiled reference (CPU only)."""
+import numpy as np
+import pytest
+
+from conftest import check_against_expect
+from oracle import pyoracle as po
+from spoa_gb300 import synth
+from spoa_gb300.gfa import gfa_lines
+
+
+def _gfa(res):
+    g = res.graph
+    return gfa_lines(g["chars"], g["edge_tail"], g["edge_head"], g["edge_weight"],
+                     g["paths"], g["consensus"], res.reversed)
+
+
+def test_spoa_test_known_answers(sample_reads, spoa_test_cases):
+    """The 18 consensus strings of test/spoa_test.cpp:154-440."""
+    reads = [s for s, _ in sample_reads]
+    quals = [q for _, q in sample_reads]
+    assert len(reads) == 55
+    for case in spoa_test_cases:
+        res = po.run_window(case["type"], *case["params"], reads,
+                            quals if case["quality"] else None)
+        assert res.status == 0, case["name"]
+        assert res.consensus == case["consensus"], case["name"]
+        # Check() of spoa_test.cpp:56-78
+        assert len(res.msa) == 55
+        rs = len(res.msa[0])
+        gaps = [0] * rs
+        for row in res.msa:
+            assert len(row) == rs
+            for k, ch in enumerate(row):
+                gaps[k] += ch == "-"
+        assert all(gc < len(res.msa) for gc in gaps)
+        for row, read in zip(res.msa, reads):
+            assert row.replace("-", "") == read.decode()
+
+
+def test_spoa_test_full_outputs(sample_reads, spoa_test_cases, spoa_test_outputs):
+    """Per-read scores/alignments, MSA and GFA of the same 18 runs, as the
+    compiled reference printed them."""
+    reads = [s for s, _ in sample_reads]
+    quals = [q for _, q in sample_reads]
+    for case in spoa_test_cases:
+        res = po.run_window(case["type"], *case["params"], reads,
+                            quals if case["quality"] else None, with_graph=True)
+        check_against_expect(spoa_test_outputs[case["name"]], res.scores, res.reversed,
+                             res.alignments, res.consensus, res.msa, _gfa(res))
+
+
+def test_reference_windows(ref_windows):
+    """209 seeded windows: every L mod 16, N characters, qualities, strand
+    ambiguity, long insertions (convex lane-boundary E), int32 width."""
+    for rec in ref_windows:
+        reads = [r.encode() for r in rec["reads"]]
+        quals = [q.encode() for q in rec["quals"]] if rec["quals"] else None
+        res = po.run_window(rec["type"], *rec["params"], reads, quals,
+                            rec["strand_ambiguous"], with_graph=True)
+        assert res.status == 0, rec["name"]
+        check_against_expect(rec["expect"], res.scores, res.reversed, res.alignments,
+                             res.consensus, res.msa, _gfa(res))
+
+
+def test_engine_errors():
+    L = po.lib()
+    import ctypes as C
+    st = C.c_int32()
+    assert not L.oracle_engine_create(4, 1, -1, -1, -1, -1, -1, C.byref(st))
+    assert st.value == 1
+    assert not L.oracle_engine_create(0, 1, -1, 1, -1, -1, -1, C.byref(st))
+    en = L.oracle_engine_create(0, 5, -4, -8, -6, -10, -4, C.byref(st))
+    assert en and L.oracle_engine_subtype(en) == 2
+    L.oracle_engine_destroy(en)
+    en = L.oracle_engine_create(0, 5, -4, -8, -8, -8, -8, C.byref(st))
+    assert L.oracle_engine_subtype(en) == 0
+    L.oracle_engine_destroy(en)
+    en = L.oracle_engine_create(0, 5, -4, -8, -6, -8, -6, C.byref(st))
+    assert L.oracle_engine_subtype(en) == 1
+    L.oracle_engine_destroy(en)
+
+
+def test_empty_inputs():
+    res = po.run_window(0, 1, -1, -1, -1, -1, -1, [b"ACGT", b""])
+    assert res.status == 0 and res.scores == [0, 0]
+    assert len(res.alignments[0]) == 0 and len(res.alignments[1]) == 0
+
+
+@pytest.mark.skipif(po.build_reference() is None, reason="reference tree not present")
+def test_live_differential_against_reference():
+    """Fresh random windows through the compiled reference and the oracle."""
+    rng = np.random.default_rng(7)
+    params = [(5, -4, -8, -6, -10, -2), (5, -4, -8, -6, -8, -6), (5, -4, -8, -8, -8, -8),
+              (4, -2, -4, -3, -12, -1)]
+    specs = []
+    for k in range(80):
+        reads = synth.random_window(rng, int(rng.integers(1, 90)), int(rng.integers(1, 9)),
+                                    err=float(rng.uniform(0.05, 0.35)))
+        specs.append((k % 3, params[k % 4], reads, None, k % 5 == 0))
+    outs = po.parse_reference_output(po.run_reference(po.format_windows(specs)))
+    for (typ, par, reads, quals, strand), ref in zip(specs, outs):
+        res = po.run_window(typ, *par, reads, quals, strand)
+        assert res.scores == ref["scores"]
+        assert all(np.array_equal(a, b) for a, b in zip(res.alignments, ref["alignments"]))
+        assert res.consensus == ref["consensus"] and res.msa == ref["msa"]
