@@ -1,0 +1,200 @@
+/*
+ * spoa_gb300.h - C ABI of the GB300 partial-order-alignment library.
+ *
+ * Plain pointers and sizes only; every call returns a status code
+ * (SPOA_GB300_OK or one of the codes below).  The library runs on one CUDA
+ * device (the current device when an object is created) and never falls back
+ * to the CPU: without a usable GPU every entry point that computes returns
+ * SPOA_GB300_ERR_CUDA.
+ *
+ * Each declaration names the spoa (v4) interface it replaces.  Paths are
+ * relative to the spoa source tree.
+ */
+#ifndef SPOA_GB300_H_
+#define SPOA_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The C++ layer maps them to the reference's
+ * std::invalid_argument messages. */
+#define SPOA_GB300_OK 0
+#define SPOA_GB300_ERR_INVALID_ARGUMENT 1 /* bad type / positive penalty */
+#define SPOA_GB300_ERR_TOO_LARGE 2        /* "too large sequence!" */
+#define SPOA_GB300_ERR_OVERFLOW 3         /* "possible overflow!" */
+#define SPOA_GB300_ERR_NO_MEMORY 4        /* "insufficient memory!" */
+#define SPOA_GB300_ERR_INVALID_ALIGNMENT 5
+#define SPOA_GB300_ERR_MISSING_SEQUENCE 6
+#define SPOA_GB300_ERR_UNEQUAL_WEIGHTS 7
+#define SPOA_GB300_ERR_CAPACITY 8 /* a window outgrew its device arena */
+#define SPOA_GB300_ERR_TRACEBACK 9
+#define SPOA_GB300_ERR_CUDA 10
+
+/* Alignment types and gap models (include/spoa/alignment_engine.hpp:16-26) */
+#define SPOA_GB300_SW 0
+#define SPOA_GB300_NW 1
+#define SPOA_GB300_OV 2
+#define SPOA_GB300_LINEAR 0
+#define SPOA_GB300_AFFINE 1
+#define SPOA_GB300_CONVEX 2
+
+typedef struct spoa_gb300_engine spoa_gb300_engine;
+typedef struct spoa_gb300_graph spoa_gb300_graph;
+typedef struct spoa_gb300_batch spoa_gb300_batch;
+
+const char* spoa_gb300_status_string(int32_t status);
+
+/* Number of CUDA devices usable by the library (0 when none). */
+int32_t spoa_gb300_device_count(void);
+
+/* ---- AlignmentEngine ---------------------------------------------------- */
+
+/* Replaces AlignmentEngine::Create (src/alignment_engine.cpp:32-73, all
+ * three overloads funnel into this 7-penalty form): validates, resolves the
+ * gap model (linear if g >= e, affine if g <= q or e >= c, else convex) and
+ * canonicalises the penalties. */
+int32_t spoa_gb300_engine_create(int32_t type, int8_t m, int8_t n, int8_t g, int8_t e,
+                                 int8_t q, int8_t c, spoa_gb300_engine** out);
+void spoa_gb300_engine_destroy(spoa_gb300_engine* engine);
+/* Resolved subtype and canonical penalties (AlignmentEngine::subtype_, m_..c_). */
+int32_t spoa_gb300_engine_params(const spoa_gb300_engine* engine, int32_t* type,
+                                 int32_t* subtype, int8_t* penalties6);
+
+/* Replaces SimdAlignmentEngine::Prealloc
+ * (src/simd_alignment_engine_implementation.hpp:381-422): sizes the device
+ * DP arena for reads up to max_len against graphs of max_len*alphabet_size
+ * nodes. */
+int32_t spoa_gb300_engine_prealloc(spoa_gb300_engine* engine, uint32_t max_len,
+                                   uint8_t alphabet_size);
+
+/* Replaces AlignmentEngine::Align (include/spoa/alignment_engine.hpp:61-69;
+ * SimdAlignmentEngine::Align, implementation.hpp:703-780).  Writes the
+ * alignment as n_pairs (node id | -1, position | -1) int32 pairs.
+ * *score_written is 1 when the reference would have written *score. */
+int32_t spoa_gb300_engine_align(spoa_gb300_engine* engine, const char* sequence,
+                                uint32_t sequence_len, const spoa_gb300_graph* graph,
+                                int32_t* score, int32_t* score_written, int32_t* pairs,
+                                uint32_t pairs_cap, uint32_t* n_pairs);
+
+/* ---- Graph --------------------------------------------------------------- */
+
+/* Replaces Graph::Graph (src/graph.cpp:65-74): an empty device-resident graph. */
+int32_t spoa_gb300_graph_create(spoa_gb300_graph** out);
+void spoa_gb300_graph_destroy(spoa_gb300_graph* graph);
+/* Replaces Graph::Clear (src/graph.cpp:649-658). */
+int32_t spoa_gb300_graph_clear(spoa_gb300_graph* graph);
+
+/* Replaces Graph::AddAlignment (src/graph.cpp:155-247) with explicit
+ * per-base weights (weights may be NULL: weight 1 per base, graph.cpp:119-125). */
+int32_t spoa_gb300_graph_add_alignment(spoa_gb300_graph* graph, const int32_t* pairs,
+                                       uint32_t n_pairs, const char* sequence,
+                                       uint32_t sequence_len, const uint32_t* weights,
+                                       uint32_t n_weights);
+/* Replaces the quality overload (src/graph.cpp:137-146): weight = q - 33. */
+int32_t spoa_gb300_graph_add_alignment_quality(spoa_gb300_graph* graph, const int32_t* pairs,
+                                               uint32_t n_pairs, const char* sequence,
+                                               uint32_t sequence_len, const char* quality,
+                                               uint32_t quality_len);
+
+/* Fused Align + AddAlignment of one read with no host round trip of the
+ * alignment (the per-read body of src/main.cpp:275-314, including the
+ * strand-ambiguous choice of main.cpp:285-302 when strand_ambiguous != 0).
+ * quality may be NULL. */
+int32_t spoa_gb300_align_add(spoa_gb300_engine* engine, spoa_gb300_graph* graph,
+                             const char* sequence, uint32_t sequence_len, const char* quality,
+                             int32_t strand_ambiguous, int32_t* score, int32_t* reversed);
+
+/* Replaces Graph::GenerateConsensus (src/graph.cpp:368-375). */
+int32_t spoa_gb300_graph_consensus(spoa_gb300_graph* graph, char* out, uint32_t cap,
+                                   uint32_t* len);
+
+/* Replaces Graph::GenerateMultipleSequenceAlignment (src/graph.cpp:339-366):
+ * rows * cols bytes, row-major. */
+int32_t spoa_gb300_graph_msa(spoa_gb300_graph* graph, int32_t include_consensus, char* out,
+                             uint64_t cap, uint32_t* rows, uint32_t* cols);
+
+/* Sizes of the graph (Graph::nodes(), edges(), sequences(), consensus()
+ * accessors, include/spoa/graph.hpp:102-132) and of its label lists. */
+int32_t spoa_gb300_graph_counts(const spoa_gb300_graph* graph, uint32_t* nodes,
+                                uint32_t* edges, uint32_t* sequences, uint32_t* consensus,
+                                uint32_t* labels, uint32_t* num_codes);
+
+/* Flat copy of the graph for the host-side views of Graph (graph.hpp:40-132):
+ * node characters and codes, in/out edge lists (CSR, insertion order),
+ * aligned-node lists (CSR), edges (tail, head, weight, label CSR), rank
+ * order, sequence begins, consensus and the coder/decoder tables.  Any
+ * pointer may be NULL to skip that array; sizes follow graph_counts. */
+int32_t spoa_gb300_graph_export(const spoa_gb300_graph* graph, uint8_t* chars, uint8_t* codes,
+                                uint32_t* in_off, uint32_t* in_edges, uint32_t* out_off,
+                                uint32_t* out_edges, uint32_t* aligned_off,
+                                uint32_t* aligned_nodes, uint32_t* edge_tail,
+                                uint32_t* edge_head, int64_t* edge_weight, uint32_t* label_off,
+                                uint32_t* labels, uint32_t* rank_to_node, uint32_t* seq_begin,
+                                uint32_t* consensus, int32_t* coder256, int32_t* decoder256);
+
+/* ---- Batched windows (no counterpart in the reference) ------------------- *
+ * Many independent windows (each one Graph driven by the per-read loop of
+ * src/main.cpp:275-314, then GenerateConsensus) in one persistent kernel:
+ * every CTA pulls windows from a device work queue.  Inputs and outputs are
+ * host pointers; the device copies happen inside the call.               */
+typedef struct {
+  int32_t type; /* default type when window_type is NULL */
+  int8_t m, n, g, e, q, c;
+  int8_t pad;
+  uint32_t n_windows;
+  const uint32_t* window_read_off; /* [n_windows + 1] */
+  const int8_t* window_type;       /* [n_windows] or NULL */
+  const int8_t* window_strand;     /* [n_windows] strand-ambiguous flags or NULL */
+  const char* seqs;                /* all reads back to back */
+  const uint64_t* seq_off;         /* [n_reads + 1] */
+  const char* quals;               /* same offsets as seqs, or NULL */
+  uint32_t max_nodes;              /* per-window node cap (0: automatic) */
+  int32_t threads_per_window;      /* 0: autotuned from the longest read */
+  int32_t columns_per_thread;      /* 0: autotuned */
+  int32_t ctas;                    /* 0: fill the device */
+  uint64_t memory_budget;          /* bytes for per-CTA arenas (0: automatic) */
+  int32_t want_alignments;         /* also return every read's alignment */
+  int32_t want_msa;                /* also return every window's MSA */
+} spoa_gb300_batch_desc;
+
+typedef struct {
+  /* filled by the library: pointers stay valid until batch_destroy */
+  const int32_t* read_scores;  /* [n_reads] */
+  const uint8_t* read_reversed;
+  const int32_t* window_status; /* [n_windows] */
+  const char* consensus;        /* back to back */
+  const uint64_t* consensus_off; /* [n_windows + 1] */
+  const int32_t* alignments;    /* pairs, when want_alignments */
+  const uint64_t* alignment_off; /* [n_reads + 1] pair offsets */
+  const char* msa;              /* when want_msa */
+  const uint64_t* msa_off;       /* [n_windows + 1] byte offsets */
+  const uint32_t* msa_rows;      /* [n_windows] */
+  const uint32_t* msa_cols;
+  uint64_t cells;               /* sum over reads of read length x graph nodes */
+  double kernel_ms;             /* device time of the persistent launch(es) */
+  int32_t threads_per_window, columns_per_thread, ctas, launches;
+} spoa_gb300_batch_result;
+
+/* Uploads a batch and sizes the device arenas. */
+int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* desc, spoa_gb300_batch** out);
+/* Runs the persistent kernel on device-resident inputs (stream may be 0).
+ * Windows that outgrow their arena are rerun with a larger one. */
+int32_t spoa_gb300_batch_launch(spoa_gb300_batch* batch, void* stream);
+/* One launch per window, one CTA each: the plain one-window-per-launch form. */
+int32_t spoa_gb300_batch_launch_plain(spoa_gb300_batch* batch, void* stream);
+/* Copies the results to the host and fills *result. */
+int32_t spoa_gb300_batch_fetch(spoa_gb300_batch* batch, spoa_gb300_batch_result* result);
+void spoa_gb300_batch_destroy(spoa_gb300_batch* batch);
+/* create + launch + fetch: host buffers in, host results out. */
+int32_t spoa_gb300_batch_run(const spoa_gb300_batch_desc* desc, spoa_gb300_batch** out,
+                             spoa_gb300_batch_result* result);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPOA_GB300_H_ */

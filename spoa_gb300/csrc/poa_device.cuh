@@ -1,0 +1,590 @@
+// poa_device.cuh - device-resident POA window: graph, DP, traceback,
+// consensus and MSA for one window, run by one CTA.
+//
+// A window is one spoa::Graph plus the per-read state of an AlignmentEngine.
+// Everything a read needs (graph arrays, DP matrices, traceback buffers)
+// lives in HBM in one arena per CTA; the graph never leaves the device
+// between reads.
+//
+// Reference correspondence (spoa v4):
+//   dp_forward / select / traceback  <- SimdAlignmentEngine::Linear/Affine/
+//        Convex (src/simd_alignment_engine_implementation.hpp:782-2131)
+//   width rule                       <- implementation.hpp:719-726 with
+//        AlignmentEngine::WorstCaseAlignmentScore (alignment_engine.cpp:101)
+//   g_add_alignment                  <- Graph::AddAlignment (graph.cpp:155)
+//   g_topo_sort                      <- Graph::TopologicalSort (graph.cpp:249)
+//   g_consensus                      <- TraverseHeaviestBundle/BranchCompletion
+//                                       (graph.cpp:433-516)
+//   g_msa                            <- GenerateMultipleSequenceAlignment
+//                                       (graph.cpp:321-366)
+#pragma once
+
+#include <cstdint>
+
+namespace spoa_gb300 {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+// Internal -infinity for row 0 of F/O.  The reference uses INT16_MIN+1024 or
+// INT32_MIN+1024; the width rule keeps every reachable score above either,
+// so row 0 of F/O never wins a max nor matches a traceback equality, and
+// any value far below the reachable range gives identical results.
+constexpr int32_t kNegBig = -(1 << 28);
+
+enum Status : int32_t {
+  kOk = 0,
+  kInvalidArgument = 1,
+  kTooLarge = 2,
+  kOverflow = 3,
+  kNoMemory = 4,
+  kInvalidAlignment = 5,
+  kMissingSequence = 6,
+  kUnequalWeights = 7,
+  kCapacity = 8,
+  kTraceback = 9,
+  kCuda = 10,
+};
+
+enum : int32_t { kSW = 0, kNW = 1, kOV = 2 };
+enum : int32_t { kLinear = 0, kAffine = 1, kConvex = 2 };
+
+struct Scoring {
+  int32_t type, sub;
+  int32_t m, n, g, e, q, c;
+};
+
+__host__ __device__ inline uint64_t align_up(uint64_t x, uint64_t a) {
+  return (x + a - 1) / a * a;
+}
+
+// ---------------------------------------------------------------------------
+// graph arena
+// ---------------------------------------------------------------------------
+struct GraphCaps {
+  uint32_t nodes, edges, labels, seqs, aligned;  // aligned: per-node slots
+};
+
+struct GraphHeader {
+  uint32_t n_nodes, n_edges, n_labels, n_seqs, num_codes, n_consensus;
+  int32_t status;
+  uint32_t pad;
+  int32_t coder[256];
+  int32_t decoder[256];
+};
+
+struct GraphView {
+  GraphHeader* hdr;
+  uint8_t* code;
+  uint32_t *in_first, *in_last, *out_first, *out_last, *in_deg;
+  uint8_t* n_aligned;
+  uint32_t* aligned;  // [nodes * caps.aligned]
+  uint32_t *rank_to_node, *node_to_rank;
+  uint32_t *e_tail, *e_head, *e_next_in, *e_next_out, *e_lab_first, *e_lab_last;
+  int64_t* e_weight;
+  uint32_t *lab_seq, *lab_next;
+  uint32_t* seq_begin;
+  uint32_t* consensus;
+  uint8_t *marks, *ignored;
+  uint32_t* stack;
+  int64_t* cscore;
+  uint32_t *cpred, *column;
+  GraphCaps caps;
+  uint64_t stack_cap;
+};
+
+// Lays out a graph arena at `base` (nullptr: only measure).  Returns bytes.
+__host__ __device__ inline uint64_t graph_layout(uint8_t* base, const GraphCaps& c,
+                                                 GraphView* v) {
+  uint64_t off = 0;
+  auto take = [&](uint64_t bytes) -> uint8_t* {
+    uint8_t* p = base ? base + off : nullptr;
+    off = align_up(off + bytes, 256);
+    return p;
+  };
+  const uint64_t N = c.nodes, E = c.edges;
+  v->caps = c;
+  v->stack_cap = E + N * (uint64_t)(c.aligned + 1) + 1;
+  v->hdr = reinterpret_cast<GraphHeader*>(take(sizeof(GraphHeader)));
+  v->code = take(N);
+  v->in_first = reinterpret_cast<uint32_t*>(take(4 * N));
+  v->in_last = reinterpret_cast<uint32_t*>(take(4 * N));
+  v->out_first = reinterpret_cast<uint32_t*>(take(4 * N));
+  v->out_last = reinterpret_cast<uint32_t*>(take(4 * N));
+  v->in_deg = reinterpret_cast<uint32_t*>(take(4 * N));
+  v->n_aligned = take(N);
+  v->aligned = reinterpret_cast<uint32_t*>(take(4 * N * c.aligned));
+  v->rank_to_node = reinterpret_cast<uint32_t*>(take(4 * N));
+  v->node_to_rank = reinterpret_cast<uint32_t*>(take(4 * N));
+  v->e_tail = reinterpret_cast<uint32_t*>(take(4 * E));
+  v->e_head = reinterpret_cast<uint32_t*>(take(4 * E));
+  v->e_next_in = reinterpret_cast<uint32_t*>(take(4 * E));
+  v->e_next_out = reinterpret_cast<uint32_t*>(take(4 * E));
+  v->e_lab_first = reinterpret_cast<uint32_t*>(take(4 * E));
+  v->e_lab_last = reinterpret_cast<uint32_t*>(take(4 * E));
+  v->e_weight = reinterpret_cast<int64_t*>(take(8 * E));
+  v->lab_seq = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.labels));
+  v->lab_next = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.labels));
+  v->seq_begin = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.seqs));
+  v->consensus = reinterpret_cast<uint32_t*>(take(4 * N));
+  v->marks = take(N);
+  v->ignored = take(N);
+  v->stack = reinterpret_cast<uint32_t*>(take(4 * v->stack_cap));
+  v->cscore = reinterpret_cast<int64_t*>(take(8 * N));
+  v->cpred = reinterpret_cast<uint32_t*>(take(4 * N));
+  v->column = reinterpret_cast<uint32_t*>(take(4 * N));
+  return off;
+}
+
+// ---------------------------------------------------------------------------
+// DP arena (per alignment engine / per CTA)
+// ---------------------------------------------------------------------------
+struct DpCaps {
+  uint32_t rows;  // graph nodes + 1
+  uint32_t ld;    // columns (>= threads * columns-per-thread)
+  uint32_t preds; // in-edges + rows
+  int32_t sub;
+};
+
+struct DpView {
+  int32_t *H, *F, *E, *O, *Q;
+  uint32_t *pred_ptr, *preds, *row_indeg;
+  uint8_t *row_char, *row_sink;
+  int32_t *fc, *fcF, *fcO;
+  int32_t *aln_a, *aln_b;  // traceback outputs, 2 ints per pair
+  uint8_t* seq_rc;         // reverse complement / staging of the read
+  DpCaps caps;
+  uint64_t aln_cap;        // pairs
+};
+
+__host__ __device__ inline uint64_t dp_layout(uint8_t* base, const DpCaps& c, DpView* v) {
+  uint64_t off = 0;
+  auto take = [&](uint64_t bytes) -> uint8_t* {
+    uint8_t* p = base ? base + off : nullptr;
+    off = align_up(off + bytes, 256);
+    return p;
+  };
+  const uint64_t cells = (uint64_t)c.rows * c.ld;
+  v->caps = c;
+  v->aln_cap = (uint64_t)c.rows + c.ld + 16;
+  v->H = reinterpret_cast<int32_t*>(take(4 * cells));
+  v->F = c.sub >= kAffine ? reinterpret_cast<int32_t*>(take(4 * cells)) : nullptr;
+  v->E = c.sub >= kAffine ? reinterpret_cast<int32_t*>(take(4 * cells)) : nullptr;
+  v->O = c.sub == kConvex ? reinterpret_cast<int32_t*>(take(4 * cells)) : nullptr;
+  v->Q = c.sub == kConvex ? reinterpret_cast<int32_t*>(take(4 * cells)) : nullptr;
+  v->pred_ptr = reinterpret_cast<uint32_t*>(take(4 * ((uint64_t)c.rows + 1)));
+  v->preds = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.preds));
+  v->row_indeg = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.rows));
+  v->row_char = take(c.rows);
+  v->row_sink = take(c.rows);
+  v->fc = reinterpret_cast<int32_t*>(take(4 * (uint64_t)c.rows));
+  v->fcF = reinterpret_cast<int32_t*>(take(4 * (uint64_t)c.rows));
+  v->fcO = reinterpret_cast<int32_t*>(take(4 * (uint64_t)c.rows));
+  v->aln_a = reinterpret_cast<int32_t*>(take(8 * v->aln_cap));
+  v->aln_b = reinterpret_cast<int32_t*>(take(8 * v->aln_cap));
+  v->seq_rc = take(c.ld);
+  return off;
+}
+
+// WorstCaseAlignmentScore (alignment_engine.cpp:101-110)
+__host__ __device__ inline int64_t gap_score(const Scoring& s, int64_t len) {
+  if (len == 0) return 0;
+  int64_t a = s.g + (len - 1) * s.e, b = s.q + (len - 1) * s.c;
+  return a < b ? a : b;
+}
+__host__ __device__ inline int64_t worst_case(const Scoring& s, int64_t i, int64_t j) {
+  int64_t d = i > j ? i - j : j - i, mn = i < j ? i : j;
+  int64_t a = -1 * (s.m * mn + gap_score(s, d));
+  int64_t b = gap_score(s, i) + gap_score(s, j);
+  return a < b ? a : b;
+}
+// Width rule (implementation.hpp:719-726): 16 int16 lanes or 8 int32 lanes
+// per AVX2 vector, or 0 for "possible overflow".
+__host__ __device__ inline int32_t lanes_for(const Scoring& s, uint32_t len, uint32_t nodes) {
+  int64_t wc = worst_case(s, (int64_t)len + 8, nodes);
+  if (wc < (int64_t)INT32_MIN + 1024) return 0;
+  return wc < (int64_t)INT16_MIN + 1024 ? 8 : 16;
+}
+
+// Reverse complement of spoa's strand-ambiguous mode (biosoup 0.10.0
+// Sequence::ReverseAndComplement: Watson-Crick / IUPAC pairing, reversed).
+__host__ __device__ inline uint8_t complement_base(uint8_t ch) {
+  switch (ch) {
+    case 'A': return 'T';
+    case 'C': return 'G';
+    case 'G': return 'C';
+    case 'T': return 'A';
+    case 'U': return 'A';
+    case 'R': return 'Y';
+    case 'Y': return 'R';
+    case 'K': return 'M';
+    case 'M': return 'K';
+    case 'B': return 'V';
+    case 'D': return 'H';
+    case 'H': return 'D';
+    case 'V': return 'B';
+    case 'a': return 't';
+    case 'c': return 'g';
+    case 'g': return 'c';
+    case 't': return 'a';
+    case 'u': return 'a';
+    default: return ch;
+  }
+}
+
+// Per-base weights of a read: explicit weights, Phred qualities (weight =
+// quality - 33, graph.cpp:137-146; read back to front for a read kept on the
+// reverse strand), or one constant weight (graph.cpp:119-125).
+struct WeightSrc {
+  const uint32_t* w;
+  const uint8_t* qual;
+  uint32_t len;
+  uint32_t reversed;
+  uint32_t wconst;
+  __device__ __forceinline__ uint32_t at(uint32_t i) const {
+    if (w) return w[i];
+    if (qual) return (uint32_t)((int32_t)qual[reversed ? len - 1 - i : i] - 33);
+    return wconst;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// graph mutation (thread 0 of the CTA)
+// ---------------------------------------------------------------------------
+__device__ inline void g_reset(GraphView& G) {
+  GraphHeader* h = G.hdr;
+  h->n_nodes = h->n_edges = h->n_labels = h->n_seqs = h->num_codes = h->n_consensus = 0;
+  h->status = kOk;
+  for (int i = 0; i < 256; ++i) h->coder[i] = h->decoder[i] = -1;
+}
+
+__device__ inline int64_t g_add_node(GraphView& G, uint32_t code) {
+  GraphHeader* h = G.hdr;
+  if (h->n_nodes >= G.caps.nodes) return -1;
+  uint32_t id = h->n_nodes++;
+  G.code[id] = (uint8_t)code;
+  G.in_first[id] = G.in_last[id] = G.out_first[id] = G.out_last[id] = kNone;
+  G.in_deg[id] = 0;
+  G.n_aligned[id] = 0;
+  return id;
+}
+
+__device__ inline int g_add_label(GraphView& G, uint32_t e) {
+  GraphHeader* h = G.hdr;
+  if (h->n_labels >= G.caps.labels) return -1;
+  uint32_t l = h->n_labels++;
+  G.lab_seq[l] = h->n_seqs;
+  G.lab_next[l] = kNone;
+  if (G.e_lab_last[e] != kNone) {
+    G.lab_next[G.e_lab_last[e]] = l;
+  } else {
+    G.e_lab_first[e] = l;
+  }
+  G.e_lab_last[e] = l;
+  return 0;
+}
+
+// Graph::AddEdge (graph.cpp:81-91)
+__device__ inline int g_add_edge(GraphView& G, uint32_t tail, uint32_t head, uint32_t w) {
+  for (uint32_t e = G.out_first[tail]; e != kNone; e = G.e_next_out[e]) {
+    if (G.e_head[e] == head) {
+      if (g_add_label(G, e)) return -1;
+      G.e_weight[e] += w;
+      return 0;
+    }
+  }
+  GraphHeader* h = G.hdr;
+  if (h->n_edges >= G.caps.edges) return -1;
+  uint32_t e = h->n_edges++;
+  G.e_tail[e] = tail;
+  G.e_head[e] = head;
+  G.e_weight[e] = w;
+  G.e_next_in[e] = G.e_next_out[e] = kNone;
+  G.e_lab_first[e] = G.e_lab_last[e] = kNone;
+  if (g_add_label(G, e)) return -1;
+  if (G.out_last[tail] != kNone) G.e_next_out[G.out_last[tail]] = e; else G.out_first[tail] = e;
+  G.out_last[tail] = e;
+  if (G.in_last[head] != kNone) G.e_next_in[G.in_last[head]] = e; else G.in_first[head] = e;
+  G.in_last[head] = e;
+  G.in_deg[head] += 1;
+  return 0;
+}
+
+// Graph::AddSequence (graph.cpp:93-110).  -1: empty range, -2: capacity.
+__device__ inline int64_t g_add_sequence(GraphView& G, const uint8_t* seq, const WeightSrc& w,
+                                         uint32_t begin, uint32_t end) {
+  if (begin == end) return -1;
+  int64_t prev = -1;
+  for (uint32_t i = begin; i < end; ++i) {
+    int64_t curr = g_add_node(G, (uint32_t)G.hdr->coder[seq[i]]);
+    if (curr < 0) return -2;
+    if (prev >= 0) {
+      if (g_add_edge(G, (uint32_t)prev, (uint32_t)curr, w.at(i - 1) + w.at(i))) return -2;
+    }
+    prev = curr;
+  }
+  return (int64_t)G.hdr->n_nodes - (end - begin);
+}
+
+// Graph::TopologicalSort (graph.cpp:249-303)
+__device__ inline int g_topo_sort(GraphView& G) {
+  const uint32_t nn = G.hdr->n_nodes;
+  for (uint32_t i = 0; i < nn; ++i) {
+    G.marks[i] = 0;
+    G.ignored[i] = 0;
+  }
+  uint64_t sp = 0;
+  uint32_t rank = 0;
+  const uint32_t K = G.caps.aligned;
+  // every iteration pops or pushes; pushes are bounded by the stack size
+  uint64_t guard = 0;
+  const uint64_t guard_max = 4 * G.stack_cap + 4 * (uint64_t)nn + 16;
+  for (uint32_t s = 0; s < nn; ++s) {
+    if (G.marks[s] != 0) continue;
+    G.stack[sp++] = s;
+    while (sp) {
+      if (++guard > guard_max) return -1;
+      uint32_t curr = G.stack[sp - 1];
+      bool valid = true;
+      if (G.marks[curr] != 2) {
+        for (uint32_t e = G.in_first[curr]; e != kNone; e = G.e_next_in[e]) {
+          uint32_t t = G.e_tail[e];
+          if (G.marks[t] != 2) {
+            if (sp >= G.stack_cap) return -1;
+            G.stack[sp++] = t;
+            valid = false;
+          }
+        }
+        const uint32_t na = G.n_aligned[curr];
+        const uint32_t* al = G.aligned + (uint64_t)curr * K;
+        if (!G.ignored[curr]) {
+          for (uint32_t k = 0; k < na; ++k) {
+            uint32_t a = al[k];
+            if (G.marks[a] != 2) {
+              if (sp >= G.stack_cap) return -1;
+              G.stack[sp++] = a;
+              G.ignored[a] = 1;
+              valid = false;
+            }
+          }
+        }
+        if (valid) {
+          G.marks[curr] = 2;
+          if (!G.ignored[curr]) {
+            G.rank_to_node[rank] = curr;
+            G.node_to_rank[curr] = rank++;
+            for (uint32_t k = 0; k < na; ++k) {
+              G.rank_to_node[rank] = al[k];
+              G.node_to_rank[al[k]] = rank++;
+            }
+          }
+        } else {
+          G.marks[curr] = 1;
+        }
+      }
+      if (valid) --sp;
+    }
+  }
+  return rank == nn ? 0 : -1;
+}
+
+__device__ inline int g_link_aligned(GraphView& G, uint32_t a, uint32_t b) {
+  const uint32_t K = G.caps.aligned;
+  if (G.n_aligned[a] >= K) return -1;
+  G.aligned[(uint64_t)a * K + G.n_aligned[a]++] = b;
+  return 0;
+}
+
+// Graph::AddAlignment (graph.cpp:155-247).  pairs: n (node id | -1,
+// position | -1).  Weights: w[] or the constant wconst.
+__device__ inline int32_t g_add_alignment(GraphView& G, const int32_t* pairs, uint32_t n_pairs,
+                                          const uint8_t* seq, uint32_t len, const WeightSrc& w) {
+  GraphHeader* h = G.hdr;
+  if (len == 0) return kOk;
+  // room for the worst case of this read
+  if ((uint64_t)h->n_nodes + len > G.caps.nodes || (uint64_t)h->n_edges + len + 1 > G.caps.edges ||
+      (uint64_t)h->n_labels + len + 1 > G.caps.labels || h->n_seqs + 1 > G.caps.seqs)
+    return kCapacity;
+  for (uint32_t i = 0; i < len; ++i) {
+    uint8_t ch = seq[i];
+    if (h->coder[ch] == -1) {
+      h->coder[ch] = (int32_t)h->num_codes;
+      h->decoder[h->num_codes++] = ch;
+    }
+  }
+  if (n_pairs == 0) {
+    int64_t b = g_add_sequence(G, seq, w, 0, len);
+    if (b < -1) return kCapacity;
+    G.seq_begin[h->n_seqs++] = (uint32_t)b;
+    return g_topo_sort(G) ? kCapacity : kOk;
+  }
+  int32_t first_valid = -1, last_valid = -1;
+  for (uint32_t k = 0; k < n_pairs; ++k) {
+    int32_t pos = pairs[2 * k + 1];
+    if (pos != -1) {
+      if (pos < 0 || pos >= (int32_t)len) return kInvalidAlignment;
+      if (first_valid == -1) first_valid = pos;
+      last_valid = pos;
+    }
+  }
+  if (first_valid == -1) return kMissingSequence;
+  for (uint32_t k = 0; k < n_pairs; ++k) {
+    int32_t nid = pairs[2 * k];
+    if (nid < -1 || nid >= (int32_t)h->n_nodes) return kInvalidAlignment;
+  }
+  int64_t begin = g_add_sequence(G, seq, w, 0, (uint32_t)first_valid);
+  if (begin < -1) return kCapacity;
+  int64_t prev = begin >= 0 ? (int64_t)h->n_nodes - 1 : -1;
+  int64_t last = g_add_sequence(G, seq, w, (uint32_t)last_valid + 1, len);
+  if (last < -1) return kCapacity;
+  const uint32_t K = G.caps.aligned;
+  for (uint32_t k = 0; k < n_pairs; ++k) {
+    int32_t nid = pairs[2 * k], pos = pairs[2 * k + 1];
+    if (pos == -1) continue;
+    uint32_t code = (uint32_t)h->coder[seq[pos]];
+    int64_t curr = -1;
+    if (nid == -1) {
+      curr = g_add_node(G, code);
+      if (curr < 0) return kCapacity;
+    } else {
+      if (G.code[nid] == code) {
+        curr = nid;
+      } else {
+        const uint32_t na = G.n_aligned[nid];
+        const uint32_t* al = G.aligned + (uint64_t)nid * K;
+        for (uint32_t a = 0; a < na; ++a) {
+          if (G.code[al[a]] == code) {
+            curr = al[a];
+            break;
+          }
+        }
+        if (curr < 0) {
+          curr = g_add_node(G, code);
+          if (curr < 0) return kCapacity;
+          for (uint32_t a = 0; a < na; ++a) {
+            uint32_t kt = al[a];
+            if (g_link_aligned(G, kt, (uint32_t)curr) || g_link_aligned(G, (uint32_t)curr, kt))
+              return kCapacity;
+          }
+          if (g_link_aligned(G, (uint32_t)nid, (uint32_t)curr) ||
+              g_link_aligned(G, (uint32_t)curr, (uint32_t)nid))
+            return kCapacity;
+        }
+      }
+    }
+    if (begin < 0) begin = curr;
+    if (prev >= 0) {
+      if (g_add_edge(G, (uint32_t)prev, (uint32_t)curr, w.at(pos - 1) + w.at(pos)))
+        return kCapacity;
+    }
+    prev = curr;
+  }
+  if (last >= 0) {
+    if (g_add_edge(G, (uint32_t)prev, (uint32_t)last, w.at(last_valid) + w.at(last_valid + 1)))
+      return kCapacity;
+  }
+  G.seq_begin[h->n_seqs++] = (uint32_t)begin;
+  return g_topo_sort(G) ? kCapacity : kOk;
+}
+
+// ---------------------------------------------------------------------------
+// consensus (graph.cpp:433-516), thread 0
+// ---------------------------------------------------------------------------
+__device__ inline uint32_t g_branch_completion(GraphView& G, uint32_t rank) {
+  const uint32_t start = G.rank_to_node[rank];
+  for (uint32_t e = G.out_first[start]; e != kNone; e = G.e_next_out[e]) {
+    uint32_t hd = G.e_head[e];
+    for (uint32_t f = G.in_first[hd]; f != kNone; f = G.e_next_in[f]) {
+      uint32_t t = G.e_tail[f];
+      if (t != start) G.cscore[t] = -1;
+    }
+  }
+  uint32_t mx = kNone;
+  const uint32_t nn = G.hdr->n_nodes;
+  for (uint32_t r = rank + 1; r < nn; ++r) {
+    uint32_t it = G.rank_to_node[r];
+    G.cscore[it] = -1;
+    G.cpred[it] = kNone;
+    for (uint32_t f = G.in_first[it]; f != kNone; f = G.e_next_in[f]) {
+      uint32_t t = G.e_tail[f];
+      if (G.cscore[t] == -1) continue;
+      int64_t w = G.e_weight[f];
+      if (G.cscore[it] < w || (G.cscore[it] == w && G.cscore[G.cpred[it]] <= G.cscore[t])) {
+        G.cscore[it] = w;
+        G.cpred[it] = t;
+      }
+    }
+    if (G.cpred[it] != kNone) G.cscore[it] += G.cscore[G.cpred[it]];
+    if (mx == kNone || G.cscore[mx] < G.cscore[it]) mx = it;
+  }
+  return mx;
+}
+
+__device__ inline void g_consensus(GraphView& G) {
+  const uint32_t nn = G.hdr->n_nodes;
+  G.hdr->n_consensus = 0;
+  if (nn == 0) return;
+  for (uint32_t i = 0; i < nn; ++i) {
+    G.cscore[i] = -1;
+    G.cpred[i] = kNone;
+  }
+  uint32_t mx = kNone;
+  for (uint32_t r = 0; r < nn; ++r) {
+    uint32_t it = G.rank_to_node[r];
+    for (uint32_t f = G.in_first[it]; f != kNone; f = G.e_next_in[f]) {
+      uint32_t t = G.e_tail[f];
+      int64_t w = G.e_weight[f];
+      if (G.cscore[it] < w || (G.cscore[it] == w && G.cscore[G.cpred[it]] <= G.cscore[t])) {
+        G.cscore[it] = w;
+        G.cpred[it] = t;
+      }
+    }
+    if (G.cpred[it] != kNone) G.cscore[it] += G.cscore[G.cpred[it]];
+    if (mx == kNone || G.cscore[mx] < G.cscore[it]) mx = it;
+  }
+  // each completion moves to a strictly later rank
+  while (G.out_first[mx] != kNone) {
+    uint32_t nx = g_branch_completion(G, G.node_to_rank[mx]);
+    if (nx == kNone) break;
+    mx = nx;
+  }
+  uint32_t n = 0;
+  while (G.cpred[mx] != kNone && n < nn) {
+    G.consensus[n++] = mx;
+    mx = G.cpred[mx];
+  }
+  G.consensus[n++] = mx;
+  for (uint32_t a = 0, b = n - 1; a < b; ++a, --b) {
+    uint32_t t = G.consensus[a];
+    G.consensus[a] = G.consensus[b];
+    G.consensus[b] = t;
+  }
+  G.hdr->n_consensus = n;
+}
+
+// Node::Successor (graph.cpp:22-30)
+__device__ inline uint32_t g_successor(const GraphView& G, uint32_t node, uint32_t label) {
+  for (uint32_t e = G.out_first[node]; e != kNone; e = G.e_next_out[e]) {
+    for (uint32_t l = G.e_lab_first[e]; l != kNone; l = G.lab_next[l]) {
+      if (G.lab_seq[l] == label) return G.e_head[e];
+      if (G.lab_seq[l] > label) break;  // labels are appended in sequence order
+    }
+  }
+  return kNone;
+}
+
+// InitializeMultipleSequenceAlignment (graph.cpp:321-337); returns row size.
+__device__ inline uint32_t g_msa_columns(GraphView& G) {
+  const uint32_t nn = G.hdr->n_nodes, K = G.caps.aligned;
+  uint32_t j = 0;
+  for (uint32_t i = 0; i < nn; ++i, ++j) {
+    uint32_t it = G.rank_to_node[i];
+    G.column[it] = j;
+    const uint32_t na = G.n_aligned[it];
+    for (uint32_t k = 0; k < na; ++k) {
+      G.column[G.aligned[(uint64_t)it * K + k]] = j;
+      ++i;
+    }
+  }
+  return j;
+}
+
+}  // namespace spoa_gb300

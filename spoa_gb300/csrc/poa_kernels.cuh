@@ -1,0 +1,480 @@
+// poa_kernels.cuh - kernel templates shared by the per-gap-model
+// translation units (inst_linear.cu, inst_affine.cu, inst_convex.cu) and the
+// host code (spoa_gb300.cu).  One CTA owns one window; the device functions
+// live in poa_device.cuh and poa_dp.cuh.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "poa_device.cuh"
+#include "poa_dp.cuh"
+
+namespace spoa_gb300 {
+
+struct ReadOut {
+  int32_t status;
+  int32_t has_score;
+  int32_t score;
+  int32_t reversed;
+  uint32_t n_pairs;
+  int32_t lanes;
+};
+
+struct SharedState {
+  int32_t status, mode, lanes, pad;
+  int64_t max_i, max_j;
+  int32_t score, has_f, score_f, has_r, score_r;
+  uint32_t np_f, np_r;
+};
+
+// Align one read (seq, or its reverse complement staged in D.seq_rc) against
+// the current graph; thread 0 leaves the pairs in `pairs` and returns
+// has_score/score through `ss`.  Every thread must call it.
+template <int SUB, int CPT>
+__device__ void read_align(const Scoring& S, const GraphView& G, DpView& D, BlockScratch& sh,
+                           SharedState& ss, const uint8_t* seq, uint32_t L, int32_t lanes,
+                           int32_t* pairs, int32_t* has, int32_t* score, uint32_t* np) {
+  int64_t mi, mj;
+  int32_t sc;
+  dp_forward<SUB, CPT>(S, D, seq, L, G.hdr->n_nodes, lanes, sh, &mi, &mj, &sc);
+  if (threadIdx.x == 0) {
+    *np = 0;
+    *has = 0;
+    if (mi >= 0) {
+      *has = 1;
+      *score = sc;
+      int32_t st = dp_traceback<SUB>(S, D, G, seq, L, G.hdr->n_nodes, mi, mj, pairs, np);
+      if (st != kOk) ss.status = st;
+    }
+  }
+  __syncthreads();
+}
+
+// Checks done before a read's DP (thread 0): mode 0 = empty alignment,
+// 1 = run the DP; status on error.
+__device__ inline void read_prologue(const Scoring& S, const GraphView& G, const DpView& D,
+                                     uint32_t L, uint32_t nthreads_cols, SharedState& ss) {
+  const uint32_t V = G.hdr->n_nodes;
+  ss.status = kOk;
+  ss.mode = 0;
+  ss.lanes = 16;
+  if (V == 0 || L == 0) return;
+  int32_t lanes = lanes_for(S, L, V);
+  if (!lanes) {
+    ss.status = kOverflow;
+    return;
+  }
+  if (L > nthreads_cols || L > D.caps.ld || V + 1 > D.caps.rows ||
+      (uint64_t)G.hdr->n_edges + V + 1 > D.caps.preds) {
+    ss.status = kCapacity;
+    return;
+  }
+  ss.lanes = lanes;
+  ss.mode = 1;
+}
+
+template <int SUB, int CPT>
+__global__ void __launch_bounds__(1024) k_align(Scoring S, GraphView G, DpView D,
+                                                const uint8_t* seq, uint32_t L, ReadOut* out) {
+  __shared__ BlockScratch sh;
+  __shared__ SharedState ss;
+  if (threadIdx.x == 0) read_prologue(S, G, D, L, blockDim.x * CPT, ss);
+  __syncthreads();
+  if (ss.status != kOk || ss.mode == 0) {
+    if (threadIdx.x == 0) {
+      out->status = ss.status;
+      out->has_score = 0;
+      out->n_pairs = 0;
+    }
+    return;
+  }
+  dp_build_rows(G, D, sh);
+  read_align<SUB, CPT>(S, G, D, sh, ss, seq, L, ss.lanes, D.aln_a, &ss.has_f, &ss.score_f,
+                       &ss.np_f);
+  if (threadIdx.x == 0) {
+    out->status = ss.status;
+    out->has_score = ss.has_f;
+    out->score = ss.score_f;
+    out->n_pairs = ss.np_f;
+    out->lanes = ss.lanes;
+  }
+}
+
+#ifdef SPOA_GB300_HOST_TU
+__global__ void k_graph_reset(GraphView G) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) g_reset(G);
+}
+#endif
+
+#ifdef SPOA_GB300_HOST_TU
+__global__ void k_add(GraphView G, const int32_t* pairs, uint32_t n_pairs, const uint8_t* seq,
+                      uint32_t L, const uint32_t* w, const uint8_t* qual, int32_t* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  WeightSrc ws{w, qual, L, 0u, 1u};
+  *status = g_add_alignment(G, pairs, n_pairs, seq, L, ws);
+}
+#endif
+
+// One read of a window: align (both strands when asked), choose, add.
+template <int SUB, int CPT>
+__device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScratch& sh,
+                            SharedState& ss, const uint8_t* seq, uint32_t L,
+                            const uint8_t* qual, bool strand, int32_t* out_score,
+                            int32_t* out_rev, const int32_t** out_pairs, uint32_t* out_np) {
+  if (threadIdx.x == 0) read_prologue(S, G, D, L, blockDim.x * CPT, ss);
+  __syncthreads();
+  if (ss.status != kOk) return;
+  const bool dp = ss.mode == 1;
+  if (threadIdx.x == 0) {
+    ss.has_f = ss.has_r = 0;
+    ss.score_f = ss.score_r = 0;
+    ss.np_f = ss.np_r = 0;
+  }
+  if (dp) {
+    dp_build_rows(G, D, sh);
+    read_align<SUB, CPT>(S, G, D, sh, ss, seq, L, ss.lanes, D.aln_a, &ss.has_f, &ss.score_f,
+                         &ss.np_f);
+  }
+  if (strand) {
+    for (uint32_t j = threadIdx.x; j < L; j += blockDim.x)
+      D.seq_rc[j] = complement_base(seq[L - 1 - j]);
+    __syncthreads();
+    if (dp && ss.status == kOk)
+      read_align<SUB, CPT>(S, G, D, sh, ss, D.seq_rc, L, ss.lanes, D.aln_b, &ss.has_r,
+                           &ss.score_r, &ss.np_r);
+  }
+  if (threadIdx.x == 0 && ss.status == kOk) {
+    // main.cpp:276-301: scores start at 0; keep forward if score >= score_rev
+    const int32_t sf = ss.has_f ? ss.score_f : 0;
+    const int32_t sr = ss.has_r ? ss.score_r : 0;
+    const bool rev = strand && !(sf >= sr);
+    const int32_t* pairs = rev ? D.aln_b : D.aln_a;
+    const uint32_t np = rev ? ss.np_r : ss.np_f;
+    WeightSrc ws{nullptr, qual, L, rev ? 1u : 0u, 1u};
+    int32_t st = g_add_alignment(G, pairs, np, rev ? D.seq_rc : seq, L, ws);
+    if (st != kOk) ss.status = st;
+    *out_score = rev ? sr : sf;
+    *out_rev = rev ? 1 : 0;
+    *out_pairs = pairs;
+    *out_np = np;
+  }
+  __syncthreads();
+}
+
+template <int SUB, int CPT>
+__global__ void __launch_bounds__(1024)
+    k_align_add(Scoring S, GraphView G, DpView D, const uint8_t* seq, uint32_t L,
+                const uint8_t* qual, int32_t strand, ReadOut* out) {
+  __shared__ BlockScratch sh;
+  __shared__ SharedState ss;
+  __shared__ const int32_t* s_pairs;
+  __shared__ int32_t s_score, s_rev;
+  __shared__ uint32_t s_np;
+  window_read<SUB, CPT>(S, G, D, sh, ss, seq, L, qual, strand != 0, &s_score, &s_rev, &s_pairs,
+                        &s_np);
+  if (threadIdx.x == 0) {
+    out->status = ss.status;
+    out->score = s_score;
+    out->reversed = s_rev;
+    out->n_pairs = s_np;
+  }
+}
+
+__device__ inline void write_consensus(GraphView& G, uint8_t* out, uint64_t cap, uint32_t* len) {
+  g_consensus(G);
+  const uint32_t n = G.hdr->n_consensus;
+  for (uint32_t k = 0; k < n && k < cap; ++k)
+    out[k] = (uint8_t)G.hdr->decoder[G.code[G.consensus[k]]];
+  *len = n;
+}
+
+#ifdef SPOA_GB300_HOST_TU
+__global__ void k_consensus(GraphView G, uint8_t* out, uint64_t cap, uint32_t* len) {
+  if (threadIdx.x == 0) write_consensus(G, out, cap, len);
+}
+#endif
+
+// MSA of the window into out[rows * cols]; every thread calls.
+__device__ inline int32_t window_msa(GraphView& G, bool include_consensus, uint8_t* out,
+                                     uint64_t cap, uint32_t* rows_out, uint32_t* cols_out,
+                                     uint32_t* s_dims) {
+  if (threadIdx.x == 0) {
+    s_dims[1] = g_msa_columns(G);
+    if (include_consensus) g_consensus(G);
+    s_dims[0] = G.hdr->n_seqs + (include_consensus ? 1 : 0);
+    *rows_out = s_dims[0];
+    *cols_out = s_dims[1];
+  }
+  __syncthreads();
+  const uint32_t rows = s_dims[0], cols = s_dims[1];
+  if ((uint64_t)rows * cols > cap) return kCapacity;
+  for (uint64_t k = threadIdx.x; k < (uint64_t)rows * cols; k += blockDim.x) out[k] = '-';
+  __syncthreads();
+  const uint32_t ns = G.hdr->n_seqs;
+  for (uint32_t s = threadIdx.x; s < ns; s += blockDim.x) {
+    uint8_t* row = out + (uint64_t)s * cols;
+    uint32_t it = G.seq_begin[s];
+    uint32_t guard = 0;
+    while (it != kNone && guard++ <= G.hdr->n_nodes) {
+      row[G.column[it]] = (uint8_t)G.hdr->decoder[G.code[it]];
+      it = g_successor(G, it, s);
+    }
+  }
+  if (include_consensus && threadIdx.x == 0) {
+    uint8_t* row = out + (uint64_t)ns * cols;
+    for (uint32_t k = 0; k < G.hdr->n_consensus; ++k) {
+      uint32_t it = G.consensus[k];
+      row[G.column[it]] = (uint8_t)G.hdr->decoder[G.code[it]];
+    }
+  }
+  __syncthreads();
+  return kOk;
+}
+
+#ifdef SPOA_GB300_HOST_TU
+__global__ void k_msa(GraphView G, int32_t include_consensus, uint8_t* out, uint64_t cap,
+                      uint32_t* dims, int32_t* status) {
+  __shared__ uint32_t s_dims[2];
+  int32_t st = window_msa(G, include_consensus != 0, out, cap, &dims[0], &dims[1], s_dims);
+  if (threadIdx.x == 0) *status = st;
+}
+#endif
+
+struct ExportPtrs {
+  uint8_t *chars, *codes;
+  uint32_t *in_off, *in_edges, *out_off, *out_edges, *al_off, *al_nodes;
+  uint32_t *e_tail, *e_head;
+  int64_t* e_weight;
+  uint32_t *lab_off, *labels, *rank, *seq_begin, *consensus;
+  int32_t *coder, *decoder;
+};
+
+#ifdef SPOA_GB300_HOST_TU
+__global__ void k_export(GraphView G, ExportPtrs x) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const GraphHeader* h = G.hdr;
+  const uint32_t nn = h->n_nodes, ne = h->n_edges, K = G.caps.aligned;
+  uint32_t io = 0, oo = 0, ao = 0;
+  for (uint32_t v = 0; v < nn; ++v) {
+    if (x.chars) x.chars[v] = (uint8_t)h->decoder[G.code[v]];
+    if (x.codes) x.codes[v] = G.code[v];
+    if (x.in_off) x.in_off[v] = io;
+    for (uint32_t e = G.in_first[v]; e != kNone; e = G.e_next_in[e]) {
+      if (x.in_edges) x.in_edges[io] = e;
+      ++io;
+    }
+    if (x.out_off) x.out_off[v] = oo;
+    for (uint32_t e = G.out_first[v]; e != kNone; e = G.e_next_out[e]) {
+      if (x.out_edges) x.out_edges[oo] = e;
+      ++oo;
+    }
+    if (x.al_off) x.al_off[v] = ao;
+    for (uint32_t k = 0; k < G.n_aligned[v]; ++k) {
+      if (x.al_nodes) x.al_nodes[ao] = G.aligned[(uint64_t)v * K + k];
+      ++ao;
+    }
+    if (x.rank) x.rank[v] = G.rank_to_node[v];
+  }
+  if (x.in_off) x.in_off[nn] = io;
+  if (x.out_off) x.out_off[nn] = oo;
+  if (x.al_off) x.al_off[nn] = ao;
+  uint32_t lo = 0;
+  for (uint32_t e = 0; e < ne; ++e) {
+    if (x.e_tail) x.e_tail[e] = G.e_tail[e];
+    if (x.e_head) x.e_head[e] = G.e_head[e];
+    if (x.e_weight) x.e_weight[e] = G.e_weight[e];
+    if (x.lab_off) x.lab_off[e] = lo;
+    for (uint32_t l = G.e_lab_first[e]; l != kNone; l = G.lab_next[l]) {
+      if (x.labels) x.labels[lo] = G.lab_seq[l];
+      ++lo;
+    }
+  }
+  if (x.lab_off) x.lab_off[ne] = lo;
+  for (uint32_t s = 0; s < h->n_seqs; ++s)
+    if (x.seq_begin) x.seq_begin[s] = G.seq_begin[s];
+  for (uint32_t k = 0; k < h->n_consensus; ++k)
+    if (x.consensus) x.consensus[k] = G.consensus[k];
+  for (int k = 0; k < 256; ++k) {
+    if (x.coder) x.coder[k] = h->coder[k];
+    if (x.decoder) x.decoder[k] = h->decoder[k];
+  }
+}
+#endif
+
+// ---------------------------------------------------------------------------
+// persistent batch kernel
+// ---------------------------------------------------------------------------
+struct BatchArgs {
+  Scoring base;
+  const int8_t* win_type;
+  const int8_t* win_strand;
+  uint32_t n_windows;
+  const uint32_t* win_read_off;
+  const uint8_t* seqs;
+  const uint64_t* seq_off;
+  const uint8_t* quals;
+  const uint32_t* work;     // window ids to process (queue order)
+  uint32_t n_work;
+  uint32_t* queue;          // atomic cursor into work
+  uint8_t* arena;
+  uint64_t arena_stride;
+  GraphCaps gcaps;
+  DpCaps dcaps;
+  int32_t* read_scores;
+  uint8_t* read_rev;
+  uint8_t* cons;
+  const uint64_t* cons_off;
+  uint32_t* cons_len;
+  int32_t* win_status;
+  int32_t* aln_out;         // optional
+  const uint64_t* aln_off;
+  uint32_t* aln_len;
+  uint8_t* msa_out;         // optional
+  const uint64_t* msa_off;
+  uint32_t* msa_rows;
+  uint32_t* msa_cols;
+  unsigned long long* cells;
+};
+
+template <int SUB, int CPT>
+__global__ void __launch_bounds__(512) k_batch(BatchArgs a) {
+  __shared__ BlockScratch sh;
+  __shared__ SharedState ss;
+  __shared__ uint32_t s_w, s_dims[2];
+  __shared__ const int32_t* s_pairs;
+  __shared__ int32_t s_score, s_rev;
+  __shared__ uint32_t s_np;
+  GraphView G;
+  DpView D;
+  uint8_t* base = a.arena + a.arena_stride * blockIdx.x;
+  const uint64_t gbytes = graph_layout(base, a.gcaps, &G);
+  dp_layout(base + gbytes, a.dcaps, &D);
+  Scoring S = a.base;
+  while (true) {
+    if (threadIdx.x == 0) {
+      uint32_t k = atomicAdd(a.queue, 1u);
+      s_w = k < a.n_work ? a.work[k] : kNone;
+    }
+    __syncthreads();
+    const uint32_t w = s_w;
+    if (w == kNone) break;
+    if (threadIdx.x == 0) g_reset(G);
+    S.type = a.win_type ? a.win_type[w] : a.base.type;
+    const bool strand = a.win_strand ? a.win_strand[w] != 0 : false;
+    __syncthreads();
+    int32_t status = kOk;
+    unsigned long long cells = 0;
+    for (uint32_t r = a.win_read_off[w]; r < a.win_read_off[w + 1]; ++r) {
+      const uint64_t off = a.seq_off[r];
+      const uint32_t L = (uint32_t)(a.seq_off[r + 1] - off);
+      cells += (unsigned long long)G.hdr->n_nodes * L * (strand ? 2u : 1u);
+      window_read<SUB, CPT>(S, G, D, sh, ss, a.seqs + off, L, a.quals ? a.quals + off : nullptr,
+                            strand, &s_score, &s_rev, &s_pairs, &s_np);
+      if (ss.status != kOk) {
+        status = ss.status;
+        break;
+      }
+      if (threadIdx.x == 0) {
+        a.read_scores[r] = s_score;
+        a.read_rev[r] = (uint8_t)s_rev;
+        if (a.aln_out) {
+          const uint64_t cap = a.aln_off[r + 1] - a.aln_off[r];
+          const uint32_t np = (uint32_t)min((uint64_t)s_np, cap);
+          for (uint32_t k = 0; k < 2 * np; ++k) a.aln_out[2 * a.aln_off[r] + k] = s_pairs[k];
+          a.aln_len[r] = s_np;
+        }
+      }
+      __syncthreads();
+    }
+    if (status == kOk) {
+      if (threadIdx.x == 0) {
+        const uint64_t cap = a.cons_off[w + 1] - a.cons_off[w];
+        write_consensus(G, a.cons + a.cons_off[w], cap, &a.cons_len[w]);
+        if (a.cons_len[w] > cap) s_dims[0] = kCapacity;
+        else s_dims[0] = kOk;
+      }
+      __syncthreads();
+      if (s_dims[0] != kOk) status = kCapacity;
+      __syncthreads();
+      if (status == kOk && a.msa_out) {
+        int32_t st = window_msa(G, false, a.msa_out + a.msa_off[w], a.msa_off[w + 1] - a.msa_off[w],
+                                &a.msa_rows[w], &a.msa_cols[w], s_dims);
+        if (st != kOk) status = st;
+      }
+    }
+    if (threadIdx.x == 0) {
+      a.win_status[w] = status;
+      if (a.cells) atomicAdd(a.cells, cells);
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace spoa_gb300
+
+
+namespace spoa_gb300 {
+
+// Launch wrappers; each gap model is explicitly instantiated in its own
+// translation unit (inst_*.cu).  cpt must be one of 8, 12, 16, 20, 24, 32.
+#define SPOA_CPT_SWITCH(cpt, LAUNCH) \
+  switch (cpt) {                     \
+    case 8: LAUNCH(8); break;        \
+    case 12: LAUNCH(12); break;      \
+    case 16: LAUNCH(16); break;      \
+    case 20: LAUNCH(20); break;      \
+    case 24: LAUNCH(24); break;      \
+    case 32: LAUNCH(32); break;      \
+    default: return kInvalidArgument; \
+  }
+
+template <int SUB>
+int32_t launch_align(int cpt, int nt, const Scoring& S, const GraphView& G, const DpView& D,
+                     const uint8_t* seq, uint32_t L, ReadOut* out) {
+#define L_(C) k_align<SUB, C><<<1, nt>>>(S, G, D, seq, L, out)
+  SPOA_CPT_SWITCH(cpt, L_)
+#undef L_
+  return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
+}
+
+template <int SUB>
+int32_t launch_align_add(int cpt, int nt, const Scoring& S, const GraphView& G,
+                         const DpView& D, const uint8_t* seq, uint32_t L, const uint8_t* qual,
+                         int32_t strand, ReadOut* out) {
+#define L_(C) k_align_add<SUB, C><<<1, nt>>>(S, G, D, seq, L, qual, strand, out)
+  SPOA_CPT_SWITCH(cpt, L_)
+#undef L_
+  return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
+}
+
+template <int SUB>
+int32_t launch_batch(int cpt, int nt, int grid, const BatchArgs& a, cudaStream_t s) {
+#define L_(C) k_batch<SUB, C><<<grid, nt, 0, s>>>(a)
+  SPOA_CPT_SWITCH(cpt, L_)
+#undef L_
+  return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
+}
+
+template <int SUB>
+int32_t occupancy_batch(int cpt, int nt, int* blocks) {
+  cudaError_t err = cudaSuccess;
+#define L_(C) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch<SUB, C>, nt, 0)
+  SPOA_CPT_SWITCH(cpt, L_)
+#undef L_
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    return kCuda;
+  }
+  return kOk;
+}
+
+#define SPOA_GB300_INSTANTIATE(SUB)                                                              \
+  template int32_t launch_align<SUB>(int, int, const Scoring&, const GraphView&, const DpView&, \
+                                     const uint8_t*, uint32_t, ReadOut*);                       \
+  template int32_t launch_align_add<SUB>(int, int, const Scoring&, const GraphView&,            \
+                                         const DpView&, const uint8_t*, uint32_t,               \
+                                         const uint8_t*, int32_t, ReadOut*);                    \
+  template int32_t launch_batch<SUB>(int, int, int, const BatchArgs&, cudaStream_t);            \
+  template int32_t occupancy_batch<SUB>(int, int, int*);
+
+}  // namespace spoa_gb300

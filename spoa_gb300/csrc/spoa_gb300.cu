@@ -1,0 +1,1018 @@
+// spoa_gb300.cu - host side and C ABI of the GB300 POA library.
+// The kernel templates are in poa_kernels.cuh.
+//
+// Kernels (one CTA owns one window; see poa_device.cuh / poa_dp.cuh):
+//   k_graph_reset       empty graph (Graph::Graph, Graph::Clear)
+//   k_align<SUB,CPT>    one read against a graph (AlignmentEngine::Align)
+//   k_add               Graph::AddAlignment + TopologicalSort
+//   k_align_add<..>     fused per-read body of spoa's CLI loop
+//   k_consensus         Graph::GenerateConsensus
+//   k_msa               Graph::GenerateMultipleSequenceAlignment
+//   k_export            flat copy for the host-side node/edge views
+//   k_batch<SUB,CPT>    persistent kernel: CTAs pull whole windows from a
+//                       device work queue and run every read of the window,
+//                       then the consensus (and optionally the MSA)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/spoa_gb300.h"
+#define SPOA_GB300_HOST_TU
+#include "poa_kernels.cuh"
+
+namespace spoa_gb300 {
+#define SPOA_EXTERN(SUB)                                                                         \
+  extern template int32_t launch_align<SUB>(int, int, const Scoring&, const GraphView&,         \
+                                            const DpView&, const uint8_t*, uint32_t, ReadOut*); \
+  extern template int32_t launch_align_add<SUB>(int, int, const Scoring&, const GraphView&,     \
+                                                const DpView&, const uint8_t*, uint32_t,        \
+                                                const uint8_t*, int32_t, ReadOut*);             \
+  extern template int32_t launch_batch<SUB>(int, int, int, const BatchArgs&, cudaStream_t);     \
+  extern template int32_t occupancy_batch<SUB>(int, int, int*);
+SPOA_EXTERN(kLinear)
+SPOA_EXTERN(kAffine)
+SPOA_EXTERN(kConvex)
+#undef SPOA_EXTERN
+}  // namespace spoa_gb300
+
+// ===========================================================================
+// host side
+// ===========================================================================
+using namespace spoa_gb300;
+
+namespace {
+
+constexpr int kCpts[] = {8, 12, 16, 20, 24, 32};
+
+#define CU(call)                                \
+  do {                                          \
+    cudaError_t err__ = (call);                 \
+    if (err__ != cudaSuccess) return kCuda;     \
+  } while (0)
+
+#define SPOA_BY_SUB(sub, fn, ...)                        \
+  ((sub) == kLinear   ? fn<kLinear>(__VA_ARGS__)          \
+   : (sub) == kAffine ? fn<kAffine>(__VA_ARGS__)          \
+   : (sub) == kConvex ? fn<kConvex>(__VA_ARGS__)          \
+                      : (int32_t)kInvalidArgument)
+
+// Latency tile: the smallest strip (most threads) that covers L.
+bool latency_tile(uint32_t L, int* cpt, int* nt) {
+  for (int c : kCpts) {
+    uint64_t t = ((uint64_t)(L + c - 1) / c + 31) / 32 * 32;
+    if (t == 0) t = 32;
+    if (t <= 1024) {
+      *cpt = c;
+      *nt = (int)t;
+      return true;
+    }
+  }
+  return false;
+}
+
+// Throughput tile: fewest padded columns, then fewest threads.
+bool throughput_tile(uint32_t L, int* cpt, int* nt) {
+  uint64_t best = ~0ull;
+  for (int c : kCpts) {
+    uint64_t t = ((uint64_t)(L + c - 1) / c + 31) / 32 * 32;
+    if (t == 0) t = 32;
+    if (t > 1024) continue;
+    uint64_t cost = t * (uint64_t)c;
+    if (cost < best || (cost == best && (int)t < *nt)) {
+      best = cost;
+      *cpt = c;
+      *nt = (int)t;
+    }
+  }
+  return best != ~0ull;
+}
+
+struct DeviceBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  ~DeviceBuf() { if (p) cudaFree(p); }
+  int32_t ensure(size_t bytes) {
+    if (bytes <= n) return kOk;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) {
+      cudaGetLastError();
+      return kNoMemory;
+    }
+    n = bytes;
+    return kOk;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct spoa_gb300_engine {
+  Scoring S;
+  DeviceBuf dp_arena;
+  DpView dv{};
+  DpCaps dcaps{};
+  DeviceBuf seq, qual, out;
+  ReadOut* h_out = nullptr;
+  int device = 0;
+  uint32_t pre_rows = 0, pre_ld = 0;
+};
+
+struct spoa_gb300_graph {
+  DeviceBuf arena;
+  GraphView v{};
+  GraphCaps caps{};
+  GraphHeader h{};  // host copy of the header, refreshed after each change
+  DeviceBuf seq, w, pairs, stat;
+  int device = 0;
+};
+
+namespace {
+
+int32_t graph_refresh(spoa_gb300_graph* g) {
+  CU(cudaMemcpy(&g->h, g->v.hdr, sizeof(GraphHeader), cudaMemcpyDeviceToHost));
+  return kOk;
+}
+
+// Grows the graph arena so that `len` more bases fit; contents are kept.
+int32_t graph_reserve(spoa_gb300_graph* g, uint32_t len) {
+  const GraphHeader& h = g->h;
+  GraphCaps need = g->caps;
+  auto grow = [](uint32_t cap, uint64_t want) {
+    uint64_t c = cap ? cap : 256;
+    while (c < want) c *= 2;
+    return (uint32_t)std::min<uint64_t>(c, 0xFFFFFFF0u);
+  };
+  need.nodes = grow(g->caps.nodes, (uint64_t)h.n_nodes + len + 1);
+  need.edges = grow(g->caps.edges, (uint64_t)h.n_edges + len + 2);
+  need.labels = grow(g->caps.labels, (uint64_t)h.n_labels + len + 2);
+  need.seqs = grow(g->caps.seqs, (uint64_t)h.n_seqs + 2);
+  if (g->arena.p && need.nodes == g->caps.nodes && need.edges == g->caps.edges &&
+      need.labels == g->caps.labels && need.seqs == g->caps.seqs)
+    return kOk;
+  GraphView nv;
+  uint64_t bytes = graph_layout(nullptr, need, &nv);
+  DeviceBuf fresh;
+  if (fresh.ensure(bytes)) return kNoMemory;
+  graph_layout(fresh.as<uint8_t>(), need, &nv);
+  if (g->arena.p) {
+    const GraphView& o = g->v;
+    const uint64_t N = h.n_nodes, E = h.n_edges, Lb = h.n_labels, Sq = h.n_seqs;
+    const uint32_t K = need.aligned;
+    CU(cudaMemcpy(nv.hdr, o.hdr, sizeof(GraphHeader), cudaMemcpyDeviceToDevice));
+#define CP(field, count, esz) \
+  if (count) CU(cudaMemcpy(nv.field, o.field, (count) * (esz), cudaMemcpyDeviceToDevice))
+    CP(code, N, 1);
+    CP(in_first, N, 4);
+    CP(in_last, N, 4);
+    CP(out_first, N, 4);
+    CP(out_last, N, 4);
+    CP(in_deg, N, 4);
+    CP(n_aligned, N, 1);
+    CP(aligned, N * K, 4);
+    CP(rank_to_node, N, 4);
+    CP(node_to_rank, N, 4);
+    CP(e_tail, E, 4);
+    CP(e_head, E, 4);
+    CP(e_next_in, E, 4);
+    CP(e_next_out, E, 4);
+    CP(e_lab_first, E, 4);
+    CP(e_lab_last, E, 4);
+    CP(e_weight, E, 8);
+    CP(lab_seq, Lb, 4);
+    CP(lab_next, Lb, 4);
+    CP(seq_begin, Sq, 4);
+    CP(consensus, N, 4);
+#undef CP
+  } else {
+    k_graph_reset<<<1, 32>>>(nv);
+    CU(cudaGetLastError());
+  }
+  std::swap(g->arena.p, fresh.p);
+  std::swap(g->arena.n, fresh.n);
+  g->v = nv;
+  g->caps = need;
+  return kOk;
+}
+
+int32_t engine_reserve(spoa_gb300_engine* en, uint32_t rows, uint32_t ld, uint32_t preds) {
+  DpCaps c = en->dcaps;
+  bool grow = !en->dp_arena.p || rows > c.rows || ld > c.ld || preds > c.preds;
+  if (!grow) return kOk;
+  c.rows = std::max(rows, c.rows);
+  c.ld = std::max(ld, c.ld);
+  c.preds = std::max(preds, c.preds);
+  c.sub = en->S.sub;
+  DpView v;
+  uint64_t bytes = dp_layout(nullptr, c, &v);
+  en->dp_arena.~DeviceBuf();
+  new (&en->dp_arena) DeviceBuf();
+  if (en->dp_arena.ensure(bytes)) {
+    en->dcaps = DpCaps{};
+    return kNoMemory;
+  }
+  dp_layout(en->dp_arena.as<uint8_t>(), c, &v);
+  en->dv = v;
+  en->dcaps = c;
+  return kOk;
+}
+
+
+
+int32_t prepare_read(spoa_gb300_engine* en, const spoa_gb300_graph* g, uint32_t L, int* cpt,
+                     int* nt) {
+  if (!latency_tile(L, cpt, nt)) return kTooLarge;
+  int32_t st = engine_reserve(en, g->h.n_nodes + 1, (uint32_t)(*cpt) * (*nt),
+                              g->h.n_edges + g->h.n_nodes + 2);
+  if (st) return st;
+  if (en->seq.ensure(std::max<size_t>(L, 1))) return kNoMemory;
+  if (en->out.ensure(sizeof(ReadOut))) return kNoMemory;
+  return kOk;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* spoa_gb300_status_string(int32_t s) {
+  switch (s) {
+    case kOk: return "ok";
+    case kInvalidArgument: return "invalid argument";
+    case kTooLarge: return "too large sequence!";
+    case kOverflow: return "possible overflow!";
+    case kNoMemory: return "insufficient memory!";
+    case kInvalidAlignment: return "invalid alignment";
+    case kMissingSequence: return "missing sequence in alignment";
+    case kUnequalWeights: return "sequence and weights are of unequal size!";
+    case kCapacity: return "device arena capacity exceeded";
+    case kTraceback: return "traceback did not terminate";
+    case kCuda: return "CUDA error";
+    default: return "unknown status";
+  }
+}
+
+int32_t spoa_gb300_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int32_t spoa_gb300_engine_create(int32_t type, int8_t m, int8_t n, int8_t g, int8_t e,
+                                 int8_t q, int8_t c, spoa_gb300_engine** out) {
+  if (!out) return kInvalidArgument;
+  *out = nullptr;
+  if (type != kSW && type != kNW && type != kOV) return kInvalidArgument;
+  if (g > 0 || q > 0) return kInvalidArgument;
+  if (e > 0 || c > 0) return kInvalidArgument;
+  int32_t sub = g >= e ? kLinear : ((g <= q || e >= c) ? kAffine : kConvex);
+  if (sub == kLinear) {
+    e = g;
+  } else if (sub == kAffine) {
+    q = g;
+    c = e;
+  }
+  if (spoa_gb300_device_count() <= 0) return kCuda;
+  auto* en = new (std::nothrow) spoa_gb300_engine();
+  if (!en) return kNoMemory;
+  en->S = Scoring{type, sub, m, n, g, e, q, c};
+  cudaGetDevice(&en->device);
+  if (cudaMallocHost(&en->h_out, sizeof(ReadOut)) != cudaSuccess) {
+    cudaGetLastError();
+    delete en;
+    return kNoMemory;
+  }
+  *out = en;
+  return kOk;
+}
+
+void spoa_gb300_engine_destroy(spoa_gb300_engine* en) {
+  if (!en) return;
+  if (en->h_out) cudaFreeHost(en->h_out);
+  delete en;
+}
+
+int32_t spoa_gb300_engine_params(const spoa_gb300_engine* en, int32_t* type, int32_t* subtype,
+                                 int8_t* p) {
+  if (!en) return kInvalidArgument;
+  if (type) *type = en->S.type;
+  if (subtype) *subtype = en->S.sub;
+  if (p) {
+    p[0] = (int8_t)en->S.m; p[1] = (int8_t)en->S.n; p[2] = (int8_t)en->S.g;
+    p[3] = (int8_t)en->S.e; p[4] = (int8_t)en->S.q; p[5] = (int8_t)en->S.c;
+  }
+  return kOk;
+}
+
+int32_t spoa_gb300_engine_prealloc(spoa_gb300_engine* en, uint32_t max_len, uint8_t alphabet) {
+  if (!en) return kInvalidArgument;
+  if (max_len > (uint32_t)INT32_MAX) return kTooLarge;
+  // same early return as the reference: nothing to size when even int32
+  // could overflow (implementation.hpp:392-397)
+  int64_t wc = worst_case(en->S, (int64_t)max_len + 8, (int64_t)max_len * alphabet);
+  if (wc < (int64_t)INT32_MIN + 1024) return kOk;
+  int cpt, nt;
+  if (!latency_tile(std::max<uint32_t>(max_len, 1), &cpt, &nt)) return kNoMemory;
+  uint64_t rows = (uint64_t)max_len * alphabet + 1;
+  if (rows > 0xFFFFFFF0ull) return kNoMemory;
+  DpCaps c{(uint32_t)rows, (uint32_t)(cpt * nt), (uint32_t)std::min<uint64_t>(3 * rows, 0xFFFFFFF0ull),
+           en->S.sub};
+  DpView v;
+  uint64_t bytes = dp_layout(nullptr, c, &v);
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return kCuda;
+  if (bytes > free_b) return kNoMemory;
+  return engine_reserve(en, c.rows, c.ld, c.preds);
+}
+
+int32_t spoa_gb300_graph_create(spoa_gb300_graph** out) {
+  if (!out) return kInvalidArgument;
+  *out = nullptr;
+  if (spoa_gb300_device_count() <= 0) return kCuda;
+  auto* g = new (std::nothrow) spoa_gb300_graph();
+  if (!g) return kNoMemory;
+  cudaGetDevice(&g->device);
+  g->caps = GraphCaps{0, 0, 0, 0, 31};
+  std::memset(&g->h, 0, sizeof(g->h));
+  int32_t st = graph_reserve(g, 1024);
+  if (st == kOk) st = g->stat.ensure(16);
+  if (st == kOk) st = graph_refresh(g);
+  if (st != kOk) {
+    delete g;
+    return st;
+  }
+  *out = g;
+  return kOk;
+}
+
+void spoa_gb300_graph_destroy(spoa_gb300_graph* g) { delete g; }
+
+int32_t spoa_gb300_graph_clear(spoa_gb300_graph* g) {
+  if (!g) return kInvalidArgument;
+  k_graph_reset<<<1, 32>>>(g->v);
+  CU(cudaGetLastError());
+  return graph_refresh(g);
+}
+
+int32_t spoa_gb300_engine_align(spoa_gb300_engine* en, const char* seq, uint32_t L,
+                                const spoa_gb300_graph* g, int32_t* score,
+                                int32_t* score_written, int32_t* pairs, uint32_t pairs_cap,
+                                uint32_t* n_pairs) {
+  if (!en || !g || !n_pairs) return kInvalidArgument;
+  *n_pairs = 0;
+  if (score_written) *score_written = 0;
+  if (L > (uint32_t)INT32_MAX) return kTooLarge;
+  if (g->h.n_nodes == 0 || L == 0) return kOk;
+  if (!lanes_for(en->S, L, g->h.n_nodes)) return kOverflow;
+  int cpt, nt;
+  int32_t st = prepare_read(en, g, L, &cpt, &nt);
+  if (st) return st;
+  CU(cudaMemcpy(en->seq.p, seq, L, cudaMemcpyHostToDevice));
+  st = SPOA_BY_SUB(en->S.sub, launch_align, cpt, nt, en->S, g->v, en->dv, en->seq.as<uint8_t>(), L,
+                   en->out.as<ReadOut>());
+  if (st) return st;
+  CU(cudaMemcpy(en->h_out, en->out.p, sizeof(ReadOut), cudaMemcpyDeviceToHost));
+  const ReadOut& r = *en->h_out;
+  if (r.status != kOk) return r.status;
+  if (r.has_score) {
+    if (score) *score = r.score;
+    if (score_written) *score_written = 1;
+  }
+  if (r.n_pairs > pairs_cap) return kCapacity;
+  if (r.n_pairs)
+    CU(cudaMemcpy(pairs, en->dv.aln_a, (size_t)r.n_pairs * 2 * sizeof(int32_t),
+                  cudaMemcpyDeviceToHost));
+  *n_pairs = r.n_pairs;
+  return kOk;
+}
+
+static int32_t add_common(spoa_gb300_graph* g, const int32_t* pairs, uint32_t n_pairs,
+                          const char* seq, uint32_t L, const uint32_t* weights,
+                          const char* quality) {
+  if (L == 0) return kOk;
+  int32_t st = graph_reserve(g, L);
+  if (st) return st;
+  if (g->seq.ensure(L) || g->pairs.ensure((size_t)std::max<uint32_t>(n_pairs, 1) * 8))
+    return kNoMemory;
+  CU(cudaMemcpy(g->seq.p, seq, L, cudaMemcpyHostToDevice));
+  if (n_pairs) CU(cudaMemcpy(g->pairs.p, pairs, (size_t)n_pairs * 8, cudaMemcpyHostToDevice));
+  const uint32_t* dw = nullptr;
+  const uint8_t* dq = nullptr;
+  if (weights || quality) {
+    if (g->w.ensure((size_t)L * 4)) return kNoMemory;
+    if (weights) {
+      CU(cudaMemcpy(g->w.p, weights, (size_t)L * 4, cudaMemcpyHostToDevice));
+      dw = g->w.as<uint32_t>();
+    } else {
+      CU(cudaMemcpy(g->w.p, quality, L, cudaMemcpyHostToDevice));
+      dq = g->w.as<uint8_t>();
+    }
+  }
+  k_add<<<1, 32>>>(g->v, g->pairs.as<int32_t>(), n_pairs, g->seq.as<uint8_t>(), L, dw, dq,
+                   g->stat.as<int32_t>());
+  CU(cudaGetLastError());
+  int32_t dst = 0;
+  CU(cudaMemcpy(&dst, g->stat.p, 4, cudaMemcpyDeviceToHost));
+  st = graph_refresh(g);
+  return dst != kOk ? dst : st;
+}
+
+int32_t spoa_gb300_graph_add_alignment(spoa_gb300_graph* g, const int32_t* pairs,
+                                       uint32_t n_pairs, const char* seq, uint32_t L,
+                                       const uint32_t* weights, uint32_t n_weights) {
+  if (!g) return kInvalidArgument;
+  if (L == 0) return kOk;
+  if (weights && n_weights != L) return kUnequalWeights;
+  return add_common(g, pairs, n_pairs, seq, L, weights, nullptr);
+}
+
+int32_t spoa_gb300_graph_add_alignment_quality(spoa_gb300_graph* g, const int32_t* pairs,
+                                               uint32_t n_pairs, const char* seq, uint32_t L,
+                                               const char* quality, uint32_t qlen) {
+  if (!g) return kInvalidArgument;
+  if (L == 0) return kOk;
+  if (qlen != L) return kUnequalWeights;
+  return add_common(g, pairs, n_pairs, seq, L, nullptr, quality);
+}
+
+int32_t spoa_gb300_align_add(spoa_gb300_engine* en, spoa_gb300_graph* g, const char* seq,
+                             uint32_t L, const char* quality, int32_t strand, int32_t* score,
+                             int32_t* reversed) {
+  if (!en || !g) return kInvalidArgument;
+  if (L > (uint32_t)INT32_MAX) return kTooLarge;
+  if (score) *score = 0;
+  if (reversed) *reversed = 0;
+  if (L == 0) return kOk;
+  if (g->h.n_nodes && !lanes_for(en->S, L, g->h.n_nodes)) return kOverflow;
+  int32_t st = graph_reserve(g, L);
+  if (st) return st;
+  int cpt, nt;
+  st = prepare_read(en, g, L, &cpt, &nt);
+  if (st) return st;
+  CU(cudaMemcpy(en->seq.p, seq, L, cudaMemcpyHostToDevice));
+  const uint8_t* dq = nullptr;
+  if (quality) {
+    if (en->qual.ensure(L)) return kNoMemory;
+    CU(cudaMemcpy(en->qual.p, quality, L, cudaMemcpyHostToDevice));
+    dq = en->qual.as<uint8_t>();
+  }
+  st = SPOA_BY_SUB(en->S.sub, launch_align_add, cpt, nt, en->S, g->v, en->dv, en->seq.as<uint8_t>(),
+                   L, dq, strand, en->out.as<ReadOut>());
+  if (st) return st;
+  CU(cudaMemcpy(en->h_out, en->out.p, sizeof(ReadOut), cudaMemcpyDeviceToHost));
+  st = graph_refresh(g);
+  if (en->h_out->status != kOk) return en->h_out->status;
+  if (score) *score = en->h_out->score;
+  if (reversed) *reversed = en->h_out->reversed;
+  return st;
+}
+
+int32_t spoa_gb300_graph_consensus(spoa_gb300_graph* g, char* out, uint32_t cap,
+                                   uint32_t* len) {
+  if (!g || !len) return kInvalidArgument;
+  DeviceBuf buf, n;
+  if (buf.ensure(std::max<uint32_t>(g->h.n_nodes, 1)) || n.ensure(4)) return kNoMemory;
+  k_consensus<<<1, 32>>>(g->v, buf.as<uint8_t>(), g->h.n_nodes, n.as<uint32_t>());
+  CU(cudaGetLastError());
+  CU(cudaMemcpy(len, n.p, 4, cudaMemcpyDeviceToHost));
+  if (*len && out) CU(cudaMemcpy(out, buf.p, std::min(*len, cap), cudaMemcpyDeviceToHost));
+  return graph_refresh(g);
+}
+
+int32_t spoa_gb300_graph_msa(spoa_gb300_graph* g, int32_t include_consensus, char* out,
+                             uint64_t cap, uint32_t* rows, uint32_t* cols) {
+  if (!g || !rows || !cols) return kInvalidArgument;
+  const uint64_t need = (uint64_t)(g->h.n_seqs + 1) * std::max<uint32_t>(g->h.n_nodes, 1);
+  DeviceBuf buf, dims, st;
+  if (buf.ensure(need) || dims.ensure(8) || st.ensure(4)) return kNoMemory;
+  k_msa<<<1, 256>>>(g->v, include_consensus, buf.as<uint8_t>(), need, dims.as<uint32_t>(),
+                    st.as<int32_t>());
+  CU(cudaGetLastError());
+  uint32_t d[2];
+  int32_t s = 0;
+  CU(cudaMemcpy(d, dims.p, 8, cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(&s, st.p, 4, cudaMemcpyDeviceToHost));
+  if (s != kOk) return s;
+  *rows = d[0];
+  *cols = d[1];
+  const uint64_t bytes = (uint64_t)d[0] * d[1];
+  if (bytes > cap) return kCapacity;
+  if (bytes && out) CU(cudaMemcpy(out, buf.p, bytes, cudaMemcpyDeviceToHost));
+  return graph_refresh(g);
+}
+
+int32_t spoa_gb300_graph_counts(const spoa_gb300_graph* g, uint32_t* nodes, uint32_t* edges,
+                                uint32_t* seqs, uint32_t* consensus, uint32_t* labels,
+                                uint32_t* num_codes) {
+  if (!g) return kInvalidArgument;
+  if (nodes) *nodes = g->h.n_nodes;
+  if (edges) *edges = g->h.n_edges;
+  if (seqs) *seqs = g->h.n_seqs;
+  if (consensus) *consensus = g->h.n_consensus;
+  if (labels) *labels = g->h.n_labels;
+  if (num_codes) *num_codes = g->h.num_codes;
+  return kOk;
+}
+
+int32_t spoa_gb300_graph_export(const spoa_gb300_graph* g, uint8_t* chars, uint8_t* codes,
+                                uint32_t* in_off, uint32_t* in_edges, uint32_t* out_off,
+                                uint32_t* out_edges, uint32_t* al_off, uint32_t* al_nodes,
+                                uint32_t* e_tail, uint32_t* e_head, int64_t* e_weight,
+                                uint32_t* lab_off, uint32_t* labels, uint32_t* rank,
+                                uint32_t* seq_begin, uint32_t* consensus, int32_t* coder,
+                                int32_t* decoder) {
+  if (!g) return kInvalidArgument;
+  const GraphHeader& h = g->h;
+  const uint64_t N = h.n_nodes, E = h.n_edges, Lb = h.n_labels, S = h.n_seqs,
+                 C = h.n_consensus, A = N * g->caps.aligned;
+  struct Item { void* host; uint64_t bytes; };
+  Item items[18] = {{chars, N}, {codes, N}, {in_off, 4 * (N + 1)}, {in_edges, 4 * E},
+                    {out_off, 4 * (N + 1)}, {out_edges, 4 * E}, {al_off, 4 * (N + 1)},
+                    {al_nodes, 4 * A}, {e_tail, 4 * E}, {e_head, 4 * E}, {e_weight, 8 * E},
+                    {lab_off, 4 * (E + 1)}, {labels, 4 * Lb}, {rank, 4 * N},
+                    {seq_begin, 4 * S}, {consensus, 4 * C}, {coder, 1024}, {decoder, 1024}};
+  uint64_t total = 0, offs[18];
+  for (int k = 0; k < 18; ++k) {
+    offs[k] = total;
+    total = align_up(total + std::max<uint64_t>(items[k].bytes, 8), 256);
+  }
+  DeviceBuf buf;
+  if (buf.ensure(total)) return kNoMemory;
+  uint8_t* b = buf.as<uint8_t>();
+  ExportPtrs x;
+  void** slots[18] = {(void**)&x.chars, (void**)&x.codes, (void**)&x.in_off, (void**)&x.in_edges,
+                      (void**)&x.out_off, (void**)&x.out_edges, (void**)&x.al_off,
+                      (void**)&x.al_nodes, (void**)&x.e_tail, (void**)&x.e_head,
+                      (void**)&x.e_weight, (void**)&x.lab_off, (void**)&x.labels, (void**)&x.rank,
+                      (void**)&x.seq_begin, (void**)&x.consensus, (void**)&x.coder,
+                      (void**)&x.decoder};
+  for (int k = 0; k < 18; ++k) *slots[k] = items[k].host ? b + offs[k] : nullptr;
+  k_export<<<1, 32>>>(g->v, x);
+  CU(cudaGetLastError());
+  for (int k = 0; k < 18; ++k)
+    if (items[k].host && items[k].bytes)
+      CU(cudaMemcpy(items[k].host, b + offs[k], items[k].bytes, cudaMemcpyDeviceToHost));
+  return kOk;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batched windows
+// ---------------------------------------------------------------------------
+namespace {
+
+
+
+struct Pass {
+  std::vector<uint32_t> windows;  // window ids in queue order
+  GraphCaps gcaps{};
+  DpCaps dcaps{};
+  int cpt = 0, nt = 0, ctas = 0;
+  uint64_t stride = 0;
+  std::vector<uint64_t> cons_off;  // per window of the batch (global index)
+};
+
+template <typename T>
+int32_t upload(DeviceBuf& d, const T* h, size_t count, cudaStream_t s) {
+  if (d.ensure(std::max<size_t>(count * sizeof(T), 8))) return kNoMemory;
+  if (count && h) CU(cudaMemcpyAsync(d.p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  return kOk;
+}
+
+}  // namespace
+
+struct spoa_gb300_batch {
+  spoa_gb300_batch_desc desc{};
+  Scoring base{};
+  uint32_t n_windows = 0, n_reads = 0;
+  std::vector<uint32_t> wro;
+  std::vector<uint64_t> seq_off;
+  std::vector<uint32_t> lmax, nreads;
+  std::vector<uint64_t> sumlen;
+  DeviceBuf d_seqs, d_seq_off, d_quals, d_wro, d_wtype, d_wstrand;
+  DeviceBuf d_work, d_queue, d_scores, d_rev, d_cons, d_cons_off, d_cons_len, d_status;
+  DeviceBuf d_aln, d_aln_off, d_aln_len, d_msa, d_msa_off, d_msa_rows, d_msa_cols, d_cells;
+  DeviceBuf arena;
+  std::vector<uint64_t> aln_off, msa_off;
+  std::vector<uint64_t> cons_off;  // first-pass regions
+  // host results
+  std::vector<int32_t> h_scores, h_status, h_aln;
+  std::vector<uint8_t> h_rev;
+  std::vector<char> h_cons, h_msa;
+  std::vector<uint64_t> h_cons_off, h_aln_off;
+  std::vector<uint32_t> h_msa_rows, h_msa_cols, h_aln_len;
+  Pass first;
+  std::vector<std::string> retry_cons;  // consensus of windows rerun with exact bounds
+  float kernel_ms = 0;
+  int launches = 0;
+  uint64_t cells = 0;
+  int sm_count = 0;
+};
+
+namespace {
+
+int32_t plan_pass(spoa_gb300_batch* b, Pass* p, bool retry) {
+  const spoa_gb300_batch_desc& d = b->desc;
+  uint32_t L = 1, maxreads = 1;
+  uint64_t maxsum = 1;
+  for (uint32_t w : p->windows) {
+    L = std::max(L, b->lmax[w]);
+    maxsum = std::max(maxsum, b->sumlen[w]);
+    maxreads = std::max(maxreads, b->nreads[w]);
+  }
+  int cpt = d.columns_per_thread, nt = d.threads_per_window;
+  if (cpt <= 0 || nt <= 0) {
+    if (!throughput_tile(L, &cpt, &nt)) return kTooLarge;
+  } else if ((uint64_t)cpt * nt < L) {
+    return kTooLarge;
+  }
+  uint64_t nodes = d.max_nodes ? d.max_nodes : std::max<uint64_t>(4096, 6ull * L + 64);
+  if (retry) nodes = maxsum + 1;
+  nodes = std::min<uint64_t>(nodes, maxsum + 1);
+  GraphCaps gc;
+  gc.nodes = (uint32_t)nodes;
+  gc.edges = (uint32_t)std::min<uint64_t>(maxsum + 2, 4 * nodes + 64);
+  gc.labels = (uint32_t)(maxsum + 2);
+  gc.seqs = maxreads + 1;
+  gc.aligned = retry ? 63 : 15;
+  DpCaps dc{(uint32_t)nodes + 1, (uint32_t)(cpt * nt), gc.edges + (uint32_t)nodes + 2,
+            b->base.sub};
+  GraphView gv;
+  DpView dv;
+  const uint64_t stride = align_up(graph_layout(nullptr, gc, &gv), 256) +
+                          align_up(dp_layout(nullptr, dc, &dv), 256);
+  int blocks = 1;
+  if (SPOA_BY_SUB(b->base.sub, occupancy_batch, cpt, nt, &blocks)) return kCuda;
+  blocks = std::max(blocks, 1);
+  size_t free_b = 0, total_b = 0;
+  CU(cudaMemGetInfo(&free_b, &total_b));
+  uint64_t budget = d.memory_budget ? d.memory_budget : (uint64_t)(free_b * 0.6);
+  uint64_t by_mem = std::max<uint64_t>(1, budget / stride);
+  uint64_t ctas = d.ctas > 0 ? (uint64_t)d.ctas : (uint64_t)b->sm_count * blocks;
+  ctas = std::min<uint64_t>(ctas, by_mem);
+  ctas = std::min<uint64_t>(ctas, p->windows.size());
+  p->gcaps = gc;
+  p->dcaps = dc;
+  p->cpt = cpt;
+  p->nt = nt;
+  p->ctas = (int)std::max<uint64_t>(ctas, 1);
+  p->stride = stride;
+  return kOk;
+}
+
+BatchArgs make_args(spoa_gb300_batch* b, const Pass& p, uint8_t* cons, const uint64_t* cons_off) {
+  BatchArgs a{};
+  a.base = b->base;
+  a.win_type = b->desc.window_type ? b->d_wtype.as<int8_t>() : nullptr;
+  a.win_strand = b->desc.window_strand ? b->d_wstrand.as<int8_t>() : nullptr;
+  a.n_windows = b->n_windows;
+  a.win_read_off = b->d_wro.as<uint32_t>();
+  a.seqs = b->d_seqs.as<uint8_t>();
+  a.seq_off = b->d_seq_off.as<uint64_t>();
+  a.quals = b->desc.quals ? b->d_quals.as<uint8_t>() : nullptr;
+  a.work = b->d_work.as<uint32_t>();
+  a.n_work = (uint32_t)p.windows.size();
+  a.queue = b->d_queue.as<uint32_t>();
+  a.arena = b->arena.as<uint8_t>();
+  a.arena_stride = p.stride;
+  a.gcaps = p.gcaps;
+  a.dcaps = p.dcaps;
+  a.read_scores = b->d_scores.as<int32_t>();
+  a.read_rev = b->d_rev.as<uint8_t>();
+  a.cons = cons;
+  a.cons_off = cons_off;
+  a.cons_len = b->d_cons_len.as<uint32_t>();
+  a.win_status = b->d_status.as<int32_t>();
+  if (b->desc.want_alignments) {
+    a.aln_out = b->d_aln.as<int32_t>();
+    a.aln_off = b->d_aln_off.as<uint64_t>();
+    a.aln_len = b->d_aln_len.as<uint32_t>();
+  }
+  if (b->desc.want_msa) {
+    a.msa_out = b->d_msa.as<uint8_t>();
+    a.msa_off = b->d_msa_off.as<uint64_t>();
+    a.msa_rows = b->d_msa_rows.as<uint32_t>();
+    a.msa_cols = b->d_msa_cols.as<uint32_t>();
+  }
+  a.cells = b->d_cells.as<unsigned long long>();
+  return a;
+}
+
+int32_t run_pass(spoa_gb300_batch* b, const Pass& p, cudaStream_t s, bool plain) {
+  if (p.windows.empty()) return kOk;
+  if (b->arena.ensure(p.stride * (plain ? 1 : p.ctas))) return kNoMemory;
+  CU(cudaMemcpyAsync(b->d_work.p, p.windows.data(), p.windows.size() * 4,
+                     cudaMemcpyHostToDevice, s));
+  CU(cudaMemsetAsync(b->d_queue.p, 0, 4 * (p.windows.size() + 1), s));
+  BatchArgs a = make_args(b, p, b->d_cons.as<uint8_t>(), b->d_cons_off.as<uint64_t>());
+  if (!plain) {
+    ++b->launches;
+    return SPOA_BY_SUB(b->base.sub, launch_batch, p.cpt, p.nt, p.ctas, a, s);
+  }
+  for (size_t k = 0; k < p.windows.size(); ++k) {
+    BatchArgs one = a;
+    one.work = a.work + k;
+    one.n_work = 1;
+    one.queue = a.queue + k;
+    ++b->launches;
+    int32_t st = SPOA_BY_SUB(b->base.sub, launch_batch, p.cpt, p.nt, 1, one, s);
+    if (st) return st;
+  }
+  return kOk;
+}
+
+int32_t launch_all(spoa_gb300_batch* b, void* stream, bool plain) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  b->launches = 0;
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  CU(cudaMemsetAsync(b->d_cells.p, 0, 8, s));
+  CU(cudaEventRecord(e0, s));
+  int32_t st = run_pass(b, b->first, s, plain);
+  CU(cudaEventRecord(e1, s));
+  if (st) return st;
+  // windows that outgrew the first-pass arena run again with exact bounds
+  std::vector<int32_t> status(b->n_windows);
+  CU(cudaMemcpyAsync(status.data(), b->d_status.p, 4ull * b->n_windows, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  float ms = 0;
+  CU(cudaEventElapsedTime(&ms, e0, e1));
+  b->kernel_ms = ms;
+  Pass retry;
+  for (uint32_t w = 0; w < b->n_windows; ++w)
+    if (status[w] == kCapacity) retry.windows.push_back(w);
+  if (!retry.windows.empty()) {
+    st = plan_pass(b, &retry, true);
+    if (st) return st;
+    // consensus regions sized by the exact bound, in a second buffer
+    std::vector<uint64_t> off(b->n_windows + 1, 0);
+    for (uint32_t w = 0; w < b->n_windows; ++w) {
+      uint64_t cap = 0;
+      for (uint32_t r : retry.windows) if (r == w) cap = b->sumlen[w] + 1;
+      off[w + 1] = off[w] + cap;
+    }
+    DeviceBuf cons2, off2;
+    if (cons2.ensure(off[b->n_windows] + 8)) return kNoMemory;
+    if (upload(off2, off.data(), off.size(), s)) return kNoMemory;
+    if (b->arena.ensure(retry.stride * retry.ctas)) return kNoMemory;
+    CU(cudaMemcpyAsync(b->d_work.p, retry.windows.data(), retry.windows.size() * 4,
+                       cudaMemcpyHostToDevice, s));
+    CU(cudaMemsetAsync(b->d_queue.p, 0, 4, s));
+    BatchArgs a = make_args(b, retry, cons2.as<uint8_t>(), off2.as<uint64_t>());
+    CU(cudaEventRecord(e0, s));
+    ++b->launches;
+    st = SPOA_BY_SUB(b->base.sub, launch_batch, retry.cpt, retry.nt, retry.ctas, a, s);
+    CU(cudaEventRecord(e1, s));
+    if (st) return st;
+    // move the retried consensus into the first-pass regions when they fit
+    std::vector<uint32_t> lens(b->n_windows);
+    CU(cudaMemcpyAsync(lens.data(), b->d_cons_len.p, 4ull * b->n_windows, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    CU(cudaEventElapsedTime(&ms, e0, e1));
+    b->kernel_ms += ms;
+    std::vector<char> tmp(off[b->n_windows] + 8);
+    CU(cudaMemcpy(tmp.data(), cons2.p, off[b->n_windows], cudaMemcpyDeviceToHost));
+    b->h_cons_off.clear();
+    b->retry_cons.assign(b->n_windows, std::string());
+    for (uint32_t w : retry.windows)
+      b->retry_cons[w].assign(tmp.data() + off[w], std::min<uint64_t>(lens[w], off[w + 1] - off[w]));
+  } else {
+    b->retry_cons.clear();
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* d, spoa_gb300_batch** out) {
+  if (!d || !out || !d->window_read_off || !d->seq_off || (!d->seqs && d->n_windows))
+    return kInvalidArgument;
+  *out = nullptr;
+  if (d->type != kSW && d->type != kNW && d->type != kOV) return kInvalidArgument;
+  spoa_gb300_engine* en = nullptr;
+  int32_t st = spoa_gb300_engine_create(d->type, d->m, d->n, d->g, d->e, d->q, d->c, &en);
+  if (st) return st;
+  Scoring base = en->S;
+  spoa_gb300_engine_destroy(en);
+  auto* b = new (std::nothrow) spoa_gb300_batch();
+  if (!b) return kNoMemory;
+  b->desc = *d;
+  b->base = base;
+  b->n_windows = d->n_windows;
+  b->wro.assign(d->window_read_off, d->window_read_off + d->n_windows + 1);
+  b->n_reads = b->wro[d->n_windows] - b->wro[0];
+  if (b->wro[0] != 0) {
+    delete b;
+    return kInvalidArgument;
+  }
+  b->seq_off.assign(d->seq_off, d->seq_off + b->n_reads + 1);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  b->lmax.assign(b->n_windows, 1);
+  b->sumlen.assign(b->n_windows, 0);
+  b->nreads.assign(b->n_windows, 0);
+  for (uint32_t w = 0; w < b->n_windows; ++w) {
+    if (d->window_type) {
+      int8_t t = d->window_type[w];
+      if (t != kSW && t != kNW && t != kOV) {
+        delete b;
+        return kInvalidArgument;
+      }
+    }
+    for (uint32_t r = b->wro[w]; r < b->wro[w + 1]; ++r) {
+      uint64_t L = b->seq_off[r + 1] - b->seq_off[r];
+      if (L > (uint64_t)INT32_MAX) {
+        delete b;
+        return kTooLarge;
+      }
+      b->lmax[w] = std::max<uint32_t>(b->lmax[w], (uint32_t)L);
+      b->sumlen[w] += L;
+    }
+    b->nreads[w] = b->wro[w + 1] - b->wro[w];
+  }
+  // queue order: longest estimated work first (largest sum of lengths x
+  // longest read), so the persistent CTAs drain evenly
+  b->first.windows.resize(b->n_windows);
+  for (uint32_t w = 0; w < b->n_windows; ++w) b->first.windows[w] = w;
+  std::stable_sort(b->first.windows.begin(), b->first.windows.end(), [&](uint32_t x, uint32_t y) {
+    return (double)b->sumlen[x] * b->lmax[x] > (double)b->sumlen[y] * b->lmax[y];
+  });
+  if (b->n_windows) {
+    st = plan_pass(b, &b->first, false);
+    if (st) {
+      delete b;
+      return st;
+    }
+  }
+  // first-pass consensus regions
+  b->cons_off.assign(b->n_windows + 1, 0);
+  for (uint32_t w = 0; w < b->n_windows; ++w)
+    b->cons_off[w + 1] = b->cons_off[w] +
+                         std::min<uint64_t>(b->sumlen[w] + 1, 2ull * b->lmax[w] + 64);
+  cudaStream_t s = 0;
+  const uint64_t nbytes = b->seq_off[b->n_reads];
+  st = upload(b->d_seqs, reinterpret_cast<const uint8_t*>(d->seqs), nbytes, s);
+  if (!st) st = upload(b->d_seq_off, b->seq_off.data(), b->seq_off.size(), s);
+  if (!st && d->quals) st = upload(b->d_quals, reinterpret_cast<const uint8_t*>(d->quals), nbytes, s);
+  if (!st) st = upload(b->d_wro, b->wro.data(), b->wro.size(), s);
+  if (!st && d->window_type) st = upload(b->d_wtype, d->window_type, b->n_windows, s);
+  if (!st && d->window_strand) st = upload(b->d_wstrand, d->window_strand, b->n_windows, s);
+  if (!st) st = upload(b->d_cons_off, b->cons_off.data(), b->cons_off.size(), s);
+  if (!st && (b->d_work.ensure(4ull * b->n_windows + 8) || b->d_queue.ensure(4ull * b->n_windows + 8) ||
+              b->d_scores.ensure(4ull * b->n_reads + 8) || b->d_rev.ensure(b->n_reads + 8) ||
+              b->d_cons.ensure(b->cons_off[b->n_windows] + 8) ||
+              b->d_cons_len.ensure(4ull * b->n_windows + 8) ||
+              b->d_status.ensure(4ull * b->n_windows + 8) || b->d_cells.ensure(8)))
+    st = kNoMemory;
+  if (!st && d->want_alignments) {
+    b->aln_off.assign(b->n_reads + 1, 0);
+    for (uint32_t w = 0; w < b->n_windows; ++w)
+      for (uint32_t r = b->wro[w]; r < b->wro[w + 1]; ++r)
+        b->aln_off[r + 1] = b->aln_off[r] + b->sumlen[w] + (b->seq_off[r + 1] - b->seq_off[r]) + 16;
+    st = upload(b->d_aln_off, b->aln_off.data(), b->aln_off.size(), s);
+    if (!st && (b->d_aln.ensure(8 * b->aln_off[b->n_reads] + 8) ||
+                b->d_aln_len.ensure(4ull * b->n_reads + 8)))
+      st = kNoMemory;
+  }
+  if (!st && d->want_msa) {
+    b->msa_off.assign(b->n_windows + 1, 0);
+    for (uint32_t w = 0; w < b->n_windows; ++w)
+      b->msa_off[w + 1] = b->msa_off[w] + (uint64_t)(b->nreads[w] + 1) * (b->sumlen[w] + 1);
+    st = upload(b->d_msa_off, b->msa_off.data(), b->msa_off.size(), s);
+    if (!st && (b->d_msa.ensure(b->msa_off[b->n_windows] + 8) ||
+                b->d_msa_rows.ensure(4ull * b->n_windows + 8) ||
+                b->d_msa_cols.ensure(4ull * b->n_windows + 8)))
+      st = kNoMemory;
+  }
+  if (!st && cudaStreamSynchronize(s) != cudaSuccess) st = kCuda;
+  if (st) {
+    cudaGetLastError();
+    delete b;
+    return st;
+  }
+  *out = b;
+  return kOk;
+}
+
+int32_t spoa_gb300_batch_launch(spoa_gb300_batch* b, void* stream) {
+  if (!b) return kInvalidArgument;
+  if (!b->n_windows) return kOk;
+  return launch_all(b, stream, false);
+}
+
+int32_t spoa_gb300_batch_launch_plain(spoa_gb300_batch* b, void* stream) {
+  if (!b) return kInvalidArgument;
+  if (!b->n_windows) return kOk;
+  return launch_all(b, stream, true);
+}
+
+int32_t spoa_gb300_batch_fetch(spoa_gb300_batch* b, spoa_gb300_batch_result* r) {
+  if (!b || !r) return kInvalidArgument;
+  std::memset(r, 0, sizeof(*r));
+  const uint32_t W = b->n_windows, R = b->n_reads;
+  b->h_scores.resize(R + 1);
+  b->h_rev.resize(R + 1);
+  b->h_status.resize(W + 1);
+  std::vector<uint32_t> lens(W + 1);
+  std::vector<char> raw(b->cons_off[W] + 1);
+  uint64_t cells = 0;
+  if (R) {
+    CU(cudaMemcpy(b->h_scores.data(), b->d_scores.p, 4ull * R, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(b->h_rev.data(), b->d_rev.p, R, cudaMemcpyDeviceToHost));
+  }
+  if (W) {
+    CU(cudaMemcpy(b->h_status.data(), b->d_status.p, 4ull * W, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(lens.data(), b->d_cons_len.p, 4ull * W, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(raw.data(), b->d_cons.p, b->cons_off[W], cudaMemcpyDeviceToHost));
+  }
+  CU(cudaMemcpy(&cells, b->d_cells.p, 8, cudaMemcpyDeviceToHost));
+  b->h_cons.clear();
+  b->h_cons_off.assign(W + 1, 0);
+  for (uint32_t w = 0; w < W; ++w) {
+    if (b->h_status[w] == kOk) {
+      if (!b->retry_cons.empty() && !b->retry_cons[w].empty()) {
+        b->h_cons.insert(b->h_cons.end(), b->retry_cons[w].begin(), b->retry_cons[w].end());
+      } else {
+        uint64_t n = std::min<uint64_t>(lens[w], b->cons_off[w + 1] - b->cons_off[w]);
+        b->h_cons.insert(b->h_cons.end(), raw.data() + b->cons_off[w], raw.data() + b->cons_off[w] + n);
+      }
+    }
+    b->h_cons_off[w + 1] = b->h_cons.size();
+  }
+  b->h_cons.push_back(0);
+  if (b->desc.want_alignments) {
+    b->h_aln_len.resize(R + 1);
+    if (R) CU(cudaMemcpy(b->h_aln_len.data(), b->d_aln_len.p, 4ull * R, cudaMemcpyDeviceToHost));
+    std::vector<int32_t> all(2 * b->aln_off[R] + 2);
+    if (R) CU(cudaMemcpy(all.data(), b->d_aln.p, 8 * b->aln_off[R], cudaMemcpyDeviceToHost));
+    b->h_aln.clear();
+    b->h_aln_off.assign(R + 1, 0);
+    for (uint32_t k = 0; k < R; ++k) {
+      uint64_t n = std::min<uint64_t>(b->h_aln_len[k], b->aln_off[k + 1] - b->aln_off[k]);
+      b->h_aln.insert(b->h_aln.end(), all.begin() + 2 * b->aln_off[k],
+                      all.begin() + 2 * (b->aln_off[k] + n));
+      b->h_aln_off[k + 1] = b->h_aln_off[k] + n;
+    }
+    b->h_aln.push_back(0);
+    r->alignments = b->h_aln.data();
+    r->alignment_off = b->h_aln_off.data();
+  }
+  if (b->desc.want_msa) {
+    b->h_msa.resize(b->msa_off[W] + 1);
+    b->h_msa_rows.resize(W + 1);
+    b->h_msa_cols.resize(W + 1);
+    if (W) {
+      CU(cudaMemcpy(b->h_msa.data(), b->d_msa.p, b->msa_off[W], cudaMemcpyDeviceToHost));
+      CU(cudaMemcpy(b->h_msa_rows.data(), b->d_msa_rows.p, 4ull * W, cudaMemcpyDeviceToHost));
+      CU(cudaMemcpy(b->h_msa_cols.data(), b->d_msa_cols.p, 4ull * W, cudaMemcpyDeviceToHost));
+    }
+    r->msa = b->h_msa.data();
+    r->msa_off = b->msa_off.data();
+    r->msa_rows = b->h_msa_rows.data();
+    r->msa_cols = b->h_msa_cols.data();
+  }
+  r->read_scores = b->h_scores.data();
+  r->read_reversed = b->h_rev.data();
+  r->window_status = b->h_status.data();
+  r->consensus = b->h_cons.data();
+  r->consensus_off = b->h_cons_off.data();
+  r->cells = cells;
+  r->kernel_ms = b->kernel_ms;
+  r->threads_per_window = b->first.nt;
+  r->columns_per_thread = b->first.cpt;
+  r->ctas = b->first.ctas;
+  r->launches = b->launches;
+  return kOk;
+}
+
+void spoa_gb300_batch_destroy(spoa_gb300_batch* b) { delete b; }
+
+int32_t spoa_gb300_batch_run(const spoa_gb300_batch_desc* d, spoa_gb300_batch** out,
+                             spoa_gb300_batch_result* r) {
+  int32_t st = spoa_gb300_batch_create(d, out);
+  if (st) return st;
+  st = spoa_gb300_batch_launch(*out, nullptr);
+  if (st) return st;
+  return spoa_gb300_batch_fetch(*out, r);
+}
+
+}  // extern "C"
