@@ -1,0 +1,407 @@
+"""Benchmark of the POA hot path on GB300 (one JSON line on stdout).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload batch_10k|uneven_2k|single_500|long_10k]
+
+A step is one pass of the path over one batch: every read of every window
+aligned (graph-to-sequence DP + traceback) and added to its window's graph
+(AddAlignment + topological sort), then each window's consensus.  The
+default workload is the 10,000-window polishing batch (450-550 nt windows,
+depth 10-60, OV convex 5/-4/-8/-6/-10/-4), seeded synthetic reads.
+
+value     windows/s of the persistent kernel with the inputs resident in HBM
+          (CUDA events on the launching stream).
+e2e       windows/s through the public batch API from pinned host buffers:
+          upload, kernel, consensus download, every step.
+plain     windows/s of the one-window-per-launch form on a sample.
+roofline  HBM view: algorithmic bytes (the 4-bit traceback state of every
+          cell) per second against the measured copy bandwidth; int_roofline
+          is the integer-pipe view (the survey's per-cell max/add counts
+          against a measured max/add rate), the bound that applies.
+cpu_baseline  the C oracle (the reference algorithm restated in C, one window
+          per host thread) on a bounded sample of the same workload.
+
+Under torchrun every rank runs its own batch (weak scaling: windows are
+independent and are sharded with no collective); value is the sum of the
+windows over the max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from spoa_gb300 import synth  # noqa: E402
+
+OPS = {0: (2, 1), 1: (3, 3), 2: (5, 4)}  # per cell: a * preds + b (SW adds 1)
+TRACEBACK_BYTES_PER_CELL = 0.5          # 4-bit traceback code per DP cell
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batch_10k",
+                    choices=["batch_10k", "uneven_2k", "single_500", "long_10k"])
+    ap.add_argument("--windows", type=int, default=0, help="override the window count")
+    ap.add_argument("--plain-sample", type=int, default=50)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name: str, n_override: int, rank: int):
+    """Returns (windows, type, params, per-window types, strand flags, config)."""
+    if name == "batch_10k":
+        n = n_override or 10000
+        wins = synth.batch_windows(n, start=rank * n)
+        typ, params = synth.SCORING["batch_10k"]
+        cfg = {"workload": "batch_10k: 10,000 polishing windows, L~U[450,550], depth U[10,60], "
+                           "8% error, 20% truncated reads, OV convex 5/-4/-8/-6/-10/-4",
+               "windows": n}
+        return wins, typ, params, None, None, cfg
+    if name == "uneven_2k":
+        n = n_override or 2000
+        wins = synth.uneven_windows(n, start=rank * n)
+        _, params = synth.SCORING["uneven_2k"]
+        cfg = {"workload": "uneven_2k: 2,000 windows, L log-uniform [100,5000], depth U[5,100], "
+                           "NW/OV per window, strand-ambiguous, affine 5/-4/-8/-6", "windows": n}
+        return (wins, 1, params, [w.type for w in wins], [1] * len(wins), cfg)
+    if name == "single_500":
+        wins = [synth.single_500(1 + rank)]
+        typ, params = synth.SCORING["single_500"]
+        return wins, typ, params, None, None, {"workload": "single_500: one 500-nt window, 30 "
+                                                            "reads, NW affine", "windows": 1}
+    wins = [synth.long_10k(2 + rank)]
+    typ, params = synth.SCORING["long_10k"]
+    return wins, typ, params, None, None, {"workload": "long_10k: one 10-kb window, 40 reads "
+                                                        "2-10 kb, SW convex", "windows": 1}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-i",
+                 os.environ.get("LOCAL_RANK", "0")],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().split("\n"):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[4 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_cell():
+    """DRAM bytes per DP cell from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh).get("dram_bytes_per_cell")
+    return None
+
+
+def cpu_baseline(wins, typ, params, wtypes, wstrand, seconds):
+    from oracle import pyoracle as po
+    threads = os.cpu_count() or 1
+    po.lib()
+    # estimate the cost of one window per thread, then size the sample
+    probe = wins[:threads]
+    t0 = time.perf_counter()
+    _run_oracle(po, probe, typ, params, wtypes, wstrand, threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    per_window = dt / max(len(probe), 1) * threads
+    n = int(min(len(wins), max(len(probe), seconds / per_window * threads)))
+    sample = wins[:n]
+    t0 = time.perf_counter()
+    cons, cells = _run_oracle(po, sample, typ, params, wtypes, wstrand, threads)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "windows/s", "cores": threads, "kind": "port",
+            "sample": f"first {n} windows of the workload, {dt:.1f} s, {cells / dt / 1e9:.3f} GCUPS",
+            "consensus": cons, "n": n}
+
+
+def _run_oracle(po, wins, typ, params, wtypes, wstrand, threads):
+    if wtypes is None:
+        return po.batch_run(typ, *params, [w.reads for w in wins], n_threads=threads)
+    # per-window type/strand: group by (type, strand)
+    cons = [None] * len(wins)
+    cells = 0
+    groups = {}
+    for k, w in enumerate(wins):
+        groups.setdefault((wtypes[k], wstrand[k]), []).append(k)
+    for (t, s), idx in groups.items():
+        c, ce = po.batch_run(t, *params, [wins[k].reads for k in idx], strand_ambiguous=bool(s),
+                             n_threads=threads)
+        cells += ce
+        for k, cc in zip(idx, c):
+            cons[k] = cc
+    return cons, cells
+
+
+def flatten(wins, pinned: bool):
+    reads = [r for w in wins for r in w.reads]
+    lens = np.fromiter((len(r) for r in reads), np.uint64, len(reads))
+    off = np.zeros(len(reads) + 1, np.uint64)
+    np.cumsum(lens, out=off[1:])
+    blob = b"".join(reads)
+    wro = np.zeros(len(wins) + 1, np.uint32)
+    wro[1:] = np.cumsum([len(w.reads) for w in wins])
+    seqs = np.frombuffer(blob + b"\0", np.uint8)
+    if pinned:
+        try:
+            import torch
+            t = torch.empty(seqs.size, dtype=torch.uint8, pin_memory=True)
+            host = t.numpy()
+            host[:] = seqs
+            seqs = host
+            seqs._keep = t  # noqa: SLF001
+        except Exception:  # noqa: BLE001
+            pass
+    return seqs, off, wro
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        return reference_arm(args)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import spoa_gb300 as sg
+    if sg.lib().spoa_gb300_device_count() <= 0:
+        raise SystemExit("no CUDA device visible")
+
+    wins, typ, params, wtypes, wstrand, cfg = workload(args.workload, args.windows, rank)
+    n_windows = len(wins)
+    seqs, off, wro = flatten(wins, pinned=True)
+
+    def make_batch():
+        return sg.Batch.from_arrays(seqs, off, wro, typ, *params, window_types=wtypes,
+                                    window_strand=wstrand)
+
+    batch = make_batch()
+    for _ in range(args.warmup):
+        batch.launch()
+    res = batch.fetch()
+    assert (res.status == 0).all(), "windows failed"
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    clocks = Clocks()
+    clocks.start()
+    barrier()
+    kernel_ms = 0.0
+    launches = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batch.launch()
+        r = batch.fetch()
+        kernel_ms += r.kernel_ms
+        launches += r.launches
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    step_s = kernel_ms / 1e3 / args.steps
+    if dist is not None:
+        t = torch.tensor([step_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_s = float(t.item())
+    total_windows = n_windows * world
+    value = total_windows / step_s
+    cells, pred_cells = res.cells, res.pred_cells
+    gcups = cells * world / step_s / 1e9
+
+    # end to end through the public API, pinned host inputs every step
+    e2e = None
+    if not args.no_e2e:
+        h2d = int(seqs.nbytes + off.nbytes + wro.nbytes)
+        barrier()
+        te = time.perf_counter()
+        d2h = 0
+        for _ in range(max(1, args.steps)):
+            b = make_batch()
+            b.launch()
+            rr = b.fetch()
+            d2h = sum(len(c) for c in rr.consensus) + rr.scores.nbytes + rr.status.nbytes
+            del b
+        barrier()
+        e2e_s = (time.perf_counter() - te) / max(1, args.steps)
+        e2e = {"value": total_windows / e2e_s, "unit": "windows/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": int(d2h)}
+
+    # one-window-per-launch form on a sample
+    plain = None
+    if rank == 0 and args.plain_sample > 0 and n_windows > 1:
+        k = min(args.plain_sample, n_windows)
+        ps, po_, pw = flatten(wins[:k], pinned=False)
+        pb = sg.Batch.from_arrays(ps, po_, pw, typ, *params,
+                                  window_types=wtypes[:k] if wtypes else None,
+                                  window_strand=wstrand[:k] if wstrand else None)
+        pb.launch_plain()
+        pr = pb.fetch()
+        plain = {"value": k / (pr.kernel_ms / 1e3), "unit": "windows/s", "sample_windows": k,
+                 "launches": pr.launches}
+        del pb
+
+    # rooflines
+    hbm_peak, peak_kind = measured_peaks()
+    achieved_gbs = cells * TRACEBACK_BYTES_PER_CELL / step_s / 1e9
+    tpc = traffic_per_cell()
+    sub = batch.subtype
+    a_, b_ = OPS[sub]
+    ops = a_ * pred_cells + b_ * cells + (cells if typ == 0 else 0)
+    int_peak = None
+    try:
+        import ctypes as C
+        pl = C.CDLL(os.path.join(ROOT, "spoa_gb300", "libspoa_peak.so"))
+        pl.spoa_gb300_int_peak_ops.restype = C.c_double
+        int_peak = pl.spoa_gb300_int_peak_ops(4096)
+    except OSError:
+        pass
+    int_roof = None
+    if int_peak and int_peak > 0:
+        int_roof = {"achieved": ops / step_s / 1e9, "peak": int_peak / 1e9, "unit": "Gop/s",
+                    "frac": ops / step_s / int_peak,
+                    "ops_per_cell": ops / max(cells, 1),
+                    "peak_kind": "measured in this run (max/add probe)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(wins, typ, params, wtypes, wstrand, args.cpu_seconds)
+        k = cpu.pop("n")
+        cons = cpu.pop("consensus")
+        cpu["parity_sample_windows"] = k
+        cpu["parity_sample_equal"] = bool(cons == res.consensus[:k])
+
+    line = {
+        "metric": "windows/s", "value": value, "unit": "windows/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded; see spoa_gb300/synth.py)",
+        "config": dict(cfg, parallelism=f"windows sharded over {world} GPU(s), no collective",
+                       l2="inputs and per-CTA arenas larger than L2 (129 MB)",
+                       threads_per_window=res.threads_per_window,
+                       columns_per_thread=res.columns_per_thread, ctas=res.ctas),
+        "gcups": gcups, "cells_per_step": cells * world,
+        "e2e": e2e, "plain": plain,
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm_peak,
+                     "traffic": (tpc * cells) if tpc else None,
+                     "peak_kind": peak_kind,
+                     "algorithmic_bytes": "0.5 B per DP cell (4-bit traceback state)"},
+        "int_roofline": int_roof,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "wall_s": wall,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def reference_arm(args):
+    """The reference algorithm on the host cores (the C oracle: the
+    reference's own build is x86-only and its tree is not on the GPU machine)."""
+    from oracle import pyoracle as po
+    wins, typ, params, wtypes, wstrand, cfg = workload(args.workload, args.windows, 0)
+    threads = os.cpu_count() or 1
+    po.lib()
+    probe = wins[:threads]
+    t0 = time.perf_counter()
+    _run_oracle(po, probe, typ, params, wtypes, wstrand, threads)
+    per_window = max(time.perf_counter() - t0, 1e-3) / max(len(probe), 1) * threads
+    total_steps = args.steps + args.warmup
+    budget = 150.0 / max(total_steps, 1)
+    n = int(min(len(wins), max(len(probe), budget / per_window * threads)))
+    sample = wins[:n]
+    for _ in range(args.warmup):
+        _run_oracle(po, sample, typ, params, wtypes, wstrand, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _run_oracle(po, sample, typ, params, wtypes, wstrand, threads)
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    value = n / dt
+    line = {"impl": "reference", "metric": "windows/s", "value": value, "unit": "windows/s",
+            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded; see spoa_gb300/synth.py)", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": "windows/s", "cores": threads,
+                             "kind": "port",
+                             "sample": f"first {n} windows of the workload per step"},
+            "e2e": {"value": value, "unit": "windows/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

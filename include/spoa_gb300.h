@@ -175,6 +175,8 @@ typedef struct {
   const uint32_t* msa_rows;      /* [n_windows] */
   const uint32_t* msa_cols;
   uint64_t cells;               /* sum over reads of read length x graph nodes */
+  uint64_t pred_cells;          /* sum over reads of read length x predecessor
+                                   entries (in-edges, row 0 for sources) */
   double kernel_ms;             /* device time of the persistent launch(es) */
   int32_t threads_per_window, columns_per_thread, ctas, launches;
 } spoa_gb300_batch_result;

@@ -85,6 +85,7 @@ class _BatchResult(C.Structure):
                 ("consensus_off", C.c_void_p), ("alignments", C.c_void_p),
                 ("alignment_off", C.c_void_p), ("msa", C.c_void_p), ("msa_off", C.c_void_p),
                 ("msa_rows", C.c_void_p), ("msa_cols", C.c_void_p), ("cells", C.c_uint64),
+                ("pred_cells", C.c_uint64),
                 ("kernel_ms", C.c_double), ("threads_per_window", C.c_int32),
                 ("columns_per_thread", C.c_int32), ("ctas", C.c_int32),
                 ("launches", C.c_int32)]
@@ -357,6 +358,7 @@ class BatchResult:
     reversed: np.ndarray
     status: np.ndarray
     cells: int
+    pred_cells: int
     kernel_ms: float
     threads_per_window: int
     columns_per_thread: int
@@ -370,24 +372,48 @@ class Batch:
     """Many windows in one persistent kernel (spoa_gb300_batch_*)."""
 
     def __init__(self, windows, type_: int, m: int, n: int, g: int, e: int, q: int, c: int,
-                 window_types=None, window_strand=None, quals=None, want_alignments=False,
-                 want_msa=False, threads_per_window=0, columns_per_thread=0, ctas=0,
-                 max_nodes=0, memory_budget=0):
+                 window_types=None, window_strand=None, quals=None, **kw):
         reads = [_bytes(r) for w in windows for r in w]
-        self.n_windows = len(windows)
-        self.n_reads = len(reads)
-        self._wro = np.zeros(len(windows) + 1, np.uint32)
-        self._wro[1:] = np.cumsum([len(w) for w in windows])
-        self._off = np.zeros(len(reads) + 1, np.uint64)
-        self._off[1:] = np.cumsum([len(r) for r in reads])
-        self._seqs = np.frombuffer(b"".join(reads) + b"\0", np.uint8)
-        self._quals = (np.frombuffer(b"".join(_bytes(x) for w in quals for x in w) + b"\0",
-                                     np.uint8) if quals is not None else None)
+        wro = np.zeros(len(windows) + 1, np.uint32)
+        wro[1:] = np.cumsum([len(w) for w in windows])
+        off = np.zeros(len(reads) + 1, np.uint64)
+        off[1:] = np.cumsum([len(r) for r in reads])
+        seqs = np.frombuffer(b"".join(reads) + b"\0", np.uint8)
+        qarr = (np.frombuffer(b"".join(_bytes(x) for w in quals for x in w) + b"\0", np.uint8)
+                if quals is not None else None)
+        self._create(seqs, off, wro, type_, m, n, g, e, q, c, window_types, window_strand, qarr,
+                     **kw)
+
+    @classmethod
+    def from_arrays(cls, seqs, seq_off, window_read_off, type_, m, n, g, e, q, c,
+                    window_types=None, window_strand=None, quals=None, **kw) -> "Batch":
+        """Batch over already flattened inputs: seqs (uint8, reads back to
+        back), seq_off (uint64, n_reads + 1), window_read_off (uint32,
+        n_windows + 1); quals shares seq_off."""
+        b = cls.__new__(cls)
+        b._create(seqs, seq_off, window_read_off, type_, m, n, g, e, q, c, window_types,
+                  window_strand, quals, **kw)
+        return b
+
+    def _create(self, seqs, off, wro, type_, m, n, g, e, q, c, window_types, window_strand,
+                quals, want_alignments=False, want_msa=False, threads_per_window=0,
+                columns_per_thread=0, ctas=0, max_nodes=0, memory_budget=0):
+        self._seqs = np.ascontiguousarray(seqs, np.uint8)
+        self._off = np.ascontiguousarray(off, np.uint64)
+        self._wro = np.ascontiguousarray(wro, np.uint32)
+        self._quals = np.ascontiguousarray(quals, np.uint8) if quals is not None else None
+        self.n_windows = int(self._wro.size - 1)
+        self.n_reads = int(self._off.size - 1)
         self._wt = np.asarray(window_types, np.int8) if window_types is not None else None
         self._ws = np.asarray(window_strand, np.int8) if window_strand is not None else None
+        g_ = g
+        e_ = e if e is not None else g
+        self.subtype = (AlignmentSubtype.kLinear if g_ >= e_ else
+                        (AlignmentSubtype.kAffine if (g_ <= q or e_ >= c)
+                         else AlignmentSubtype.kConvex))
         d = _BatchDesc()
         d.type, d.m, d.n, d.g, d.e, d.q, d.c = type_, m, n, g, e, q, c
-        d.n_windows = len(windows)
+        d.n_windows = self.n_windows
         d.window_read_off = _ptr(self._wro).value
         d.window_type = _ptr(self._wt).value if self._wt is not None else None
         d.window_strand = _ptr(self._ws).value if self._ws is not None else None
@@ -435,6 +461,7 @@ class Batch:
         res = BatchResult(consensus=cons, scores=arr(r.read_scores, np.int32, R),
                           reversed=arr(r.read_reversed, np.uint8, R),
                           status=arr(r.window_status, np.int32, W), cells=r.cells,
+                          pred_cells=r.pred_cells,
                           kernel_ms=r.kernel_ms, threads_per_window=r.threads_per_window,
                           columns_per_thread=r.columns_per_thread, ctas=r.ctas,
                           launches=r.launches)

@@ -20,8 +20,9 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libspoa_gb300.so")
 CPPLIB = os.path.join(HERE, "libspoa.so")
+PEAKLIB = os.path.join(HERE, "libspoa_peak.so")
 
-TUS = ["spoa_gb300", "inst_linear", "inst_affine", "inst_convex"]
+TUS = ["spoa_gb300"] + [f"inst_{m}{w}" for m in ("linear", "affine", "convex") for w in (16, 32)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -67,6 +68,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs = list(ex.map(compile_one, TUS))
     if force or _stale(LIB, objs):
         subprocess.run([cc] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs, check=True)
+    # integer-pipe peak probe used by the benchmark (not part of the C ABI)
+    peak_src = os.path.join(CSRC, "int_peak.cu")
+    if force or _stale(PEAKLIB, [peak_src]):
+        subprocess.run([cc] + ARCH + ["-O3", "-Xcompiler", "-fPIC", "-shared", "-cudart",
+                                      "static", peak_src, "-o", PEAKLIB], check=True)
     # C++ drop-in layer over the C ABI
     cpp_src = os.path.join(CSRC, "spoa_api.cpp")
     if os.path.exists(cpp_src):

@@ -1,0 +1,7 @@
+// inst_linear32.cu - kernels of the linear gap model with 32-bit lanes
+// (one translation unit per gap model and width so they build in parallel).
+#include "poa_kernels.cuh"
+
+namespace spoa_gb300 {
+SPOA_GB300_INSTANTIATE(kLinear, int32_t)
+}  // namespace spoa_gb300

@@ -42,6 +42,7 @@ enum Status : int32_t {
   kCapacity = 8,
   kTraceback = 9,
   kCuda = 10,
+  kNeedWide = 11,  // internal: the window needs the int32 kernel
 };
 
 enum : int32_t { kSW = 0, kNW = 1, kOV = 2 };
@@ -145,7 +146,13 @@ struct DpCaps {
 };
 
 struct DpView {
-  int32_t *H, *F, *E, *O, *Q;
+  // H/F/O rows in "pair layout": thread t's strip of CPT columns is stored as
+  // CPT/2 pairs, pair k = (column t*CPT + k, column t*CPT + CPT/2 + k), one
+  // pair per 32-bit word (int16 lanes) or per 64-bit word (int32 lanes).
+  // Element index of column j: t*CPT + 2*(r % (CPT/2)) + r / (CPT/2) with
+  // t = j / CPT, r = j % CPT.  Capacity is sized for 4-byte elements.
+  void *H, *F, *O;
+  uint8_t* code;           // per cell: horizontal traceback class + E/Q run bit
   uint32_t *pred_ptr, *preds, *row_indeg;
   uint8_t *row_char, *row_sink;
   int32_t *fc, *fcF, *fcO;
@@ -165,11 +172,10 @@ __host__ __device__ inline uint64_t dp_layout(uint8_t* base, const DpCaps& c, Dp
   const uint64_t cells = (uint64_t)c.rows * c.ld;
   v->caps = c;
   v->aln_cap = (uint64_t)c.rows + c.ld + 16;
-  v->H = reinterpret_cast<int32_t*>(take(4 * cells));
-  v->F = c.sub >= kAffine ? reinterpret_cast<int32_t*>(take(4 * cells)) : nullptr;
-  v->E = c.sub >= kAffine ? reinterpret_cast<int32_t*>(take(4 * cells)) : nullptr;
-  v->O = c.sub == kConvex ? reinterpret_cast<int32_t*>(take(4 * cells)) : nullptr;
-  v->Q = c.sub == kConvex ? reinterpret_cast<int32_t*>(take(4 * cells)) : nullptr;
+  v->H = take(4 * cells);
+  v->F = c.sub >= kAffine ? take(4 * cells) : nullptr;
+  v->O = c.sub == kConvex ? take(4 * cells) : nullptr;
+  v->code = c.sub >= kAffine ? take(cells) : take(cells);
   v->pred_ptr = reinterpret_cast<uint32_t*>(take(4 * ((uint64_t)c.rows + 1)));
   v->preds = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.preds));
   v->row_indeg = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.rows));
@@ -325,7 +331,7 @@ __device__ inline int64_t g_add_sequence(GraphView& G, const uint8_t* seq, const
 }
 
 // Graph::TopologicalSort (graph.cpp:249-303)
-__device__ inline int g_topo_sort(GraphView& G) {
+static __device__ __noinline__ int g_topo_sort(GraphView& G) {
   const uint32_t nn = G.hdr->n_nodes;
   for (uint32_t i = 0; i < nn; ++i) {
     G.marks[i] = 0;
@@ -395,7 +401,7 @@ __device__ inline int g_link_aligned(GraphView& G, uint32_t a, uint32_t b) {
 
 // Graph::AddAlignment (graph.cpp:155-247).  pairs: n (node id | -1,
 // position | -1).  Weights: w[] or the constant wconst.
-__device__ inline int32_t g_add_alignment(GraphView& G, const int32_t* pairs, uint32_t n_pairs,
+static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32_t* pairs, uint32_t n_pairs,
                                           const uint8_t* seq, uint32_t len, const WeightSrc& w) {
   GraphHeader* h = G.hdr;
   if (len == 0) return kOk;
@@ -518,7 +524,7 @@ __device__ inline uint32_t g_branch_completion(GraphView& G, uint32_t rank) {
   return mx;
 }
 
-__device__ inline void g_consensus(GraphView& G) {
+static __device__ __noinline__ void g_consensus(GraphView& G) {
   const uint32_t nn = G.hdr->n_nodes;
   G.hdr->n_consensus = 0;
   if (nn == 0) return;

@@ -3,9 +3,11 @@
 //
 // Layout: row i (1-based rank + 1, row 0 is the initial row) x column j
 // (read position).  Thread t owns the strip of CPT consecutive columns
-// [t*CPT, (t+1)*CPT).  Rows are processed in rank order; the predecessor
-// rows of row i are read back from the H/F/O matrices in HBM (they can be
-// any earlier row).  The in-row gap recurrences are max-plus linear scans
+// [t*CPT, (t+1)*CPT), held as CPT/2 lane pairs (column s+k with column
+// s+CPT/2+k) so one int16x2 DPX instruction advances both half-strips.
+// Rows are processed in rank order; the previous row stays in registers and
+// other predecessor rows are read back from the H/F/O rows in HBM (they can
+// be any earlier row).  The in-row gap recurrences are max-plus linear scans
 //     X[j] = max(a[j], X[j-1] + pen)
 // computed as a per-thread strip scan, a CTA-wide exclusive prefix-max of
 // the strip aggregates (warp shuffles + shared memory) and a fix-up pass.
@@ -42,6 +44,7 @@ __device__ __forceinline__ int32_t addmax(int32_t a, int32_t b, int32_t c) {
 struct BlockScratch {
   int32_t wv[32];
   int32_t wv2[32];
+  int32_t edge[32];
   int32_t bcast[8];
 };
 
@@ -117,9 +120,11 @@ __device__ __forceinline__ int32_t scan_carry(int32_t agg, int32_t init, int32_t
   return t == 0 ? init : ex + (t - 1) * D;
 }
 
+constexpr uint8_t kRowSink = 1, kRowPrevPred = 2;
+
 // Builds the rank-ordered predecessor lists of the graph into the DP arena:
 // row i = rank + 1; preds of a source row = {0}.
-__device__ inline void dp_build_rows(const GraphView& G, DpView& D, BlockScratch& sh) {
+static __device__ __noinline__ void dp_build_rows(const GraphView& G, DpView& D, BlockScratch& sh) {
   const uint32_t V = G.hdr->n_nodes;
   const uint32_t nt = blockDim.x, t = threadIdx.x;
   const uint32_t chunk = (V + nt - 1) / nt;
@@ -151,90 +156,335 @@ __device__ inline void dp_build_rows(const GraphView& G, DpView& D, BlockScratch
     const uint32_t d = G.in_deg[node];
     D.row_indeg[i] = d;
     D.row_char[i] = (uint8_t)G.hdr->decoder[G.code[node]];
-    D.row_sink[i] = G.out_first[node] == kNone;
+    uint8_t flags = G.out_first[node] == kNone ? kRowSink : 0;
     if (d == 0) {
       D.preds[off++] = 0;
+      if (i == 1) flags |= kRowPrevPred;
     } else {
-      for (uint32_t e = G.in_first[node]; e != kNone; e = G.e_next_in[e])
-        D.preds[off++] = G.node_to_rank[G.e_tail[e]] + 1;
+      for (uint32_t e = G.in_first[node]; e != kNone; e = G.e_next_in[e]) {
+        const uint32_t p = G.node_to_rank[G.e_tail[e]] + 1;
+        D.preds[off++] = p;
+        if (p == i - 1) flags |= kRowPrevPred;
+      }
     }
+    D.row_sink[i] = flags;
   }
   if (t == nt - 1) D.pred_ptr[V + 1] = off;
   __syncthreads();
 }
 
-struct AlignResult {
-  int32_t status;
-  int32_t has_score;  // 0: score not written (reference returns early)
-  int32_t score;
-  uint32_t n_pairs;
-  int32_t lanes;
+// ---------------------------------------------------------------------------
+// lane pairs: two DP columns per operation
+// ---------------------------------------------------------------------------
+// Lanes<int16_t>: the pair lives in one 32-bit register (int16x2) and every
+// max/add is one DPX or SIMD instruction for both columns; used when the
+// reference's width rule picks int16 (16 lanes).  Lanes<int32_t>: two
+// registers, scalar DPX instructions; used for the int32 width (8 lanes).
+// Comparison masks have the same format in both: 0xFFFF in the low half for
+// the first column, 0xFFFF0000 for the second.
+template <typename T>
+struct Lanes;
+
+template <>
+struct Lanes<int16_t> {
+  struct P {
+    uint32_t v;
+  };
+  static constexpr int32_t kNeg = INT16_MIN + 1024;
+  __device__ __forceinline__ static P make(int32_t lo, int32_t hi) {
+    return {(uint32_t)(uint16_t)lo | ((uint32_t)(uint16_t)hi << 16)};
+  }
+  __device__ __forceinline__ static P splat(int32_t x) { return make(x, x); }
+  __device__ __forceinline__ static int32_t lo(P a) { return (int32_t)(int16_t)(a.v & 0xFFFFu); }
+  __device__ __forceinline__ static int32_t hi(P a) { return (int32_t)(int16_t)(a.v >> 16); }
+  __device__ __forceinline__ static P add(P a, P b) { return {__vadd2(a.v, b.v)}; }
+  __device__ __forceinline__ static P max(P a, P b) { return {__vmaxs2(a.v, b.v)}; }
+  __device__ __forceinline__ static P max3(P a, P b, P c) {
+    return {__vimax3_s16x2(a.v, b.v, c.v)};
+  }
+  // max(a + b, c)
+  __device__ __forceinline__ static P addmax(P a, P b, P c) {
+    return {__viaddmax_s16x2(a.v, b.v, c.v)};
+  }
+  __device__ __forceinline__ static uint32_t eq(P a, P b) { return __vcmpeq2(a.v, b.v); }
+  __device__ __forceinline__ static P select(uint32_t m, P a, P b) {
+    return {(a.v & m) | (b.v & ~m)};
+  }
+  // 2 pairs per 8-byte access
+  __device__ __forceinline__ static void load2(const void* base, uint64_t w, P& a, P& b) {
+    uint2 x = reinterpret_cast<const uint2*>(base)[w >> 1];
+    a.v = x.x;
+    b.v = x.y;
+  }
+  __device__ __forceinline__ static void store2(void* base, uint64_t w, P a, P b) {
+    reinterpret_cast<uint2*>(base)[w >> 1] = make_uint2(a.v, b.v);
+  }
+  __device__ __forceinline__ static int32_t elem(const void* base, uint64_t i) {
+    return reinterpret_cast<const int16_t*>(base)[i];
+  }
 };
 
-// Forward pass + row selection + max_j.  Returns (in smem-broadcast values)
-// max_i, max_j and the score; traceback is run by the caller on thread 0.
-template <int SUB, int CPT>
-__device__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restrict__ seq,
+template <>
+struct Lanes<int32_t> {
+  struct P {
+    int32_t l, h;
+  };
+  static constexpr int32_t kNeg = kNegBig;
+  __device__ __forceinline__ static P make(int32_t lo, int32_t hi) { return {lo, hi}; }
+  __device__ __forceinline__ static P splat(int32_t x) { return {x, x}; }
+  __device__ __forceinline__ static int32_t lo(P a) { return a.l; }
+  __device__ __forceinline__ static int32_t hi(P a) { return a.h; }
+  __device__ __forceinline__ static P add(P a, P b) { return {a.l + b.l, a.h + b.h}; }
+  __device__ __forceinline__ static P max(P a, P b) {
+    return {a.l > b.l ? a.l : b.l, a.h > b.h ? a.h : b.h};
+  }
+  __device__ __forceinline__ static P max3(P a, P b, P c) {
+    return {__vimax3_s32(a.l, b.l, c.l), __vimax3_s32(a.h, b.h, c.h)};
+  }
+  __device__ __forceinline__ static P addmax(P a, P b, P c) {
+    return {__viaddmax_s32(a.l, b.l, c.l), __viaddmax_s32(a.h, b.h, c.h)};
+  }
+  __device__ __forceinline__ static uint32_t eq(P a, P b) {
+    return (a.l == b.l ? 0x0000FFFFu : 0u) | (a.h == b.h ? 0xFFFF0000u : 0u);
+  }
+  __device__ __forceinline__ static P select(uint32_t m, P a, P b) {
+    return {(m & 0xFFFFu) ? a.l : b.l, (m & 0xFFFF0000u) ? a.h : b.h};
+  }
+  __device__ __forceinline__ static void load2(const void* base, uint64_t w, P& a, P& b) {
+    int4 x = reinterpret_cast<const int4*>(base)[w >> 1];
+    a = {x.x, x.y};
+    b = {x.z, x.w};
+  }
+  __device__ __forceinline__ static void store2(void* base, uint64_t w, P a, P b) {
+    reinterpret_cast<int4*>(base)[w >> 1] = make_int4(a.l, a.h, b.l, b.h);
+  }
+  __device__ __forceinline__ static int32_t elem(const void* base, uint64_t i) {
+    return reinterpret_cast<const int32_t*>(base)[i];
+  }
+};
+
+// Element index of column j in a pair-layout row (see DpView).
+template <int CPT>
+__host__ __device__ __forceinline__ uint64_t colmap(uint64_t j) {
+  const uint64_t t = j / CPT, r = j % CPT;
+  return t * CPT + 2 * (r % (CPT / 2)) + r / (CPT / 2);
+}
+
+// Value of thread t-1 (thread 0 gets `fill`), for three values at once.
+__device__ __forceinline__ void from_left3(int32_t a, int32_t b, int32_t c, int32_t fill,
+                                           int32_t* la, int32_t* lb, int32_t* lc,
+                                           BlockScratch& sh) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t xa = __shfl_up_sync(0xffffffffu, a, 1);
+  int32_t xb = __shfl_up_sync(0xffffffffu, b, 1);
+  int32_t xc = __shfl_up_sync(0xffffffffu, c, 1);
+  if ((blockDim.x >> 5) > 1) {
+    if (lane == 31) {
+      sh.wv[warp] = a;
+      sh.wv2[warp] = b;
+      sh.edge[warp] = c;
+    }
+    __syncthreads();
+    if (lane == 0 && warp > 0) {
+      xa = sh.wv[warp - 1];
+      xb = sh.wv2[warp - 1];
+      xc = sh.edge[warp - 1];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) xa = xb = xc = fill;
+  *la = xa;
+  *lb = xb;
+  *lc = xc;
+}
+
+// Strip scan of X[j] = max(a[j], X[j-1] + pen) over this thread's pairs with
+// the CTA carry.  On return x[k] holds X at the columns of pair k; returns
+// X[s-1], the value carried into the strip (init for thread 0).
+template <int CPT, typename Lx>
+__device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, int32_t pen,
+                                             BlockScratch& sh) {
+  constexpr int HP = CPT / 2;
+  using P = typename Lx::P;
+  const P pen2 = Lx::splat(pen);
+#pragma unroll
+  for (int k = 1; k < HP; ++k) x[k] = Lx::addmax(x[k - 1], pen2, x[k]);
+  const int32_t lo_agg = Lx::lo(x[HP - 1]), hi_agg = Lx::hi(x[HP - 1]);
+  const int32_t agg = imax(hi_agg, lo_agg + HP * pen);
+  const int32_t c = scan_carry<CPT>(agg, init, pen, sh);  // X[s-1]
+  const int32_t c_hi = imax(lo_agg, c + HP * pen);          // X[s+HP-1]
+  const P carry = Lx::make(c, c_hi);
+#pragma unroll
+  for (int k = 0; k < HP; ++k) x[k] = Lx::addmax(carry, Lx::splat((k + 1) * pen), x[k]);
+  return c;
+}
+
+// Horizontal traceback code of a cell (one byte):
+//   bits 0-1  first match of the horizontal tests of the traceback
+//             (implementation.hpp:1977-1990): 0 none, 1 gap open
+//             (H[j-1] + g or H[j-1] + q), 3 gap extension (E[j-1] + e or
+//             Q[j-1] + c, the extend_left case)
+//   bit 2     E[j-1] + e == E[j] and Q[j-1] + c == Q[j]: the extend_left
+//             loop continues past column j (2031-2035)
+constexpr uint8_t kCodeAny = 1, kCodeExt = 2, kCodeRun = 4;
+
+// Forward pass + row selection + max_j (identical in every thread on
+// return).  T = int16_t for the 16-lane width, int32_t for the 8-lane one.
+template <int SUB, int CPT, typename T>
+__device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restrict__ seq,
                            uint32_t L, uint32_t V, int32_t lanes, BlockScratch& sh,
                            int64_t* out_max_i, int64_t* out_max_j, int32_t* out_score) {
+  using Lx = Lanes<T>;
+  using P = typename Lx::P;
+  using L16 = Lanes<int16_t>;
+  constexpr int HP = CPT / 2;
   const uint32_t t = threadIdx.x;
   const uint32_t s0 = t * CPT;
-  const uint64_t ld = D.caps.ld;
+  const uint64_t ld = D.caps.ld;        // elements per row
+  const uint64_t wrow = ld / 2;         // pair words per row
+  const uint64_t w0 = (uint64_t)t * HP; // this thread's first pair word
   const int32_t type = S.type;
   const int32_t m = S.m, n = S.n, g = S.g, e = S.e, q = S.q, c = S.c;
   const int32_t NEGW = lanes == 8 ? (INT32_MIN + 1024) : (INT16_MIN + 1024);
-  int32_t* __restrict__ H = D.H;
-  int32_t* __restrict__ F = D.F;
-  int32_t* __restrict__ E = D.E;
-  int32_t* __restrict__ O = D.O;
-  int32_t* __restrict__ Q = D.Q;
+  void* __restrict__ H = D.H;
+  void* __restrict__ F = D.F;
+  void* __restrict__ O = D.O;
+  uint8_t* __restrict__ CODE = D.code;
+  const P NEG2 = Lx::splat(Lx::kNeg);
+  const P m2 = Lx::splat(m), n2 = Lx::splat(n);
+  const P g2 = Lx::splat(g), e2 = Lx::splat(e), q2 = Lx::splat(q), c2 = Lx::splat(c);
+  const P ge2 = Lx::splat(g - e), qc2 = Lx::splat(q - c);
+  const bool edge_thread = s0 + CPT > L;  // strip reaches past the read
 
-  uint8_t sc[CPT];
+  // read characters as 16-bit lanes (0xFFFF past the read never matches)
+  L16::P sq[HP];
 #pragma unroll
-  for (int k = 0; k < CPT; ++k) {
-    uint32_t j = s0 + k;
-    sc[k] = j < L ? seq[j] : 0;
+  for (int k = 0; k < HP; ++k) {
+    uint32_t jl = s0 + k, jh = s0 + HP + k;
+    sq[k] = L16::make(jl < L ? seq[jl] : 0xFFFF, jh < L ? seq[jh] : 0xFFFF);
+  }
+  // convex: columns whose E' input also takes Q (vector starts of the
+  // reference, (col + 1) % lanes == 0), as a bitmap (bit k low, 16+k high)
+  uint32_t bmap = 0;
+  if (SUB == kConvex) {
+#pragma unroll
+    for (int k = 0; k < HP; ++k) {
+      if ((s0 + k + 1) % (uint32_t)lanes == 0) bmap |= 1u << k;
+      if ((s0 + HP + k + 1) % (uint32_t)lanes == 0) bmap |= 1u << (16 + k);
+    }
   }
 
-  // row 0 and first column (implementation.hpp:555-694)
+  // row 0 (implementation.hpp:555-694) and its registers
+  P ph[HP], pf[HP], po[HP];
 #pragma unroll
-  for (int k = 0; k < CPT; ++k) {
-    int32_t j = (int32_t)(s0 + k);
-    int32_t h0;
-    if (type == kSW) {
-      h0 = 0;
-    } else if (SUB == kConvex) {
-      h0 = imax(g + j * e, q + j * c);
-    } else if (SUB == kAffine) {
-      h0 = g + j * e;
-    } else {
-      h0 = g + j * g;
+  for (int k = 0; k < HP; ++k) {
+    int32_t v[2];
+#pragma unroll
+    for (int hf = 0; hf < 2; ++hf) {
+      const int32_t j = (int32_t)(s0 + hf * HP + k);
+      if (type == kSW) {
+        v[hf] = 0;
+      } else if (SUB == kConvex) {
+        v[hf] = imax(g + j * e, q + j * c);
+      } else if (SUB == kAffine) {
+        v[hf] = g + j * e;
+      } else {
+        v[hf] = g + j * g;
+      }
     }
-    H[s0 + k] = h0;
-    if (SUB >= kAffine) F[s0 + k] = kNegBig;
-    if (SUB == kConvex) O[s0 + k] = kNegBig;
+    ph[k] = Lx::make(v[0], v[1]);
+    pf[k] = NEG2;
+    po[k] = NEG2;
+  }
+#pragma unroll
+  for (int k = 0; k < HP; k += 2) {
+    Lx::store2(H, w0 + k, ph[k], ph[k + 1]);
+    if (SUB >= kAffine) Lx::store2(F, w0 + k, pf[k], pf[k + 1]);
+    if (SUB == kConvex) Lx::store2(O, w0 + k, po[k], po[k + 1]);
+  }
+  int32_t left_prev;  // row i-1 at column s0-1 (thread 0: its first column)
+  {
+    const int32_t j = (int32_t)s0 - 1;
+    int32_t v;
+    if (type == kSW) {
+      v = 0;
+    } else if (SUB == kConvex) {
+      v = imax(g + j * e, q + j * c);
+    } else if (SUB == kAffine) {
+      v = g + j * e;
+    } else {
+      v = g + j * g;
+    }
+    left_prev = t == 0 ? 0 : v;
   }
   if (t == 0) {
     D.fc[0] = 0;
     D.fcF[0] = 0;
     D.fcO[0] = 0;
   }
-  // selection state (strict <: the earliest row wins a tie)
   int32_t bval = type == kSW ? 0 : (type == kOV ? kNegBig : NEGW);
   int32_t brow = -1;
   int32_t first_sink = -1;
+  // the thread holding column L-1 (NW selection)
+  const uint32_t jl = L - 1;
+  const bool owns_last = jl >= s0 && jl < s0 + CPT;
+  const int32_t last_k = (int32_t)((jl - s0) % HP), last_hi = (int32_t)((jl - s0) / HP);
   __syncthreads();
 
   for (uint32_t i = 1; i <= V; ++i) {
     const uint32_t pb = D.pred_ptr[i], pe = D.pred_ptr[i + 1];
     const uint8_t rc = D.row_char[i];
-    int32_t h[CPT], f[CPT], o[CPT];
-    // fc of this row (thread 0 only): NW first column
-    int32_t fci = 0;
+    const L16::P rc2 = L16::splat(rc);
+    P h[HP], f[HP], o[HP];
     int32_t fl = kNegBig, fa = kNegBig, fo = kNegBig;
+    // candidates of one predecessor row, max-accumulated into h/f/o (the
+    // forward pass takes the maximum over predecessors, so their order only
+    // matters to the traceback, which keeps the reference's order)
+    auto accumulate = [&](const P* hp, const P* fp, const P* op, int32_t hleft, bool first) {
+#pragma unroll
+      for (int k = 0; k < HP; ++k) {
+        const P left = k == 0 ? Lx::make(hleft, Lx::lo(hp[HP - 1])) : hp[k - 1];
+        const uint32_t mt = L16::eq(sq[k], rc2);
+        const P d = Lx::add(left, Lx::select(mt, m2, n2));
+        if (SUB == kLinear) {
+          const P cand = Lx::addmax(hp[k], g2, d);
+          h[k] = first ? cand : Lx::max(h[k], cand);
+        } else {
+          h[k] = first ? d : Lx::max(h[k], d);
+          const P fc_ = Lx::add(Lx::addmax(hp[k], ge2, fp[k]), e2);
+          f[k] = first ? fc_ : Lx::max(f[k], fc_);
+          if (SUB == kConvex) {
+            const P oc_ = Lx::add(Lx::addmax(hp[k], qc2, op[k]), c2);
+            o[k] = first ? oc_ : Lx::max(o[k], oc_);
+          }
+        }
+      }
+    };
+    const uint8_t rflags = D.row_sink[i];
+    bool first = true;
+    if (rflags & kRowPrevPred) {
+      // the previous rank is a predecessor: its row is in registers
+      if (t == 0) {
+        fl = imax(fl, D.fc[i - 1]);
+        if (SUB >= kAffine) fa = imax(fa, D.fcF[i - 1]);
+        if (SUB == kConvex) fo = imax(fo, D.fcO[i - 1]);
+      }
+      accumulate(ph, pf, po, t == 0 ? D.fc[i - 1] : left_prev, true);
+      first = false;
+    }
     for (uint32_t pi = pb; pi < pe; ++pi) {
       const uint32_t p = D.preds[pi];
-      const int32_t* __restrict__ Hp = H + (uint64_t)p * ld + s0;
+      if (p == i - 1) continue;
+      P hp[HP], fp[HP], op[HP];
+      const uint64_t rwp = (uint64_t)p * wrow + w0;
+#pragma unroll
+      for (int k = 0; k < HP; k += 2) {
+        Lx::load2(H, rwp + k, hp[k], hp[k + 1]);
+        if (SUB >= kAffine) Lx::load2(F, rwp + k, fp[k], fp[k + 1]);
+        if (SUB == kConvex) Lx::load2(O, rwp + k, op[k], op[k + 1]);
+      }
+      // column s0-1 is the high half of the left thread's last pair, which
+      // the pair layout puts at element s0-1
       int32_t hleft;
       if (t == 0) {
         hleft = D.fc[p];
@@ -242,62 +492,23 @@ __device__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restric
         if (SUB >= kAffine) fa = imax(fa, D.fcF[p]);
         if (SUB == kConvex) fo = imax(fo, D.fcO[p]);
       } else {
-        hleft = Hp[-1];
+        hleft = Lx::elem(H, (uint64_t)p * ld + (uint64_t)s0 - 1);
       }
-      int32_t hp[CPT];
-#pragma unroll
-      for (int k = 0; k < CPT; k += 4) {
-        int4 v = *reinterpret_cast<const int4*>(Hp + k);
-        hp[k] = v.x; hp[k + 1] = v.y; hp[k + 2] = v.z; hp[k + 3] = v.w;
-      }
-#pragma unroll
-      for (int k = 0; k < CPT; ++k) {
-        int32_t dg = (k == 0 ? hleft : hp[k - 1]) + (sc[k] == rc ? m : n);
-        int32_t cand;
-        if (SUB == kLinear) {
-          cand = addmax(hp[k], g, dg);
-        } else {
-          cand = dg;
-        }
-        h[k] = pi == pb ? cand : imax(h[k], cand);
-      }
-      if (SUB >= kAffine) {
-        const int32_t* __restrict__ Fp = F + (uint64_t)p * ld + s0;
-#pragma unroll
-        for (int k = 0; k < CPT; k += 4) {
-          int4 v = *reinterpret_cast<const int4*>(Fp + k);
-          int32_t fv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            int32_t cand = addmax(hp[k + u], g - e, fv[u]) + e;
-            f[k + u] = pi == pb ? cand : imax(f[k + u], cand);
-          }
-        }
-      }
-      if (SUB == kConvex) {
-        const int32_t* __restrict__ Op = O + (uint64_t)p * ld + s0;
-#pragma unroll
-        for (int k = 0; k < CPT; k += 4) {
-          int4 v = *reinterpret_cast<const int4*>(Op + k);
-          int32_t ov[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            int32_t cand = addmax(hp[k + u], q - c, ov[u]) + c;
-            o[k + u] = pi == pb ? cand : imax(o[k + u], cand);
-          }
-        }
-      }
+      accumulate(hp, fp, op, hleft, first);
+      first = false;
     }
+    // NW first column (thread 0)
+    int32_t fci = 0;
     if (t == 0) {
       const bool source = D.row_indeg[i] == 0;
       if (type == kNW) {
         if (SUB == kLinear) {
           fci = (source ? 0 : fl) + g;
         } else {
-          int32_t vF = (source ? g - e : fa) + e;
+          const int32_t vF = (source ? g - e : fa) + e;
           D.fcF[i] = vF;
           if (SUB == kConvex) {
-            int32_t vO = (source ? q - c : fo) + c;
+            const int32_t vO = (source ? q - c : fo) + c;
             D.fcO[i] = vO;
             fci = imax(vF, vO);
           } else {
@@ -307,115 +518,148 @@ __device__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restric
       }
       D.fc[i] = fci;
     }
-    int32_t* __restrict__ Hi = H + (uint64_t)i * ld + s0;
-    // H1 and the stored F/O rows
+    const uint64_t rw = (uint64_t)i * wrow + w0;
     if (SUB >= kAffine) {
-      int32_t* __restrict__ Fi = F + (uint64_t)i * ld + s0;
 #pragma unroll
-      for (int k = 0; k < CPT; k += 4)
-        *reinterpret_cast<int4*>(Fi + k) = make_int4(f[k], f[k + 1], f[k + 2], f[k + 3]);
-      if (SUB == kConvex) {
-        int32_t* __restrict__ Oi = O + (uint64_t)i * ld + s0;
+      for (int k = 0; k < HP; k += 2) {
+        Lx::store2(F, rw + k, f[k], f[k + 1]);
+        if (SUB == kConvex) Lx::store2(O, rw + k, o[k], o[k + 1]);
+      }
 #pragma unroll
-        for (int k = 0; k < CPT; k += 4)
-          *reinterpret_cast<int4*>(Oi + k) = make_int4(o[k], o[k + 1], o[k + 2], o[k + 3]);
+      for (int k = 0; k < HP; ++k)
+        h[k] = SUB == kConvex ? Lx::max3(h[k], f[k], o[k]) : Lx::max(h[k], f[k]);
+    }
+    if (edge_thread) {
 #pragma unroll
-        for (int k = 0; k < CPT; ++k) h[k] = imax3(h[k], f[k], o[k]);
-      } else {
-#pragma unroll
-        for (int k = 0; k < CPT; ++k) h[k] = imax(h[k], f[k]);
+      for (int k = 0; k < HP; ++k) {
+        const uint32_t vm = (s0 + k < L ? 0x0000FFFFu : 0u) | (s0 + HP + k < L ? 0xFFFF0000u : 0u);
+        h[k] = Lx::select(vm, h[k], NEG2);
       }
     }
-    // columns past the read never feed real columns (scans run rightwards)
-#pragma unroll
-    for (int k = 0; k < CPT; ++k)
-      if (s0 + k >= L) h[k] = kNegBig;
-
-    int32_t hs[CPT];
+    P hs[HP], ee[HP], qq[HP];
     if (SUB == kLinear) {
-      int32_t loc[CPT];
-      loc[0] = h[0];
 #pragma unroll
-      for (int k = 1; k < CPT; ++k) loc[k] = addmax(loc[k - 1], g, h[k]);
-      int32_t carry = scan_carry<CPT>(loc[CPT - 1], fci, g, sh);
+      for (int k = 0; k < HP; ++k) hs[k] = h[k];
+      pair_scan<CPT, Lx>(hs, fci, g, sh);
+      if (type == kSW) {
+        const P z = Lx::splat(0);
 #pragma unroll
-      for (int k = 0; k < CPT; ++k) {
-        int32_t hf = addmax(carry, (k + 1) * g, loc[k]);
-        hs[k] = type == kSW ? imax(hf, 0) : hf;
+        for (int k = 0; k < HP; ++k) hs[k] = Lx::max(hs[k], z);
       }
     } else {
-      int32_t qq[CPT];  // Q[s0 + k]
       if (SUB == kConvex) {
-        int32_t loc[CPT];
-        loc[0] = h[0] + q;
+        P x[HP];
 #pragma unroll
-        for (int k = 1; k < CPT; ++k) loc[k] = addmax(loc[k - 1], c, h[k] + q);
-        int32_t carry = scan_carry<CPT>(loc[CPT - 1], fci + q, c, sh);
-        qq[0] = carry;
+        for (int k = 0; k < HP; ++k) x[k] = Lx::add(h[k], q2);
+        // x = Q' (Q of the next column); Q[s0] = Q'[s0-1] is the carry
+        const int32_t qin = pair_scan<CPT, Lx>(x, fci + q, c, sh);
+        qq[0] = Lx::make(qin, Lx::lo(x[HP - 1]));
 #pragma unroll
-        for (int k = 1; k < CPT; ++k) qq[k] = addmax(carry, k * c, loc[k - 1]);
-        int32_t* __restrict__ Qi = Q + (uint64_t)i * ld + s0;
-#pragma unroll
-        for (int k = 0; k < CPT; k += 4)
-          *reinterpret_cast<int4*>(Qi + k) = make_int4(qq[k], qq[k + 1], qq[k + 2], qq[k + 3]);
+        for (int k = 1; k < HP; ++k) qq[k] = x[k - 1];
       }
-      int32_t ee[CPT];  // E[s0 + k]
       {
-        int32_t loc[CPT];
+        P x[HP];
 #pragma unroll
-        for (int k = 0; k < CPT; ++k) {
-          int32_t a = h[k] + g;
-          if (SUB == kConvex && ((s0 + k + 1) % (uint32_t)lanes) == 0) a = imax(a, qq[k] + g);
-          loc[k] = k == 0 ? a : addmax(loc[k - 1], e, a);
+        for (int k = 0; k < HP; ++k) {
+          P a = Lx::add(h[k], g2);
+          if (SUB == kConvex) {
+            const uint32_t bm = (((bmap >> k) & 1u) ? 0x0000FFFFu : 0u) |
+                                (((bmap >> (16 + k)) & 1u) ? 0xFFFF0000u : 0u);
+            a = Lx::max(a, Lx::select(bm, Lx::add(qq[k], g2), NEG2));
+          }
+          x[k] = a;
         }
-        int32_t carry = scan_carry<CPT>(loc[CPT - 1], fci + g, e, sh);
-        ee[0] = carry;
+        const int32_t ein = pair_scan<CPT, Lx>(x, fci + g, e, sh);  // x = E'
+        ee[0] = Lx::make(ein, Lx::lo(x[HP - 1]));
 #pragma unroll
-        for (int k = 1; k < CPT; ++k) ee[k] = addmax(carry, k * e, loc[k - 1]);
-        int32_t* __restrict__ Ei = E + (uint64_t)i * ld + s0;
-#pragma unroll
-        for (int k = 0; k < CPT; k += 4)
-          *reinterpret_cast<int4*>(Ei + k) = make_int4(ee[k], ee[k + 1], ee[k + 2], ee[k + 3]);
+        for (int k = 1; k < HP; ++k) ee[k] = x[k - 1];
       }
 #pragma unroll
-      for (int k = 0; k < CPT; ++k) {
-        int32_t hf = SUB == kConvex ? imax3(h[k], ee[k], qq[k]) : imax(h[k], ee[k]);
-        hs[k] = type == kSW ? imax(hf, 0) : hf;
+      for (int k = 0; k < HP; ++k) {
+        const P hf = SUB == kConvex ? Lx::max3(h[k], ee[k], qq[k]) : Lx::max(h[k], ee[k]);
+        hs[k] = type == kSW ? Lx::max(hf, Lx::splat(0)) : hf;
       }
     }
+    // values of column s0-1 of this row (thread 0: the first column fc)
+    int32_t lH, lE, lQ;
+    from_left3(Lx::hi(hs[HP - 1]), SUB >= kAffine ? Lx::hi(ee[HP - 1]) : 0,
+               SUB == kConvex ? Lx::hi(qq[HP - 1]) : 0, fci, &lH, &lE, &lQ, sh);
+    // horizontal traceback codes
 #pragma unroll
-    for (int k = 0; k < CPT; k += 4)
-      *reinterpret_cast<int4*>(Hi + k) = make_int4(hs[k], hs[k + 1], hs[k + 2], hs[k + 3]);
+    for (int k = 0; k < HP; ++k) {
+      const P Hl = k == 0 ? Lx::make(lH, Lx::lo(hs[HP - 1])) : hs[k - 1];
+      const uint32_t mB = Lx::eq(hs[k], Lx::add(Hl, g2));
+      uint32_t code;
+      if (SUB == kLinear) {
+        code = mB & 0x00010001u;
+      } else {
+        const P El = k == 0 ? Lx::make(lE, Lx::lo(ee[HP - 1])) : ee[k - 1];
+        const P Ele = Lx::add(El, e2);
+        const uint32_t mA = Lx::eq(hs[k], Ele);
+        uint32_t any = mA | mB, ext = mA, run = Lx::eq(ee[k], Ele);
+        if (SUB == kConvex) {
+          const P Ql = k == 0 ? Lx::make(lQ, Lx::lo(qq[HP - 1])) : qq[k - 1];
+          const P Qlc = Lx::add(Ql, c2);
+          const uint32_t mC = Lx::eq(hs[k], Qlc);
+          const uint32_t mD = Lx::eq(hs[k], Lx::add(Hl, q2));
+          any |= mC | mD;
+          ext |= ~mB & mC;
+          run &= Lx::eq(qq[k], Qlc);
+        }
+        code = (any & 0x00010001u) | (ext & 0x00020002u) | (run & 0x00040004u);
+      }
+      const uint16_t two = (uint16_t)((code & 0xFFu) | ((code >> 8) & 0xFF00u));
+      reinterpret_cast<uint16_t*>(CODE + (uint64_t)i * ld)[w0 + k] = two;
+    }
+#pragma unroll
+    for (int k = 0; k < HP; k += 2) Lx::store2(H, rw + k, hs[k], hs[k + 1]);
 
-    // row selection
+    // row selection (strict <: the earliest row wins a tie)
     if (type == kNW) {
-      if (D.row_sink[i] && L - 1 >= s0 && L - 1 < s0 + CPT) {
+      if ((rflags & kRowSink) && owns_last) {
         int32_t v = kNegBig;
 #pragma unroll
-        for (int k = 0; k < CPT; ++k)
-          if (s0 + k == L - 1) v = hs[k];
+        for (int k = 0; k < HP; ++k)
+          if (k == last_k) v = last_hi ? Lx::hi(hs[k]) : Lx::lo(hs[k]);
         if (v > bval) {
           bval = v;
           brow = (int32_t)i;
         }
       }
-    } else if (type == kSW || D.row_sink[i]) {
-      int32_t tm = kNegBig;
+    } else if (type == kSW || (rflags & kRowSink)) {
+      P mx = hs[0];
+      if (edge_thread) {
 #pragma unroll
-      for (int k = 0; k < CPT; ++k)
-        if (s0 + k < L) tm = imax(tm, hs[k]);
+        for (int k = 0; k < HP; ++k) {
+          const uint32_t vm = (s0 + k < L ? 0x0000FFFFu : 0u) | (s0 + HP + k < L ? 0xFFFF0000u : 0u);
+          const P x = Lx::select(vm, hs[k], NEG2);
+          mx = k == 0 ? x : Lx::max(mx, x);
+        }
+      } else {
+#pragma unroll
+        for (int k = 1; k < HP; ++k) mx = Lx::max(mx, hs[k]);
+      }
+      const int32_t tm = s0 < L ? imax(Lx::lo(mx), Lx::hi(mx)) : kNegBig;
       if (tm > bval) {
         bval = tm;
         brow = (int32_t)i;
       }
       if (type == kOV && first_sink < 0) first_sink = (int32_t)i;
     }
+    // this row becomes the registers of row i-1
+#pragma unroll
+    for (int k = 0; k < HP; ++k) {
+      ph[k] = hs[k];
+      if (SUB >= kAffine) pf[k] = f[k];
+      if (SUB == kConvex) po[k] = o[k];
+    }
+    left_prev = t == 0 ? 0 : lH;
     __syncthreads();
   }
 
   // global selection: best value, then the earliest row reaching it
-  int32_t B = block_max(bval, sh);
-  int32_t R = block_min(bval == B && brow >= 0 ? brow : 0x7fffffff, sh);
+  const int32_t B = block_max(bval, sh);
+  const int32_t R = block_min(bval == B && brow >= 0 ? brow : 0x7fffffff, sh);
   int64_t max_i = -1;
   int32_t score = 0;
   if (type == kSW) {
@@ -425,12 +669,12 @@ __device__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restric
     }
   } else if (type == kOV) {
     // _mmxxx_max_value starts from 0: a sink row never scores below 0, and
-    // when no sink row is positive the first sink row wins with score 0.
+    // when no sink row is positive the first sink row wins with score 0
     if (B > 0) {
       max_i = R;
       score = B;
     } else {
-      max_i = first_sink;  // identical in every thread
+      max_i = first_sink;
       score = 0;
     }
   } else {
@@ -444,11 +688,12 @@ __device__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restric
     if (type == kNW) {
       max_j = (int64_t)L - 1;
     } else {
-      const int32_t* Hm = H + (uint64_t)max_i * ld + s0;
+      const uint64_t base = (uint64_t)max_i * ld + s0;
       int32_t jj = 0x7fffffff;
-#pragma unroll
-      for (int k = 0; k < CPT; ++k)
-        if (s0 + k < L && Hm[k] == score && jj == 0x7fffffff) jj = (int32_t)(s0 + k);
+      for (int r = 0; r < CPT && jj == 0x7fffffff; ++r) {
+        const uint32_t j = s0 + r;
+        if (j < L && Lx::elem(H, base + 2 * (r % HP) + r / HP) == score) jj = (int32_t)j;
+      }
       jj = block_min(jj, sh);
       max_j = jj == 0x7fffffff ? -1 : jj;
     }
@@ -459,46 +704,55 @@ __device__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restric
 }
 
 // Traceback from (max_i, max_j) (implementation.hpp:955-1124, 1324-1574,
-// 1826-2121), thread 0.  Pairs are written to `out` in forward order.
-template <int SUB>
-__device__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphView& G,
+// 1826-2121), thread 0.  Diagonal and vertical moves are re-derived from the
+// stored H/F/O rows exactly as the reference does; horizontal moves and the
+// extend_left run come from the per-cell codes.  Pairs are written to `out`
+// in forward order.
+template <int SUB, int CPT, typename T>
+static __device__ __noinline__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphView& G,
                                 const uint8_t* seq, uint32_t L, uint32_t V, int64_t max_i,
                                 int64_t max_j, int32_t* out, uint32_t* n_out) {
+  using Lx = Lanes<T>;
   const uint64_t ld = D.caps.ld;
   const int32_t type = S.type;
   const int32_t m = S.m, n = S.n, g = S.g, e = S.e, q = S.q, c = S.c;
-  const int32_t* H = D.H;
-  const int32_t* F = D.F;
-  const int32_t* E = D.E;
-  const int32_t* O = D.O;
-  const int32_t* Q = D.Q;
+  const void* H = D.H;
+  const void* F = D.F;
+  const void* O = D.O;
+  const uint8_t* CODE = D.code;
+  auto at = [&](const void* M, int64_t row, int64_t col) -> int32_t {
+    return Lx::elem(M, (uint64_t)row * ld + colmap<CPT>((uint64_t)col));
+  };
+  auto code = [&](int64_t row, int64_t col) -> uint8_t {
+    return CODE[(uint64_t)row * ld + colmap<CPT>((uint64_t)col)];
+  };
   int32_t* tb = out;  // written back to front, reversed at the end
   uint64_t np = 0;
   const uint64_t cap = D.aln_cap;
   int64_t i = max_i, j = max_j, prev_i = 0, prev_j = 0;
   uint64_t guard = 0;
   const uint64_t guard_max = 4 * ((uint64_t)V + L) + 64;
-#define EMIT(a, b)                      \
-  do {                                  \
-    if (np >= cap) return kTraceback;   \
-    tb[2 * np] = (a);                   \
-    tb[2 * np + 1] = (b);               \
-    ++np;                               \
+#define EMIT(a, b)                    \
+  do {                                \
+    if (np >= cap) return kTraceback; \
+    tb[2 * np] = (a);                 \
+    tb[2 * np + 1] = (b);             \
+    ++np;                             \
   } while (0)
   while (true) {
     if (++guard > guard_max) return kTraceback;
     if (j == -1 || i == 0) break;
     const uint32_t node = G.rank_to_node[i - 1];
-    const int32_t h = H[(uint64_t)i * ld + j];
+    const int32_t h = at(H, i, j);
     if (type == kSW && h == 0) break;
     const uint32_t pb = D.pred_ptr[i], pe = D.pred_ptr[i + 1];
     const int32_t prf = D.row_char[i] == seq[j] ? m : n;
     bool found = false, ext_left = false, ext_up = false;
     for (uint32_t pi = pb; pi < pe; ++pi) {
-      const uint64_t p = D.preds[pi];
-      const int32_t hd = j ? H[p * ld + j - 1] : D.fc[p];
+      const int64_t p = D.preds[pi];
+      const int32_t hd = j ? at(H, p, j - 1) : D.fc[p];
       if (h == hd + prf) {
-        prev_i = (int64_t)p;
+        prev_i = p;
         prev_j = j - 1;
         found = true;
         break;
@@ -506,27 +760,27 @@ __device__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphVi
     }
     if (!found) {
       for (uint32_t pi = pb; pi < pe; ++pi) {
-        const uint64_t p = D.preds[pi];
-        const int32_t hp = H[p * ld + j];
+        const int64_t p = D.preds[pi];
+        const int32_t hp = at(H, p, j);
         bool take;
         if (SUB == kLinear) {
           take = h == hp + g;
         } else if (SUB == kAffine) {
-          ext_up = h == F[p * ld + j] + e;
+          ext_up = h == at(F, p, j) + e;
           take = ext_up || h == hp + g;
         } else {
-          ext_up = h == F[p * ld + j] + e;
+          ext_up = h == at(F, p, j) + e;
           if (ext_up) {
             take = true;
           } else if (h == hp + g) {
             take = true;
           } else {
-            ext_up = h == O[p * ld + j] + c;
+            ext_up = h == at(O, p, j) + c;
             take = ext_up || h == hp + q;
           }
         }
         if (take) {
-          prev_i = (int64_t)p;
+          prev_i = p;
           prev_j = j;
           found = true;
           break;
@@ -534,29 +788,9 @@ __device__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphVi
       }
     }
     if (!found) {
-      const uint64_t row = (uint64_t)i * ld;
-      const int32_t hl = j ? H[row + j - 1] : D.fc[i];
-      bool take;
-      if (SUB == kLinear) {
-        take = h == hl + g;
-      } else if (SUB == kAffine) {
-        const int32_t el = j ? E[row + j - 1] : D.fc[i];
-        ext_left = h == el + e;
-        take = ext_left || h == hl + g;
-      } else {
-        const int32_t el = j ? E[row + j - 1] : D.fc[i];
-        const int32_t ql = j ? Q[row + j - 1] : D.fc[i];
-        ext_left = h == el + e;
-        if (ext_left) {
-          take = true;
-        } else if (h == hl + g) {
-          take = true;
-        } else {
-          ext_left = h == ql + c;
-          take = ext_left || h == hl + q;
-        }
-      }
-      if (take) {
+      const uint8_t cd = code(i, j);
+      if (cd & kCodeAny) {
+        ext_left = SUB >= kAffine && (cd & kCodeExt);
         prev_i = i;
         prev_j = j - 1;
         found = true;
@@ -566,21 +800,18 @@ __device__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphVi
     i = prev_i;
     j = prev_j;
     if (SUB >= kAffine && ext_left) {
-      const uint64_t row = (uint64_t)i * ld;
       while (true) {
         if (++guard > guard_max) return kTraceback;
         EMIT(-1, (int32_t)j);
         --j;
         if (j == -1) break;
-        if (E[row + j] + e != E[row + j + 1]) break;
-        if (SUB == kConvex && Q[row + j] + c != Q[row + j + 1]) break;
+        if (!(code(i, j + 1) & kCodeRun)) break;
       }
     } else if (SUB >= kAffine && ext_up) {
       while (true) {
         if (++guard > guard_max) return kTraceback;
         const uint32_t un = G.rank_to_node[i - 1];
-        const uint64_t row = (uint64_t)i * ld;
-        const int32_t fv = F[row + j];
+        const int32_t fv = at(F, i, j);
         const uint32_t pb2 = D.pred_ptr[i];
         const uint32_t pe2 = D.row_indeg[i] ? D.pred_ptr[i + 1] : pb2;  // sources: none
         bool stop;
@@ -588,29 +819,30 @@ __device__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphVi
         if (SUB == kAffine) {
           stop = false;
           for (uint32_t pi = pb2; pi < pe2; ++pi) {
-            const uint64_t p = D.preds[pi];
-            stop = fv == H[p * ld + j] + g;
-            if (stop || fv == F[p * ld + j] + e) {
-              prev_i = (int64_t)p;
+            const int64_t p = D.preds[pi];
+            stop = fv == at(H, p, j) + g;
+            if (stop || fv == at(F, p, j) + e) {
+              prev_i = p;
               break;
             }
           }
         } else {
-          const int32_t ov = O[row + j];
+          const int32_t ov = at(O, i, j);
           stop = true;
           for (uint32_t pi = pb2; pi < pe2; ++pi) {
-            const uint64_t p = D.preds[pi];
-            if (fv == F[p * ld + j] + e || ov == O[p * ld + j] + c) {
-              prev_i = (int64_t)p;
+            const int64_t p = D.preds[pi];
+            if (fv == at(F, p, j) + e || ov == at(O, p, j) + c) {
+              prev_i = p;
               stop = false;
               break;
             }
           }
           if (stop) {
             for (uint32_t pi = pb2; pi < pe2; ++pi) {
-              const uint64_t p = D.preds[pi];
-              if (fv == H[p * ld + j] + g || ov == H[p * ld + j] + q) {
-                prev_i = (int64_t)p;
+              const int64_t p = D.preds[pi];
+              const int32_t hp = at(H, p, j);
+              if (fv == hp + g || ov == hp + q) {
+                prev_i = p;
                 break;
               }
             }
@@ -635,7 +867,7 @@ __device__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphVi
         i = 0;
       } else {
         for (uint32_t pi = D.pred_ptr[i]; pi < D.pred_ptr[i + 1]; ++pi) {
-          const uint64_t p = D.preds[pi];
+          const int64_t p = D.preds[pi];
           bool hit;
           if (SUB == kLinear) {
             hit = D.fc[i] == D.fc[p] + g;
@@ -645,7 +877,7 @@ __device__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphVi
             hit = D.fcF[i] == D.fcF[p] + e || D.fcO[i] == D.fcO[p] + c;
           }
           if (hit) {
-            i = (int64_t)p;
+            i = p;
             break;
           }
         }
@@ -654,7 +886,7 @@ __device__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphVi
   }
 #undef EMIT
   for (uint64_t a = 0, b = np ? np - 1 : 0; a < b; ++a, --b) {
-    int32_t x0 = tb[2 * a], x1 = tb[2 * a + 1];
+    const int32_t x0 = tb[2 * a], x1 = tb[2 * a + 1];
     tb[2 * a] = tb[2 * b];
     tb[2 * a + 1] = tb[2 * b + 1];
     tb[2 * b] = x0;

@@ -30,20 +30,26 @@ struct SharedState {
 // Align one read (seq, or its reverse complement staged in D.seq_rc) against
 // the current graph; thread 0 leaves the pairs in `pairs` and returns
 // has_score/score through `ss`.  Every thread must call it.
-template <int SUB, int CPT>
+// T is the arithmetic of the kernel: int16 pairs when every read of the
+// window passes the reference's int16 width rule (implementation.hpp:719-775),
+// int32 otherwise.  An int32 kernel runs int16-width reads with the 16-lane
+// semantics (vector starts of the convex E recurrence, -infinity of the NW
+// row selection), which gives the same results.
+template <int SUB, int CPT, typename T>
 __device__ void read_align(const Scoring& S, const GraphView& G, DpView& D, BlockScratch& sh,
                            SharedState& ss, const uint8_t* seq, uint32_t L, int32_t lanes,
                            int32_t* pairs, int32_t* has, int32_t* score, uint32_t* np) {
   int64_t mi, mj;
   int32_t sc;
-  dp_forward<SUB, CPT>(S, D, seq, L, G.hdr->n_nodes, lanes, sh, &mi, &mj, &sc);
+  const uint32_t V = G.hdr->n_nodes;
+  dp_forward<SUB, CPT, T>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
   if (threadIdx.x == 0) {
     *np = 0;
     *has = 0;
     if (mi >= 0) {
       *has = 1;
       *score = sc;
-      int32_t st = dp_traceback<SUB>(S, D, G, seq, L, G.hdr->n_nodes, mi, mj, pairs, np);
+      const int32_t st = dp_traceback<SUB, CPT, T>(S, D, G, seq, L, V, mi, mj, pairs, np);
       if (st != kOk) ss.status = st;
     }
   }
@@ -53,7 +59,8 @@ __device__ void read_align(const Scoring& S, const GraphView& G, DpView& D, Bloc
 // Checks done before a read's DP (thread 0): mode 0 = empty alignment,
 // 1 = run the DP; status on error.
 __device__ inline void read_prologue(const Scoring& S, const GraphView& G, const DpView& D,
-                                     uint32_t L, uint32_t nthreads_cols, SharedState& ss) {
+                                     uint32_t L, uint32_t nthreads_cols, bool wide_ok,
+                                     SharedState& ss) {
   const uint32_t V = G.hdr->n_nodes;
   ss.status = kOk;
   ss.mode = 0;
@@ -62,6 +69,10 @@ __device__ inline void read_prologue(const Scoring& S, const GraphView& G, const
   int32_t lanes = lanes_for(S, L, V);
   if (!lanes) {
     ss.status = kOverflow;
+    return;
+  }
+  if (lanes == 8 && !wide_ok) {
+    ss.status = kNeedWide;  // rerun the window with the int32 kernel
     return;
   }
   if (L > nthreads_cols || L > D.caps.ld || V + 1 > D.caps.rows ||
@@ -73,12 +84,12 @@ __device__ inline void read_prologue(const Scoring& S, const GraphView& G, const
   ss.mode = 1;
 }
 
-template <int SUB, int CPT>
+template <int SUB, int CPT, typename T>
 __global__ void __launch_bounds__(1024) k_align(Scoring S, GraphView G, DpView D,
                                                 const uint8_t* seq, uint32_t L, ReadOut* out) {
   __shared__ BlockScratch sh;
   __shared__ SharedState ss;
-  if (threadIdx.x == 0) read_prologue(S, G, D, L, blockDim.x * CPT, ss);
+  if (threadIdx.x == 0) read_prologue(S, G, D, L, blockDim.x * CPT, sizeof(T) == 4, ss);
   __syncthreads();
   if (ss.status != kOk || ss.mode == 0) {
     if (threadIdx.x == 0) {
@@ -89,8 +100,8 @@ __global__ void __launch_bounds__(1024) k_align(Scoring S, GraphView G, DpView D
     return;
   }
   dp_build_rows(G, D, sh);
-  read_align<SUB, CPT>(S, G, D, sh, ss, seq, L, ss.lanes, D.aln_a, &ss.has_f, &ss.score_f,
-                       &ss.np_f);
+  read_align<SUB, CPT, T>(S, G, D, sh, ss, seq, L, ss.lanes, D.aln_a, &ss.has_f, &ss.score_f,
+                          &ss.np_f);
   if (threadIdx.x == 0) {
     out->status = ss.status;
     out->has_score = ss.has_f;
@@ -116,12 +127,12 @@ __global__ void k_add(GraphView G, const int32_t* pairs, uint32_t n_pairs, const
 #endif
 
 // One read of a window: align (both strands when asked), choose, add.
-template <int SUB, int CPT>
+template <int SUB, int CPT, typename T>
 __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScratch& sh,
                             SharedState& ss, const uint8_t* seq, uint32_t L,
                             const uint8_t* qual, bool strand, int32_t* out_score,
                             int32_t* out_rev, const int32_t** out_pairs, uint32_t* out_np) {
-  if (threadIdx.x == 0) read_prologue(S, G, D, L, blockDim.x * CPT, ss);
+  if (threadIdx.x == 0) read_prologue(S, G, D, L, blockDim.x * CPT, sizeof(T) == 4, ss);
   __syncthreads();
   if (ss.status != kOk) return;
   const bool dp = ss.mode == 1;
@@ -132,16 +143,16 @@ __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScra
   }
   if (dp) {
     dp_build_rows(G, D, sh);
-    read_align<SUB, CPT>(S, G, D, sh, ss, seq, L, ss.lanes, D.aln_a, &ss.has_f, &ss.score_f,
-                         &ss.np_f);
+    read_align<SUB, CPT, T>(S, G, D, sh, ss, seq, L, ss.lanes, D.aln_a, &ss.has_f, &ss.score_f,
+                            &ss.np_f);
   }
   if (strand) {
     for (uint32_t j = threadIdx.x; j < L; j += blockDim.x)
       D.seq_rc[j] = complement_base(seq[L - 1 - j]);
     __syncthreads();
     if (dp && ss.status == kOk)
-      read_align<SUB, CPT>(S, G, D, sh, ss, D.seq_rc, L, ss.lanes, D.aln_b, &ss.has_r,
-                           &ss.score_r, &ss.np_r);
+      read_align<SUB, CPT, T>(S, G, D, sh, ss, D.seq_rc, L, ss.lanes, D.aln_b, &ss.has_r,
+                              &ss.score_r, &ss.np_r);
   }
   if (threadIdx.x == 0 && ss.status == kOk) {
     // main.cpp:276-301: scores start at 0; keep forward if score >= score_rev
@@ -161,7 +172,7 @@ __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScra
   __syncthreads();
 }
 
-template <int SUB, int CPT>
+template <int SUB, int CPT, typename T>
 __global__ void __launch_bounds__(1024)
     k_align_add(Scoring S, GraphView G, DpView D, const uint8_t* seq, uint32_t L,
                 const uint8_t* qual, int32_t strand, ReadOut* out) {
@@ -170,8 +181,8 @@ __global__ void __launch_bounds__(1024)
   __shared__ const int32_t* s_pairs;
   __shared__ int32_t s_score, s_rev;
   __shared__ uint32_t s_np;
-  window_read<SUB, CPT>(S, G, D, sh, ss, seq, L, qual, strand != 0, &s_score, &s_rev, &s_pairs,
-                        &s_np);
+  window_read<SUB, CPT, T>(S, G, D, sh, ss, seq, L, qual, strand != 0, &s_score, &s_rev,
+                           &s_pairs, &s_np);
   if (threadIdx.x == 0) {
     out->status = ss.status;
     out->score = s_score;
@@ -195,7 +206,7 @@ __global__ void k_consensus(GraphView G, uint8_t* out, uint64_t cap, uint32_t* l
 #endif
 
 // MSA of the window into out[rows * cols]; every thread calls.
-__device__ inline int32_t window_msa(GraphView& G, bool include_consensus, uint8_t* out,
+static __device__ __noinline__ int32_t window_msa(GraphView& G, bool include_consensus, uint8_t* out,
                                      uint64_t cap, uint32_t* rows_out, uint32_t* cols_out,
                                      uint32_t* s_dims) {
   if (threadIdx.x == 0) {
@@ -333,22 +344,28 @@ struct BatchArgs {
   const uint64_t* msa_off;
   uint32_t* msa_rows;
   uint32_t* msa_cols;
-  unsigned long long* cells;
+  unsigned long long* cells;       // sum of read length x graph nodes
+  unsigned long long* pred_cells;  // sum of read length x predecessor entries
 };
 
-template <int SUB, int CPT>
-__global__ void __launch_bounds__(512) k_batch(BatchArgs a) {
+template <int SUB, int CPT, typename T>
+__global__ void __maxnreg__(128) k_batch(BatchArgs a) {
   __shared__ BlockScratch sh;
   __shared__ SharedState ss;
   __shared__ uint32_t s_w, s_dims[2];
   __shared__ const int32_t* s_pairs;
   __shared__ int32_t s_score, s_rev;
   __shared__ uint32_t s_np;
-  GraphView G;
-  DpView D;
-  uint8_t* base = a.arena + a.arena_stride * blockIdx.x;
-  const uint64_t gbytes = graph_layout(base, a.gcaps, &G);
-  dp_layout(base + gbytes, a.dcaps, &D);
+  // the arena views live in shared memory: each phase loads only the
+  // pointers it uses instead of holding ~45 of them in registers
+  __shared__ GraphView G;
+  __shared__ DpView D;
+  if (threadIdx.x == 0) {
+    uint8_t* base = a.arena + a.arena_stride * blockIdx.x;
+    const uint64_t gbytes = graph_layout(base, a.gcaps, &G);
+    dp_layout(base + gbytes, a.dcaps, &D);
+  }
+  __syncthreads();
   Scoring S = a.base;
   while (true) {
     if (threadIdx.x == 0) {
@@ -363,17 +380,24 @@ __global__ void __launch_bounds__(512) k_batch(BatchArgs a) {
     const bool strand = a.win_strand ? a.win_strand[w] != 0 : false;
     __syncthreads();
     int32_t status = kOk;
-    unsigned long long cells = 0;
+    unsigned long long cells = 0, pred_cells = 0;
     for (uint32_t r = a.win_read_off[w]; r < a.win_read_off[w + 1]; ++r) {
       const uint64_t off = a.seq_off[r];
       const uint32_t L = (uint32_t)(a.seq_off[r + 1] - off);
-      cells += (unsigned long long)G.hdr->n_nodes * L * (strand ? 2u : 1u);
-      window_read<SUB, CPT>(S, G, D, sh, ss, a.seqs + off, L, a.quals ? a.quals + off : nullptr,
-                            strand, &s_score, &s_rev, &s_pairs, &s_np);
+      const uint32_t V0 = G.hdr->n_nodes;
+      // predecessor entries of this read's DP: every in-edge, plus row 0
+      // for each source node; known once the rows are built
+      const uint64_t npred_before = V0 ? 1 : 0;
+      cells += (unsigned long long)V0 * L * (strand ? 2u : 1u);
+      window_read<SUB, CPT, T>(S, G, D, sh, ss, a.seqs + off, L,
+                               a.quals ? a.quals + off : nullptr, strand, &s_score, &s_rev,
+                               &s_pairs, &s_np);
       if (ss.status != kOk) {
         status = ss.status;
         break;
       }
+      if (npred_before && ss.mode == 1)
+        pred_cells += (unsigned long long)D.pred_ptr[V0 + 1] * L * (strand ? 2u : 1u);
       if (threadIdx.x == 0) {
         a.read_scores[r] = s_score;
         a.read_rev[r] = (uint8_t)s_rev;
@@ -405,6 +429,7 @@ __global__ void __launch_bounds__(512) k_batch(BatchArgs a) {
     if (threadIdx.x == 0) {
       a.win_status[w] = status;
       if (a.cells) atomicAdd(a.cells, cells);
+      if (a.pred_cells) atomicAdd(a.pred_cells, pred_cells);
     }
     __syncthreads();
   }
@@ -415,51 +440,69 @@ __global__ void __launch_bounds__(512) k_batch(BatchArgs a) {
 
 namespace spoa_gb300 {
 
-// Launch wrappers; each gap model is explicitly instantiated in its own
-// translation unit (inst_*.cu).  cpt must be one of 8, 12, 16, 20, 24, 32.
-#define SPOA_CPT_SWITCH(cpt, LAUNCH) \
-  switch (cpt) {                     \
-    case 8: LAUNCH(8); break;        \
-    case 12: LAUNCH(12); break;      \
-    case 16: LAUNCH(16); break;      \
-    case 20: LAUNCH(20); break;      \
-    case 24: LAUNCH(24); break;      \
-    case 32: LAUNCH(32); break;      \
-    default: return kInvalidArgument; \
+// Launch wrappers; each (gap model, width) pair is explicitly instantiated in
+// its own translation unit (inst_*.cu).  Columns per thread: 8, 12, 16, 20,
+// 24 or 32 for int16 pairs; 8, 12, 16, 24 or 32 for int32 pairs.
+template <typename T>
+__host__ __device__ constexpr bool cpt_supported(int cpt) {
+  return sizeof(T) == 2 ? (cpt == 8 || cpt == 12 || cpt == 16 || cpt == 20 || cpt == 24 || cpt == 32)
+                        : (cpt == 8 || cpt == 12 || cpt == 16 || cpt == 24 || cpt == 32);
+}
+
+#define SPOA_CPT_SWITCH(T, cpt, LAUNCH)                  \
+  if (sizeof(T) == 2) {                                  \
+    switch (cpt) {                                       \
+      case 8: LAUNCH(8); break;                          \
+      case 12: LAUNCH(12); break;                        \
+      case 16: LAUNCH(16); break;                        \
+      case 20: LAUNCH(20); break;                        \
+      case 24: LAUNCH(24); break;                        \
+      case 32: LAUNCH(32); break;                        \
+      default: return kInvalidArgument;                  \
+    }                                                    \
+  } else {                                               \
+    switch (cpt) {                                       \
+      case 8: LAUNCH(8); break;                          \
+      case 12: LAUNCH(12); break;                        \
+      case 16: LAUNCH(16); break;                        \
+      case 24: LAUNCH(24); break;                        \
+      case 32: LAUNCH(32); break;                        \
+      default: return kInvalidArgument;                  \
+    }                                                    \
   }
 
-template <int SUB>
+template <int SUB, typename T>
 int32_t launch_align(int cpt, int nt, const Scoring& S, const GraphView& G, const DpView& D,
                      const uint8_t* seq, uint32_t L, ReadOut* out) {
-#define L_(C) k_align<SUB, C><<<1, nt>>>(S, G, D, seq, L, out)
-  SPOA_CPT_SWITCH(cpt, L_)
+#define L_(C) k_align<SUB, C, T><<<1, nt>>>(S, G, D, seq, L, out)
+  SPOA_CPT_SWITCH(T, cpt, L_)
 #undef L_
   return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
 }
 
-template <int SUB>
+template <int SUB, typename T>
 int32_t launch_align_add(int cpt, int nt, const Scoring& S, const GraphView& G,
                          const DpView& D, const uint8_t* seq, uint32_t L, const uint8_t* qual,
                          int32_t strand, ReadOut* out) {
-#define L_(C) k_align_add<SUB, C><<<1, nt>>>(S, G, D, seq, L, qual, strand, out)
-  SPOA_CPT_SWITCH(cpt, L_)
+#define L_(C) k_align_add<SUB, C, T><<<1, nt>>>(S, G, D, seq, L, qual, strand, out)
+  SPOA_CPT_SWITCH(T, cpt, L_)
 #undef L_
   return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
 }
 
-template <int SUB>
+template <int SUB, typename T>
 int32_t launch_batch(int cpt, int nt, int grid, const BatchArgs& a, cudaStream_t s) {
-#define L_(C) k_batch<SUB, C><<<grid, nt, 0, s>>>(a)
-  SPOA_CPT_SWITCH(cpt, L_)
+#define L_(C) k_batch<SUB, C, T><<<grid, nt, 0, s>>>(a)
+  SPOA_CPT_SWITCH(T, cpt, L_)
 #undef L_
   return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
 }
 
-template <int SUB>
+template <int SUB, typename T>
 int32_t occupancy_batch(int cpt, int nt, int* blocks) {
   cudaError_t err = cudaSuccess;
-#define L_(C) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch<SUB, C>, nt, 0)
-  SPOA_CPT_SWITCH(cpt, L_)
+#define L_(C) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch<SUB, C, T>, nt, 0)
+  SPOA_CPT_SWITCH(T, cpt, L_)
 #undef L_
   if (err != cudaSuccess) {
     cudaGetLastError();
@@ -468,13 +511,13 @@ int32_t occupancy_batch(int cpt, int nt, int* blocks) {
   return kOk;
 }
 
-#define SPOA_GB300_INSTANTIATE(SUB)                                                              \
-  template int32_t launch_align<SUB>(int, int, const Scoring&, const GraphView&, const DpView&, \
-                                     const uint8_t*, uint32_t, ReadOut*);                       \
-  template int32_t launch_align_add<SUB>(int, int, const Scoring&, const GraphView&,            \
-                                         const DpView&, const uint8_t*, uint32_t,               \
-                                         const uint8_t*, int32_t, ReadOut*);                    \
-  template int32_t launch_batch<SUB>(int, int, int, const BatchArgs&, cudaStream_t);            \
-  template int32_t occupancy_batch<SUB>(int, int, int*);
+#define SPOA_GB300_INSTANTIATE(SUB, T)                                                          \
+  template int32_t launch_align<SUB, T>(int, int, const Scoring&, const GraphView&,             \
+                                        const DpView&, const uint8_t*, uint32_t, ReadOut*);     \
+  template int32_t launch_align_add<SUB, T>(int, int, const Scoring&, const GraphView&,         \
+                                            const DpView&, const uint8_t*, uint32_t,            \
+                                            const uint8_t*, int32_t, ReadOut*);                 \
+  template int32_t launch_batch<SUB, T>(int, int, int, const BatchArgs&, cudaStream_t);         \
+  template int32_t occupancy_batch<SUB, T>(int, int, int*);
 
 }  // namespace spoa_gb300

@@ -27,17 +27,21 @@
 #include "poa_kernels.cuh"
 
 namespace spoa_gb300 {
-#define SPOA_EXTERN(SUB)                                                                         \
-  extern template int32_t launch_align<SUB>(int, int, const Scoring&, const GraphView&,         \
-                                            const DpView&, const uint8_t*, uint32_t, ReadOut*); \
-  extern template int32_t launch_align_add<SUB>(int, int, const Scoring&, const GraphView&,     \
-                                                const DpView&, const uint8_t*, uint32_t,        \
-                                                const uint8_t*, int32_t, ReadOut*);             \
-  extern template int32_t launch_batch<SUB>(int, int, int, const BatchArgs&, cudaStream_t);     \
-  extern template int32_t occupancy_batch<SUB>(int, int, int*);
-SPOA_EXTERN(kLinear)
-SPOA_EXTERN(kAffine)
-SPOA_EXTERN(kConvex)
+#define SPOA_EXTERN(SUB, T)                                                                      \
+  extern template int32_t launch_align<SUB, T>(int, int, const Scoring&, const GraphView&,      \
+                                               const DpView&, const uint8_t*, uint32_t,         \
+                                               ReadOut*);                                       \
+  extern template int32_t launch_align_add<SUB, T>(int, int, const Scoring&, const GraphView&,  \
+                                                   const DpView&, const uint8_t*, uint32_t,     \
+                                                   const uint8_t*, int32_t, ReadOut*);          \
+  extern template int32_t launch_batch<SUB, T>(int, int, int, const BatchArgs&, cudaStream_t);  \
+  extern template int32_t occupancy_batch<SUB, T>(int, int, int*);
+SPOA_EXTERN(kLinear, int16_t)
+SPOA_EXTERN(kAffine, int16_t)
+SPOA_EXTERN(kConvex, int16_t)
+SPOA_EXTERN(kLinear, int32_t)
+SPOA_EXTERN(kAffine, int32_t)
+SPOA_EXTERN(kConvex, int32_t)
 #undef SPOA_EXTERN
 }  // namespace spoa_gb300
 
@@ -48,7 +52,8 @@ using namespace spoa_gb300;
 
 namespace {
 
-constexpr int kCpts[] = {8, 12, 16, 20, 24, 32};
+constexpr int kCpts16[] = {8, 12, 16, 20, 24, 32};
+constexpr int kCpts32[] = {8, 12, 16, 24, 32};
 
 #define CU(call)                                \
   do {                                          \
@@ -56,15 +61,23 @@ constexpr int kCpts[] = {8, 12, 16, 20, 24, 32};
     if (err__ != cudaSuccess) return kCuda;     \
   } while (0)
 
-#define SPOA_BY_SUB(sub, fn, ...)                        \
-  ((sub) == kLinear   ? fn<kLinear>(__VA_ARGS__)          \
-   : (sub) == kAffine ? fn<kAffine>(__VA_ARGS__)          \
-   : (sub) == kConvex ? fn<kConvex>(__VA_ARGS__)          \
-                      : (int32_t)kInvalidArgument)
+// fn<gap model, lane type>(...) for a runtime gap model and width
+#define SPOA_BY_SUB(sub, wide, fn, ...)                                                  \
+  ((wide) ? ((sub) == kLinear   ? fn<kLinear, int32_t>(__VA_ARGS__)                      \
+             : (sub) == kAffine ? fn<kAffine, int32_t>(__VA_ARGS__)                      \
+             : (sub) == kConvex ? fn<kConvex, int32_t>(__VA_ARGS__)                      \
+                                : (int32_t)kInvalidArgument)                             \
+          : ((sub) == kLinear   ? fn<kLinear, int16_t>(__VA_ARGS__)                      \
+             : (sub) == kAffine ? fn<kAffine, int16_t>(__VA_ARGS__)                      \
+             : (sub) == kConvex ? fn<kConvex, int16_t>(__VA_ARGS__)                      \
+                                : (int32_t)kInvalidArgument))
 
 // Latency tile: the smallest strip (most threads) that covers L.
-bool latency_tile(uint32_t L, int* cpt, int* nt) {
-  for (int c : kCpts) {
+bool latency_tile(uint32_t L, bool wide, int* cpt, int* nt) {
+  const int* cs = wide ? kCpts32 : kCpts16;
+  const int nc = wide ? 5 : 6;
+  for (int k = 0; k < nc; ++k) {
+    const int c = cs[k];
     uint64_t t = ((uint64_t)(L + c - 1) / c + 31) / 32 * 32;
     if (t == 0) t = 32;
     if (t <= 1024) {
@@ -77,12 +90,15 @@ bool latency_tile(uint32_t L, int* cpt, int* nt) {
 }
 
 // Throughput tile: fewest padded columns, then fewest threads.
-bool throughput_tile(uint32_t L, int* cpt, int* nt) {
+bool throughput_tile(uint32_t L, bool wide, int* cpt, int* nt) {
   uint64_t best = ~0ull;
-  for (int c : kCpts) {
+  const int* cs = wide ? kCpts32 : kCpts16;
+  const int nc = wide ? 5 : 6;
+  for (int k = 0; k < nc; ++k) {
+    const int c = cs[k];
     uint64_t t = ((uint64_t)(L + c - 1) / c + 31) / 32 * 32;
     if (t == 0) t = 32;
-    if (t > 1024) continue;
+    if (t > 512) continue;  // the persistent kernel is capped at 128 registers
     uint64_t cost = t * (uint64_t)c;
     if (cost < best || (cost == best && (int)t < *nt)) {
       best = cost;
@@ -226,9 +242,9 @@ int32_t engine_reserve(spoa_gb300_engine* en, uint32_t rows, uint32_t ld, uint32
 
 
 
-int32_t prepare_read(spoa_gb300_engine* en, const spoa_gb300_graph* g, uint32_t L, int* cpt,
-                     int* nt) {
-  if (!latency_tile(L, cpt, nt)) return kTooLarge;
+int32_t prepare_read(spoa_gb300_engine* en, const spoa_gb300_graph* g, uint32_t L, bool wide,
+                     int* cpt, int* nt) {
+  if (!latency_tile(L, wide, cpt, nt)) return kTooLarge;
   int32_t st = engine_reserve(en, g->h.n_nodes + 1, (uint32_t)(*cpt) * (*nt),
                               g->h.n_edges + g->h.n_nodes + 2);
   if (st) return st;
@@ -324,7 +340,9 @@ int32_t spoa_gb300_engine_prealloc(spoa_gb300_engine* en, uint32_t max_len, uint
   int64_t wc = worst_case(en->S, (int64_t)max_len + 8, (int64_t)max_len * alphabet);
   if (wc < (int64_t)INT32_MIN + 1024) return kOk;
   int cpt, nt;
-  if (!latency_tile(std::max<uint32_t>(max_len, 1), &cpt, &nt)) return kNoMemory;
+  if (!latency_tile(std::max<uint32_t>(max_len, 1), true, &cpt, &nt) &&
+      !latency_tile(std::max<uint32_t>(max_len, 1), false, &cpt, &nt))
+    return kNoMemory;
   uint64_t rows = (uint64_t)max_len * alphabet + 1;
   if (rows > 0xFFFFFFF0ull) return kNoMemory;
   DpCaps c{(uint32_t)rows, (uint32_t)(cpt * nt), (uint32_t)std::min<uint64_t>(3 * rows, 0xFFFFFFF0ull),
@@ -375,13 +393,15 @@ int32_t spoa_gb300_engine_align(spoa_gb300_engine* en, const char* seq, uint32_t
   if (score_written) *score_written = 0;
   if (L > (uint32_t)INT32_MAX) return kTooLarge;
   if (g->h.n_nodes == 0 || L == 0) return kOk;
-  if (!lanes_for(en->S, L, g->h.n_nodes)) return kOverflow;
+  const int32_t lanes = lanes_for(en->S, L, g->h.n_nodes);
+  if (!lanes) return kOverflow;
+  const bool wide = lanes == 8;
   int cpt, nt;
-  int32_t st = prepare_read(en, g, L, &cpt, &nt);
+  int32_t st = prepare_read(en, g, L, wide, &cpt, &nt);
   if (st) return st;
   CU(cudaMemcpy(en->seq.p, seq, L, cudaMemcpyHostToDevice));
-  st = SPOA_BY_SUB(en->S.sub, launch_align, cpt, nt, en->S, g->v, en->dv, en->seq.as<uint8_t>(), L,
-                   en->out.as<ReadOut>());
+  st = SPOA_BY_SUB(en->S.sub, wide, launch_align, cpt, nt, en->S, g->v, en->dv,
+                   en->seq.as<uint8_t>(), L, en->out.as<ReadOut>());
   if (st) return st;
   CU(cudaMemcpy(en->h_out, en->out.p, sizeof(ReadOut), cudaMemcpyDeviceToHost));
   const ReadOut& r = *en->h_out;
@@ -455,11 +475,13 @@ int32_t spoa_gb300_align_add(spoa_gb300_engine* en, spoa_gb300_graph* g, const c
   if (score) *score = 0;
   if (reversed) *reversed = 0;
   if (L == 0) return kOk;
-  if (g->h.n_nodes && !lanes_for(en->S, L, g->h.n_nodes)) return kOverflow;
+  const int32_t lanes = g->h.n_nodes ? lanes_for(en->S, L, g->h.n_nodes) : 16;
+  if (!lanes) return kOverflow;
+  const bool wide = lanes == 8;
   int32_t st = graph_reserve(g, L);
   if (st) return st;
   int cpt, nt;
-  st = prepare_read(en, g, L, &cpt, &nt);
+  st = prepare_read(en, g, L, wide, &cpt, &nt);
   if (st) return st;
   CU(cudaMemcpy(en->seq.p, seq, L, cudaMemcpyHostToDevice));
   const uint8_t* dq = nullptr;
@@ -468,8 +490,8 @@ int32_t spoa_gb300_align_add(spoa_gb300_engine* en, spoa_gb300_graph* g, const c
     CU(cudaMemcpy(en->qual.p, quality, L, cudaMemcpyHostToDevice));
     dq = en->qual.as<uint8_t>();
   }
-  st = SPOA_BY_SUB(en->S.sub, launch_align_add, cpt, nt, en->S, g->v, en->dv, en->seq.as<uint8_t>(),
-                   L, dq, strand, en->out.as<ReadOut>());
+  st = SPOA_BY_SUB(en->S.sub, wide, launch_align_add, cpt, nt, en->S, g->v, en->dv,
+                   en->seq.as<uint8_t>(), L, dq, strand, en->out.as<ReadOut>());
   if (st) return st;
   CU(cudaMemcpy(en->h_out, en->out.p, sizeof(ReadOut), cudaMemcpyDeviceToHost));
   st = graph_refresh(g);
@@ -577,6 +599,7 @@ namespace {
 
 
 struct Pass {
+  bool wide = false;              // int32 kernel
   std::vector<uint32_t> windows;  // window ids in queue order
   GraphCaps gcaps{};
   DpCaps dcaps{};
@@ -634,8 +657,9 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, bool retry) {
     maxreads = std::max(maxreads, b->nreads[w]);
   }
   int cpt = d.columns_per_thread, nt = d.threads_per_window;
-  if (cpt <= 0 || nt <= 0) {
-    if (!throughput_tile(L, &cpt, &nt)) return kTooLarge;
+  if (cpt <= 0 || nt <= 0 || (p->wide && !cpt_supported<int32_t>(cpt)) ||
+      (!p->wide && !cpt_supported<int16_t>(cpt))) {
+    if (!throughput_tile(L, p->wide, &cpt, &nt)) return kTooLarge;
   } else if ((uint64_t)cpt * nt < L) {
     return kTooLarge;
   }
@@ -655,7 +679,7 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, bool retry) {
   const uint64_t stride = align_up(graph_layout(nullptr, gc, &gv), 256) +
                           align_up(dp_layout(nullptr, dc, &dv), 256);
   int blocks = 1;
-  if (SPOA_BY_SUB(b->base.sub, occupancy_batch, cpt, nt, &blocks)) return kCuda;
+  if (SPOA_BY_SUB(b->base.sub, p->wide, occupancy_batch, cpt, nt, &blocks)) return kCuda;
   blocks = std::max(blocks, 1);
   size_t free_b = 0, total_b = 0;
   CU(cudaMemGetInfo(&free_b, &total_b));
@@ -708,6 +732,7 @@ BatchArgs make_args(spoa_gb300_batch* b, const Pass& p, uint8_t* cons, const uin
     a.msa_cols = b->d_msa_cols.as<uint32_t>();
   }
   a.cells = b->d_cells.as<unsigned long long>();
+  a.pred_cells = a.cells + 1;
   return a;
 }
 
@@ -720,7 +745,7 @@ int32_t run_pass(spoa_gb300_batch* b, const Pass& p, cudaStream_t s, bool plain)
   BatchArgs a = make_args(b, p, b->d_cons.as<uint8_t>(), b->d_cons_off.as<uint64_t>());
   if (!plain) {
     ++b->launches;
-    return SPOA_BY_SUB(b->base.sub, launch_batch, p.cpt, p.nt, p.ctas, a, s);
+    return SPOA_BY_SUB(b->base.sub, p.wide, launch_batch, p.cpt, p.nt, p.ctas, a, s);
   }
   for (size_t k = 0; k < p.windows.size(); ++k) {
     BatchArgs one = a;
@@ -728,7 +753,7 @@ int32_t run_pass(spoa_gb300_batch* b, const Pass& p, cudaStream_t s, bool plain)
     one.n_work = 1;
     one.queue = a.queue + k;
     ++b->launches;
-    int32_t st = SPOA_BY_SUB(b->base.sub, launch_batch, p.cpt, p.nt, 1, one, s);
+    int32_t st = SPOA_BY_SUB(b->base.sub, p.wide, launch_batch, p.cpt, p.nt, 1, one, s);
     if (st) return st;
   }
   return kOk;
@@ -740,7 +765,7 @@ int32_t launch_all(spoa_gb300_batch* b, void* stream, bool plain) {
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
-  CU(cudaMemsetAsync(b->d_cells.p, 0, 8, s));
+  CU(cudaMemsetAsync(b->d_cells.p, 0, 16, s));
   CU(cudaEventRecord(e0, s));
   int32_t st = run_pass(b, b->first, s, plain);
   CU(cudaEventRecord(e1, s));
@@ -752,9 +777,12 @@ int32_t launch_all(spoa_gb300_batch* b, void* stream, bool plain) {
   float ms = 0;
   CU(cudaEventElapsedTime(&ms, e0, e1));
   b->kernel_ms = ms;
+  // windows that outgrew the arena or need the int32 width run again with
+  // exact bounds in the int32 kernel
   Pass retry;
+  retry.wide = true;
   for (uint32_t w = 0; w < b->n_windows; ++w)
-    if (status[w] == kCapacity) retry.windows.push_back(w);
+    if (status[w] == kCapacity || status[w] == kNeedWide) retry.windows.push_back(w);
   if (!retry.windows.empty()) {
     st = plan_pass(b, &retry, true);
     if (st) return st;
@@ -775,7 +803,7 @@ int32_t launch_all(spoa_gb300_batch* b, void* stream, bool plain) {
     BatchArgs a = make_args(b, retry, cons2.as<uint8_t>(), off2.as<uint64_t>());
     CU(cudaEventRecord(e0, s));
     ++b->launches;
-    st = SPOA_BY_SUB(b->base.sub, launch_batch, retry.cpt, retry.nt, retry.ctas, a, s);
+    st = SPOA_BY_SUB(b->base.sub, true, launch_batch, retry.cpt, retry.nt, retry.ctas, a, s);
     CU(cudaEventRecord(e1, s));
     if (st) return st;
     // move the retried consensus into the first-pass regions when they fit
@@ -877,7 +905,7 @@ int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* d, spoa_gb300_batch
   if (!st && d->window_type) st = upload(b->d_wtype, d->window_type, b->n_windows, s);
   if (!st && d->window_strand) st = upload(b->d_wstrand, d->window_strand, b->n_windows, s);
   if (!st) st = upload(b->d_cons_off, b->cons_off.data(), b->cons_off.size(), s);
-  if (!st && (b->d_work.ensure(4ull * b->n_windows + 8) || b->d_queue.ensure(4ull * b->n_windows + 8) ||
+  if (!st && (b->d_work.ensure(4ull * b->n_windows + 8) || b->d_cells.ensure(16) || b->d_queue.ensure(4ull * b->n_windows + 8) ||
               b->d_scores.ensure(4ull * b->n_reads + 8) || b->d_rev.ensure(b->n_reads + 8) ||
               b->d_cons.ensure(b->cons_off[b->n_windows] + 8) ||
               b->d_cons_len.ensure(4ull * b->n_windows + 8) ||
@@ -934,7 +962,7 @@ int32_t spoa_gb300_batch_fetch(spoa_gb300_batch* b, spoa_gb300_batch_result* r) 
   b->h_status.resize(W + 1);
   std::vector<uint32_t> lens(W + 1);
   std::vector<char> raw(b->cons_off[W] + 1);
-  uint64_t cells = 0;
+  uint64_t cells2[2] = {0, 0};
   if (R) {
     CU(cudaMemcpy(b->h_scores.data(), b->d_scores.p, 4ull * R, cudaMemcpyDeviceToHost));
     CU(cudaMemcpy(b->h_rev.data(), b->d_rev.p, R, cudaMemcpyDeviceToHost));
@@ -944,7 +972,7 @@ int32_t spoa_gb300_batch_fetch(spoa_gb300_batch* b, spoa_gb300_batch_result* r) 
     CU(cudaMemcpy(lens.data(), b->d_cons_len.p, 4ull * W, cudaMemcpyDeviceToHost));
     CU(cudaMemcpy(raw.data(), b->d_cons.p, b->cons_off[W], cudaMemcpyDeviceToHost));
   }
-  CU(cudaMemcpy(&cells, b->d_cells.p, 8, cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(cells2, b->d_cells.p, 16, cudaMemcpyDeviceToHost));
   b->h_cons.clear();
   b->h_cons_off.assign(W + 1, 0);
   for (uint32_t w = 0; w < W; ++w) {
@@ -995,7 +1023,8 @@ int32_t spoa_gb300_batch_fetch(spoa_gb300_batch* b, spoa_gb300_batch_result* r) 
   r->window_status = b->h_status.data();
   r->consensus = b->h_cons.data();
   r->consensus_off = b->h_cons_off.data();
-  r->cells = cells;
+  r->cells = cells2[0];
+  r->pred_cells = cells2[1];
   r->kernel_ms = b->kernel_ms;
   r->threads_per_window = b->first.nt;
   r->columns_per_thread = b->first.cpt;
