@@ -63,11 +63,27 @@ def parse():
     return ap.parse_args()
 
 
+def shard_start(n_per_rank: int, rank: int) -> int:
+    """First window id of a rank: ranks own disjoint, equally sized ranges of
+    independent windows (weak scaling; no data crosses ranks)."""
+    return rank * n_per_rank
+
+
+def max_over_ranks(value: float, dist, device: str) -> float:
+    """The step time every rank reports is the maximum over ranks."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload(name: str, n_override: int, rank: int):
     """Returns (windows, type, params, per-window types, strand flags, config)."""
     if name == "batch_10k":
         n = n_override or 10000
-        wins = synth.batch_windows(n, start=rank * n)
+        wins = synth.batch_windows(n, start=shard_start(n, rank))
         typ, params = synth.SCORING["batch_10k"]
         cfg = {"workload": "batch_10k: 10,000 polishing windows, L~U[450,550], depth U[10,60], "
                            "8% error, 20% truncated reads, OV convex 5/-4/-8/-6/-10/-4",
@@ -75,7 +91,7 @@ def workload(name: str, n_override: int, rank: int):
         return wins, typ, params, None, None, cfg
     if name == "uneven_2k":
         n = n_override or 2000
-        wins = synth.uneven_windows(n, start=rank * n)
+        wins = synth.uneven_windows(n, start=shard_start(n, rank))
         _, params = synth.SCORING["uneven_2k"]
         cfg = {"workload": "uneven_2k: 2,000 windows, L log-uniform [100,5000], depth U[5,100], "
                            "NW/OV per window, strand-ambiguous, affine 5/-4/-8/-6", "windows": n}
@@ -267,11 +283,7 @@ def main():
     barrier()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
-    step_s = kernel_ms / 1e3 / args.steps
-    if dist is not None:
-        t = torch.tensor([step_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_s = float(t.item())
+    step_s = max_over_ranks(kernel_ms / 1e3 / args.steps, dist, "cuda")
     total_windows = n_windows * world
     value = total_windows / step_s
     cells, pred_cells = res.cells, res.pred_cells
