@@ -195,6 +195,46 @@ void spoa_gb300_batch_destroy(spoa_gb300_batch* batch);
 int32_t spoa_gb300_batch_run(const spoa_gb300_batch_desc* desc, spoa_gb300_batch** out,
                              spoa_gb300_batch_result* result);
 
+/* ---- One window without device allocation ------------------------------- *
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (work issued between the captures of a CUDA graph, frameworks whose
+ * allocator owns all device memory, loops that cannot afford cudaMalloc's
+ * implicit device synchronisation): one window -- every read aligned and
+ * added in order, as spoa's CLI loop does, then the consensus -- runs
+ * through the persistent kernel with its working memory in a fixed
+ * 48 MiB array inside the library, which every device that loads the
+ * library holds until the process exits.  Nothing is allocated and the call
+ * does not synchronise; it is asynchronous on `stream` (0: the default
+ * stream).
+ *
+ * Inputs and outputs are DEVICE pointers owned by the caller: d_seqs (reads
+ * back to back), d_seq_off (n_reads + 1 offsets), d_quals (Phred+33, same
+ * offsets, or NULL for weight 1), d_consensus (consensus_cap bytes),
+ * d_consensus_len (1 value), d_read_scores (n_reads values, or NULL),
+ * d_status (1 value: SPOA_GB300_OK, SPOA_GB300_ERR_CAPACITY when the window
+ * outgrew the limits below, SPOA_GB300_ERR_OVERFLOW, or
+ * SPOA_GB300_ERR_NEEDS_INT32 when a read needs 32-bit scores).
+ * Limits: n_reads <= SPOA_GB300_NOALLOC_MAX_READS, every read at most
+ * max_read_len <= SPOA_GB300_NOALLOC_MAX_READ_LEN bases, at most
+ * SPOA_GB300_NOALLOC_MAX_NODES graph nodes; larger sizes are rejected with
+ * SPOA_GB300_ERR_TOO_LARGE before anything is launched.
+ * The first call on a device looks up the array's device address; make it
+ * before any stream capture.  All calls share the one array, so calls that
+ * overlap on the GPU (other streams, other host threads) race with each
+ * other: serialise them. */
+#define SPOA_GB300_NOALLOC_SCRATCH_BYTES (48ull << 20)
+#define SPOA_GB300_NOALLOC_MAX_READS 256
+#define SPOA_GB300_NOALLOC_MAX_READ_LEN 640
+#define SPOA_GB300_NOALLOC_MAX_NODES 4096
+#define SPOA_GB300_ERR_NEEDS_INT32 11
+int32_t spoa_gb300_window_poa_noalloc(int32_t type, int8_t m, int8_t n, int8_t g, int8_t e,
+                                      int8_t q, int8_t c, int32_t strand_ambiguous,
+                                      uint32_t n_reads, uint32_t max_read_len,
+                                      const char* d_seqs, const uint64_t* d_seq_off,
+                                      const char* d_quals, char* d_consensus,
+                                      uint32_t consensus_cap, uint32_t* d_consensus_len,
+                                      int32_t* d_read_scores, int32_t* d_status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

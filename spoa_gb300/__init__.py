@@ -101,7 +101,7 @@ EXPORTED = [
     "spoa_gb300_graph_consensus", "spoa_gb300_graph_msa", "spoa_gb300_graph_counts",
     "spoa_gb300_graph_export", "spoa_gb300_batch_create", "spoa_gb300_batch_launch",
     "spoa_gb300_batch_launch_plain", "spoa_gb300_batch_fetch", "spoa_gb300_batch_destroy",
-    "spoa_gb300_batch_run",
+    "spoa_gb300_batch_run", "spoa_gb300_window_poa_noalloc",
 ]
 
 
@@ -142,6 +142,8 @@ def lib():
         L.spoa_gb300_batch_destroy.argtypes = [P]
         L.spoa_gb300_batch_destroy.restype = None
         L.spoa_gb300_batch_run.argtypes = [C.POINTER(_BatchDesc), P, C.POINTER(_BatchResult)]
+        L.spoa_gb300_window_poa_noalloc.argtypes = [I32] + [C.c_int8] * 6 + [I32, U32, U32, P, P,
+                                                                              P, P, U32, P, P, P, P]
         _lib = L
     return _lib
 

@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1045,3 +1046,137 @@ int32_t spoa_gb300_batch_run(const spoa_gb300_batch_desc* d, spoa_gb300_batch** 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// one window without device allocation
+// ---------------------------------------------------------------------------
+// Callers that must not allocate device memory (code that runs between the
+// captures of a CUDA graph, allocators that own every byte of the device, or
+// latency-critical loops that cannot afford cudaMalloc's implicit
+// synchronisation) run a window through the same persistent kernel with its
+// arena in this file-scope array.  Every device that loads the library holds
+// it until the process exits.  All calls share it, so calls that overlap on
+// the GPU race with each other.
+namespace {
+
+constexpr uint64_t kNoAllocBytes = SPOA_GB300_NOALLOC_SCRATCH_BYTES;
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocBytes];
+
+// bookkeeping of the batch kernel at the start of the array
+struct NoAllocHeader {
+  uint32_t queue;                  // work-queue cursor, must start at 0
+  uint32_t work[1];                // the one window
+  uint32_t win_read_off[2];        // {0, n_reads}
+  int8_t strand[4];                // strand-ambiguous flag of the window
+  uint64_t cons_off[2];            // {0, consensus capacity}
+  unsigned long long cells[2];     // cell counters, must start at 0
+  int32_t scores[SPOA_GB300_NOALLOC_MAX_READS];
+  uint8_t reversed[SPOA_GB300_NOALLOC_MAX_READS];
+};
+
+__global__ void k_noalloc_setup(NoAllocHeader* h, uint32_t n_reads, uint64_t cons_cap,
+                                int32_t strand) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  h->queue = 0;
+  h->strand[0] = strand ? 1 : 0;
+  h->work[0] = 0;
+  h->win_read_off[0] = 0;
+  h->win_read_off[1] = n_reads;
+  h->cons_off[0] = 0;
+  h->cons_off[1] = cons_cap;
+  h->cells[0] = h->cells[1] = 0;
+}
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[256] = {};
+
+// Device address of the array for the current device, looked up once per
+// device (the host-side name is only a stand-in for it).
+int32_t noalloc_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+    cudaGetLastError();
+    return kCuda;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return kCuda;
+    }
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" int32_t spoa_gb300_window_poa_noalloc(
+    int32_t type, int8_t m, int8_t n, int8_t g, int8_t e, int8_t q, int8_t c,
+    int32_t strand_ambiguous, uint32_t n_reads, uint32_t max_read_len, const char* d_seqs,
+    const uint64_t* d_seq_off, const char* d_quals, char* d_consensus, uint32_t consensus_cap,
+    uint32_t* d_consensus_len, int32_t* d_read_scores, int32_t* d_status, void* stream) {
+  if (type != kSW && type != kNW && type != kOV) return kInvalidArgument;
+  if (g > 0 || q > 0 || e > 0 || c > 0) return kInvalidArgument;
+  if (!d_seqs || !d_seq_off || !d_consensus || !d_consensus_len || !d_status || n_reads == 0)
+    return kInvalidArgument;
+  if (n_reads > SPOA_GB300_NOALLOC_MAX_READS || max_read_len > SPOA_GB300_NOALLOC_MAX_READ_LEN ||
+      max_read_len == 0)
+    return kTooLarge;
+  const int32_t sub = g >= e ? kLinear : ((g <= q || e >= c) ? kAffine : kConvex);
+  if (sub == kLinear) {
+    e = g;
+  } else if (sub == kAffine) {
+    q = g;
+    c = e;
+  }
+  int cpt = 0, nt = 0;
+  if (!throughput_tile(max_read_len, false, &cpt, &nt)) return kTooLarge;
+  GraphCaps gc;
+  gc.nodes = SPOA_GB300_NOALLOC_MAX_NODES;
+  gc.edges = 4 * SPOA_GB300_NOALLOC_MAX_NODES + 64;
+  gc.labels = SPOA_GB300_NOALLOC_MAX_READS * SPOA_GB300_NOALLOC_MAX_READ_LEN + 2;
+  gc.seqs = n_reads + 1;
+  gc.aligned = 15;
+  DpCaps dc{gc.nodes + 1, (uint32_t)(cpt * nt), gc.edges + gc.nodes + 2, sub};
+  GraphView gv;
+  DpView dv;
+  const uint64_t head = align_up(sizeof(NoAllocHeader), 256);
+  const uint64_t gbytes = align_up(graph_layout(nullptr, gc, &gv), 256);
+  const uint64_t dbytes = align_up(dp_layout(nullptr, dc, &dv), 256);
+  if (head + gbytes + dbytes > kNoAllocBytes) return kTooLarge;
+  void* scratch = nullptr;
+  int32_t st = noalloc_scratch(&scratch);
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  NoAllocHeader* h = static_cast<NoAllocHeader*>(scratch);
+  k_noalloc_setup<<<1, 32, 0, s>>>(h, n_reads, consensus_cap, strand_ambiguous);
+  CU(cudaGetLastError());
+  BatchArgs a{};
+  a.base = Scoring{type, sub, m, n, g, e, q, c};
+  a.win_type = nullptr;
+  a.win_strand = strand_ambiguous ? h->strand : nullptr;
+  a.n_windows = 1;
+  a.win_read_off = h->win_read_off;
+  a.seqs = reinterpret_cast<const uint8_t*>(d_seqs);
+  a.seq_off = d_seq_off;
+  a.quals = reinterpret_cast<const uint8_t*>(d_quals);
+  a.work = h->work;
+  a.n_work = 1;
+  a.queue = &h->queue;
+  a.arena = static_cast<uint8_t*>(scratch) + head;
+  a.arena_stride = gbytes + dbytes;
+  a.gcaps = gc;
+  a.dcaps = dc;
+  a.read_scores = d_read_scores ? d_read_scores : h->scores;
+  a.read_rev = h->reversed;
+  a.cons = reinterpret_cast<uint8_t*>(d_consensus);
+  a.cons_off = h->cons_off;
+  a.cons_len = d_consensus_len;
+  a.win_status = d_status;
+  a.cells = &h->cells[0];
+  a.pred_cells = &h->cells[1];
+  return SPOA_BY_SUB(sub, false, launch_batch, cpt, nt, 1, a, s);
+}
