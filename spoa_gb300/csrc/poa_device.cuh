@@ -51,6 +51,10 @@ enum : int32_t { kLinear = 0, kAffine = 1, kConvex = 2 };
 struct Scoring {
   int32_t type, sub;
   int32_t m, n, g, e, q, c;
+  // INT16_MIN in both 16-bit lanes.  Read from memory at run time so the
+  // compiler cannot fold it: max3(a, b, min16x2) is one DPX instruction,
+  // while a two-input 16x2 max compiles to a slower sequence.
+  uint32_t min16x2 = 0x80008000u;
 };
 
 __host__ __device__ inline uint64_t align_up(uint64_t x, uint64_t a) {
@@ -78,13 +82,18 @@ struct GraphView {
   uint32_t *in_first, *in_last, *out_first, *out_last, *in_deg;
   uint8_t* n_aligned;
   uint32_t* aligned;  // [nodes * caps.aligned]
+  // per node: x = in-degree | aligned count << 16, y/z/w = the first three
+  // in-edge tails in insertion order (one 16-byte load per DFS step)
+  uint4* nrec;
   uint32_t *rank_to_node, *node_to_rank;
   uint32_t *e_tail, *e_head, *e_next_in, *e_next_out, *e_lab_first, *e_lab_last;
   int64_t* e_weight;
   uint32_t *lab_seq, *lab_next;
   uint32_t* seq_begin;
   uint32_t* consensus;
-  uint8_t *marks, *ignored;
+  // DFS state of the topological sort: per 32 nodes three words (in
+  // progress, done, ignored), interleaved so one node's bits share a line
+  uint32_t* sort_bits;
   uint32_t* stack;
   int64_t* cscore;
   uint32_t *cpred, *column;
@@ -113,6 +122,7 @@ __host__ __device__ inline uint64_t graph_layout(uint8_t* base, const GraphCaps&
   v->in_deg = reinterpret_cast<uint32_t*>(take(4 * N));
   v->n_aligned = take(N);
   v->aligned = reinterpret_cast<uint32_t*>(take(4 * N * c.aligned));
+  v->nrec = reinterpret_cast<uint4*>(take(16 * N));
   v->rank_to_node = reinterpret_cast<uint32_t*>(take(4 * N));
   v->node_to_rank = reinterpret_cast<uint32_t*>(take(4 * N));
   v->e_tail = reinterpret_cast<uint32_t*>(take(4 * E));
@@ -126,8 +136,7 @@ __host__ __device__ inline uint64_t graph_layout(uint8_t* base, const GraphCaps&
   v->lab_next = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.labels));
   v->seq_begin = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.seqs));
   v->consensus = reinterpret_cast<uint32_t*>(take(4 * N));
-  v->marks = take(N);
-  v->ignored = take(N);
+  v->sort_bits = reinterpret_cast<uint32_t*>(take(12 * ((N + 31) / 32)));
   v->stack = reinterpret_cast<uint32_t*>(take(4 * v->stack_cap));
   v->cscore = reinterpret_cast<int64_t*>(take(8 * N));
   v->cpred = reinterpret_cast<uint32_t*>(take(4 * N));
@@ -146,11 +155,14 @@ struct DpCaps {
 };
 
 struct DpView {
-  // H/F/O rows in "pair layout": thread t's strip of CPT columns is stored as
+  // H/F/O rows in "pair layout": thread t's strip of CPT columns is held as
   // CPT/2 pairs, pair k = (column t*CPT + k, column t*CPT + CPT/2 + k), one
   // pair per 32-bit word (int16 lanes) or per 64-bit word (int32 lanes).
-  // Element index of column j: t*CPT + 2*(r % (CPT/2)) + r / (CPT/2) with
-  // t = j / CPT, r = j % CPT.  Capacity is sized for 4-byte elements.
+  // Pair k of thread t (of nt) is pair word (k/2)*2*nt + 2*t + k%2 of the
+  // row, so pairs k, k+1 of all threads are contiguous and every row access
+  // of the forward pass is a fully coalesced warp access (colmap<CPT>).  The
+  // code plane uses the same element index with one byte per element.
+  // Capacity is sized for 4-byte elements.
   void *H, *F, *O;
   uint8_t* code;           // per cell: horizontal traceback class + E/Q run bit
   uint32_t *pred_ptr, *preds, *row_indeg;
@@ -270,6 +282,7 @@ __device__ inline int64_t g_add_node(GraphView& G, uint32_t code) {
   G.in_first[id] = G.in_last[id] = G.out_first[id] = G.out_last[id] = kNone;
   G.in_deg[id] = 0;
   G.n_aligned[id] = 0;
+  G.nrec[id] = make_uint4(0, kNone, kNone, kNone);
   return id;
 }
 
@@ -310,7 +323,14 @@ __device__ inline int g_add_edge(GraphView& G, uint32_t tail, uint32_t head, uin
   G.out_last[tail] = e;
   if (G.in_last[head] != kNone) G.e_next_in[G.in_last[head]] = e; else G.in_first[head] = e;
   G.in_last[head] = e;
-  G.in_deg[head] += 1;
+  const uint32_t d = G.in_deg[head];
+  G.in_deg[head] = d + 1;
+  uint4 r = G.nrec[head];
+  r.x = (r.x & 0xFFFF0000u) | min(d + 1, 0xFFFFu);
+  if (d == 0) r.y = tail;
+  if (d == 1) r.z = tail;
+  if (d == 2) r.w = tail;
+  G.nrec[head] = r;
   return 0;
 }
 
@@ -330,77 +350,108 @@ __device__ inline int64_t g_add_sequence(GraphView& G, const uint8_t* seq, const
   return (int64_t)G.hdr->n_nodes - (end - begin);
 }
 
-// Graph::TopologicalSort (graph.cpp:249-303)
-static __device__ __noinline__ int g_topo_sort(GraphView& G) {
+// Graph::TopologicalSort (graph.cpp:249-303): the reference's iterative DFS
+// over in-edges and aligned nodes, with its mark states (0 new, 1 in
+// progress, 2 done) and ignored flags held as bitmaps in the graph arena.
+// Every thread clears the bitmaps and prefetches the node records into L1,
+// then thread 0 runs the DFS.  Returns 0, or -1 when the stack or the guard
+// runs out (identical in every thread).
+static __device__ __noinline__ int g_topo_sort_cta(GraphView& G, int* s_ret) {
   const uint32_t nn = G.hdr->n_nodes;
-  for (uint32_t i = 0; i < nn; ++i) {
-    G.marks[i] = 0;
-    G.ignored[i] = 0;
-  }
-  uint64_t sp = 0;
-  uint32_t rank = 0;
-  const uint32_t K = G.caps.aligned;
-  // every iteration pops or pushes; pushes are bounded by the stack size
-  uint64_t guard = 0;
-  const uint64_t guard_max = 4 * G.stack_cap + 4 * (uint64_t)nn + 16;
-  for (uint32_t s = 0; s < nn; ++s) {
-    if (G.marks[s] != 0) continue;
-    G.stack[sp++] = s;
-    while (sp) {
-      if (++guard > guard_max) return -1;
-      uint32_t curr = G.stack[sp - 1];
-      bool valid = true;
-      if (G.marks[curr] != 2) {
-        for (uint32_t e = G.in_first[curr]; e != kNone; e = G.e_next_in[e]) {
-          uint32_t t = G.e_tail[e];
-          if (G.marks[t] != 2) {
-            if (sp >= G.stack_cap) return -1;
-            G.stack[sp++] = t;
-            valid = false;
-          }
-        }
-        const uint32_t na = G.n_aligned[curr];
-        const uint32_t* al = G.aligned + (uint64_t)curr * K;
-        if (!G.ignored[curr]) {
-          for (uint32_t k = 0; k < na; ++k) {
-            uint32_t a = al[k];
-            if (G.marks[a] != 2) {
-              if (sp >= G.stack_cap) return -1;
-              G.stack[sp++] = a;
-              G.ignored[a] = 1;
-              valid = false;
+  uint32_t* __restrict__ bits = G.sort_bits;
+  const uint32_t words = 3 * ((nn + 31) / 32);
+  for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) bits[w] = 0;
+  for (uint32_t v = threadIdx.x * 8; v < nn; v += blockDim.x * 8)
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(G.nrec + v));
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    auto bit = [&](uint32_t v, uint32_t kind) { return (bits[3 * (v >> 5) + kind] >> (v & 31)) & 1u; };
+    auto set = [&](uint32_t v, uint32_t kind) { bits[3 * (v >> 5) + kind] |= 1u << (v & 31); };
+    constexpr uint32_t kBusy = 0, kDone = 1, kIgn = 2;
+    uint32_t* __restrict__ stack = G.stack;
+    uint64_t sp = 0;
+    auto push = [&](uint32_t v) -> bool {
+      if (sp >= G.stack_cap) return false;
+      stack[sp++] = v;
+      return true;
+    };
+    uint32_t rank = 0;
+    const uint32_t K = G.caps.aligned;
+    // every iteration pops or pushes; pushes are bounded by the stack size
+    uint64_t guard = 0;
+    const uint64_t guard_max = 4 * G.stack_cap + 4 * (uint64_t)nn + 16;
+    int rc = 0;
+    for (uint32_t s = 0; s < nn && rc == 0; ++s) {
+      if (bit(s, kDone) || bit(s, kBusy)) continue;
+      push(s);
+      while (sp) {
+        if (++guard > guard_max) { rc = -1; break; }
+        const uint32_t curr = stack[sp - 1];
+        bool valid = true;
+        if (!bit(curr, kDone)) {
+          const uint4 r = G.nrec[curr];
+          const uint32_t deg = r.x & 0xFFFFu, na = r.x >> 16;
+          // in-edge tails in insertion order: three from the record, the
+          // rest from the edge list
+          if (deg > 0 && !bit(r.y, kDone)) { if (!push(r.y)) { rc = -1; break; } valid = false; }
+          if (deg > 1 && !bit(r.z, kDone)) { if (!push(r.z)) { rc = -1; break; } valid = false; }
+          if (deg > 2 && !bit(r.w, kDone)) { if (!push(r.w)) { rc = -1; break; } valid = false; }
+          if (deg > 3) {
+            uint32_t e = G.in_first[curr];
+            for (int k = 0; k < 3 && e != kNone; ++k) e = G.e_next_in[e];
+            for (; e != kNone; e = G.e_next_in[e]) {
+              const uint32_t tl = G.e_tail[e];
+              if (!bit(tl, kDone)) { if (!push(tl)) { rc = -1; break; } valid = false; }
             }
+            if (rc) break;
           }
-        }
-        if (valid) {
-          G.marks[curr] = 2;
-          if (!G.ignored[curr]) {
-            G.rank_to_node[rank] = curr;
-            G.node_to_rank[curr] = rank++;
+          const uint32_t* al = G.aligned + (uint64_t)curr * K;
+          const bool ign = bit(curr, kIgn);
+          if (!ign) {
             for (uint32_t k = 0; k < na; ++k) {
-              G.rank_to_node[rank] = al[k];
-              G.node_to_rank[al[k]] = rank++;
+              const uint32_t a = al[k];
+              if (!bit(a, kDone)) {
+                if (!push(a)) { rc = -1; break; }
+                set(a, kIgn);
+                valid = false;
+              }
             }
+            if (rc) break;
           }
-        } else {
-          G.marks[curr] = 1;
+          if (valid) {
+            set(curr, kDone);
+            if (!ign) {
+              G.rank_to_node[rank] = curr;
+              G.node_to_rank[curr] = rank++;
+              for (uint32_t k = 0; k < na; ++k) {
+                G.rank_to_node[rank] = al[k];
+                G.node_to_rank[al[k]] = rank++;
+              }
+            }
+          } else {
+            set(curr, kBusy);
+          }
         }
+        if (valid) --sp;
       }
-      if (valid) --sp;
     }
+    *s_ret = (rc == 0 && rank == nn) ? 0 : -1;
   }
-  return rank == nn ? 0 : -1;
+  __syncthreads();
+  return *s_ret;
 }
 
 __device__ inline int g_link_aligned(GraphView& G, uint32_t a, uint32_t b) {
   const uint32_t K = G.caps.aligned;
   if (G.n_aligned[a] >= K) return -1;
   G.aligned[(uint64_t)a * K + G.n_aligned[a]++] = b;
+  G.nrec[a].x = (G.nrec[a].x & 0xFFFFu) | ((uint32_t)G.n_aligned[a] << 16);
   return 0;
 }
 
-// Graph::AddAlignment (graph.cpp:155-247).  pairs: n (node id | -1,
-// position | -1).  Weights: w[] or the constant wconst.
+// Graph::AddAlignment (graph.cpp:155-247) without its final
+// TopologicalSort, which the caller runs with the whole CTA
+// (g_topo_sort_cta).  pairs: n (node id | -1, position | -1).
 static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32_t* pairs, uint32_t n_pairs,
                                           const uint8_t* seq, uint32_t len, const WeightSrc& w) {
   GraphHeader* h = G.hdr;
@@ -420,7 +471,7 @@ static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32
     int64_t b = g_add_sequence(G, seq, w, 0, len);
     if (b < -1) return kCapacity;
     G.seq_begin[h->n_seqs++] = (uint32_t)b;
-    return g_topo_sort(G) ? kCapacity : kOk;
+    return kOk;  // the caller re-sorts (g_topo_sort_cta)
   }
   int32_t first_valid = -1, last_valid = -1;
   for (uint32_t k = 0; k < n_pairs; ++k) {
@@ -488,7 +539,7 @@ static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32
       return kCapacity;
   }
   G.seq_begin[h->n_seqs++] = (uint32_t)begin;
-  return g_topo_sort(G) ? kCapacity : kOk;
+  return kOk;  // the caller re-sorts (g_topo_sort_cta)
 }
 
 // ---------------------------------------------------------------------------

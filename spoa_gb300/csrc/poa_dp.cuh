@@ -180,8 +180,9 @@ static __device__ __noinline__ void dp_build_rows(const GraphView& G, DpView& D,
 // max/add is one DPX or SIMD instruction for both columns; used when the
 // reference's width rule picks int16 (16 lanes).  Lanes<int32_t>: two
 // registers, scalar DPX instructions; used for the int32 width (8 lanes).
-// Comparison masks have the same format in both: 0xFFFF in the low half for
-// the first column, 0xFFFF0000 for the second.
+// Select masks have the same format in both: 0xFFFF in the low half for the
+// first column, 0xFFFF0000 for the second; equality tests (eqb) return bit 15
+// for the first column and bit 31 for the second.
 template <typename T>
 struct Lanes;
 
@@ -198,7 +199,15 @@ struct Lanes<int16_t> {
   __device__ __forceinline__ static int32_t lo(P a) { return (int32_t)(int16_t)(a.v & 0xFFFFu); }
   __device__ __forceinline__ static int32_t hi(P a) { return (int32_t)(int16_t)(a.v >> 16); }
   __device__ __forceinline__ static P add(P a, P b) { return {__vadd2(a.v, b.v)}; }
-  __device__ __forceinline__ static P max(P a, P b) { return {__vmaxs2(a.v, b.v)}; }
+  // max(a, b) as one DPX instruction; nz must be INT16_MIN in both lanes,
+  // held in a register (Scoring::min16x2)
+  __device__ __forceinline__ static P max(P a, P b, uint32_t nz) {
+    return {__vimax3_s16x2(a.v, b.v, nz)};
+  }
+  // max(a, b, c, 0)
+  __device__ __forceinline__ static P max3_relu(P a, P b, P c) {
+    return {__vimax3_s16x2_relu(a.v, b.v, c.v)};
+  }
   __device__ __forceinline__ static P max3(P a, P b, P c) {
     return {__vimax3_s16x2(a.v, b.v, c.v)};
   }
@@ -206,9 +215,26 @@ struct Lanes<int16_t> {
   __device__ __forceinline__ static P addmax(P a, P b, P c) {
     return {__viaddmax_s16x2(a.v, b.v, c.v)};
   }
-  __device__ __forceinline__ static uint32_t eq(P a, P b) { return __vcmpeq2(a.v, b.v); }
+  // Equality per lane as bit 15 (low) and bit 31 (high): a lane of x = a ^ b
+  // is zero iff the values are equal; for a non-zero lane either x has its
+  // top bit set or x + 0x7FFF does.  Three full-rate instructions (xor,
+  // 16x2 add, one three-input logic op).
+  __device__ __forceinline__ static uint32_t eqb(P a, P b) {
+    const uint32_t x = a.v ^ b.v;
+    return ~(__vadd2(x, 0x7FFF7FFFu) | x) & 0x80008000u;
+  }
   __device__ __forceinline__ static P select(uint32_t m, P a, P b) {
     return {(a.v & m) | (b.v & ~m)};
+  }
+  // Substitution score of a pair of read characters (16-bit lanes holding
+  // bytes) against row character rc2: m where equal, n elsewhere.  A lane of
+  // (x ^ rc2) - 1 is 0xFFFF iff the characters are equal and below 0x00FF
+  // otherwise; prmt replicates the sign of its high byte over the lane.
+  __device__ __forceinline__ static P profile(uint32_t chars2, uint32_t rc2, P m2, P n2) {
+    const uint32_t y = __vadd2(chars2 ^ rc2, 0xFFFFFFFFu);
+    uint32_t mask;
+    asm("prmt.b32 %0, %1, 0, 0xBB99;" : "=r"(mask) : "r"(y));
+    return select(mask, m2, n2);
   }
   // 2 pairs per 8-byte access
   __device__ __forceinline__ static void load2(const void* base, uint64_t w, P& a, P& b) {
@@ -235,8 +261,11 @@ struct Lanes<int32_t> {
   __device__ __forceinline__ static int32_t lo(P a) { return a.l; }
   __device__ __forceinline__ static int32_t hi(P a) { return a.h; }
   __device__ __forceinline__ static P add(P a, P b) { return {a.l + b.l, a.h + b.h}; }
-  __device__ __forceinline__ static P max(P a, P b) {
+  __device__ __forceinline__ static P max(P a, P b, uint32_t) {
     return {a.l > b.l ? a.l : b.l, a.h > b.h ? a.h : b.h};
+  }
+  __device__ __forceinline__ static P max3_relu(P a, P b, P c) {
+    return {__vimax3_s32_relu(a.l, b.l, c.l), __vimax3_s32_relu(a.h, b.h, c.h)};
   }
   __device__ __forceinline__ static P max3(P a, P b, P c) {
     return {__vimax3_s32(a.l, b.l, c.l), __vimax3_s32(a.h, b.h, c.h)};
@@ -244,11 +273,15 @@ struct Lanes<int32_t> {
   __device__ __forceinline__ static P addmax(P a, P b, P c) {
     return {__viaddmax_s32(a.l, b.l, c.l), __viaddmax_s32(a.h, b.h, c.h)};
   }
-  __device__ __forceinline__ static uint32_t eq(P a, P b) {
-    return (a.l == b.l ? 0x0000FFFFu : 0u) | (a.h == b.h ? 0xFFFF0000u : 0u);
+  __device__ __forceinline__ static uint32_t eqb(P a, P b) {
+    return (a.l == b.l ? 0x00008000u : 0u) | (a.h == b.h ? 0x80000000u : 0u);
   }
   __device__ __forceinline__ static P select(uint32_t m, P a, P b) {
     return {(m & 0xFFFFu) ? a.l : b.l, (m & 0xFFFF0000u) ? a.h : b.h};
+  }
+  __device__ __forceinline__ static P profile(uint32_t chars2, uint32_t rc2, P m2, P n2) {
+    return {(chars2 & 0xFFFFu) == (rc2 & 0xFFFFu) ? m2.l : n2.l,
+            (chars2 >> 16) == (rc2 >> 16) ? m2.h : n2.h};
   }
   __device__ __forceinline__ static void load2(const void* base, uint64_t w, P& a, P& b) {
     int4 x = reinterpret_cast<const int4*>(base)[w >> 1];
@@ -263,11 +296,14 @@ struct Lanes<int32_t> {
   }
 };
 
-// Element index of column j in a pair-layout row (see DpView).
+// Element index of column j in a row of a CTA of nt threads (see DpView):
+// column j is lane r / (CPT/2) of pair k = r % (CPT/2) of thread t = j / CPT
+// (r = j % CPT), and pair k of thread t is pair word
+// (k / 2) * 2 * nt + 2 * t + k % 2.
 template <int CPT>
-__host__ __device__ __forceinline__ uint64_t colmap(uint64_t j) {
-  const uint64_t t = j / CPT, r = j % CPT;
-  return t * CPT + 2 * (r % (CPT / 2)) + r / (CPT / 2);
+__host__ __device__ __forceinline__ uint64_t colmap(uint64_t j, uint64_t nt) {
+  const uint64_t t = j / CPT, r = j % CPT, k = r % (CPT / 2);
+  return 2 * ((k >> 1) * 2 * nt + 2 * t + (k & 1)) + r / (CPT / 2);
 }
 
 // Value of thread t-1 (thread 0 gets `fill`), for three values at once.
@@ -331,7 +367,7 @@ constexpr uint8_t kCodeAny = 1, kCodeExt = 2, kCodeRun = 4;
 // Forward pass + row selection + max_j (identical in every thread on
 // return).  T = int16_t for the 16-lane width, int32_t for the 8-lane one.
 template <int SUB, int CPT, typename T>
-__device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restrict__ seq,
+__device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restrict__ seq,
                            uint32_t L, uint32_t V, int32_t lanes, BlockScratch& sh,
                            int64_t* out_max_i, int64_t* out_max_j, int32_t* out_score) {
   using Lx = Lanes<T>;
@@ -342,7 +378,10 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
   const uint32_t s0 = t * CPT;
   const uint64_t ld = D.caps.ld;        // elements per row
   const uint64_t wrow = ld / 2;         // pair words per row
-  const uint64_t w0 = (uint64_t)t * HP; // this thread's first pair word
+  // pairs k and k+1 (k even) of this thread: pair words w0 + (k/2) * st2
+  // and the next; the warp's accesses to them are contiguous
+  const uint64_t w0 = 2 * (uint64_t)t;
+  const uint64_t st2 = 2 * (uint64_t)blockDim.x;
   const int32_t type = S.type;
   const int32_t m = S.m, n = S.n, g = S.g, e = S.e, q = S.q, c = S.c;
   const int32_t NEGW = lanes == 8 ? (INT32_MIN + 1024) : (INT16_MIN + 1024);
@@ -351,18 +390,35 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
   void* __restrict__ O = D.O;
   uint8_t* __restrict__ CODE = D.code;
   const P NEG2 = Lx::splat(Lx::kNeg);
+  const uint32_t NZ = S.min16x2;  // neutral operand of Lx::max
   const P m2 = Lx::splat(m), n2 = Lx::splat(n);
   const P g2 = Lx::splat(g), e2 = Lx::splat(e), q2 = Lx::splat(q), c2 = Lx::splat(c);
   const P ge2 = Lx::splat(g - e), qc2 = Lx::splat(q - c);
   const bool edge_thread = s0 + CPT > L;  // strip reaches past the read
 
-  // read characters as 16-bit lanes (0xFFFF past the read never matches)
-  L16::P sq[HP];
+  // read characters, 4 per register: byte b of sq8[k/4] is column s0+k of
+  // the low half-strip (k = 4*(k/4) + b), sqh8 the same for the high half;
+  // columns past the read hold 0xFF (whatever they match only feeds columns
+  // past the read)
+  uint32_t sq8[(HP + 3) / 4], sqh8[(HP + 3) / 4];
 #pragma unroll
-  for (int k = 0; k < HP; ++k) {
-    uint32_t jl = s0 + k, jh = s0 + HP + k;
-    sq[k] = L16::make(jl < L ? seq[jl] : 0xFFFF, jh < L ? seq[jh] : 0xFFFF);
+  for (int k4 = 0; k4 < (HP + 3) / 4; ++k4) {
+    uint32_t lo = 0, hi = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const uint32_t k = k4 * 4 + b;
+      const uint32_t jl = s0 + k, jh = s0 + HP + k;
+      lo |= (k < HP && jl < L ? (uint32_t)seq[jl] : 0xFFu) << (8 * b);
+      hi |= (k < HP && jh < L ? (uint32_t)seq[jh] : 0xFFu) << (8 * b);
+    }
+    sq8[k4] = lo;
+    sqh8[k4] = hi;
   }
+  // the two characters of pair k as 16-bit lanes
+  auto sq = [&](int k) -> L16::P {
+    return L16::P{__byte_perm(sq8[k / 4], sqh8[k / 4], (uint32_t)(k % 4) | (0x4u + k % 4) << 8) &
+                  0x00FF00FFu};
+  };
   // convex: columns whose E' input also takes Q (vector starts of the
   // reference, (col + 1) % lanes == 0), as a bitmap (bit k low, 16+k high)
   uint32_t bmap = 0;
@@ -398,9 +454,10 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
   }
 #pragma unroll
   for (int k = 0; k < HP; k += 2) {
-    Lx::store2(H, w0 + k, ph[k], ph[k + 1]);
-    if (SUB >= kAffine) Lx::store2(F, w0 + k, pf[k], pf[k + 1]);
-    if (SUB == kConvex) Lx::store2(O, w0 + k, po[k], po[k + 1]);
+    const uint64_t wk = w0 + (k / 2) * st2;
+    Lx::store2(H, wk, ph[k], ph[k + 1]);
+    if (SUB >= kAffine) Lx::store2(F, wk, pf[k], pf[k + 1]);
+    if (SUB == kConvex) Lx::store2(O, wk, po[k], po[k + 1]);
   }
   int32_t left_prev;  // row i-1 at column s0-1 (thread 0: its first column)
   {
@@ -435,28 +492,28 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
     const uint32_t pb = D.pred_ptr[i], pe = D.pred_ptr[i + 1];
     const uint8_t rc = D.row_char[i];
     const L16::P rc2 = L16::splat(rc);
-    P h[HP], f[HP], o[HP];
+    // Over the predecessors only maxima are taken: the diagonal source
+    // max_p H_p[j-1] (hd), for linear gaps the vertical max_p H_p[j] (f),
+    // for affine/convex max_p max(H_p + g - e, F_p) (f) and
+    // max_p max(H_p + q - c, O_p) (o).  The substitution score and the gap
+    // extension are the same for every predecessor and are added once per
+    // row; max_p(x_p) + s = max_p(x_p + s) exactly (no value wraps: the width
+    // rule keeps every finite value and the -infinity margin in range).
+    P hd[HP], f[HP], o[HP];
     int32_t fl = kNegBig, fa = kNegBig, fo = kNegBig;
-    // candidates of one predecessor row, max-accumulated into h/f/o (the
-    // forward pass takes the maximum over predecessors, so their order only
-    // matters to the traceback, which keeps the reference's order)
+    // the predecessor order only matters to the traceback, which keeps the
+    // reference's order
     auto accumulate = [&](const P* hp, const P* fp, const P* op, int32_t hleft, bool first) {
 #pragma unroll
       for (int k = 0; k < HP; ++k) {
         const P left = k == 0 ? Lx::make(hleft, Lx::lo(hp[HP - 1])) : hp[k - 1];
-        const uint32_t mt = L16::eq(sq[k], rc2);
-        const P d = Lx::add(left, Lx::select(mt, m2, n2));
+        hd[k] = first ? left : Lx::max(hd[k], left, NZ);
         if (SUB == kLinear) {
-          const P cand = Lx::addmax(hp[k], g2, d);
-          h[k] = first ? cand : Lx::max(h[k], cand);
+          f[k] = first ? hp[k] : Lx::max(f[k], hp[k], NZ);
         } else {
-          h[k] = first ? d : Lx::max(h[k], d);
-          const P fc_ = Lx::add(Lx::addmax(hp[k], ge2, fp[k]), e2);
-          f[k] = first ? fc_ : Lx::max(f[k], fc_);
-          if (SUB == kConvex) {
-            const P oc_ = Lx::add(Lx::addmax(hp[k], qc2, op[k]), c2);
-            o[k] = first ? oc_ : Lx::max(o[k], oc_);
-          }
+          f[k] = first ? Lx::addmax(hp[k], ge2, fp[k]) : Lx::max3(f[k], Lx::add(hp[k], ge2), fp[k]);
+          if (SUB == kConvex)
+            o[k] = first ? Lx::addmax(hp[k], qc2, op[k]) : Lx::max3(o[k], Lx::add(hp[k], qc2), op[k]);
         }
       }
     };
@@ -479,12 +536,13 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
       const uint64_t rwp = (uint64_t)p * wrow + w0;
 #pragma unroll
       for (int k = 0; k < HP; k += 2) {
-        Lx::load2(H, rwp + k, hp[k], hp[k + 1]);
-        if (SUB >= kAffine) Lx::load2(F, rwp + k, fp[k], fp[k + 1]);
-        if (SUB == kConvex) Lx::load2(O, rwp + k, op[k], op[k + 1]);
+        const uint64_t wk = rwp + (k / 2) * st2;
+        Lx::load2(H, wk, hp[k], hp[k + 1]);
+        if (SUB >= kAffine) Lx::load2(F, wk, fp[k], fp[k + 1]);
+        if (SUB == kConvex) Lx::load2(O, wk, op[k], op[k + 1]);
       }
-      // column s0-1 is the high half of the left thread's last pair, which
-      // the pair layout puts at element s0-1
+      // column s0-1: the high lane of the left thread's last pair (HP-1,
+      // odd), pair word (HP/2 - 1) * st2 + w0 - 1
       int32_t hleft;
       if (t == 0) {
         hleft = D.fc[p];
@@ -492,7 +550,7 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
         if (SUB >= kAffine) fa = imax(fa, D.fcF[p]);
         if (SUB == kConvex) fo = imax(fo, D.fcO[p]);
       } else {
-        hleft = Lx::elem(H, (uint64_t)p * ld + (uint64_t)s0 - 1);
+        hleft = Lx::elem(H, (uint64_t)p * ld + 2 * ((HP / 2 - 1) * st2 + w0 - 1) + 1);
       }
       accumulate(hp, fp, op, hleft, first);
       first = false;
@@ -519,15 +577,28 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
       D.fc[i] = fci;
     }
     const uint64_t rw = (uint64_t)i * wrow + w0;
+    P h[HP];
+#pragma unroll
+    for (int k = 0; k < HP; ++k) {
+      const P d = Lx::add(hd[k], Lx::profile(sq(k).v, rc2.v, m2, n2));
+      if (SUB == kLinear) {
+        h[k] = Lx::addmax(f[k], g2, d);
+      } else {
+        f[k] = Lx::add(f[k], e2);
+        if (SUB == kConvex) {
+          o[k] = Lx::add(o[k], c2);
+          h[k] = Lx::max3(d, f[k], o[k]);
+        } else {
+          h[k] = Lx::max(d, f[k], NZ);
+        }
+      }
+    }
     if (SUB >= kAffine) {
 #pragma unroll
       for (int k = 0; k < HP; k += 2) {
-        Lx::store2(F, rw + k, f[k], f[k + 1]);
-        if (SUB == kConvex) Lx::store2(O, rw + k, o[k], o[k + 1]);
+        Lx::store2(F, rw + (k / 2) * st2, f[k], f[k + 1]);
+        if (SUB == kConvex) Lx::store2(O, rw + (k / 2) * st2, o[k], o[k + 1]);
       }
-#pragma unroll
-      for (int k = 0; k < HP; ++k)
-        h[k] = SUB == kConvex ? Lx::max3(h[k], f[k], o[k]) : Lx::max(h[k], f[k]);
     }
     if (edge_thread) {
 #pragma unroll
@@ -544,7 +615,7 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
       if (type == kSW) {
         const P z = Lx::splat(0);
 #pragma unroll
-        for (int k = 0; k < HP; ++k) hs[k] = Lx::max(hs[k], z);
+        for (int k = 0; k < HP; ++k) hs[k] = Lx::max(hs[k], z, NZ);
       }
     } else {
       if (SUB == kConvex) {
@@ -561,13 +632,13 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
         P x[HP];
 #pragma unroll
         for (int k = 0; k < HP; ++k) {
-          P a = Lx::add(h[k], g2);
           if (SUB == kConvex) {
             const uint32_t bm = (((bmap >> k) & 1u) ? 0x0000FFFFu : 0u) |
                                 (((bmap >> (16 + k)) & 1u) ? 0xFFFF0000u : 0u);
-            a = Lx::max(a, Lx::select(bm, Lx::add(qq[k], g2), NEG2));
+            x[k] = Lx::addmax(h[k], g2, Lx::select(bm, Lx::add(qq[k], g2), NEG2));
+          } else {
+            x[k] = Lx::add(h[k], g2);
           }
-          x[k] = a;
         }
         const int32_t ein = pair_scan<CPT, Lx>(x, fci + g, e, sh);  // x = E'
         ee[0] = Lx::make(ein, Lx::lo(x[HP - 1]));
@@ -576,43 +647,52 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
       }
 #pragma unroll
       for (int k = 0; k < HP; ++k) {
-        const P hf = SUB == kConvex ? Lx::max3(h[k], ee[k], qq[k]) : Lx::max(h[k], ee[k]);
-        hs[k] = type == kSW ? Lx::max(hf, Lx::splat(0)) : hf;
+        if (SUB == kConvex)
+          hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], qq[k]) : Lx::max3(h[k], ee[k], qq[k]);
+        else
+          hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], ee[k]) : Lx::max(h[k], ee[k], NZ);
       }
     }
     // values of column s0-1 of this row (thread 0: the first column fc)
     int32_t lH, lE, lQ;
     from_left3(Lx::hi(hs[HP - 1]), SUB >= kAffine ? Lx::hi(ee[HP - 1]) : 0,
                SUB == kConvex ? Lx::hi(qq[HP - 1]) : 0, fci, &lH, &lE, &lQ, sh);
-    // horizontal traceback codes
+    // horizontal traceback codes (equality bits at 15 / 31 of each pair);
+    // the codes of pairs k, k+1 go out as one 32-bit word
+    uint32_t two_prev = 0;
 #pragma unroll
     for (int k = 0; k < HP; ++k) {
       const P Hl = k == 0 ? Lx::make(lH, Lx::lo(hs[HP - 1])) : hs[k - 1];
-      const uint32_t mB = Lx::eq(hs[k], Lx::add(Hl, g2));
+      const uint32_t mB = Lx::eqb(hs[k], Lx::add(Hl, g2));
       uint32_t code;
       if (SUB == kLinear) {
-        code = mB & 0x00010001u;
+        code = mB >> 15;
       } else {
         const P El = k == 0 ? Lx::make(lE, Lx::lo(ee[HP - 1])) : ee[k - 1];
         const P Ele = Lx::add(El, e2);
-        const uint32_t mA = Lx::eq(hs[k], Ele);
-        uint32_t any = mA | mB, ext = mA, run = Lx::eq(ee[k], Ele);
+        const uint32_t mA = Lx::eqb(hs[k], Ele);
+        uint32_t any = mA | mB, ext = mA, run = Lx::eqb(ee[k], Ele);
         if (SUB == kConvex) {
           const P Ql = k == 0 ? Lx::make(lQ, Lx::lo(qq[HP - 1])) : qq[k - 1];
           const P Qlc = Lx::add(Ql, c2);
-          const uint32_t mC = Lx::eq(hs[k], Qlc);
-          const uint32_t mD = Lx::eq(hs[k], Lx::add(Hl, q2));
+          const uint32_t mC = Lx::eqb(hs[k], Qlc);
+          const uint32_t mD = Lx::eqb(hs[k], Lx::add(Hl, q2));
           any |= mC | mD;
           ext |= ~mB & mC;
-          run &= Lx::eq(qq[k], Qlc);
+          run &= Lx::eqb(qq[k], Qlc);
         }
-        code = (any & 0x00010001u) | (ext & 0x00020002u) | (run & 0x00040004u);
+        code = (any >> 15) | ((ext & 0x80008000u) >> 14) | (run >> 13);
       }
-      const uint16_t two = (uint16_t)((code & 0xFFu) | ((code >> 8) & 0xFF00u));
-      reinterpret_cast<uint16_t*>(CODE + (uint64_t)i * ld)[w0 + k] = two;
+      // bytes 0 and 2 of code: the codes of the pair's two columns
+      if (k & 1) {
+        reinterpret_cast<uint32_t*>(CODE + (uint64_t)i * ld)[(w0 + (k / 2) * st2) >> 1] =
+            __byte_perm(two_prev, code, 0x6420u);
+      } else {
+        two_prev = code;
+      }
     }
 #pragma unroll
-    for (int k = 0; k < HP; k += 2) Lx::store2(H, rw + k, hs[k], hs[k + 1]);
+    for (int k = 0; k < HP; k += 2) Lx::store2(H, rw + (k / 2) * st2, hs[k], hs[k + 1]);
 
     // row selection (strict <: the earliest row wins a tie)
     if (type == kNW) {
@@ -633,11 +713,11 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
         for (int k = 0; k < HP; ++k) {
           const uint32_t vm = (s0 + k < L ? 0x0000FFFFu : 0u) | (s0 + HP + k < L ? 0xFFFF0000u : 0u);
           const P x = Lx::select(vm, hs[k], NEG2);
-          mx = k == 0 ? x : Lx::max(mx, x);
+          mx = k == 0 ? x : Lx::max(mx, x, NZ);
         }
       } else {
 #pragma unroll
-        for (int k = 1; k < HP; ++k) mx = Lx::max(mx, hs[k]);
+        for (int k = 1; k < HP; ++k) mx = Lx::max(mx, hs[k], NZ);
       }
       const int32_t tm = s0 < L ? imax(Lx::lo(mx), Lx::hi(mx)) : kNegBig;
       if (tm > bval) {
@@ -688,11 +768,11 @@ __device__ __forceinline__ void dp_forward(const Scoring& S, DpView& D, const ui
     if (type == kNW) {
       max_j = (int64_t)L - 1;
     } else {
-      const uint64_t base = (uint64_t)max_i * ld + s0;
+      const uint64_t base = (uint64_t)max_i * ld;
       int32_t jj = 0x7fffffff;
       for (int r = 0; r < CPT && jj == 0x7fffffff; ++r) {
         const uint32_t j = s0 + r;
-        if (j < L && Lx::elem(H, base + 2 * (r % HP) + r / HP) == score) jj = (int32_t)j;
+        if (j < L && Lx::elem(H, base + colmap<CPT>(j, blockDim.x)) == score) jj = (int32_t)j;
       }
       jj = block_min(jj, sh);
       max_j = jj == 0x7fffffff ? -1 : jj;
@@ -720,11 +800,12 @@ static __device__ __noinline__ int32_t dp_traceback(const Scoring& S, const DpVi
   const void* F = D.F;
   const void* O = D.O;
   const uint8_t* CODE = D.code;
+  const uint64_t nt = blockDim.x;  // the forward pass's CTA width
   auto at = [&](const void* M, int64_t row, int64_t col) -> int32_t {
-    return Lx::elem(M, (uint64_t)row * ld + colmap<CPT>((uint64_t)col));
+    return Lx::elem(M, (uint64_t)row * ld + colmap<CPT>((uint64_t)col, nt));
   };
   auto code = [&](int64_t row, int64_t col) -> uint8_t {
-    return CODE[(uint64_t)row * ld + colmap<CPT>((uint64_t)col)];
+    return CODE[(uint64_t)row * ld + colmap<CPT>((uint64_t)col, nt)];
   };
   int32_t* tb = out;  // written back to front, reversed at the end
   uint64_t np = 0;

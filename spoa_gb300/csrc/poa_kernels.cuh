@@ -120,11 +120,20 @@ __global__ void k_graph_reset(GraphView G) {
 #ifdef SPOA_GB300_HOST_TU
 __global__ void k_add(GraphView G, const int32_t* pairs, uint32_t n_pairs, const uint8_t* seq,
                       uint32_t L, const uint32_t* w, const uint8_t* qual, int32_t* status) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  WeightSrc ws{w, qual, L, 0u, 1u};
-  *status = g_add_alignment(G, pairs, n_pairs, seq, L, ws);
+  __shared__ int s_st;
+  if (threadIdx.x == 0) {
+    WeightSrc ws{w, qual, L, 0u, 1u};
+    s_st = g_add_alignment(G, pairs, n_pairs, seq, L, ws);
+  }
+  __syncthreads();
+  if (s_st == kOk && L > 0 && g_topo_sort_cta(G, &s_st) != 0) {
+    if (threadIdx.x == 0) s_st = kCapacity;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *status = s_st;
 }
 #endif
+
 
 // One read of a window: align (both strands when asked), choose, add.
 template <int SUB, int CPT, typename T>
@@ -170,6 +179,11 @@ __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScra
     *out_np = np;
   }
   __syncthreads();
+  if (ss.status == kOk && L > 0) {
+    int* ret = &ss.pad;
+    if (g_topo_sort_cta(G, ret) != 0 && threadIdx.x == 0) ss.status = kCapacity;
+    __syncthreads();
+  }
 }
 
 template <int SUB, int CPT, typename T>

@@ -194,6 +194,7 @@ int32_t graph_reserve(spoa_gb300_graph* g, uint32_t len) {
     CP(in_deg, N, 4);
     CP(n_aligned, N, 1);
     CP(aligned, N * K, 4);
+    CP(nrec, N, 16);
     CP(rank_to_node, N, 4);
     CP(node_to_rank, N, 4);
     CP(e_tail, E, 4);
@@ -672,7 +673,7 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, bool retry) {
   gc.edges = (uint32_t)std::min<uint64_t>(maxsum + 2, 4 * nodes + 64);
   gc.labels = (uint32_t)(maxsum + 2);
   gc.seqs = maxreads + 1;
-  gc.aligned = retry ? 63 : 15;
+  gc.aligned = retry ? 63 : 4;  // DNA columns hold at most 5 codes; more reruns
   DpCaps dc{(uint32_t)nodes + 1, (uint32_t)(cpt * nt), gc.edges + (uint32_t)nodes + 2,
             b->base.sub};
   GraphView gv;
