@@ -152,6 +152,7 @@ struct DpCaps {
   uint32_t ld;    // columns (>= threads * columns-per-thread)
   uint32_t preds; // in-edges + rows
   int32_t sub;
+  int32_t esize = 4;  // bytes per DP element: 2 when only int16 kernels use it
 };
 
 struct DpView {
@@ -160,13 +161,19 @@ struct DpView {
   // pair per 32-bit word (int16 lanes) or per 64-bit word (int32 lanes).
   // Pair k of thread t (of nt) is pair word (k/2)*2*nt + 2*t + k%2 of the
   // row, so pairs k, k+1 of all threads are contiguous and every row access
-  // of the forward pass is a fully coalesced warp access (colmap<CPT>).  The
-  // code plane uses the same element index with one byte per element.
-  // Capacity is sized for 4-byte elements.
-  void *H, *F, *O;
-  uint8_t* code;           // per cell: horizontal traceback class + E/Q run bit
+  // of the forward pass is a fully coalesced warp access (colmap<CPT>).
+  // Elements are caps.esize bytes (2 for arenas only int16 kernels use).
+  // H, F (affine, convex), O (convex) and the in-row gap rows E (affine,
+  // convex) and Q (convex) as the recurrences computed them
+  void *H, *F, *O, *E, *Q;
   uint32_t *pred_ptr, *preds, *row_indeg;
   uint8_t *row_char, *row_sink;
+  // per row, what the forward pass needs in one 16-byte load: x = first
+  // predecessor entry, y = predecessor count (saturated at 0xFFFF) |
+  // flags << 16 | character << 24,
+  // z / w = the first two predecessors other than the previous row (kNone
+  // when absent)
+  uint4* rowrec;
   int32_t *fc, *fcF, *fcO;
   int32_t *aln_a, *aln_b;  // traceback outputs, 2 ints per pair
   uint8_t* seq_rc;         // reverse complement / staging of the read
@@ -184,15 +191,18 @@ __host__ __device__ inline uint64_t dp_layout(uint8_t* base, const DpCaps& c, Dp
   const uint64_t cells = (uint64_t)c.rows * c.ld;
   v->caps = c;
   v->aln_cap = (uint64_t)c.rows + c.ld + 16;
-  v->H = take(4 * cells);
-  v->F = c.sub >= kAffine ? take(4 * cells) : nullptr;
-  v->O = c.sub == kConvex ? take(4 * cells) : nullptr;
-  v->code = c.sub >= kAffine ? take(cells) : take(cells);
+  const uint64_t mbytes = (uint64_t)c.esize * cells;
+  v->H = take(mbytes);
+  v->F = c.sub >= kAffine ? take(mbytes) : nullptr;
+  v->O = c.sub == kConvex ? take(mbytes) : nullptr;
+  v->E = c.sub >= kAffine ? take(mbytes) : nullptr;
+  v->Q = c.sub == kConvex ? take(mbytes) : nullptr;
   v->pred_ptr = reinterpret_cast<uint32_t*>(take(4 * ((uint64_t)c.rows + 1)));
   v->preds = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.preds));
   v->row_indeg = reinterpret_cast<uint32_t*>(take(4 * (uint64_t)c.rows));
   v->row_char = take(c.rows);
   v->row_sink = take(c.rows);
+  v->rowrec = reinterpret_cast<uint4*>(take(16 * (uint64_t)c.rows));
   v->fc = reinterpret_cast<int32_t*>(take(4 * (uint64_t)c.rows));
   v->fcF = reinterpret_cast<int32_t*>(take(4 * (uint64_t)c.rows));
   v->fcO = reinterpret_cast<int32_t*>(take(4 * (uint64_t)c.rows));

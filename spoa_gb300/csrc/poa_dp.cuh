@@ -120,7 +120,10 @@ __device__ __forceinline__ int32_t scan_carry(int32_t agg, int32_t init, int32_t
   return t == 0 ? init : ex + (t - 1) * D;
 }
 
-constexpr uint8_t kRowSink = 1, kRowPrevPred = 2;
+// row flags: sink node; the previous row is a predecessor; source node (row
+// 0 is its only predecessor); more than two predecessors besides the
+// previous row
+constexpr uint8_t kRowSink = 1, kRowPrevPred = 2, kRowSource = 4, kRowMore = 8;
 
 // Builds the rank-ordered predecessor lists of the graph into the DP arena:
 // row i = rank + 1; preds of a source row = {0}.
@@ -155,19 +158,33 @@ static __device__ __noinline__ void dp_build_rows(const GraphView& G, DpView& D,
     D.pred_ptr[i] = off;
     const uint32_t d = G.in_deg[node];
     D.row_indeg[i] = d;
-    D.row_char[i] = (uint8_t)G.hdr->decoder[G.code[node]];
+    const uint8_t ch = (uint8_t)G.hdr->decoder[G.code[node]];
+    D.row_char[i] = ch;
     uint8_t flags = G.out_first[node] == kNone ? kRowSink : 0;
+    const uint32_t begin = off;
+    uint32_t other[2] = {kNone, kNone}, n_other = 0;
     if (d == 0) {
       D.preds[off++] = 0;
+      flags |= kRowSource;
       if (i == 1) flags |= kRowPrevPred;
+      else other[n_other++] = 0;
     } else {
       for (uint32_t e = G.in_first[node]; e != kNone; e = G.e_next_in[e]) {
         const uint32_t p = G.node_to_rank[G.e_tail[e]] + 1;
         D.preds[off++] = p;
-        if (p == i - 1) flags |= kRowPrevPred;
+        if (p == i - 1) {
+          flags |= kRowPrevPred;
+        } else {
+          if (n_other < 2) other[n_other] = p;
+          ++n_other;
+        }
       }
     }
+    if (n_other > 2) flags |= kRowMore;
     D.row_sink[i] = flags;
+    D.rowrec[i] = make_uint4(begin, min(off - begin, 0xFFFFu) | (uint32_t)flags << 16 |
+                                        (uint32_t)ch << 24,
+                             other[0], other[1]);
   }
   if (t == nt - 1) D.pred_ptr[V + 1] = off;
   __syncthreads();
@@ -306,32 +323,17 @@ __host__ __device__ __forceinline__ uint64_t colmap(uint64_t j, uint64_t nt) {
   return 2 * ((k >> 1) * 2 * nt + 2 * t + (k & 1)) + r / (CPT / 2);
 }
 
-// Value of thread t-1 (thread 0 gets `fill`), for three values at once.
-__device__ __forceinline__ void from_left3(int32_t a, int32_t b, int32_t c, int32_t fill,
-                                           int32_t* la, int32_t* lb, int32_t* lc,
-                                           BlockScratch& sh) {
+// Value of thread t-1 (thread 0 gets `fill`).
+__device__ __forceinline__ int32_t from_left(int32_t a, int32_t fill, BlockScratch& sh) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int32_t xa = __shfl_up_sync(0xffffffffu, a, 1);
-  int32_t xb = __shfl_up_sync(0xffffffffu, b, 1);
-  int32_t xc = __shfl_up_sync(0xffffffffu, c, 1);
+  int32_t x = __shfl_up_sync(0xffffffffu, a, 1);
   if ((blockDim.x >> 5) > 1) {
-    if (lane == 31) {
-      sh.wv[warp] = a;
-      sh.wv2[warp] = b;
-      sh.edge[warp] = c;
-    }
+    if (lane == 31) sh.wv[warp] = a;
     __syncthreads();
-    if (lane == 0 && warp > 0) {
-      xa = sh.wv[warp - 1];
-      xb = sh.wv2[warp - 1];
-      xc = sh.edge[warp - 1];
-    }
+    if (lane == 0 && warp > 0) x = sh.wv[warp - 1];
     __syncthreads();
   }
-  if (threadIdx.x == 0) xa = xb = xc = fill;
-  *la = xa;
-  *lb = xb;
-  *lc = xc;
+  return threadIdx.x == 0 ? fill : x;
 }
 
 // Strip scan of X[j] = max(a[j], X[j-1] + pen) over this thread's pairs with
@@ -355,14 +357,6 @@ __device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, in
   return c;
 }
 
-// Horizontal traceback code of a cell (one byte):
-//   bits 0-1  first match of the horizontal tests of the traceback
-//             (implementation.hpp:1977-1990): 0 none, 1 gap open
-//             (H[j-1] + g or H[j-1] + q), 3 gap extension (E[j-1] + e or
-//             Q[j-1] + c, the extend_left case)
-//   bit 2     E[j-1] + e == E[j] and Q[j-1] + c == Q[j]: the extend_left
-//             loop continues past column j (2031-2035)
-constexpr uint8_t kCodeAny = 1, kCodeExt = 2, kCodeRun = 4;
 
 // Forward pass + row selection + max_j (identical in every thread on
 // return).  T = int16_t for the 16-lane width, int32_t for the 8-lane one.
@@ -388,7 +382,8 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
   void* __restrict__ H = D.H;
   void* __restrict__ F = D.F;
   void* __restrict__ O = D.O;
-  uint8_t* __restrict__ CODE = D.code;
+  void* __restrict__ E = D.E;
+  void* __restrict__ Q = D.Q;
   const P NEG2 = Lx::splat(Lx::kNeg);
   const uint32_t NZ = S.min16x2;  // neutral operand of Lx::max
   const P m2 = Lx::splat(m), n2 = Lx::splat(n);
@@ -486,12 +481,17 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
   const uint32_t jl = L - 1;
   const bool owns_last = jl >= s0 && jl < s0 + CPT;
   const int32_t last_k = (int32_t)((jl - s0) % HP), last_hi = (int32_t)((jl - s0) / HP);
+  // first column of the previous row (thread 0), kept in registers
+  int32_t fc_prev = 0, fcF_prev = 0, fcO_prev = 0;
+  // the next row's record is loaded one row ahead, off the critical path
+  uint4 rec_next = D.rowrec[1];
   __syncthreads();
 
   for (uint32_t i = 1; i <= V; ++i) {
-    const uint32_t pb = D.pred_ptr[i], pe = D.pred_ptr[i + 1];
-    const uint8_t rc = D.row_char[i];
-    const L16::P rc2 = L16::splat(rc);
+    const uint4 rec = rec_next;
+    if (i < V) rec_next = D.rowrec[i + 1];
+    const uint32_t rflags = (rec.y >> 16) & 0xFFu;
+    const L16::P rc2 = L16::splat(rec.y >> 24);
     // Over the predecessors only maxima are taken: the diagonal source
     // max_p H_p[j-1] (hd), for linear gaps the vertical max_p H_p[j] (f),
     // for affine/convex max_p max(H_p + g - e, F_p) (f) and
@@ -517,21 +517,24 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
         }
       }
     };
-    const uint8_t rflags = D.row_sink[i];
     bool first = true;
     if (rflags & kRowPrevPred) {
       // the previous rank is a predecessor: its row is in registers
       if (t == 0) {
-        fl = imax(fl, D.fc[i - 1]);
-        if (SUB >= kAffine) fa = imax(fa, D.fcF[i - 1]);
-        if (SUB == kConvex) fo = imax(fo, D.fcO[i - 1]);
+        fl = imax(fl, fc_prev);
+        if (SUB >= kAffine) fa = imax(fa, fcF_prev);
+        if (SUB == kConvex) fo = imax(fo, fcO_prev);
       }
-      accumulate(ph, pf, po, t == 0 ? D.fc[i - 1] : left_prev, true);
+      accumulate(ph, pf, po, t == 0 ? fc_prev : left_prev, true);
       first = false;
     }
-    for (uint32_t pi = pb; pi < pe; ++pi) {
-      const uint32_t p = D.preds[pi];
-      if (p == i - 1) continue;
+    // the other predecessors: two from the record, any further ones from the
+    // predecessor list (rows with more than two are rare)
+    uint32_t p = rec.z;
+    uint32_t visited = 0, skipped = 0;
+    uint32_t pi = rec.x;
+    const uint32_t pend = (rflags & kRowMore) ? D.pred_ptr[i + 1] : rec.x;
+    while (p != kNone) {
       P hp[HP], fp[HP], op[HP];
       const uint64_t rwp = (uint64_t)p * wrow + w0;
 #pragma unroll
@@ -554,20 +557,37 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
       }
       accumulate(hp, fp, op, hleft, first);
       first = false;
+      if (++visited == 1) {
+        p = rec.w;
+      } else {
+        p = kNone;
+        while (pi < pend) {
+          const uint32_t q = D.preds[pi++];
+          if (q == i - 1) continue;
+          if (skipped < 2) {
+            ++skipped;
+            continue;
+          }
+          p = q;
+          break;
+        }
+      }
     }
     // NW first column (thread 0)
     int32_t fci = 0;
     if (t == 0) {
-      const bool source = D.row_indeg[i] == 0;
+      const bool source = (rflags & kRowSource) != 0;
       if (type == kNW) {
         if (SUB == kLinear) {
           fci = (source ? 0 : fl) + g;
         } else {
           const int32_t vF = (source ? g - e : fa) + e;
           D.fcF[i] = vF;
+          fcF_prev = vF;
           if (SUB == kConvex) {
             const int32_t vO = (source ? q - c : fo) + c;
             D.fcO[i] = vO;
+            fcO_prev = vO;
             fci = imax(vF, vO);
           } else {
             fci = vF;
@@ -575,6 +595,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
         }
       }
       D.fc[i] = fci;
+      fc_prev = fci;
     }
     const uint64_t rw = (uint64_t)i * wrow + w0;
     P h[HP];
@@ -600,13 +621,10 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
         if (SUB == kConvex) Lx::store2(O, rw + (k / 2) * st2, o[k], o[k + 1]);
       }
     }
-    if (edge_thread) {
-#pragma unroll
-      for (int k = 0; k < HP; ++k) {
-        const uint32_t vm = (s0 + k < L ? 0x0000FFFFu : 0u) | (s0 + HP + k < L ? 0xFFFF0000u : 0u);
-        h[k] = Lx::select(vm, h[k], NEG2);
-      }
-    }
+    // Columns past the read are computed like the others and never masked:
+    // they only feed columns to their right (the in-row scans run left to
+    // right, the diagonal reads column j-1), the row selection below masks
+    // them, and the traceback never reaches them.
     P hs[HP], ee[HP], qq[HP];
     if (SUB == kLinear) {
 #pragma unroll
@@ -653,42 +671,15 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
           hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], ee[k]) : Lx::max(h[k], ee[k], NZ);
       }
     }
-    // values of column s0-1 of this row (thread 0: the first column fc)
-    int32_t lH, lE, lQ;
-    from_left3(Lx::hi(hs[HP - 1]), SUB >= kAffine ? Lx::hi(ee[HP - 1]) : 0,
-               SUB == kConvex ? Lx::hi(qq[HP - 1]) : 0, fci, &lH, &lE, &lQ, sh);
-    // horizontal traceback codes (equality bits at 15 / 31 of each pair);
-    // the codes of pairs k, k+1 go out as one 32-bit word
-    uint32_t two_prev = 0;
+    // column s0-1 of this row (thread 0: the first column fc)
+    const int32_t lH = from_left(Lx::hi(hs[HP - 1]), fci, sh);
+    // the gap rows E and Q as the recurrences computed them: the traceback
+    // re-derives its horizontal tests from them
+    if (SUB >= kAffine) {
 #pragma unroll
-    for (int k = 0; k < HP; ++k) {
-      const P Hl = k == 0 ? Lx::make(lH, Lx::lo(hs[HP - 1])) : hs[k - 1];
-      const uint32_t mB = Lx::eqb(hs[k], Lx::add(Hl, g2));
-      uint32_t code;
-      if (SUB == kLinear) {
-        code = mB >> 15;
-      } else {
-        const P El = k == 0 ? Lx::make(lE, Lx::lo(ee[HP - 1])) : ee[k - 1];
-        const P Ele = Lx::add(El, e2);
-        const uint32_t mA = Lx::eqb(hs[k], Ele);
-        uint32_t any = mA | mB, ext = mA, run = Lx::eqb(ee[k], Ele);
-        if (SUB == kConvex) {
-          const P Ql = k == 0 ? Lx::make(lQ, Lx::lo(qq[HP - 1])) : qq[k - 1];
-          const P Qlc = Lx::add(Ql, c2);
-          const uint32_t mC = Lx::eqb(hs[k], Qlc);
-          const uint32_t mD = Lx::eqb(hs[k], Lx::add(Hl, q2));
-          any |= mC | mD;
-          ext |= ~mB & mC;
-          run &= Lx::eqb(qq[k], Qlc);
-        }
-        code = (any >> 15) | ((ext & 0x80008000u) >> 14) | (run >> 13);
-      }
-      // bytes 0 and 2 of code: the codes of the pair's two columns
-      if (k & 1) {
-        reinterpret_cast<uint32_t*>(CODE + (uint64_t)i * ld)[(w0 + (k / 2) * st2) >> 1] =
-            __byte_perm(two_prev, code, 0x6420u);
-      } else {
-        two_prev = code;
+      for (int k = 0; k < HP; k += 2) {
+        Lx::store2(E, rw + (k / 2) * st2, ee[k], ee[k + 1]);
+        if (SUB == kConvex) Lx::store2(Q, rw + (k / 2) * st2, qq[k], qq[k + 1]);
       }
     }
 #pragma unroll
@@ -799,13 +790,23 @@ static __device__ __noinline__ int32_t dp_traceback(const Scoring& S, const DpVi
   const void* H = D.H;
   const void* F = D.F;
   const void* O = D.O;
-  const uint8_t* CODE = D.code;
+  const void* E = D.E;
+  const void* Q = D.Q;
   const uint64_t nt = blockDim.x;  // the forward pass's CTA width
   auto at = [&](const void* M, int64_t row, int64_t col) -> int32_t {
     return Lx::elem(M, (uint64_t)row * ld + colmap<CPT>((uint64_t)col, nt));
   };
-  auto code = [&](int64_t row, int64_t col) -> uint8_t {
-    return CODE[(uint64_t)row * ld + colmap<CPT>((uint64_t)col, nt)];
+  // H, E or Q of column col, where column -1 is the first column: the
+  // forward pass starts all three in-row recurrences from it
+  auto left = [&](const void* M, int64_t row, int64_t col) -> int32_t {
+    return col < 0 ? D.fc[row] : at(M, row, col);
+  };
+  // extend_left continues past column cc (implementation.hpp:2031-2035):
+  // E (and Q, convex) of cc extend the values of column cc-1
+  auto run = [&](int64_t row, int64_t cc) -> bool {
+    bool r = at(E, row, cc) == left(E, row, cc - 1) + e;
+    if (SUB == kConvex) r = r && at(Q, row, cc) == left(Q, row, cc - 1) + c;
+    return r;
   };
   int32_t* tb = out;  // written back to front, reversed at the end
   uint64_t np = 0;
@@ -869,9 +870,24 @@ static __device__ __noinline__ int32_t dp_traceback(const Scoring& S, const DpVi
       }
     }
     if (!found) {
-      const uint8_t cd = code(i, j);
-      if (cd & kCodeAny) {
-        ext_left = SUB >= kAffine && (cd & kCodeExt);
+      // horizontal tests in the reference's order (implementation.hpp
+      // 1977-1990): E extension, H + g, Q extension, H + q
+      const int32_t hl = left(H, i, j - 1);
+      bool any;
+      if (SUB == kLinear) {
+        any = h == hl + g;
+      } else {
+        const bool mA = h == left(E, i, j - 1) + e;
+        const bool mB = h == hl + g;
+        any = mA || mB;
+        ext_left = mA;
+        if (SUB == kConvex && !any) {
+          const bool mC = h == left(Q, i, j - 1) + c;
+          any = mC || h == hl + q;
+          ext_left = mC;
+        }
+      }
+      if (any) {
         prev_i = i;
         prev_j = j - 1;
         found = true;
@@ -886,7 +902,7 @@ static __device__ __noinline__ int32_t dp_traceback(const Scoring& S, const DpVi
         EMIT(-1, (int32_t)j);
         --j;
         if (j == -1) break;
-        if (!(code(i, j + 1) & kCodeRun)) break;
+        if (!run(i, j + 1)) break;
       }
     } else if (SUB >= kAffine && ext_up) {
       while (true) {

@@ -675,7 +675,7 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, bool retry) {
   gc.seqs = maxreads + 1;
   gc.aligned = retry ? 63 : 4;  // DNA columns hold at most 5 codes; more reruns
   DpCaps dc{(uint32_t)nodes + 1, (uint32_t)(cpt * nt), gc.edges + (uint32_t)nodes + 2,
-            b->base.sub};
+            b->base.sub, p->wide ? 4 : 2};
   GraphView gv;
   DpView dv;
   const uint64_t stride = align_up(graph_layout(nullptr, gc, &gv), 256) +
@@ -1141,7 +1141,7 @@ extern "C" int32_t spoa_gb300_window_poa_noalloc(
   gc.labels = SPOA_GB300_NOALLOC_MAX_READS * SPOA_GB300_NOALLOC_MAX_READ_LEN + 2;
   gc.seqs = n_reads + 1;
   gc.aligned = 15;
-  DpCaps dc{gc.nodes + 1, (uint32_t)(cpt * nt), gc.edges + gc.nodes + 2, sub};
+  DpCaps dc{gc.nodes + 1, (uint32_t)(cpt * nt), gc.edges + gc.nodes + 2, sub, 2};  // int16 only
   GraphView gv;
   DpView dv;
   const uint64_t head = align_up(sizeof(NoAllocHeader), 256);
