@@ -99,7 +99,7 @@ bool throughput_tile(uint32_t L, bool wide, int* cpt, int* nt) {
     const int c = cs[k];
     uint64_t t = ((uint64_t)(L + c - 1) / c + 31) / 32 * 32;
     if (t == 0) t = 32;
-    if (t > 512) continue;  // the persistent kernel is capped at 128 registers
+    if (t > 512) continue;  // 512 threads x 128 registers fill the register file
     uint64_t cost = t * (uint64_t)c;
     if (cost < best || (cost == best && (int)t < *nt)) {
       best = cost;
