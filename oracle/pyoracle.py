@@ -246,7 +246,8 @@ def parse_reference_output(text: str) -> list:
         tag, _, rest = line.partition(" ")
         if tag == "W":
             cur = {"scores": [], "reversed": [], "alignments": [], "consensus": "",
-                   "msa": [], "gfa": [], "error": None}
+                   "msa": [], "gfa": [], "error": None, "summary": None,
+                   "summary_verbose": None}
         elif tag == "R":
             parts = rest.split(" ")
             cur["scores"].append(int(parts[1]))
@@ -259,6 +260,9 @@ def parse_reference_output(text: str) -> list:
             cur["consensus"] = rest
         elif tag == "M":
             cur["msa"].append(rest)
+        elif tag in ("Y", "V"):
+            vals = [int(x) for x in rest.split(",")] if rest else []
+            cur["summary" if tag == "Y" else "summary_verbose"] = vals
         elif tag == "G":
             cur["gfa"].append(rest)
         elif tag == "X":

@@ -171,6 +171,14 @@ int main(int argc, char** argv) {
       auto consensus = graph.GenerateConsensus();
       if (!timing_only) {
         os << "C " << consensus << "\n";
+        // per-base support (graph.cpp:377-431), both forms
+        for (int verbose = 0; verbose < 2; ++verbose) {
+          std::vector<std::uint32_t> summary;
+          graph.GenerateConsensus(&summary, verbose != 0);
+          os << (verbose ? "V" : "Y");
+          for (std::size_t k = 0; k < summary.size(); ++k) os << (k ? "," : " ") << summary[k];
+          os << "\n";
+        }
         auto msa = graph.GenerateMultipleSequenceAlignment();
         for (const auto& row : msa) os << "M " << row << "\n";
         WriteGfa(graph, is_reversed, os);

@@ -21,6 +21,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libspoa_gb300.so")
 CPPLIB = os.path.join(HERE, "libspoa.so")
 PEAKLIB = os.path.join(HERE, "libspoa_peak.so")
+CPPTEST = os.path.join(OUT, "spoa_api_test")
 
 TUS = ["spoa_gb300"] + [f"inst_{m}{w}" for m in ("linear", "affine", "convex") for w in (16, 32)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -79,9 +80,15 @@ def build(verbose: bool = False, force: bool = False) -> str:
         cpp_hdrs = [os.path.join(ROOT, "include", "spoa", f)
                     for f in os.listdir(os.path.join(ROOT, "include", "spoa"))]
         if force or _stale(CPPLIB, [cpp_src, LIB] + cpp_hdrs + hdrs):
-            subprocess.run(["g++", "-std=c++11", "-O2", "-fPIC", "-shared",
+            subprocess.run(["g++", "-std=c++11", "-O2", "-Wall", "-fPIC", "-shared",
                             "-I", os.path.join(ROOT, "include"), cpp_src, "-o", CPPLIB,
                             "-L", HERE, "-lspoa_gb300", "-Wl,-rpath,$ORIGIN"], check=True)
+        # the C++ API test driver (tests/test_cpp_api.py runs it)
+        test_src = os.path.join(ROOT, "tests", "cpp", "spoa_api_test.cpp")
+        if os.path.exists(test_src) and (force or _stale(CPPTEST, [test_src, CPPLIB] + cpp_hdrs)):
+            subprocess.run(["g++", "-std=c++11", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+                            test_src, "-o", CPPTEST, "-L", HERE, "-lspoa",
+                            "-Wl,-rpath," + HERE], check=True)
     return LIB
 
 

@@ -11,7 +11,9 @@ It writes
                            flag, golden consensus), parsed from the file;
   spoa_test_outputs.json   what the compiled reference prints for those 18
                            runs (per-read scores, sha256 of alignments, MSA
-                           and GFA);
+                           and GFA, the consensus summary of
+                           GenerateConsensus(summary) and the sha256 of its
+                           verbose form);
   ref_windows.json.gz      seeded synthetic windows (inputs verbatim) with the
                            reference's outputs: scores, strand flags,
                            consensus, and sha256 of alignments, MSA and GFA.
@@ -156,6 +158,10 @@ def main():
         assert o["error"] is None
         assert o["consensus"] == cs["consensus"], cs["name"]
         test_out[cs["name"]] = canon_outputs(o)
+        # GenerateConsensus(summary, verbose) of the reference, both forms
+        test_out[cs["name"]]["summary"] = o["summary"]
+        test_out[cs["name"]]["summary_verbose_sha"] = sha(
+            ",".join(str(x) for x in o["summary_verbose"]))
     with open(os.path.join(HERE, "spoa_test_outputs.json"), "w") as fh:
         json.dump(test_out, fh, indent=1)
 
