@@ -54,7 +54,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batch_10k",
-                    choices=["batch_10k", "uneven_2k", "single_500", "long_10k"])
+                    choices=["batch_10k", "uneven_2k", "single_500", "long_10k", "serve"])
+    ap.add_argument("--rates", default="1000,10000,50000",
+                    help="serve: offered loads in windows/s")
+    ap.add_argument("--serve-windows", type=int, default=600,
+                    help="serve: windows per offered load")
     ap.add_argument("--windows", type=int, default=0, help="override the window count")
     ap.add_argument("--plain-sample", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -249,6 +253,8 @@ def main():
     import spoa_gb300 as sg
     if sg.lib().spoa_gb300_device_count() <= 0:
         raise SystemExit("no CUDA device visible")
+    if args.workload == "serve":
+        return serve(args, sg, rank, world, dist)
 
     wins, typ, params, wtypes, wstrand, cfg = workload(args.workload, args.windows, rank)
     n_windows = len(wins)
@@ -373,6 +379,73 @@ def main():
         "clocks": clk,
         "wall_s": wall,
     }
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def serve_stream(n: int, rate: float, seed: int):
+    """A Poisson arrival stream: n windows drawn 70/30 from the polishing and
+    the uneven distributions, exponential gaps at `rate` windows/s.
+    Returns [(reads, type, strand, arrival seconds)]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t, out = 0.0, []
+    for k in range(n):
+        t += rng.exponential(1.0 / rate)
+        if rng.random() < 0.7:
+            w = synth.batch_window(5_000_000 + seed * 100_000 + k)
+            out.append((w.reads, 2, False, t))
+        else:
+            w = synth.uneven_window(6_000_000 + seed * 100_000 + k)
+            out.append((w.reads, w.type, True, t))
+    return out
+
+
+def serve(args, sg, rank, world, dist):
+    """Served form: windows arrive over time (Poisson, at each offered load
+    of --rates) and go through the continuous-batching server; reports the
+    completed windows/s and the latency (completion minus arrival)
+    percentiles.  Windows of 70/30 polishing/uneven shape; the polishing
+    scoring (OV convex) for all, per-window type for the uneven ones."""
+    params = synth.SCORING["batch_10k"][1]
+    rates = [float(x) for x in args.rates.split(",") if x]
+    sweep = []
+    clocks = Clocks()
+    clocks.start()
+    for i, rate in enumerate(rates):
+        stream = serve_stream(args.serve_windows, rate, seed=rank * 101 + i)
+        # warm-up: the kernels of every width and class once
+        with sg.Server(2, *params) as sv:
+            for reads, typ, strand, _ in stream[:8]:
+                sv.wait(sv.submit(reads, typ, strand), timeout=600)
+        cells = 0
+        with sg.Server(2, *params, gather_seconds=0.0005) as sv:
+            t0 = time.perf_counter()
+            tickets = [sv.submit(r, t, s, a) for r, t, s, a in stream]
+            res = [sv.wait(t, timeout=3600) for t in tickets]
+            wall = time.perf_counter() - t0
+            st = sv.stats()
+        lat = np.array([x[2] for x in res])
+        ok = sum(1 for x in res if x[0] == 0)
+        wall = max_over_ranks(wall, dist, "cuda")
+        sweep.append({"offered_windows_per_s": rate, "windows": len(stream) * world,
+                      "completed_ok": ok, "windows_per_s": len(stream) * world / wall,
+                      "p50_latency_s": float(np.percentile(lat, 50)),
+                      "p99_latency_s": float(np.percentile(lat, 99)),
+                      "launches": st["launches"], "wall_s": wall})
+    clk = clocks.stop()
+    best = max(sweep, key=lambda x: x["windows_per_s"])
+    line = {"metric": "windows/s (served)", "value": best["windows_per_s"], "unit": "windows/s",
+            "n_gpus": world, "steps": len(rates), "warmup": 1,
+            "ms_per_step": best["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int16/int32", "data": "synthetic (seeded; see bench.py serve_stream)",
+            "config": {"workload": "serve: Poisson arrivals, 70/30 polishing (batch_10k shape) / "
+                                   "uneven (uneven_2k shape) windows, OV convex 5/-4/-8/-6/-10/-4",
+                       "windows_per_rate": args.serve_windows, "rates": rates,
+                       "parallelism": f"arrival streams sharded over {world} GPU(s), no collective"},
+            "serving": sweep, "gpu_launches": sum(x["launches"] for x in sweep), "clocks": clk}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:

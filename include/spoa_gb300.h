@@ -195,6 +195,53 @@ void spoa_gb300_batch_destroy(spoa_gb300_batch* batch);
 int32_t spoa_gb300_batch_run(const spoa_gb300_batch_desc* desc, spoa_gb300_batch** out,
                              spoa_gb300_batch_result* result);
 
+/* ---- Served windows (no counterpart in the reference) -------------------- *
+ * Continuous batching of windows that arrive over time.  A host thread of
+ * the server admits arrived windows in arrival order while the memory their
+ * arenas need (graph plus DP-and-traceback bytes) fits a fixed device
+ * budget, gathers them into launches of the persistent kernel (one CTA per
+ * window) on a pool of streams, so windows that arrive while others run
+ * start on the GPU beside them, and frees each launch's memory when it
+ * completes.  A window whose reads turn out to need 32-bit scores, or whose
+ * graph outgrows its arena, is admitted again with the wider kernel or twice
+ * the capacity.  Every window is the CLI loop of src/main.cpp:275-314 (reads
+ * in order, optionally strand-ambiguous) followed by GenerateConsensus. */
+typedef struct spoa_gb300_server spoa_gb300_server;
+typedef struct {
+  int32_t type; /* default alignment type of submitted windows */
+  int8_t m, n, g, e, q, c, pad;
+  uint64_t memory_budget;       /* device bytes for in-flight windows (0: 40% of free) */
+  int32_t max_streams;          /* launches in flight (0: 32) */
+  int32_t max_windows_per_launch; /* (0: 4096) */
+  double gather_seconds;        /* wait this long after the oldest arrival to gather
+                                   more windows into one launch (0: none) */
+} spoa_gb300_server_desc;
+
+int32_t spoa_gb300_server_create(const spoa_gb300_server_desc* desc, spoa_gb300_server** out);
+/* Submits one window: n_reads reads back to back in seqs with n_reads + 1
+ * offsets (inputs are copied).  type -1 uses the server's type.  The window
+ * counts as arrived `delay_seconds` after the call (0: now), which lets a
+ * caller replay an arrival schedule.  Returns a ticket. */
+int32_t spoa_gb300_server_submit(spoa_gb300_server* server, const char* seqs,
+                                 const uint64_t* seq_off, uint32_t n_reads, int32_t type,
+                                 int32_t strand_ambiguous, double delay_seconds,
+                                 uint64_t* ticket);
+/* Blocks until the window of `ticket` is done (timeout_seconds <= 0: no
+ * limit), then copies its consensus (up to cap bytes), its status and its
+ * latency (completion minus arrival, seconds).  Each ticket can be waited
+ * for once.  SPOA_GB300_ERR_INVALID_ARGUMENT for an unknown ticket,
+ * SPOA_GB300_ERR_TIMEOUT when the limit passes first (wait again later);
+ * the window's own status is in *status. */
+#define SPOA_GB300_ERR_TIMEOUT 12
+int32_t spoa_gb300_server_wait(spoa_gb300_server* server, uint64_t ticket,
+                               double timeout_seconds, char* consensus, uint32_t cap,
+                               uint32_t* len, int32_t* status, double* latency_seconds);
+/* Launches issued and windows completed so far. */
+int32_t spoa_gb300_server_stats(const spoa_gb300_server* server, uint64_t* launches,
+                                uint64_t* completed);
+/* Stops the server once every submitted window has finished. */
+void spoa_gb300_server_destroy(spoa_gb300_server* server);
+
 /* ---- One window without device allocation ------------------------------- *
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (work issued between the captures of a CUDA graph, frameworks whose

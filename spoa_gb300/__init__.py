@@ -55,6 +55,8 @@ _MESSAGES = {
     8: "device arena capacity exceeded",
     9: "traceback did not terminate",
     10: "CUDA error",
+    11: "a read needs 32-bit scores",
+    12: "timed out",
 }
 
 
@@ -91,6 +93,13 @@ class _BatchResult(C.Structure):
                 ("launches", C.c_int32)]
 
 
+class _ServerDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("m", C.c_int8), ("n", C.c_int8), ("g", C.c_int8),
+                ("e", C.c_int8), ("q", C.c_int8), ("c", C.c_int8), ("pad", C.c_int8),
+                ("memory_budget", C.c_uint64), ("max_streams", C.c_int32),
+                ("max_windows_per_launch", C.c_int32), ("gather_seconds", C.c_double)]
+
+
 # Every symbol of include/spoa_gb300.h
 EXPORTED = [
     "spoa_gb300_status_string", "spoa_gb300_device_count", "spoa_gb300_engine_create",
@@ -101,7 +110,9 @@ EXPORTED = [
     "spoa_gb300_graph_consensus", "spoa_gb300_graph_msa", "spoa_gb300_graph_counts",
     "spoa_gb300_graph_export", "spoa_gb300_batch_create", "spoa_gb300_batch_launch",
     "spoa_gb300_batch_launch_plain", "spoa_gb300_batch_fetch", "spoa_gb300_batch_destroy",
-    "spoa_gb300_batch_run", "spoa_gb300_window_poa_noalloc",
+    "spoa_gb300_batch_run", "spoa_gb300_server_create", "spoa_gb300_server_submit",
+    "spoa_gb300_server_wait", "spoa_gb300_server_stats", "spoa_gb300_server_destroy",
+    "spoa_gb300_window_poa_noalloc",
 ]
 
 
@@ -144,6 +155,12 @@ def lib():
         L.spoa_gb300_batch_run.argtypes = [C.POINTER(_BatchDesc), P, C.POINTER(_BatchResult)]
         L.spoa_gb300_window_poa_noalloc.argtypes = [I32] + [C.c_int8] * 6 + [I32, U32, U32, P, P,
                                                                               P, P, U32, P, P, P, P]
+        L.spoa_gb300_server_create.argtypes = [C.POINTER(_ServerDesc), P]
+        L.spoa_gb300_server_submit.argtypes = [P, C.c_char_p, P, U32, I32, I32, C.c_double, P]
+        L.spoa_gb300_server_wait.argtypes = [P, U64, C.c_double, C.c_char_p, U32, P, P, P]
+        L.spoa_gb300_server_stats.argtypes = [P, P, P]
+        L.spoa_gb300_server_destroy.argtypes = [P]
+        L.spoa_gb300_server_destroy.restype = None
         _lib = L
     return _lib
 
@@ -495,3 +512,72 @@ def batch_poa(windows, type_: int, m: int, n: int, g: int, e: int | None = None,
     b = Batch(windows, type_, m, n, g, e, q, c, **kw)
     b.launch()
     return b.fetch()
+
+
+TIMEOUT = 12
+
+
+class Server:
+    """Served windows (continuous batching, include/spoa_gb300.h): submit
+    windows as they arrive, wait for each one's consensus.  Each window is the
+    per-read loop of spoa's CLI (src/main.cpp:275-314) and GenerateConsensus."""
+
+    def __init__(self, type_: int, m: int, n: int, g: int, e: int | None = None,
+                 q: int | None = None, c: int | None = None, memory_budget: int = 0,
+                 max_streams: int = 0, max_windows_per_launch: int = 0,
+                 gather_seconds: float = 0.0):
+        e = g if e is None else e
+        if q is None or c is None:
+            q, c = g, e
+        d = _ServerDesc(type_, m, n, g, e, q, c, 0, memory_budget, max_streams,
+                        max_windows_per_launch, gather_seconds)
+        h = C.c_void_p()
+        _check("Server::Create", lib().spoa_gb300_server_create(C.byref(d), C.byref(h)))
+        self._h = h
+
+    def submit(self, reads, type_: int = -1, strand_ambiguous: bool = False,
+               delay: float = 0.0) -> int:
+        """Queues one window (a list of reads); it counts as arrived `delay`
+        seconds from now.  Returns its ticket."""
+        rs = [_bytes(r) for r in reads]
+        off = np.zeros(len(rs) + 1, np.uint64)
+        off[1:] = np.cumsum([len(r) for r in rs])
+        t = C.c_uint64()
+        _check("Server::Submit", lib().spoa_gb300_server_submit(
+            self._h, b"".join(rs), _ptr(off), len(rs), type_, 1 if strand_ambiguous else 0,
+            float(delay), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = 0.0):
+        """(status, consensus, latency seconds) of a submitted window."""
+        cap = 1 << 20
+        buf = C.create_string_buffer(cap)
+        n, st, lat = C.c_uint32(), C.c_int32(), C.c_double()
+        r = lib().spoa_gb300_server_wait(self._h, ticket, float(timeout), buf, cap, C.byref(n),
+                                         C.byref(st), C.byref(lat))
+        _check("Server::Wait", r)
+        if n.value > cap:
+            raise SpoaError("Server::Wait", 8, "consensus longer than the buffer")
+        return st.value, buf.raw[:n.value].decode(), lat.value
+
+    def stats(self):
+        la, co = C.c_uint64(), C.c_uint64()
+        _check("Server::Stats", lib().spoa_gb300_server_stats(self._h, C.byref(la), C.byref(co)))
+        return {"launches": la.value, "completed": co.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().spoa_gb300_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

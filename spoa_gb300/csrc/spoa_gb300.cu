@@ -15,12 +15,21 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
+#include <tuple>
+#include <unordered_map>
+#include <deque>
 #include <vector>
 
 #include "../../include/spoa_gb300.h"
@@ -275,6 +284,8 @@ const char* spoa_gb300_status_string(int32_t s) {
     case kCapacity: return "device arena capacity exceeded";
     case kTraceback: return "traceback did not terminate";
     case kCuda: return "CUDA error";
+    case SPOA_GB300_ERR_NEEDS_INT32: return "a read needs 32-bit scores";
+    case SPOA_GB300_ERR_TIMEOUT: return "timed out";
     default: return "unknown status";
   }
 }
@@ -600,6 +611,8 @@ namespace {
 
 
 
+// One persistent launch over a group of windows that share a tile (columns
+// per thread x threads) and a lane width.
 struct Pass {
   bool wide = false;              // int32 kernel
   std::vector<uint32_t> windows;  // window ids in queue order
@@ -607,7 +620,18 @@ struct Pass {
   DpCaps dcaps{};
   int cpt = 0, nt = 0, ctas = 0;
   uint64_t stride = 0;
-  std::vector<uint64_t> cons_off;  // per window of the batch (global index)
+  double work = 0;          // estimated DP work (sum of read lengths x longest read)
+  uint64_t arena_off = 0;   // byte offset of this pass's arenas in the batch arena
+  uint32_t work_off = 0;    // offset of its window list in the device work array
+};
+
+// How one window runs next: lane width and graph-node capacity of its arena
+// (a window that outgrows it is rerun with twice the nodes, up to the sum of
+// its read lengths, which no graph exceeds).
+struct WindowPlan {
+  bool wide = false;
+  bool many_aligned = false;  // room for 63 aligned nodes per node, not 4
+  uint64_t nodes = 0;
 };
 
 template <typename T>
@@ -639,8 +663,15 @@ struct spoa_gb300_batch {
   std::vector<char> h_cons, h_msa;
   std::vector<uint64_t> h_cons_off, h_aln_off;
   std::vector<uint32_t> h_msa_rows, h_msa_cols, h_aln_len;
-  Pass first;
-  std::vector<std::string> retry_cons;  // consensus of windows rerun with exact bounds
+  std::vector<Pass> passes;           // first launch: one pass per tile bucket
+  uint64_t budget = 0;                // device bytes for arenas
+  std::vector<cudaStream_t> streams;  // one per concurrent pass
+  ~spoa_gb300_batch() {
+    for (cudaStream_t st : streams) cudaStreamDestroy(st);
+  }
+  std::vector<WindowPlan> plan0;      // per window, as created
+  std::vector<std::string> retry_cons;  // consensus of windows that ran again
+  std::vector<uint8_t> retried;         // per window: retry_cons holds its consensus
   float kernel_ms = 0;
   int launches = 0;
   uint64_t cells = 0;
@@ -649,14 +680,35 @@ struct spoa_gb300_batch {
 
 namespace {
 
-int32_t plan_pass(spoa_gb300_batch* b, Pass* p, bool retry) {
+// Capacities of one window's arenas (graph + DP) for a tile: graph nodes
+// (at most the sum of the read lengths, which no graph exceeds), edges,
+// labels, sequences and aligned-node slots; returns the bytes per CTA.
+uint64_t arena_caps(int32_t sub, bool wide, int cpt, int nt, uint64_t nodes, uint64_t maxsum,
+                    uint32_t maxreads, bool many_aligned, GraphCaps* gc, DpCaps* dc) {
+  nodes = std::min<uint64_t>(nodes, maxsum + 1);
+  gc->nodes = (uint32_t)nodes;
+  gc->edges = (uint32_t)std::min<uint64_t>(maxsum + 2, 4 * nodes + 64);
+  gc->labels = (uint32_t)(maxsum + 2);
+  gc->seqs = maxreads + 1;
+  gc->aligned = many_aligned ? 63 : 4;  // DNA columns hold at most 5 codes; more reruns
+  *dc = DpCaps{(uint32_t)nodes + 1, (uint32_t)(cpt * nt), gc->edges + (uint32_t)nodes + 2, sub,
+               wide ? 4 : 2};
+  GraphView gv;
+  DpView dv;
+  return align_up(graph_layout(nullptr, *gc, &gv), 256) + align_up(dp_layout(nullptr, *dc, &dv), 256);
+}
+
+int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& wp) {
   const spoa_gb300_batch_desc& d = b->desc;
   uint32_t L = 1, maxreads = 1;
-  uint64_t maxsum = 1;
+  uint64_t maxsum = 1, wnodes = 1;
+  bool many_aligned = false;
   for (uint32_t w : p->windows) {
     L = std::max(L, b->lmax[w]);
     maxsum = std::max(maxsum, b->sumlen[w]);
     maxreads = std::max(maxreads, b->nreads[w]);
+    wnodes = std::max(wnodes, wp[w].nodes);
+    many_aligned = many_aligned || wp[w].many_aligned;
   }
   int cpt = d.columns_per_thread, nt = d.threads_per_window;
   if (cpt <= 0 || nt <= 0 || (p->wide && !cpt_supported<int32_t>(cpt)) ||
@@ -665,28 +717,15 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, bool retry) {
   } else if ((uint64_t)cpt * nt < L) {
     return kTooLarge;
   }
-  uint64_t nodes = d.max_nodes ? d.max_nodes : std::max<uint64_t>(4096, 6ull * L + 64);
-  if (retry) nodes = maxsum + 1;
-  nodes = std::min<uint64_t>(nodes, maxsum + 1);
+  uint64_t nodes = d.max_nodes ? std::max<uint64_t>(d.max_nodes, wnodes) : wnodes;
   GraphCaps gc;
-  gc.nodes = (uint32_t)nodes;
-  gc.edges = (uint32_t)std::min<uint64_t>(maxsum + 2, 4 * nodes + 64);
-  gc.labels = (uint32_t)(maxsum + 2);
-  gc.seqs = maxreads + 1;
-  gc.aligned = retry ? 63 : 4;  // DNA columns hold at most 5 codes; more reruns
-  DpCaps dc{(uint32_t)nodes + 1, (uint32_t)(cpt * nt), gc.edges + (uint32_t)nodes + 2,
-            b->base.sub, p->wide ? 4 : 2};
-  GraphView gv;
-  DpView dv;
-  const uint64_t stride = align_up(graph_layout(nullptr, gc, &gv), 256) +
-                          align_up(dp_layout(nullptr, dc, &dv), 256);
+  DpCaps dc;
+  const uint64_t stride =
+      arena_caps(b->base.sub, p->wide, cpt, nt, nodes, maxsum, maxreads, many_aligned, &gc, &dc);
   int blocks = 1;
   if (SPOA_BY_SUB(b->base.sub, p->wide, occupancy_batch, cpt, nt, &blocks)) return kCuda;
   blocks = std::max(blocks, 1);
-  size_t free_b = 0, total_b = 0;
-  CU(cudaMemGetInfo(&free_b, &total_b));
-  uint64_t budget = d.memory_budget ? d.memory_budget : (uint64_t)(free_b * 0.6);
-  uint64_t by_mem = std::max<uint64_t>(1, budget / stride);
+  uint64_t by_mem = std::max<uint64_t>(1, b->budget / stride);
   uint64_t ctas = d.ctas > 0 ? (uint64_t)d.ctas : (uint64_t)b->sm_count * blocks;
   ctas = std::min<uint64_t>(ctas, by_mem);
   ctas = std::min<uint64_t>(ctas, p->windows.size());
@@ -709,10 +748,10 @@ BatchArgs make_args(spoa_gb300_batch* b, const Pass& p, uint8_t* cons, const uin
   a.seqs = b->d_seqs.as<uint8_t>();
   a.seq_off = b->d_seq_off.as<uint64_t>();
   a.quals = b->desc.quals ? b->d_quals.as<uint8_t>() : nullptr;
-  a.work = b->d_work.as<uint32_t>();
+  a.work = b->d_work.as<uint32_t>() + p.work_off;
   a.n_work = (uint32_t)p.windows.size();
-  a.queue = b->d_queue.as<uint32_t>();
-  a.arena = b->arena.as<uint8_t>();
+  a.queue = b->d_queue.as<uint32_t>() + p.work_off;
+  a.arena = b->arena.as<uint8_t>() + p.arena_off;
   a.arena_stride = p.stride;
   a.gcaps = p.gcaps;
   a.dcaps = p.dcaps;
@@ -738,13 +777,13 @@ BatchArgs make_args(spoa_gb300_batch* b, const Pass& p, uint8_t* cons, const uin
   return a;
 }
 
-int32_t run_pass(spoa_gb300_batch* b, const Pass& p, cudaStream_t s, bool plain) {
+int32_t run_pass(spoa_gb300_batch* b, const Pass& p, cudaStream_t s, bool plain, uint8_t* cons,
+                 const uint64_t* cons_off) {
   if (p.windows.empty()) return kOk;
-  if (b->arena.ensure(p.stride * (plain ? 1 : p.ctas))) return kNoMemory;
-  CU(cudaMemcpyAsync(b->d_work.p, p.windows.data(), p.windows.size() * 4,
-                     cudaMemcpyHostToDevice, s));
-  CU(cudaMemsetAsync(b->d_queue.p, 0, 4 * (p.windows.size() + 1), s));
-  BatchArgs a = make_args(b, p, b->d_cons.as<uint8_t>(), b->d_cons_off.as<uint64_t>());
+  CU(cudaMemcpyAsync(b->d_work.as<uint32_t>() + p.work_off, p.windows.data(),
+                     p.windows.size() * 4, cudaMemcpyHostToDevice, s));
+  CU(cudaMemsetAsync(b->d_queue.as<uint32_t>() + p.work_off, 0, 4 * p.windows.size(), s));
+  BatchArgs a = make_args(b, p, cons, cons_off);
   if (!plain) {
     ++b->launches;
     return SPOA_BY_SUB(b->base.sub, p.wide, launch_batch, p.cpt, p.nt, p.ctas, a, s);
@@ -761,68 +800,163 @@ int32_t run_pass(spoa_gb300_batch* b, const Pass& p, cudaStream_t s, bool plain)
   return kOk;
 }
 
+// Groups windows into passes by lane width and length class (longest read
+// up to 640 columns, i.e. one warp, then doublings: 1280, 2560, ...); each
+// pass takes the tile of its longest read.  Classes are coarse on purpose:
+// a persistent pass ends with a tail of its last windows, so fewer, fuller
+// passes beat a tighter tile per window.  Passes with the longest windows
+// come first.
+int32_t make_passes(spoa_gb300_batch* b, const std::vector<uint32_t>& windows,
+                    const std::vector<WindowPlan>& wp, std::vector<Pass>* out) {
+  const spoa_gb300_batch_desc& d = b->desc;
+  std::map<std::tuple<bool, int, int>, std::vector<uint32_t>> groups;
+  const bool forced = d.columns_per_thread > 0 && d.threads_per_window > 0;
+  for (uint32_t w : windows) {
+    const bool wide = wp[w].wide;
+    int cls = 0;
+    if (!forced)
+      for (uint64_t cap = 640; cap < b->lmax[w]; cap *= 2) ++cls;
+    groups[std::make_tuple(wide, cls, 0)].push_back(w);
+  }
+  auto work = [&](uint32_t w) { return (double)b->sumlen[w] * b->lmax[w]; };
+  std::vector<std::pair<double, Pass>> ps;
+  for (auto& g : groups) {
+    Pass p;
+    p.wide = std::get<0>(g.first);
+    p.windows = std::move(g.second);
+    std::stable_sort(p.windows.begin(), p.windows.end(),
+                     [&](uint32_t x, uint32_t y) { return work(x) > work(y); });
+    double total = 0;
+    for (uint32_t w : p.windows) total += work(w);
+    p.work = total;
+    int32_t st = plan_pass(b, &p, wp);
+    if (st) return st;
+    ps.emplace_back(total, std::move(p));
+  }
+  std::stable_sort(ps.begin(), ps.end(),
+                   [](const std::pair<double, Pass>& x, const std::pair<double, Pass>& y) {
+                     return x.second.dcaps.ld > y.second.dcaps.ld;
+                   });
+  out->clear();
+  for (auto& x : ps) out->push_back(std::move(x.second));
+  // The passes of one launch are issued together, each on its own stream,
+  // longest windows first: the block scheduler places their CTAs first and
+  // the passes of shorter windows fill the rest of the GPU and take over the
+  // slots of any pass whose queue runs dry.  Each pass keeps its full CTA
+  // count; the arena budget is split in proportion to the passes' work.
+  double all = 0;
+  for (const Pass& p : *out) all += p.work;
+  uint64_t arena = 0, woff = 0;
+  for (Pass& p : *out) {
+    const double share = all > 0 ? p.work / all : 1.0;
+    uint64_t by_mem = std::max<uint64_t>(1, (uint64_t)(share * (double)b->budget) / p.stride);
+    if (out->size() > 1)
+      p.ctas = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)p.ctas, by_mem));
+    p.arena_off = arena;
+    arena += align_up(p.stride * (uint64_t)p.ctas, 256);
+    p.work_off = (uint32_t)woff;
+    woff += p.windows.size();
+  }
+  if (b->arena.ensure(std::max<uint64_t>(arena, 256))) return kNoMemory;
+  return kOk;
+}
+
 int32_t launch_all(spoa_gb300_batch* b, void* stream, bool plain) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   b->launches = 0;
+  b->kernel_ms = 0;
+  b->retry_cons.clear();
+  b->retried.assign(b->n_windows, 0);
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
   CU(cudaMemsetAsync(b->d_cells.p, 0, 16, s));
-  CU(cudaEventRecord(e0, s));
-  int32_t st = run_pass(b, b->first, s, plain);
-  CU(cudaEventRecord(e1, s));
-  if (st) return st;
-  // windows that outgrew the first-pass arena run again with exact bounds
+  std::vector<WindowPlan> wp = b->plan0;
+  std::vector<Pass> passes = b->passes;
   std::vector<int32_t> status(b->n_windows);
-  CU(cudaMemcpyAsync(status.data(), b->d_status.p, 4ull * b->n_windows, cudaMemcpyDeviceToHost, s));
-  CU(cudaStreamSynchronize(s));
-  float ms = 0;
-  CU(cudaEventElapsedTime(&ms, e0, e1));
-  b->kernel_ms = ms;
-  // windows that outgrew the arena or need the int32 width run again with
-  // exact bounds in the int32 kernel
-  Pass retry;
-  retry.wide = true;
-  for (uint32_t w = 0; w < b->n_windows; ++w)
-    if (status[w] == kCapacity || status[w] == kNeedWide) retry.windows.push_back(w);
-  if (!retry.windows.empty()) {
-    st = plan_pass(b, &retry, true);
-    if (st) return st;
-    // consensus regions sized by the exact bound, in a second buffer
-    std::vector<uint64_t> off(b->n_windows + 1, 0);
-    for (uint32_t w = 0; w < b->n_windows; ++w) {
-      uint64_t cap = 0;
-      for (uint32_t r : retry.windows) if (r == w) cap = b->sumlen[w] + 1;
-      off[w + 1] = off[w] + cap;
+  // consensus regions of rerun windows: the exact bound, in a second buffer
+  std::vector<uint64_t> off2(b->n_windows + 1, 0);
+  for (uint32_t w = 0; w < b->n_windows; ++w) off2[w + 1] = off2[w] + b->sumlen[w] + 1;
+  DeviceBuf cons2, doff2;
+  bool rerun = false;
+  for (int round = 0; !passes.empty(); ++round) {
+    if (round == 1) {
+      if (cons2.ensure(off2[b->n_windows] + 8)) return kNoMemory;
+      if (upload(doff2, off2.data(), off2.size(), s)) return kNoMemory;
     }
-    DeviceBuf cons2, off2;
-    if (cons2.ensure(off[b->n_windows] + 8)) return kNoMemory;
-    if (upload(off2, off.data(), off.size(), s)) return kNoMemory;
-    if (b->arena.ensure(retry.stride * retry.ctas)) return kNoMemory;
-    CU(cudaMemcpyAsync(b->d_work.p, retry.windows.data(), retry.windows.size() * 4,
-                       cudaMemcpyHostToDevice, s));
-    CU(cudaMemsetAsync(b->d_queue.p, 0, 4, s));
-    BatchArgs a = make_args(b, retry, cons2.as<uint8_t>(), off2.as<uint64_t>());
+    uint8_t* cons = round == 0 ? b->d_cons.as<uint8_t>() : cons2.as<uint8_t>();
+    const uint64_t* coff = round == 0 ? b->d_cons_off.as<uint64_t>() : doff2.as<uint64_t>();
     CU(cudaEventRecord(e0, s));
-    ++b->launches;
-    st = SPOA_BY_SUB(b->base.sub, true, launch_batch, retry.cpt, retry.nt, retry.ctas, a, s);
+    if (plain || passes.size() == 1) {
+      for (const Pass& p : passes) {
+        int32_t st = run_pass(b, p, s, plain, cons, coff);
+        if (st) return st;
+      }
+    } else {
+      // fork: every pass on its own stream, joined back into s
+      while (b->streams.size() < passes.size()) {
+        cudaStream_t st = nullptr;
+        CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        b->streams.push_back(st);
+      }
+      cudaEvent_t fork;
+      CU(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+      CU(cudaEventRecord(fork, s));
+      std::vector<cudaEvent_t> joins(passes.size());
+      for (size_t k = 0; k < passes.size(); ++k) {
+        CU(cudaStreamWaitEvent(b->streams[k], fork, 0));
+        int32_t st = run_pass(b, passes[k], b->streams[k], plain, cons, coff);
+        if (st) return st;
+        CU(cudaEventCreateWithFlags(&joins[k], cudaEventDisableTiming));
+        CU(cudaEventRecord(joins[k], b->streams[k]));
+        CU(cudaStreamWaitEvent(s, joins[k], 0));
+      }
+      cudaEventDestroy(fork);
+      for (cudaEvent_t ev : joins) cudaEventDestroy(ev);
+    }
     CU(cudaEventRecord(e1, s));
-    if (st) return st;
-    // move the retried consensus into the first-pass regions when they fit
-    std::vector<uint32_t> lens(b->n_windows);
-    CU(cudaMemcpyAsync(lens.data(), b->d_cons_len.p, 4ull * b->n_windows, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(status.data(), b->d_status.p, 4ull * b->n_windows, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
+    float ms = 0;
     CU(cudaEventElapsedTime(&ms, e0, e1));
     b->kernel_ms += ms;
-    std::vector<char> tmp(off[b->n_windows] + 8);
-    CU(cudaMemcpy(tmp.data(), cons2.p, off[b->n_windows], cudaMemcpyDeviceToHost));
-    b->h_cons_off.clear();
-    b->retry_cons.assign(b->n_windows, std::string());
-    for (uint32_t w : retry.windows)
-      b->retry_cons[w].assign(tmp.data() + off[w], std::min<uint64_t>(lens[w], off[w + 1] - off[w]));
-  } else {
-    b->retry_cons.clear();
+    if (round > 0) {
+      // keep the consensus of the windows this round ran
+      std::vector<uint32_t> lens(b->n_windows);
+      CU(cudaMemcpy(lens.data(), b->d_cons_len.p, 4ull * b->n_windows, cudaMemcpyDeviceToHost));
+      std::vector<char> tmp(off2[b->n_windows] + 8);
+      CU(cudaMemcpy(tmp.data(), cons2.p, off2[b->n_windows], cudaMemcpyDeviceToHost));
+      b->retry_cons.resize(b->n_windows);
+      for (const Pass& p : passes)
+        for (uint32_t w : p.windows) {
+          b->retry_cons[w].assign(tmp.data() + off2[w],
+                                  std::min<uint64_t>(lens[w], off2[w + 1] - off2[w]));
+          b->retried[w] = 1;
+        }
+    }
+    // windows that need the int32 width or outgrew their arena run again
+    std::vector<uint32_t> again;
+    for (const Pass& p : passes) {
+      for (uint32_t w : p.windows) {
+        if (status[w] == kNeedWide) {
+          wp[w].wide = true;
+          again.push_back(w);
+        } else if (status[w] == kCapacity && wp[w].nodes < b->sumlen[w] + 1) {
+          wp[w].nodes = std::min<uint64_t>(2 * wp[w].nodes, b->sumlen[w] + 1);
+          wp[w].many_aligned = true;
+          again.push_back(w);
+        } else if (status[w] == kCapacity && !wp[w].many_aligned) {
+          wp[w].many_aligned = true;
+          again.push_back(w);
+        }
+      }
+    }
+    if (!again.empty()) rerun = true;
+    int32_t st = make_passes(b, again, wp, &passes);
+    if (st) return st;
+    if (round > 64) break;  // unreachable: every rerun doubles a bounded capacity
   }
+  if (!rerun) b->retry_cons.clear();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return kOk;
@@ -879,15 +1013,33 @@ int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* d, spoa_gb300_batch
     }
     b->nreads[w] = b->wro[w + 1] - b->wro[w];
   }
-  // queue order: longest estimated work first (largest sum of lengths x
-  // longest read), so the persistent CTAs drain evenly
-  b->first.windows.resize(b->n_windows);
-  for (uint32_t w = 0; w < b->n_windows; ++w) b->first.windows[w] = w;
-  std::stable_sort(b->first.windows.begin(), b->first.windows.end(), [&](uint32_t x, uint32_t y) {
-    return (double)b->sumlen[x] * b->lmax[x] > (double)b->sumlen[y] * b->lmax[y];
-  });
-  if (b->n_windows) {
-    st = plan_pass(b, &b->first, false);
+  // Per window: the lane width its reads are expected to need (the int16
+  // rule of the reference evaluated against an estimate of the final graph,
+  // L x (1 + reads / 10) nodes; a window that turns out to need int32 is
+  // rerun with the int32 kernel) and the first graph capacity.  Windows are
+  // then grouped into one pass per (width, tile) bucket, so short windows do
+  // not run in the tile of the longest one; each pass is longest work first.
+  {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      cudaGetLastError();
+      delete b;
+      return kCuda;
+    }
+    b->budget = d->memory_budget ? d->memory_budget : (uint64_t)(free_b * 0.6);
+  }
+  b->plan0.assign(b->n_windows, WindowPlan{});
+  for (uint32_t w = 0; w < b->n_windows; ++w) {
+    const uint64_t est = std::min<uint64_t>(
+        b->sumlen[w], (uint64_t)b->lmax[w] + (uint64_t)b->lmax[w] * b->nreads[w] / 10);
+    b->plan0[w].wide = lanes_for(base, b->lmax[w], (uint32_t)std::min<uint64_t>(est, 0xFFFFFFFFu)) == 8;
+    b->plan0[w].nodes =
+        std::min<uint64_t>(std::max<uint64_t>(4096, 6ull * b->lmax[w] + 64), b->sumlen[w] + 1);
+  }
+  {
+    std::vector<uint32_t> all(b->n_windows);
+    for (uint32_t w = 0; w < b->n_windows; ++w) all[w] = w;
+    st = make_passes(b, all, b->plan0, &b->passes);
     if (st) {
       delete b;
       return st;
@@ -979,7 +1131,7 @@ int32_t spoa_gb300_batch_fetch(spoa_gb300_batch* b, spoa_gb300_batch_result* r) 
   b->h_cons_off.assign(W + 1, 0);
   for (uint32_t w = 0; w < W; ++w) {
     if (b->h_status[w] == kOk) {
-      if (!b->retry_cons.empty() && !b->retry_cons[w].empty()) {
+      if (w < b->retried.size() && b->retried[w]) {
         b->h_cons.insert(b->h_cons.end(), b->retry_cons[w].begin(), b->retry_cons[w].end());
       } else {
         uint64_t n = std::min<uint64_t>(lens[w], b->cons_off[w + 1] - b->cons_off[w]);
@@ -1028,9 +1180,13 @@ int32_t spoa_gb300_batch_fetch(spoa_gb300_batch* b, spoa_gb300_batch_result* r) 
   r->cells = cells2[0];
   r->pred_cells = cells2[1];
   r->kernel_ms = b->kernel_ms;
-  r->threads_per_window = b->first.nt;
-  r->columns_per_thread = b->first.cpt;
-  r->ctas = b->first.ctas;
+  // the tile of the pass with the most windows
+  const Pass* big = nullptr;
+  for (const Pass& p : b->passes)
+    if (!big || p.windows.size() > big->windows.size()) big = &p;
+  r->threads_per_window = big ? big->nt : 0;
+  r->columns_per_thread = big ? big->cpt : 0;
+  r->ctas = big ? big->ctas : 0;
   r->launches = b->launches;
   return kOk;
 }
@@ -1181,3 +1337,537 @@ extern "C" int32_t spoa_gb300_window_poa_noalloc(
   a.pred_cells = &h->cells[1];
   return SPOA_BY_SUB(sub, false, launch_batch, cpt, nt, 1, a, s);
 }
+
+// ===========================================================================
+// served windows: continuous batching
+// ===========================================================================
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// First-fit allocator over one device region (the admission budget): a
+// launch is admitted only when its whole footprint fits.
+class DevicePool {
+ public:
+  int32_t init(uint64_t bytes) {
+    if (cudaMalloc(&base_, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      base_ = nullptr;
+      return kNoMemory;
+    }
+    size_ = bytes;
+    free_[0] = bytes;
+    return kOk;
+  }
+  ~DevicePool() {
+    if (base_) cudaFree(base_);
+  }
+  // offset of a free block of `bytes` (256-aligned), or ~0ull
+  uint64_t alloc(uint64_t bytes) {
+    bytes = align_up(std::max<uint64_t>(bytes, 256), 256);
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second < bytes) continue;
+      const uint64_t off = it->first, len = it->second;
+      free_.erase(it);
+      if (len > bytes) free_[off + bytes] = len - bytes;
+      used_[off] = bytes;
+      return off;
+    }
+    return ~0ull;
+  }
+  void release(uint64_t off) {
+    auto u = used_.find(off);
+    if (u == used_.end()) return;
+    uint64_t len = u->second;
+    used_.erase(u);
+    auto next = free_.lower_bound(off);
+    if (next != free_.end() && off + len == next->first) {
+      len += next->second;
+      next = free_.erase(next);
+    }
+    if (next != free_.begin()) {
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == off) {
+        prev->second += len;
+        return;
+      }
+    }
+    free_[off] = len;
+  }
+  uint8_t* ptr(uint64_t off) const { return static_cast<uint8_t*>(base_) + off; }
+  uint64_t size() const { return size_; }
+
+ private:
+  void* base_ = nullptr;
+  uint64_t size_ = 0;
+  std::map<uint64_t, uint64_t> free_, used_;
+};
+
+// One submitted window.
+struct ServedWindow {
+  uint64_t ticket = 0;
+  std::string seqs;
+  std::vector<uint64_t> off;  // n_reads + 1
+  int8_t type = 0, strand = 0;
+  uint32_t lmax = 1;
+  uint64_t sumlen = 0;
+  WindowPlan plan;
+  Clock::time_point arrival;
+  // results
+  bool done = false;
+  int32_t status = kOk;
+  std::string consensus;
+  Clock::time_point finished;
+};
+
+// One launch in flight: its windows, its block of the pool, its pinned
+// staging buffer and the offsets of the parts inside both.
+struct ServedLaunch {
+  std::vector<std::shared_ptr<ServedWindow>> windows;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  uint64_t pool_off = ~0ull;
+  uint8_t* pinned = nullptr;
+  uint64_t pinned_cap = 0;
+  uint64_t in_bytes = 0, out_off = 0, out_bytes = 0;
+  uint64_t o_cons_off = 0, o_cons = 0, o_cons_len = 0, o_status = 0;
+  std::vector<uint64_t> cons_off;
+  bool busy = false;
+};
+
+}  // namespace
+
+struct spoa_gb300_server {
+  spoa_gb300_server_desc desc{};
+  Scoring base{};
+  int device = 0;
+  DevicePool pool;
+  std::vector<ServedLaunch> slots;
+  std::mutex mu;
+  std::condition_variable cv;  // completions, for wait()
+  std::multimap<Clock::time_point, std::shared_ptr<ServedWindow>> incoming;  // not yet arrived
+  std::deque<std::shared_ptr<ServedWindow>> pending;  // arrived, waiting for admission
+  std::unordered_map<uint64_t, std::shared_ptr<ServedWindow>> tickets;
+  uint64_t next_ticket = 1;
+  std::atomic<uint64_t> launches{0}, completed{0};
+  std::atomic<bool> stop{false};
+  std::thread loop;
+};
+
+namespace {
+
+uint64_t a16(uint64_t x) { return align_up(x, 16); }
+
+// Length class of a window: up to 640 columns, then doublings (the classes
+// of the batched passes); windows of one launch share class and width.
+int length_class(uint32_t lmax) {
+  int cls = 0;
+  for (uint64_t cap = 640; cap < lmax; cap *= 2) ++cls;
+  return cls;
+}
+
+// Marks a window finished (under the lock) and wakes the waiters.
+void finish_window(spoa_gb300_server* sv, const std::shared_ptr<ServedWindow>& w, int32_t status,
+                   std::string consensus) {
+  std::lock_guard<std::mutex> lk(sv->mu);
+  w->status = status;
+  w->consensus = std::move(consensus);
+  w->finished = Clock::now();
+  w->done = true;
+  ++sv->completed;
+  sv->cv.notify_all();
+}
+
+// Takes arrived windows of the front window's class and width (in arrival
+// order) into a free slot while their footprint fits the pool; false when
+// nothing could be admitted.
+bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
+  std::vector<std::shared_ptr<ServedWindow>> take;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->pending.empty()) return false;
+    const auto& f = sv->pending.front();
+    const bool wide = f->plan.wide;
+    const int cls = length_class(f->lmax);
+    const size_t cap = (size_t)std::max(1, sv->desc.max_windows_per_launch);
+    for (auto it = sv->pending.begin(); it != sv->pending.end() && take.size() < cap; ++it)
+      if ((*it)->plan.wide == wide && length_class((*it)->lmax) == cls) take.push_back(*it);
+  }
+  const bool wide = take.front()->plan.wide;
+  // footprint of the first k windows; halve k until it fits the pool
+  size_t k = take.size();
+  while (k > 0) {
+    uint32_t lmax = 1, maxreads = 1;
+    uint64_t maxsum = 1, nodes = 1, R = 0, S = 0;
+    bool many = false;
+    for (size_t i = 0; i < k; ++i) {
+      const ServedWindow& w = *take[i];
+      lmax = std::max(lmax, w.lmax);
+      maxsum = std::max(maxsum, w.sumlen);
+      maxreads = std::max<uint32_t>(maxreads, (uint32_t)(w.off.size() - 1));
+      nodes = std::max(nodes, w.plan.nodes);
+      many = many || w.plan.many_aligned;
+      R += w.off.size() - 1;
+      S += w.sumlen;
+    }
+    int cpt = 0, nt = 0;
+    if (!throughput_tile(lmax, wide, &cpt, &nt)) {
+      // a read longer than any tile: the window fails alone
+      auto w = take.front();
+      {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->pending.erase(std::find(sv->pending.begin(), sv->pending.end(), w));
+      }
+      finish_window(sv, w, kTooLarge, std::string());
+      return true;
+    }
+    GraphCaps gc;
+    DpCaps dc;
+    const uint64_t stride =
+        arena_caps(sv->base.sub, wide, cpt, nt, nodes, maxsum, maxreads, many, &gc, &dc);
+    // inputs: work, queue, window read offsets, read offsets, types, strands,
+    // consensus offsets, reads; outputs: scores, strands, lengths, status,
+    // cell counters, consensus; then the arenas
+    const uint64_t n = k;
+    uint64_t o = 0;
+    const uint64_t i_work = o; o = a16(o + 4 * n);
+    const uint64_t i_queue = o; o = a16(o + 16);
+    const uint64_t i_wro = o; o = a16(o + 4 * (n + 1));
+    const uint64_t i_soff = o; o = a16(o + 8 * (R + 1));
+    const uint64_t i_type = o; o = a16(o + n);
+    const uint64_t i_strand = o; o = a16(o + n);
+    const uint64_t i_coff = o; o = a16(o + 8 * (n + 1));
+    const uint64_t i_seqs = o; o = a16(o + S);
+    const uint64_t in_bytes = o;
+    const uint64_t o_scores = o; o = a16(o + 4 * R);
+    const uint64_t o_rev = o; o = a16(o + R);
+    const uint64_t o_clen = o; o = a16(o + 4 * n);
+    const uint64_t o_status = o; o = a16(o + 4 * n);
+    const uint64_t o_cells = o; o = a16(o + 16);
+    const uint64_t o_cons = o; o = a16(o + S + n);
+    const uint64_t arena_off = align_up(o, 256);
+    const uint64_t total = arena_off + stride * n;
+    if (total > sv->pool.size()) {
+      if (k == 1) {  // can never fit: fail it
+        auto w = take.front();
+        {
+          std::lock_guard<std::mutex> lk(sv->mu);
+          sv->pending.erase(std::find(sv->pending.begin(), sv->pending.end(), w));
+        }
+        finish_window(sv, w, kNoMemory, std::string());
+        return true;
+      }
+      k /= 2;
+      continue;
+    }
+    const uint64_t off = sv->pool.alloc(total);
+    if (off == ~0ull) {
+      if (k == 1) return false;  // wait for memory to free up
+      k /= 2;
+      continue;
+    }
+    // admitted: stage the inputs in the slot's pinned buffer
+    if (L.pinned_cap < arena_off) {
+      if (L.pinned) cudaFreeHost(L.pinned);
+      L.pinned = nullptr;
+      L.pinned_cap = 0;
+      if (cudaHostAlloc(&L.pinned, arena_off, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        sv->pool.release(off);
+        return false;
+      }
+      L.pinned_cap = arena_off;
+    }
+    uint8_t* h = L.pinned;
+    auto* work = reinterpret_cast<uint32_t*>(h + i_work);
+    auto* wro = reinterpret_cast<uint32_t*>(h + i_wro);
+    auto* soff = reinterpret_cast<uint64_t*>(h + i_soff);
+    auto* wtype = reinterpret_cast<int8_t*>(h + i_type);
+    auto* wstr = reinterpret_cast<int8_t*>(h + i_strand);
+    auto* coff = reinterpret_cast<uint64_t*>(h + i_coff);
+    std::memset(h + i_queue, 0, 16);
+    L.cons_off.assign(n + 1, 0);
+    uint64_t r = 0, sb = 0;
+    wro[0] = 0;
+    soff[0] = 0;
+    coff[0] = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+      const ServedWindow& w = *take[i];
+      work[i] = (uint32_t)i;
+      wtype[i] = w.type;
+      wstr[i] = w.strand;
+      std::memcpy(h + i_seqs + sb, w.seqs.data(), w.sumlen);
+      for (size_t j = 0; j + 1 < w.off.size(); ++j) soff[r + j + 1] = sb + w.off[j + 1];
+      r += w.off.size() - 1;
+      sb += w.sumlen;
+      wro[i + 1] = (uint32_t)r;
+      coff[i + 1] = coff[i] + w.sumlen + 1;
+      L.cons_off[i + 1] = coff[i + 1];
+    }
+    uint8_t* d = sv->pool.ptr(off);
+    BatchArgs a{};
+    a.base = sv->base;
+    a.win_type = reinterpret_cast<int8_t*>(d + i_type);
+    a.win_strand = reinterpret_cast<int8_t*>(d + i_strand);
+    a.n_windows = (uint32_t)n;
+    a.win_read_off = reinterpret_cast<uint32_t*>(d + i_wro);
+    a.seqs = d + i_seqs;
+    a.seq_off = reinterpret_cast<uint64_t*>(d + i_soff);
+    a.work = reinterpret_cast<uint32_t*>(d + i_work);
+    a.n_work = (uint32_t)n;
+    a.queue = reinterpret_cast<uint32_t*>(d + i_queue);
+    a.arena = d + arena_off;
+    a.arena_stride = stride;
+    a.gcaps = gc;
+    a.dcaps = dc;
+    a.read_scores = reinterpret_cast<int32_t*>(d + o_scores);
+    a.read_rev = d + o_rev;
+    a.cons = d + o_cons;
+    a.cons_off = reinterpret_cast<uint64_t*>(d + i_coff);
+    a.cons_len = reinterpret_cast<uint32_t*>(d + o_clen);
+    a.win_status = reinterpret_cast<int32_t*>(d + o_status);
+    a.cells = reinterpret_cast<unsigned long long*>(d + o_cells);
+    a.pred_cells = a.cells + 1;
+    bool ok = cudaMemcpyAsync(d, h, in_bytes, cudaMemcpyHostToDevice, L.stream) == cudaSuccess &&
+              cudaMemsetAsync(d + o_cells, 0, 16, L.stream) == cudaSuccess;
+    if (ok)
+      ok = SPOA_BY_SUB(sv->base.sub, wide, launch_batch, cpt, nt, (int)n, a, L.stream) == kOk;
+    if (ok)
+      ok = cudaMemcpyAsync(h + o_scores, d + o_scores, arena_off - o_scores, cudaMemcpyDeviceToHost,
+                           L.stream) == cudaSuccess &&
+           cudaEventRecord(L.done, L.stream) == cudaSuccess;
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      for (size_t i = 0; i < k; ++i)
+        sv->pending.erase(std::find(sv->pending.begin(), sv->pending.end(), take[i]));
+    }
+    L.windows.assign(take.begin(), take.begin() + k);
+    L.pool_off = off;
+    L.out_off = o_scores;
+    L.o_cons = o_cons;
+    L.o_cons_len = o_clen;
+    L.o_status = o_status;
+    L.busy = true;
+    ++sv->launches;
+    if (!ok) {
+      cudaGetLastError();
+      cudaStreamSynchronize(L.stream);
+      sv->pool.release(off);
+      L.busy = false;
+      for (auto& w : L.windows) finish_window(sv, w, kCuda, std::string());
+      L.windows.clear();
+    }
+    return true;
+  }
+  return false;
+}
+
+// A launch completed: hand out the results, or send windows that need the
+// int32 width or a bigger arena back to the front of the queue.
+void complete(spoa_gb300_server* sv, ServedLaunch& L, bool ok) {
+  const uint8_t* h = L.pinned;
+  const auto* status = reinterpret_cast<const int32_t*>(h + L.o_status);
+  const auto* clen = reinterpret_cast<const uint32_t*>(h + L.o_cons_len);
+  std::vector<std::shared_ptr<ServedWindow>> again;
+  for (size_t i = 0; i < L.windows.size(); ++i) {
+    auto& w = L.windows[i];
+    const int32_t st = ok ? status[i] : kCuda;
+    if (st == kNeedWide && !w->plan.wide) {
+      w->plan.wide = true;
+      again.push_back(w);
+    } else if (st == kCapacity && (w->plan.nodes < w->sumlen + 1 || !w->plan.many_aligned)) {
+      w->plan.nodes = std::min<uint64_t>(2 * w->plan.nodes, w->sumlen + 1);
+      w->plan.many_aligned = true;
+      again.push_back(w);
+    } else {
+      std::string cons;
+      if (st == kOk) {
+        const uint64_t cap = L.cons_off[i + 1] - L.cons_off[i];
+        cons.assign(reinterpret_cast<const char*>(h + L.o_cons + L.cons_off[i]),
+                    std::min<uint64_t>(clen[i], cap));
+      }
+      finish_window(sv, w, st, std::move(cons));
+    }
+  }
+  if (!again.empty()) {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    for (auto it = again.rbegin(); it != again.rend(); ++it) sv->pending.push_front(*it);
+  }
+  sv->pool.release(L.pool_off);
+  L.windows.clear();
+  L.busy = false;
+}
+
+void serve_loop(spoa_gb300_server* sv) {
+  cudaSetDevice(sv->device);
+  const auto gather = std::chrono::duration<double>(std::max(0.0, sv->desc.gather_seconds));
+  while (true) {
+    bool progress = false, in_flight = false;
+    for (ServedLaunch& L : sv->slots) {
+      if (!L.busy) continue;
+      const cudaError_t q = cudaEventQuery(L.done);
+      if (q == cudaErrorNotReady) {
+        in_flight = true;
+        continue;
+      }
+      if (q != cudaSuccess) cudaGetLastError();
+      complete(sv, L, q == cudaSuccess);
+      progress = true;
+    }
+    bool waiting;
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      const auto now = Clock::now();
+      while (!sv->incoming.empty() && sv->incoming.begin()->first <= now) {
+        sv->pending.push_back(sv->incoming.begin()->second);
+        sv->incoming.erase(sv->incoming.begin());
+      }
+      waiting = !sv->pending.empty() || !sv->incoming.empty();
+    }
+    for (ServedLaunch& L : sv->slots) {
+      if (L.busy) continue;
+      bool go;
+      {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        go = !sv->pending.empty() &&
+             (gather.count() <= 0 ||
+              (int64_t)sv->pending.size() >= sv->desc.max_windows_per_launch ||
+              Clock::now() - sv->pending.front()->arrival >= gather);
+      }
+      if (!go || !admit(sv, L)) break;
+      progress = true;
+      in_flight = true;
+    }
+    if (sv->stop && !in_flight && !waiting) break;
+    if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t spoa_gb300_server_create(const spoa_gb300_server_desc* d, spoa_gb300_server** out) {
+  if (!d || !out) return kInvalidArgument;
+  *out = nullptr;
+  spoa_gb300_engine* en = nullptr;
+  int32_t st = spoa_gb300_engine_create(d->type, d->m, d->n, d->g, d->e, d->q, d->c, &en);
+  if (st) return st;
+  auto* sv = new (std::nothrow) spoa_gb300_server();
+  if (!sv) {
+    spoa_gb300_engine_destroy(en);
+    return kNoMemory;
+  }
+  sv->base = en->S;
+  spoa_gb300_engine_destroy(en);
+  sv->desc = *d;
+  if (sv->desc.max_streams <= 0) sv->desc.max_streams = 32;
+  if (sv->desc.max_windows_per_launch <= 0) sv->desc.max_windows_per_launch = 4096;
+  if (cudaGetDevice(&sv->device) != cudaSuccess) {
+    cudaGetLastError();
+    delete sv;
+    return kCuda;
+  }
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+    cudaGetLastError();
+    delete sv;
+    return kCuda;
+  }
+  const uint64_t budget = d->memory_budget ? d->memory_budget : (uint64_t)(free_b * 0.4);
+  if (budget > free_b || sv->pool.init(budget)) {
+    delete sv;
+    return kNoMemory;
+  }
+  sv->slots.resize(sv->desc.max_streams);
+  for (ServedLaunch& L : sv->slots) {
+    if (cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      spoa_gb300_server_destroy(sv);
+      return kCuda;
+    }
+  }
+  sv->loop = std::thread(serve_loop, sv);
+  *out = sv;
+  return kOk;
+}
+
+int32_t spoa_gb300_server_submit(spoa_gb300_server* sv, const char* seqs, const uint64_t* seq_off,
+                                 uint32_t n_reads, int32_t type, int32_t strand, double delay,
+                                 uint64_t* ticket) {
+  if (!sv || !seq_off || !ticket || (n_reads && !seqs) || sv->stop) return kInvalidArgument;
+  if (type == -1) type = sv->desc.type;
+  if (type != kSW && type != kNW && type != kOV) return kInvalidArgument;
+  auto w = std::make_shared<ServedWindow>();
+  w->type = (int8_t)type;
+  w->strand = strand ? 1 : 0;
+  w->off.assign(seq_off, seq_off + n_reads + 1);
+  for (uint32_t r = 0; r < n_reads; ++r) {
+    if (w->off[r + 1] < w->off[r]) return kInvalidArgument;
+    const uint64_t L = w->off[r + 1] - w->off[r];
+    if (L > (uint64_t)INT32_MAX) return kTooLarge;
+    w->lmax = std::max<uint32_t>(w->lmax, (uint32_t)L);
+  }
+  for (auto& o : w->off) o -= seq_off[0];
+  w->sumlen = w->off[n_reads];
+  w->seqs.assign(seqs ? seqs + seq_off[0] : "", w->sumlen);
+  // the plan of the batched passes: width from the estimated final graph,
+  // the first graph capacity
+  const uint64_t est = std::min<uint64_t>(w->sumlen, (uint64_t)w->lmax + (uint64_t)w->lmax * n_reads / 10);
+  w->plan.wide = lanes_for(sv->base, w->lmax, (uint32_t)std::min<uint64_t>(est, 0xFFFFFFFFu)) == 8;
+  w->plan.nodes = std::min<uint64_t>(std::max<uint64_t>(4096, 6ull * w->lmax + 64), w->sumlen + 1);
+  w->arrival = Clock::now() + std::chrono::duration_cast<Clock::duration>(
+                                  std::chrono::duration<double>(std::max(0.0, delay)));
+  std::lock_guard<std::mutex> lk(sv->mu);
+  w->ticket = sv->next_ticket++;
+  sv->tickets[w->ticket] = w;
+  sv->incoming.emplace(w->arrival, w);
+  *ticket = w->ticket;
+  return kOk;
+}
+
+int32_t spoa_gb300_server_wait(spoa_gb300_server* sv, uint64_t ticket, double timeout,
+                               char* consensus, uint32_t cap, uint32_t* len, int32_t* status,
+                               double* latency) {
+  if (!sv) return kInvalidArgument;
+  std::unique_lock<std::mutex> lk(sv->mu);
+  auto it = sv->tickets.find(ticket);
+  if (it == sv->tickets.end()) return kInvalidArgument;
+  std::shared_ptr<ServedWindow> w = it->second;
+  auto ready = [&] { return w->done; };
+  if (timeout > 0) {
+    if (!sv->cv.wait_for(lk, std::chrono::duration<double>(timeout), ready))
+      return SPOA_GB300_ERR_TIMEOUT;
+  } else {
+    sv->cv.wait(lk, ready);
+  }
+  sv->tickets.erase(it);
+  if (status) *status = w->status;
+  if (len) *len = (uint32_t)w->consensus.size();
+  if (consensus && cap) std::memcpy(consensus, w->consensus.data(), std::min<size_t>(cap, w->consensus.size()));
+  if (latency) *latency = std::chrono::duration<double>(w->finished - w->arrival).count();
+  return kOk;
+}
+
+int32_t spoa_gb300_server_stats(const spoa_gb300_server* sv, uint64_t* launches,
+                                uint64_t* completed) {
+  if (!sv) return kInvalidArgument;
+  if (launches) *launches = sv->launches;
+  if (completed) *completed = sv->completed;
+  return kOk;
+}
+
+void spoa_gb300_server_destroy(spoa_gb300_server* sv) {
+  if (!sv) return;
+  sv->stop = true;
+  if (sv->loop.joinable()) sv->loop.join();
+  for (ServedLaunch& L : sv->slots) {
+    if (L.stream) cudaStreamDestroy(L.stream);
+    if (L.done) cudaEventDestroy(L.done);
+    if (L.pinned) cudaFreeHost(L.pinned);
+  }
+  delete sv;
+}
+
+}  // extern "C"

@@ -1,0 +1,81 @@
+"""Served windows (continuous batching): windows submitted over time, each
+result identical to the same window run alone and to the oracle."""
+import numpy as np
+import pytest
+
+import spoa_gb300 as sg
+from spoa_gb300 import synth
+from oracle import pyoracle as po
+
+PARAMS = synth.SCORING["batch_10k"][1]
+
+
+def _mix(n, seed):
+    """70/30 polishing-shaped (OV, convex) and uneven-shaped windows (NW/OV,
+    strand-ambiguous), the uneven ones kept short so the test stays small."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for k in range(n):
+        if rng.random() < 0.7:
+            w = synth.batch_window(10_000 + k)
+            out.append((w.reads, 2, False))
+        else:
+            w = synth.uneven_window(20_000 + k)
+            out.append(([r[:700] for r in w.reads[:12]], w.type, True))
+    return out
+
+
+@pytest.mark.skipif(sg.lib().spoa_gb300_device_count() > 0, reason="a GPU is visible")
+def test_server_fails_loudly_without_a_gpu():
+    with pytest.raises(sg.SpoaError):
+        sg.Server(2, *PARAMS)
+
+
+@pytest.mark.gpu
+def test_served_results_are_the_same_alone_and_in_the_mix():
+    wins = _mix(40, 1)
+    rng = np.random.Generator(np.random.PCG64(2))
+    delays = np.sort(rng.uniform(0, 0.05, len(wins)))
+    with sg.Server(2, *PARAMS, max_streams=4, gather_seconds=0.002) as sv:
+        tickets = [sv.submit(r, t, s, d) for (r, t, s), d in zip(wins, delays)]
+        got = [sv.wait(t, timeout=600) for t in tickets]
+        stats = sv.stats()
+    assert stats["completed"] == len(wins)
+    assert stats["launches"] >= 2  # arrivals spread over time: several launches overlap
+    for (reads, typ, strand), (st, cons, lat) in zip(wins, got):
+        assert st == 0
+        assert lat >= 0
+        alone = sg.batch_poa([reads], typ, *PARAMS, window_strand=[1 if strand else 0])
+        assert alone.consensus[0] == cons
+    for (reads, typ, strand), (st, cons, lat) in list(zip(wins, got))[:8]:
+        ref = po.run_window(typ, *PARAMS, reads, strand_ambiguous=strand, with_msa=False)
+        assert ref.consensus == cons
+
+
+@pytest.mark.gpu
+def test_admission_waits_for_memory():
+    """A budget that holds only a few windows at a time: windows queue for
+    memory and still all finish with the batched results."""
+    wins = _mix(24, 3)
+    with sg.Server(2, *PARAMS, memory_budget=400 << 20, max_streams=8) as sv:
+        tickets = [sv.submit(r, t, s) for r, t, s in wins]
+        got = [sv.wait(t, timeout=600) for t in tickets]
+        stats = sv.stats()
+    ref = sg.batch_poa([w[0] for w in wins], 2, *PARAMS, window_types=[w[1] for w in wins],
+                       window_strand=[1 if w[2] else 0 for w in wins])
+    assert [g[1] for g in got] == ref.consensus
+    assert all(g[0] == 0 for g in got)
+    assert stats["launches"] > 3
+
+
+@pytest.mark.gpu
+def test_wait_timeout_and_unknown_ticket():
+    with sg.Server(2, *PARAMS) as sv:
+        t = sv.submit(synth.batch_window(5).reads, delay=1.0)
+        with pytest.raises(sg.SpoaError) as ex:
+            sv.wait(t, timeout=0.05)
+        assert ex.value.status == sg.TIMEOUT
+        with pytest.raises(sg.SpoaError):
+            sv.wait(t + 1000)
+        st, cons, lat = sv.wait(t, timeout=120)
+        assert st == 0 and cons
