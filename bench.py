@@ -262,7 +262,7 @@ def main():
 
     def make_batch():
         return sg.Batch.from_arrays(seqs, off, wro, typ, *params, window_types=wtypes,
-                                    window_strand=wstrand)
+                                    window_strand=wstrand, autotune=True)
 
     batch = make_batch()
     for _ in range(args.warmup):

@@ -108,6 +108,19 @@ int32_t spoa_gb300_align_add(spoa_gb300_engine* engine, spoa_gb300_graph* graph,
                              const char* sequence, uint32_t sequence_len, const char* quality,
                              int32_t strand_ambiguous, int32_t* score, int32_t* reversed);
 
+/* The per-read loop of src/main.cpp:275-314 over n_reads reads (back to
+ * back in seqs, n_reads + 1 offsets; quals with the same offsets or NULL):
+ * the same as spoa_gb300_align_add once per read in order, but every read's
+ * launch is recorded into one CUDA graph, replayed with no host round trip
+ * between reads.  No counterpart in the reference.  scores / reversed get
+ * one value per added read (either may be NULL); *n_done is the number of
+ * reads added: on an error the reads before the failing one stay in the
+ * graph and the failing read's status is returned. */
+int32_t spoa_gb300_align_add_reads(spoa_gb300_engine* engine, spoa_gb300_graph* graph,
+                                   uint32_t n_reads, const char* seqs, const uint64_t* seq_off,
+                                   const char* quals, int32_t strand_ambiguous, int32_t* scores,
+                                   int32_t* reversed, uint32_t* n_done);
+
 /* Replaces Graph::GenerateConsensus (src/graph.cpp:368-375). */
 int32_t spoa_gb300_graph_consensus(spoa_gb300_graph* graph, char* out, uint32_t cap,
                                    uint32_t* len);
@@ -153,12 +166,16 @@ typedef struct {
   const uint64_t* seq_off;         /* [n_reads + 1] */
   const char* quals;               /* same offsets as seqs, or NULL */
   uint32_t max_nodes;              /* per-window node cap (0: automatic) */
-  int32_t threads_per_window;      /* 0: autotuned from the longest read */
-  int32_t columns_per_thread;      /* 0: autotuned */
+  int32_t threads_per_window;      /* 0: chosen per length class */
+  int32_t columns_per_thread;      /* 0: chosen per length class */
   int32_t ctas;                    /* 0: fill the device */
   uint64_t memory_budget;          /* bytes for per-CTA arenas (0: automatic) */
   int32_t want_alignments;         /* also return every read's alignment */
   int32_t want_msa;                /* also return every window's MSA */
+  int32_t autotune;                /* time the candidate tiles of every length
+                                      class on a sample of its windows at the
+                                      first launch and keep the fastest (cached
+                                      per process) */
 } spoa_gb300_batch_desc;
 
 typedef struct {

@@ -78,7 +78,7 @@ class _BatchDesc(C.Structure):
                 ("max_nodes", C.c_uint32), ("threads_per_window", C.c_int32),
                 ("columns_per_thread", C.c_int32), ("ctas", C.c_int32),
                 ("memory_budget", C.c_uint64), ("want_alignments", C.c_int32),
-                ("want_msa", C.c_int32)]
+                ("want_msa", C.c_int32), ("autotune", C.c_int32)]
 
 
 class _BatchResult(C.Structure):
@@ -107,6 +107,7 @@ EXPORTED = [
     "spoa_gb300_engine_align", "spoa_gb300_graph_create", "spoa_gb300_graph_destroy",
     "spoa_gb300_graph_clear", "spoa_gb300_graph_add_alignment",
     "spoa_gb300_graph_add_alignment_quality", "spoa_gb300_align_add",
+    "spoa_gb300_align_add_reads",
     "spoa_gb300_graph_consensus", "spoa_gb300_graph_msa", "spoa_gb300_graph_counts",
     "spoa_gb300_graph_export", "spoa_gb300_batch_create", "spoa_gb300_batch_launch",
     "spoa_gb300_batch_launch_plain", "spoa_gb300_batch_fetch", "spoa_gb300_batch_destroy",
@@ -142,6 +143,8 @@ def lib():
         L.spoa_gb300_graph_add_alignment_quality.argtypes = [P, P, U32, C.c_char_p, U32,
                                                              C.c_char_p, U32]
         L.spoa_gb300_align_add.argtypes = [P, P, C.c_char_p, U32, C.c_char_p, I32, P, P]
+        L.spoa_gb300_align_add_reads.argtypes = [P, P, U32, C.c_char_p, P, C.c_char_p, I32, P,
+                                                 P, P]
         L.spoa_gb300_graph_consensus.argtypes = [P, C.c_char_p, U32, P]
         L.spoa_gb300_graph_msa.argtypes = [P, I32, C.c_char_p, U64, P, P]
         L.spoa_gb300_graph_counts.argtypes = [P] * 7
@@ -357,6 +360,24 @@ class Graph:
                          headers, include_consensus)
 
 
+def align_add_reads(engine: AlignmentEngine, graph: Graph, reads, quals=None,
+                    strand_ambiguous: bool = False):
+    """The per-read Align + AddAlignment loop over `reads`, recorded into one
+    CUDA graph (include/spoa_gb300.h).  Returns (scores, reversed)."""
+    rs = [_bytes(r) for r in reads]
+    off = np.zeros(len(rs) + 1, np.uint64)
+    off[1:] = np.cumsum([len(r) for r in rs])
+    qs = b"".join(_bytes(q) for q in quals) if quals is not None else None
+    scores = np.zeros(max(len(rs), 1), np.int32)
+    rev = np.zeros(max(len(rs), 1), np.int32)
+    done = C.c_uint32()
+    st = lib().spoa_gb300_align_add_reads(engine._h, graph._h, len(rs), b"".join(rs), _ptr(off),
+                                          qs, 1 if strand_ambiguous else 0, _ptr(scores),
+                                          _ptr(rev), C.byref(done))
+    _check("AlignmentEngine::Align", st)
+    return scores[:len(rs)].tolist(), [bool(x) for x in rev[:len(rs)]]
+
+
 def align_add(engine: AlignmentEngine, graph: Graph, sequence, quality=None,
               strand_ambiguous: bool = False):
     """Align + AddAlignment of one read on the device (src/main.cpp:275-314).
@@ -416,7 +437,7 @@ class Batch:
 
     def _create(self, seqs, off, wro, type_, m, n, g, e, q, c, window_types, window_strand,
                 quals, want_alignments=False, want_msa=False, threads_per_window=0,
-                columns_per_thread=0, ctas=0, max_nodes=0, memory_budget=0):
+                columns_per_thread=0, ctas=0, max_nodes=0, memory_budget=0, autotune=False):
         self._seqs = np.ascontiguousarray(seqs, np.uint8)
         self._off = np.ascontiguousarray(off, np.uint64)
         self._wro = np.ascontiguousarray(wro, np.uint32)
@@ -446,6 +467,7 @@ class Batch:
         d.memory_budget = memory_budget
         d.want_alignments = 1 if want_alignments else 0
         d.want_msa = 1 if want_msa else 0
+        d.autotune = 1 if autotune else 0
         self._desc = d
         h = C.c_void_p()
         _check("batch_create", lib().spoa_gb300_batch_create(C.byref(d), C.byref(h)))

@@ -189,12 +189,27 @@ __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScra
 template <int SUB, int CPT, typename T>
 __global__ void __launch_bounds__(1024)
     k_align_add(Scoring S, GraphView G, DpView D, const uint8_t* seq, uint32_t L,
-                const uint8_t* qual, int32_t strand, ReadOut* out) {
+                const uint8_t* qual, int32_t strand, ReadOut* out, const ReadOut* prev) {
   __shared__ BlockScratch sh;
   __shared__ SharedState ss;
   __shared__ const int32_t* s_pairs;
   __shared__ int32_t s_score, s_rev;
   __shared__ uint32_t s_np;
+  // in a chain of reads (one launch each, in stream order), a read after a
+  // failed one is not added: it repeats the first failure's status
+  if (prev) {
+    if (threadIdx.x == 0) ss.pad = prev->status;
+    __syncthreads();
+    if (ss.pad != kOk) {
+      if (threadIdx.x == 0) {
+        out->status = ss.pad;
+        out->score = 0;
+        out->reversed = 0;
+        out->n_pairs = 0;
+      }
+      return;
+    }
+  }
   window_read<SUB, CPT, T>(S, G, D, sh, ss, seq, L, qual, strand != 0, &s_score, &s_rev,
                            &s_pairs, &s_np);
   if (threadIdx.x == 0) {
@@ -504,8 +519,8 @@ int32_t launch_align(int cpt, int nt, const Scoring& S, const GraphView& G, cons
 template <int SUB, typename T>
 int32_t launch_align_add(int cpt, int nt, const Scoring& S, const GraphView& G,
                          const DpView& D, const uint8_t* seq, uint32_t L, const uint8_t* qual,
-                         int32_t strand, ReadOut* out) {
-#define L_(C) k_align_add<SUB, C, T><<<1, nt>>>(S, G, D, seq, L, qual, strand, out)
+                         int32_t strand, ReadOut* out, const ReadOut* prev, cudaStream_t s) {
+#define L_(C) k_align_add<SUB, C, T><<<1, nt, 0, s>>>(S, G, D, seq, L, qual, strand, out, prev)
   SPOA_CPT_SWITCH(T, cpt, L_)
 #undef L_
   return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
@@ -537,7 +552,8 @@ int32_t occupancy_batch(int cpt, int nt, int* blocks) {
                                         const DpView&, const uint8_t*, uint32_t, ReadOut*);     \
   template int32_t launch_align_add<SUB, T>(int, int, const Scoring&, const GraphView&,         \
                                             const DpView&, const uint8_t*, uint32_t,            \
-                                            const uint8_t*, int32_t, ReadOut*);                 \
+                                            const uint8_t*, int32_t, ReadOut*, const ReadOut*,  \
+                                            cudaStream_t);                                      \
   template int32_t launch_batch<SUB, T>(int, int, int, const BatchArgs&, cudaStream_t);         \
   template int32_t occupancy_batch<SUB, T>(int, int, int*);
 

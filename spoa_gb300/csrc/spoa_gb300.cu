@@ -43,7 +43,8 @@ namespace spoa_gb300 {
                                                ReadOut*);                                       \
   extern template int32_t launch_align_add<SUB, T>(int, int, const Scoring&, const GraphView&,  \
                                                    const DpView&, const uint8_t*, uint32_t,     \
-                                                   const uint8_t*, int32_t, ReadOut*);          \
+                                                   const uint8_t*, int32_t, ReadOut*,           \
+                                                   const ReadOut*, cudaStream_t);               \
   extern template int32_t launch_batch<SUB, T>(int, int, int, const BatchArgs&, cudaStream_t);  \
   extern template int32_t occupancy_batch<SUB, T>(int, int, int*);
 SPOA_EXTERN(kLinear, int16_t)
@@ -168,7 +169,7 @@ int32_t graph_refresh(spoa_gb300_graph* g) {
 }
 
 // Grows the graph arena so that `len` more bases fit; contents are kept.
-int32_t graph_reserve(spoa_gb300_graph* g, uint32_t len) {
+int32_t graph_reserve(spoa_gb300_graph* g, uint64_t len, uint64_t reads = 1) {
   const GraphHeader& h = g->h;
   GraphCaps need = g->caps;
   auto grow = [](uint32_t cap, uint64_t want) {
@@ -177,9 +178,9 @@ int32_t graph_reserve(spoa_gb300_graph* g, uint32_t len) {
     return (uint32_t)std::min<uint64_t>(c, 0xFFFFFFF0u);
   };
   need.nodes = grow(g->caps.nodes, (uint64_t)h.n_nodes + len + 1);
-  need.edges = grow(g->caps.edges, (uint64_t)h.n_edges + len + 2);
-  need.labels = grow(g->caps.labels, (uint64_t)h.n_labels + len + 2);
-  need.seqs = grow(g->caps.seqs, (uint64_t)h.n_seqs + 2);
+  need.edges = grow(g->caps.edges, (uint64_t)h.n_edges + len + reads + 1);
+  need.labels = grow(g->caps.labels, (uint64_t)h.n_labels + len + reads + 1);
+  need.seqs = grow(g->caps.seqs, (uint64_t)h.n_seqs + reads + 1);
   if (g->arena.p && need.nodes == g->caps.nodes && need.edges == g->caps.edges &&
       need.labels == g->caps.labels && need.seqs == g->caps.seqs)
     return kOk;
@@ -504,13 +505,93 @@ int32_t spoa_gb300_align_add(spoa_gb300_engine* en, spoa_gb300_graph* g, const c
     dq = en->qual.as<uint8_t>();
   }
   st = SPOA_BY_SUB(en->S.sub, wide, launch_align_add, cpt, nt, en->S, g->v, en->dv,
-                   en->seq.as<uint8_t>(), L, dq, strand, en->out.as<ReadOut>());
+                   en->seq.as<uint8_t>(), L, dq, strand, en->out.as<ReadOut>(), nullptr,
+                   (cudaStream_t)0);
   if (st) return st;
   CU(cudaMemcpy(en->h_out, en->out.p, sizeof(ReadOut), cudaMemcpyDeviceToHost));
   st = graph_refresh(g);
   if (en->h_out->status != kOk) return en->h_out->status;
   if (score) *score = en->h_out->score;
   if (reversed) *reversed = en->h_out->reversed;
+  return st;
+}
+
+int32_t spoa_gb300_align_add_reads(spoa_gb300_engine* en, spoa_gb300_graph* g, uint32_t n_reads,
+                                   const char* seqs, const uint64_t* seq_off, const char* quals,
+                                   int32_t strand, int32_t* scores, int32_t* reversed,
+                                   uint32_t* n_done) {
+  if (!en || !g || !seq_off || (n_reads && !seqs)) return kInvalidArgument;
+  if (n_done) *n_done = 0;
+  if (!n_reads) return kOk;
+  uint64_t sum = 0;
+  uint32_t lmax = 1;
+  for (uint32_t r = 0; r < n_reads; ++r) {
+    if (seq_off[r + 1] < seq_off[r]) return kInvalidArgument;
+    const uint64_t L = seq_off[r + 1] - seq_off[r];
+    if (L > (uint64_t)INT32_MAX) return kTooLarge;
+    lmax = std::max<uint32_t>(lmax, (uint32_t)L);
+    sum += L;
+  }
+  // room for every read, and one width and tile for the whole chain: int32
+  // when the reference's rule could pick it for any read (the int32 kernel
+  // gives int16-width reads the same results)
+  const uint64_t vmax = (uint64_t)g->h.n_nodes + sum;
+  const int32_t lanes = lanes_for(en->S, lmax, (uint32_t)std::min<uint64_t>(vmax, 0xFFFFFFFFu));
+  const bool wide = lanes != 16;
+  int32_t st = graph_reserve(g, sum, n_reads);
+  if (st) return st;
+  int cpt, nt;
+  if (!latency_tile(lmax, wide, &cpt, &nt)) return kTooLarge;
+  st = engine_reserve(en, (uint32_t)std::min<uint64_t>(vmax + 1, 0xFFFFFFF0u), (uint32_t)(cpt * nt),
+                      (uint32_t)std::min<uint64_t>((uint64_t)g->h.n_edges + sum + n_reads +
+                                                       vmax + 2, 0xFFFFFFF0u));
+  if (st) return st;
+  DeviceBuf d_seqs, d_quals, d_out;
+  const uint64_t base = seq_off[0];
+  if (d_seqs.ensure(std::max<uint64_t>(sum, 1)) || d_out.ensure(sizeof(ReadOut) * n_reads) ||
+      (quals && d_quals.ensure(std::max<uint64_t>(sum, 1))))
+    return kNoMemory;
+  cudaStream_t s = nullptr;
+  CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct Cleanup {
+    cudaStream_t s;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~Cleanup() {
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+      cudaStreamDestroy(s);
+    }
+  } c{s};
+  CU(cudaMemcpyAsync(d_seqs.p, seqs + base, sum, cudaMemcpyHostToDevice, s));
+  if (quals) CU(cudaMemcpyAsync(d_quals.p, quals + base, sum, cudaMemcpyHostToDevice, s));
+  CU(cudaStreamSynchronize(s));
+  // the per-read loop, one launch per read in order, recorded into a graph
+  ReadOut* out = d_out.as<ReadOut>();
+  CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  for (uint32_t r = 0; r < n_reads && st == kOk; ++r) {
+    const uint64_t o = seq_off[r] - base;
+    st = SPOA_BY_SUB(en->S.sub, wide, launch_align_add, cpt, nt, en->S, g->v, en->dv,
+                     d_seqs.as<uint8_t>() + o, (uint32_t)(seq_off[r + 1] - seq_off[r]),
+                     quals ? d_quals.as<uint8_t>() + o : nullptr, strand, out + r,
+                     r ? out + r - 1 : nullptr, s);
+  }
+  const cudaError_t ec = cudaStreamEndCapture(s, &c.graph);
+  if (st) return st;
+  CU(ec);
+  CU(cudaGraphInstantiate(&c.exec, c.graph, 0));
+  CU(cudaGraphLaunch(c.exec, s));
+  std::vector<ReadOut> h(n_reads);
+  CU(cudaMemcpyAsync(h.data(), out, sizeof(ReadOut) * n_reads, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  st = graph_refresh(g);
+  uint32_t done = 0;
+  for (; done < n_reads && h[done].status == kOk; ++done) {
+    if (scores) scores[done] = h[done].score;
+    if (reversed) reversed[done] = h[done].reversed;
+  }
+  if (n_done) *n_done = done;
+  if (done < n_reads) return h[done].status;
   return st;
 }
 
@@ -620,6 +701,8 @@ struct Pass {
   DpCaps dcaps{};
   int cpt = 0, nt = 0, ctas = 0;
   uint64_t stride = 0;
+  int tuned_cpt = 0, tuned_nt = 0;  // tile chosen by the tuner (0: the default)
+  int cls = 0;              // length class
   double work = 0;          // estimated DP work (sum of read lengths x longest read)
   uint64_t arena_off = 0;   // byte offset of this pass's arenas in the batch arena
   uint32_t work_off = 0;    // offset of its window list in the device work array
@@ -711,6 +794,10 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
     many_aligned = many_aligned || wp[w].many_aligned;
   }
   int cpt = d.columns_per_thread, nt = d.threads_per_window;
+  if (p->tuned_cpt > 0 && (uint64_t)p->tuned_cpt * p->tuned_nt >= L) {
+    cpt = p->tuned_cpt;
+    nt = p->tuned_nt;
+  }
   if (cpt <= 0 || nt <= 0 || (p->wide && !cpt_supported<int32_t>(cpt)) ||
       (!p->wide && !cpt_supported<int16_t>(cpt))) {
     if (!throughput_tile(L, p->wide, &cpt, &nt)) return kTooLarge;
@@ -800,6 +887,40 @@ int32_t run_pass(spoa_gb300_batch* b, const Pass& p, cudaStream_t s, bool plain,
   return kOk;
 }
 
+// ---- tile tuner ------------------------------------------------------------
+// Candidate tiles for windows up to L columns: every columns-per-thread of
+// the width with its thread count (a multiple of 32, at most 512), kept when
+// its padded row is at most 1.5x the tightest; at most four, tightest first.
+std::vector<std::pair<int, int>> tile_candidates(uint32_t L, bool wide) {
+  std::vector<std::tuple<uint64_t, int, int>> c;
+  const int* cs = wide ? kCpts32 : kCpts16;
+  const int nc = wide ? 5 : 6;
+  for (int k = 0; k < nc; ++k) {
+    const uint64_t t = std::max<uint64_t>(32, ((uint64_t)(L + cs[k] - 1) / cs[k] + 31) / 32 * 32);
+    if (t <= 512) c.emplace_back(t * cs[k], cs[k], (int)t);
+  }
+  std::sort(c.begin(), c.end());
+  std::vector<std::pair<int, int>> out;
+  for (const auto& x : c)
+    if (std::get<0>(x) * 2 <= std::get<0>(c.front()) * 3 && out.size() < 4)
+      out.emplace_back(std::get<1>(x), std::get<2>(x));
+  return out;
+}
+
+// Tiles chosen by timing, per (gap model, width, length class), for the
+// life of the process.
+std::mutex g_tune_mu;
+std::map<std::tuple<int, bool, int>, std::pair<int, int>> g_tuned;
+
+bool tuned_tile(int sub, bool wide, int cls, int* cpt, int* nt) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tuned.find(std::make_tuple(sub, wide, cls));
+  if (it == g_tuned.end()) return false;
+  *cpt = it->second.first;
+  *nt = it->second.second;
+  return true;
+}
+
 // Groups windows into passes by lane width and length class (longest read
 // up to 640 columns, i.e. one warp, then doublings: 1280, 2560, ...); each
 // pass takes the tile of its longest read.  Classes are coarse on purpose:
@@ -823,7 +944,9 @@ int32_t make_passes(spoa_gb300_batch* b, const std::vector<uint32_t>& windows,
   for (auto& g : groups) {
     Pass p;
     p.wide = std::get<0>(g.first);
+    p.cls = std::get<1>(g.first);
     p.windows = std::move(g.second);
+    if (!forced) tuned_tile(b->base.sub, p.wide, p.cls, &p.tuned_cpt, &p.tuned_nt);
     std::stable_sort(p.windows.begin(), p.windows.end(),
                      [&](uint32_t x, uint32_t y) { return work(x) > work(y); });
     double total = 0;
@@ -861,8 +984,85 @@ int32_t make_passes(spoa_gb300_batch* b, const std::vector<uint32_t>& windows,
   return kOk;
 }
 
+// Times the candidate tiles of every pass whose class has no tuned tile
+// yet, each on the same sample of the pass's windows (its longest, enough to
+// fill the GPU), keeps the fastest per window, then re-plans the passes.
+// The sample's results are overwritten by the real launch.
+int32_t autotune(spoa_gb300_batch* b, cudaStream_t s) {
+  bool changed = false;
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  for (const Pass& p : b->passes) {
+    int c0, n0;
+    if (tuned_tile(b->base.sub, p.wide, p.cls, &c0, &n0)) continue;
+    uint32_t L = 1;
+    for (uint32_t w : p.windows) L = std::max(L, b->lmax[w]);
+    const auto cands = tile_candidates(L, p.wide);
+    std::pair<int, int> best = cands.empty() ? std::make_pair(0, 0) : cands.front();
+    if (cands.size() > 1) {
+      // one sample for every candidate: at least four windows per CTA of the
+      // candidate with the most CTAs, so the pass's tail does not decide
+      Pass q;
+      q.wide = p.wide;
+      q.cls = p.cls;
+      q.windows = p.windows;
+      size_t n = 1;
+      for (const auto& c : cands) {
+        q.tuned_cpt = c.first;
+        q.tuned_nt = c.second;
+        int32_t st = plan_pass(b, &q, b->plan0);
+        if (st) return st;
+        n = std::max<size_t>(n, 4 * (size_t)q.ctas);
+      }
+      // evenly spaced over the pass (longest first), so the sample keeps
+      // its mix of window sizes
+      std::vector<uint32_t> sample;
+      const size_t step = std::max<size_t>(1, p.windows.size() / std::max<size_t>(n, 1));
+      for (size_t k = 0; k < p.windows.size() && sample.size() < n; k += step)
+        sample.push_back(p.windows[k]);
+      q.windows = sample;
+      float best_ms = 0;
+      for (const auto& c : cands) {
+        q.tuned_cpt = c.first;
+        q.tuned_nt = c.second;
+        int32_t st = plan_pass(b, &q, b->plan0);
+        if (st) return st;
+        if (b->arena.ensure(q.stride * (uint64_t)q.ctas)) return kNoMemory;
+        CU(cudaEventRecord(e0, s));
+        st = run_pass(b, q, s, false, b->d_cons.as<uint8_t>(), b->d_cons_off.as<uint64_t>());
+        if (st) return st;
+        CU(cudaEventRecord(e1, s));
+        CU(cudaEventSynchronize(e1));
+        float ms = 0;
+        CU(cudaEventElapsedTime(&ms, e0, e1));
+        if (best_ms == 0 || ms < best_ms) {
+          best_ms = ms;
+          best = c;
+        }
+      }
+    }
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[std::make_tuple((int)b->base.sub, p.wide, p.cls)] = best;
+    changed = true;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (changed) {
+    std::vector<uint32_t> all(b->n_windows);
+    for (uint32_t w = 0; w < b->n_windows; ++w) all[w] = w;
+    return make_passes(b, all, b->plan0, &b->passes);
+  }
+  return kOk;
+}
+
 int32_t launch_all(spoa_gb300_batch* b, void* stream, bool plain) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const bool forced = b->desc.columns_per_thread > 0 && b->desc.threads_per_window > 0;
+  if (b->desc.autotune && !forced && !plain) {
+    int32_t st = autotune(b, s);
+    if (st) return st;
+  }
   b->launches = 0;
   b->kernel_ms = 0;
   b->retry_cons.clear();

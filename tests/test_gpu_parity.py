@@ -186,3 +186,32 @@ def test_clear_reproduces_consensus(sample_reads):
     for r in reads:
         sg.align_add(engine, graph, r)
     assert graph.generate_consensus() == c1
+
+
+def test_autotuned_tiles_give_the_same_results():
+    """The tile tuner (timed candidates per length class) changes only speed."""
+    wins = synth.batch_windows(300, start=500) + [synth.uneven_window(k) for k in range(6)]
+    reads = [w.reads for w in wins]
+    params = synth.SCORING["batch_10k"][1]
+    kw = dict(window_types=[2] * 300 + [w.type for w in wins[300:]],
+              window_strand=[0] * 300 + [1] * 6)
+    a = sg.batch_poa(reads, 2, *params, **kw)
+    b = sg.batch_poa(reads, 2, *params, autotune=True, **kw)
+    assert (a.status == 0).all() and (b.status == 0).all()
+    assert a.consensus == b.consensus
+    assert np.array_equal(a.scores, b.scores)
+
+
+def test_per_read_loop_recorded_in_a_cuda_graph(ref_windows):
+    """align_add_reads (one launch per read, recorded into a CUDA graph)
+    gives the reference's per-read scores, strands and consensus."""
+    for rec in ref_windows[:40]:
+        engine = sg.AlignmentEngine.create(rec["type"], *rec["params"])
+        graph = sg.Graph()
+        reads = [r.encode() for r in rec["reads"]]
+        quals = [q.encode() for q in rec["quals"]] if rec["quals"] else None
+        scores, rev = sg.align_add_reads(engine, graph, reads, quals,
+                                         strand_ambiguous=rec["strand_ambiguous"])
+        assert scores == rec["expect"]["scores"], rec["name"]
+        assert [int(x) for x in rev] == rec["expect"]["reversed"], rec["name"]
+        assert graph.generate_consensus() == rec["expect"]["consensus"], rec["name"]
