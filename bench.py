@@ -43,6 +43,10 @@ sys.path.insert(0, ROOT)
 
 from spoa_gb300 import synth  # noqa: E402
 
+# tiles chosen by the tuner are kept per device model for later runs
+os.environ.setdefault("SPOA_GB300_TILE_CACHE",
+                      os.path.join(ROOT, "spoa_gb300", "_build", "tile_cache.txt"))
+
 OPS = {0: (2, 1), 1: (3, 3), 2: (5, 4)}  # per cell: a * preds + b (SW adds 1)
 TRACEBACK_BYTES_PER_CELL = 0.5          # 4-bit traceback code per DP cell
 
@@ -262,7 +266,8 @@ def main():
 
     def make_batch():
         return sg.Batch.from_arrays(seqs, off, wro, typ, *params, window_types=wtypes,
-                                    window_strand=wstrand, autotune=True)
+                                    window_strand=wstrand,
+                                    autotune=args.workload == "batch_10k")
 
     batch = make_batch()
     for _ in range(args.warmup):

@@ -175,7 +175,8 @@ typedef struct {
   int32_t autotune;                /* time the candidate tiles of every length
                                       class on a sample of its windows at the
                                       first launch and keep the fastest (cached
-                                      per process) */
+                                      per process, and per device model in the
+                                      file named by SPOA_GB300_TILE_CACHE) */
 } spoa_gb300_batch_desc;
 
 typedef struct {

@@ -908,12 +908,55 @@ std::vector<std::pair<int, int>> tile_candidates(uint32_t L, bool wide) {
 }
 
 // Tiles chosen by timing, per (gap model, width, length class), for the
-// life of the process.
+// life of the process; when SPOA_GB300_TILE_CACHE names a file they are also
+// kept there (one "device sub wide class cpt nt" line each) and reused by
+// later processes on the same device model.
 std::mutex g_tune_mu;
 std::map<std::tuple<int, bool, int>, std::pair<int, int>> g_tuned;
+bool g_tune_loaded = false;
+
+std::string device_tag() {
+  int dev = 0;
+  cudaDeviceProp prop;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return "unknown";
+  }
+  std::string t = prop.name;
+  for (char& ch : t)
+    if (ch == ' ') ch = '_';
+  return t + "_sm" + std::to_string(prop.multiProcessorCount);
+}
+
+void load_tile_cache() {  // under g_tune_mu
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char* path = std::getenv("SPOA_GB300_TILE_CACHE");
+  if (!path) return;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return;
+  const std::string tag = device_tag();
+  char dev[256];
+  int sub, wide, cls, cpt, nt;
+  while (std::fscanf(f, "%255s %d %d %d %d %d", dev, &sub, &wide, &cls, &cpt, &nt) == 6)
+    if (tag == dev && cpt > 0 && nt > 0)
+      g_tuned[std::make_tuple(sub, wide != 0, cls)] = std::make_pair(cpt, nt);
+  std::fclose(f);
+}
+
+void save_tile(int sub, bool wide, int cls, int cpt, int nt) {  // under g_tune_mu
+  g_tuned[std::make_tuple(sub, wide, cls)] = std::make_pair(cpt, nt);
+  const char* path = std::getenv("SPOA_GB300_TILE_CACHE");
+  if (!path) return;
+  if (FILE* f = std::fopen(path, "a")) {
+    std::fprintf(f, "%s %d %d %d %d %d\n", device_tag().c_str(), sub, wide ? 1 : 0, cls, cpt, nt);
+    std::fclose(f);
+  }
+}
 
 bool tuned_tile(int sub, bool wide, int cls, int* cpt, int* nt) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
+  load_tile_cache();
   auto it = g_tuned.find(std::make_tuple(sub, wide, cls));
   if (it == g_tuned.end()) return false;
   *cpt = it->second.first;
@@ -1043,7 +1086,7 @@ int32_t autotune(spoa_gb300_batch* b, cudaStream_t s) {
       }
     }
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tuned[std::make_tuple((int)b->base.sub, p.wide, p.cls)] = best;
+    save_tile((int)b->base.sub, p.wide, p.cls, best.first, best.second);
     changed = true;
   }
   cudaEventDestroy(e0);
