@@ -215,3 +215,28 @@ def test_per_read_loop_recorded_in_a_cuda_graph(ref_windows):
         assert scores == rec["expect"]["scores"], rec["name"]
         assert [int(x) for x in rev] == rec["expect"]["reversed"], rec["name"]
         assert graph.generate_consensus() == rec["expect"]["consensus"], rec["name"]
+
+
+def test_windows_that_outgrow_their_arena_and_the_int16_width():
+    """20-letter noisy windows grow to ~10k nodes: more than the first arena
+    (4,096 nodes, 4 aligned nodes per node) and past the int16 rule, which
+    the width estimate did not foresee; they rerun with twice the capacity
+    and the int32 kernel, in the batch and in the server."""
+    rng = np.random.Generator(np.random.PCG64(79))
+    wins = [synth.random_window(rng, 300, 40, err=0.6, alphabet=b"ACDEFGHIKLMNPQRSTVWY")
+            for _ in range(3)] + [w.reads for w in synth.batch_windows(3, start=900)]
+    params = synth.SCORING["batch_10k"][1]
+    res = sg.batch_poa(wins, 2, *params)
+    assert (res.status == 0).all()
+    assert res.launches > 1  # the reruns
+    r0 = 0
+    for k, w in enumerate(wins):
+        ref = po.run_window(2, *params, w, with_msa=False)
+        assert res.scores[r0:r0 + len(w)].tolist() == ref.scores, k
+        assert res.consensus[k] == ref.consensus, k
+        r0 += len(w)
+    with sg.Server(2, *params) as sv:
+        tickets = [sv.submit(w) for w in wins]
+        got = [sv.wait(t, timeout=600) for t in tickets]
+    assert [g[0] for g in got] == [0] * len(wins)
+    assert [g[1] for g in got] == res.consensus
