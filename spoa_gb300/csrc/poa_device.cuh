@@ -79,14 +79,20 @@ struct GraphHeader {
 struct GraphView {
   GraphHeader* hdr;
   uint8_t* code;
-  uint32_t *in_first, *in_last, *out_first, *out_last, *in_deg;
+  // per node: x = first in-edge, y = last in-edge, z = first out-edge,
+  // w = last out-edge (edge lists in insertion order); one line per node
+  uint4* nlink;
+  uint32_t* in_deg;
   uint8_t* n_aligned;
   uint32_t* aligned;  // [nodes * caps.aligned]
   // per node: x = in-degree | aligned count << 16, y/z/w = the first three
   // in-edge tails in insertion order (one 16-byte load per DFS step)
   uint4* nrec;
   uint32_t *rank_to_node, *node_to_rank;
-  uint32_t *e_tail, *e_head, *e_next_in, *e_next_out, *e_lab_first, *e_lab_last;
+  // per edge: x = tail, y = head, z = next in-edge of the head, w = next
+  // out-edge of the tail; one 16-byte load per step of a list walk
+  uint4* erec;
+  uint32_t *e_lab_first, *e_lab_last;
   int64_t* e_weight;
   uint32_t *lab_seq, *lab_next;
   uint32_t* seq_begin;
@@ -115,20 +121,14 @@ __host__ __device__ inline uint64_t graph_layout(uint8_t* base, const GraphCaps&
   v->stack_cap = E + N * (uint64_t)(c.aligned + 1) + 1;
   v->hdr = reinterpret_cast<GraphHeader*>(take(sizeof(GraphHeader)));
   v->code = take(N);
-  v->in_first = reinterpret_cast<uint32_t*>(take(4 * N));
-  v->in_last = reinterpret_cast<uint32_t*>(take(4 * N));
-  v->out_first = reinterpret_cast<uint32_t*>(take(4 * N));
-  v->out_last = reinterpret_cast<uint32_t*>(take(4 * N));
+  v->nlink = reinterpret_cast<uint4*>(take(16 * N));
   v->in_deg = reinterpret_cast<uint32_t*>(take(4 * N));
   v->n_aligned = take(N);
   v->aligned = reinterpret_cast<uint32_t*>(take(4 * N * c.aligned));
   v->nrec = reinterpret_cast<uint4*>(take(16 * N));
   v->rank_to_node = reinterpret_cast<uint32_t*>(take(4 * N));
   v->node_to_rank = reinterpret_cast<uint32_t*>(take(4 * N));
-  v->e_tail = reinterpret_cast<uint32_t*>(take(4 * E));
-  v->e_head = reinterpret_cast<uint32_t*>(take(4 * E));
-  v->e_next_in = reinterpret_cast<uint32_t*>(take(4 * E));
-  v->e_next_out = reinterpret_cast<uint32_t*>(take(4 * E));
+  v->erec = reinterpret_cast<uint4*>(take(16 * E));
   v->e_lab_first = reinterpret_cast<uint32_t*>(take(4 * E));
   v->e_lab_last = reinterpret_cast<uint32_t*>(take(4 * E));
   v->e_weight = reinterpret_cast<int64_t*>(take(8 * E));
@@ -289,7 +289,7 @@ __device__ inline int64_t g_add_node(GraphView& G, uint32_t code) {
   if (h->n_nodes >= G.caps.nodes) return -1;
   uint32_t id = h->n_nodes++;
   G.code[id] = (uint8_t)code;
-  G.in_first[id] = G.in_last[id] = G.out_first[id] = G.out_last[id] = kNone;
+  G.nlink[id] = make_uint4(kNone, kNone, kNone, kNone);
   G.in_deg[id] = 0;
   G.n_aligned[id] = 0;
   G.nrec[id] = make_uint4(0, kNone, kNone, kNone);
@@ -313,26 +313,28 @@ __device__ inline int g_add_label(GraphView& G, uint32_t e) {
 
 // Graph::AddEdge (graph.cpp:81-91)
 __device__ inline int g_add_edge(GraphView& G, uint32_t tail, uint32_t head, uint32_t w) {
-  for (uint32_t e = G.out_first[tail]; e != kNone; e = G.e_next_out[e]) {
-    if (G.e_head[e] == head) {
+  for (uint32_t e = G.nlink[tail].z; e != kNone;) {
+    const uint4 er = G.erec[e];
+    if (er.y == head) {
       if (g_add_label(G, e)) return -1;
       G.e_weight[e] += w;
       return 0;
     }
+    e = er.w;
   }
   GraphHeader* h = G.hdr;
   if (h->n_edges >= G.caps.edges) return -1;
   uint32_t e = h->n_edges++;
-  G.e_tail[e] = tail;
-  G.e_head[e] = head;
+  G.erec[e] = make_uint4(tail, head, kNone, kNone);
   G.e_weight[e] = w;
-  G.e_next_in[e] = G.e_next_out[e] = kNone;
   G.e_lab_first[e] = G.e_lab_last[e] = kNone;
   if (g_add_label(G, e)) return -1;
-  if (G.out_last[tail] != kNone) G.e_next_out[G.out_last[tail]] = e; else G.out_first[tail] = e;
-  G.out_last[tail] = e;
-  if (G.in_last[head] != kNone) G.e_next_in[G.in_last[head]] = e; else G.in_first[head] = e;
-  G.in_last[head] = e;
+  const uint4 lt = G.nlink[tail];
+  if (lt.w != kNone) G.erec[lt.w].w = e; else G.nlink[tail].z = e;
+  G.nlink[tail].w = e;
+  const uint4 lh = G.nlink[head];
+  if (lh.y != kNone) G.erec[lh.y].z = e; else G.nlink[head].x = e;
+  G.nlink[head].y = e;
   const uint32_t d = G.in_deg[head];
   G.in_deg[head] = d + 1;
   uint4 r = G.nrec[head];
@@ -407,10 +409,10 @@ static __device__ __noinline__ int g_topo_sort_cta(GraphView& G, int* s_ret) {
           if (deg > 1 && !bit(r.z, kDone)) { if (!push(r.z)) { rc = -1; break; } valid = false; }
           if (deg > 2 && !bit(r.w, kDone)) { if (!push(r.w)) { rc = -1; break; } valid = false; }
           if (deg > 3) {
-            uint32_t e = G.in_first[curr];
-            for (int k = 0; k < 3 && e != kNone; ++k) e = G.e_next_in[e];
-            for (; e != kNone; e = G.e_next_in[e]) {
-              const uint32_t tl = G.e_tail[e];
+            uint32_t e = G.nlink[curr].x;
+            for (int k = 0; k < 3 && e != kNone; ++k) e = G.erec[e].z;
+            for (; e != kNone; e = G.erec[e].z) {
+              const uint32_t tl = G.erec[e].x;
               if (!bit(tl, kDone)) { if (!push(tl)) { rc = -1; break; } valid = false; }
             }
             if (rc) break;
@@ -557,10 +559,10 @@ static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32
 // ---------------------------------------------------------------------------
 __device__ inline uint32_t g_branch_completion(GraphView& G, uint32_t rank) {
   const uint32_t start = G.rank_to_node[rank];
-  for (uint32_t e = G.out_first[start]; e != kNone; e = G.e_next_out[e]) {
-    uint32_t hd = G.e_head[e];
-    for (uint32_t f = G.in_first[hd]; f != kNone; f = G.e_next_in[f]) {
-      uint32_t t = G.e_tail[f];
+  for (uint32_t e = G.nlink[start].z; e != kNone; e = G.erec[e].w) {
+    uint32_t hd = G.erec[e].y;
+    for (uint32_t f = G.nlink[hd].x; f != kNone; f = G.erec[f].z) {
+      uint32_t t = G.erec[f].x;
       if (t != start) G.cscore[t] = -1;
     }
   }
@@ -570,8 +572,8 @@ __device__ inline uint32_t g_branch_completion(GraphView& G, uint32_t rank) {
     uint32_t it = G.rank_to_node[r];
     G.cscore[it] = -1;
     G.cpred[it] = kNone;
-    for (uint32_t f = G.in_first[it]; f != kNone; f = G.e_next_in[f]) {
-      uint32_t t = G.e_tail[f];
+    for (uint32_t f = G.nlink[it].x; f != kNone; f = G.erec[f].z) {
+      uint32_t t = G.erec[f].x;
       if (G.cscore[t] == -1) continue;
       int64_t w = G.e_weight[f];
       if (G.cscore[it] < w || (G.cscore[it] == w && G.cscore[G.cpred[it]] <= G.cscore[t])) {
@@ -596,8 +598,8 @@ static __device__ __noinline__ void g_consensus(GraphView& G) {
   uint32_t mx = kNone;
   for (uint32_t r = 0; r < nn; ++r) {
     uint32_t it = G.rank_to_node[r];
-    for (uint32_t f = G.in_first[it]; f != kNone; f = G.e_next_in[f]) {
-      uint32_t t = G.e_tail[f];
+    for (uint32_t f = G.nlink[it].x; f != kNone; f = G.erec[f].z) {
+      uint32_t t = G.erec[f].x;
       int64_t w = G.e_weight[f];
       if (G.cscore[it] < w || (G.cscore[it] == w && G.cscore[G.cpred[it]] <= G.cscore[t])) {
         G.cscore[it] = w;
@@ -608,7 +610,7 @@ static __device__ __noinline__ void g_consensus(GraphView& G) {
     if (mx == kNone || G.cscore[mx] < G.cscore[it]) mx = it;
   }
   // each completion moves to a strictly later rank
-  while (G.out_first[mx] != kNone) {
+  while (G.nlink[mx].z != kNone) {
     uint32_t nx = g_branch_completion(G, G.node_to_rank[mx]);
     if (nx == kNone) break;
     mx = nx;
@@ -629,9 +631,9 @@ static __device__ __noinline__ void g_consensus(GraphView& G) {
 
 // Node::Successor (graph.cpp:22-30)
 __device__ inline uint32_t g_successor(const GraphView& G, uint32_t node, uint32_t label) {
-  for (uint32_t e = G.out_first[node]; e != kNone; e = G.e_next_out[e]) {
+  for (uint32_t e = G.nlink[node].z; e != kNone; e = G.erec[e].w) {
     for (uint32_t l = G.e_lab_first[e]; l != kNone; l = G.lab_next[l]) {
-      if (G.lab_seq[l] == label) return G.e_head[e];
+      if (G.lab_seq[l] == label) return G.erec[e].y;
       if (G.lab_seq[l] > label) break;  // labels are appended in sequence order
     }
   }

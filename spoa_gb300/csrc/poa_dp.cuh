@@ -160,7 +160,7 @@ static __device__ __noinline__ void dp_build_rows(const GraphView& G, DpView& D,
     D.row_indeg[i] = d;
     const uint8_t ch = (uint8_t)G.hdr->decoder[G.code[node]];
     D.row_char[i] = ch;
-    uint8_t flags = G.out_first[node] == kNone ? kRowSink : 0;
+    uint8_t flags = G.nlink[node].z == kNone ? kRowSink : 0;
     const uint32_t begin = off;
     uint32_t other[2] = {kNone, kNone}, n_other = 0;
     if (d == 0) {
@@ -169,8 +169,8 @@ static __device__ __noinline__ void dp_build_rows(const GraphView& G, DpView& D,
       if (i == 1) flags |= kRowPrevPred;
       else other[n_other++] = 0;
     } else {
-      for (uint32_t e = G.in_first[node]; e != kNone; e = G.e_next_in[e]) {
-        const uint32_t p = G.node_to_rank[G.e_tail[e]] + 1;
+      for (uint32_t e = G.nlink[node].x; e != kNone; e = G.erec[e].z) {
+        const uint32_t p = G.node_to_rank[G.erec[e].x] + 1;
         D.preds[off++] = p;
         if (p == i - 1) {
           flags |= kRowPrevPred;

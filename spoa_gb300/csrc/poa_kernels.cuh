@@ -299,12 +299,12 @@ __global__ void k_export(GraphView G, ExportPtrs x) {
     if (x.chars) x.chars[v] = (uint8_t)h->decoder[G.code[v]];
     if (x.codes) x.codes[v] = G.code[v];
     if (x.in_off) x.in_off[v] = io;
-    for (uint32_t e = G.in_first[v]; e != kNone; e = G.e_next_in[e]) {
+    for (uint32_t e = G.nlink[v].x; e != kNone; e = G.erec[e].z) {
       if (x.in_edges) x.in_edges[io] = e;
       ++io;
     }
     if (x.out_off) x.out_off[v] = oo;
-    for (uint32_t e = G.out_first[v]; e != kNone; e = G.e_next_out[e]) {
+    for (uint32_t e = G.nlink[v].z; e != kNone; e = G.erec[e].w) {
       if (x.out_edges) x.out_edges[oo] = e;
       ++oo;
     }
@@ -320,8 +320,8 @@ __global__ void k_export(GraphView G, ExportPtrs x) {
   if (x.al_off) x.al_off[nn] = ao;
   uint32_t lo = 0;
   for (uint32_t e = 0; e < ne; ++e) {
-    if (x.e_tail) x.e_tail[e] = G.e_tail[e];
-    if (x.e_head) x.e_head[e] = G.e_head[e];
+    if (x.e_tail) x.e_tail[e] = G.erec[e].x;
+    if (x.e_head) x.e_head[e] = G.erec[e].y;
     if (x.e_weight) x.e_weight[e] = G.e_weight[e];
     if (x.lab_off) x.lab_off[e] = lo;
     for (uint32_t l = G.e_lab_first[e]; l != kNone; l = G.lab_next[l]) {

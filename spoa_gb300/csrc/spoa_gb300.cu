@@ -197,20 +197,14 @@ int32_t graph_reserve(spoa_gb300_graph* g, uint64_t len, uint64_t reads = 1) {
 #define CP(field, count, esz) \
   if (count) CU(cudaMemcpy(nv.field, o.field, (count) * (esz), cudaMemcpyDeviceToDevice))
     CP(code, N, 1);
-    CP(in_first, N, 4);
-    CP(in_last, N, 4);
-    CP(out_first, N, 4);
-    CP(out_last, N, 4);
+    CP(nlink, N, 16);
     CP(in_deg, N, 4);
     CP(n_aligned, N, 1);
     CP(aligned, N * K, 4);
     CP(nrec, N, 16);
     CP(rank_to_node, N, 4);
     CP(node_to_rank, N, 4);
-    CP(e_tail, E, 4);
-    CP(e_head, E, 4);
-    CP(e_next_in, E, 4);
-    CP(e_next_out, E, 4);
+    CP(erec, E, 16);
     CP(e_lab_first, E, 4);
     CP(e_lab_last, E, 4);
     CP(e_weight, E, 8);
