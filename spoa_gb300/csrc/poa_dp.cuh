@@ -775,10 +775,9 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
 }
 
 // Traceback from (max_i, max_j) (implementation.hpp:955-1124, 1324-1574,
-// 1826-2121), thread 0.  Diagonal and vertical moves are re-derived from the
-// stored H/F/O rows exactly as the reference does; horizontal moves and the
-// extend_left run come from the per-cell codes.  Pairs are written to `out`
-// in forward order.
+// 1826-2121), thread 0.  Every move is re-derived from the stored
+// H/F/O/E/Q rows with the reference's tests in the reference's order.
+// Pairs are written to `out` in forward order.
 template <int SUB, int CPT, typename T>
 static __device__ __noinline__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphView& G,
                                 const uint8_t* seq, uint32_t L, uint32_t V, int64_t max_i,
