@@ -4,4 +4,5 @@
 
 namespace spoa_gb300 {
 SPOA_GB300_INSTANTIATE(kLinear, int32_t)
+SPOA_GB300_INSTANTIATE_SEG(kLinear)
 }  // namespace spoa_gb300

@@ -774,6 +774,338 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
   *out_score = score;
 }
 
+// Forward pass for rows longer than one strip per thread can hold: thread t
+// owns SEGS strips of CPT columns, strip g being virtual thread g*nt + t of
+// a CTA of SEGS*nt virtual threads (the row layout and colmap use that
+// width).  Per row the strips are processed left to right; every scan of a
+// strip starts from the carry of the strip before it (passed through shared
+// memory from its last thread), and the previous row is read back from
+// memory like any other predecessor instead of being kept in registers.
+// Same results as dp_forward, cell by cell.
+template <int SUB, int CPT, typename T, int SEGS>
+__device__ __noinline__ void dp_forward_seg(const Scoring& S, DpView& D,
+                                            const uint8_t* __restrict__ seq, uint32_t L,
+                                            uint32_t V, int32_t lanes, BlockScratch& sh,
+                                            int64_t* out_max_i, int64_t* out_max_j,
+                                            int32_t* out_score) {
+  using Lx = Lanes<T>;
+  using P = typename Lx::P;
+  using L16 = Lanes<int16_t>;
+  constexpr int HP = CPT / 2;
+  const uint32_t t = threadIdx.x, nt = blockDim.x, ntv = nt * SEGS;
+  const uint64_t ld = D.caps.ld;
+  const uint64_t wrow = ld / 2;
+  const uint64_t st2 = 2 * (uint64_t)ntv;
+  const int32_t type = S.type;
+  const int32_t m = S.m, n = S.n, g = S.g, e = S.e, q = S.q, c = S.c;
+  const int32_t NEGW = lanes == 8 ? (INT32_MIN + 1024) : (INT16_MIN + 1024);
+  void* __restrict__ H = D.H;
+  void* __restrict__ F = D.F;
+  void* __restrict__ O = D.O;
+  void* __restrict__ E = D.E;
+  void* __restrict__ Q = D.Q;
+  const P NEG2 = Lx::splat(Lx::kNeg);
+  const uint32_t NZ = S.min16x2;
+  const P m2 = Lx::splat(m), n2 = Lx::splat(n);
+  const P g2 = Lx::splat(g), e2 = Lx::splat(e), q2 = Lx::splat(q), c2 = Lx::splat(c);
+  const P ge2 = Lx::splat(g - e), qc2 = Lx::splat(q - c);
+  auto first_col = [&](uint32_t sg) { return (sg * nt + t) * CPT; };
+  // row 0 (implementation.hpp:555-694)
+  auto ramp = [&](int32_t j) -> int32_t {
+    if (type == kSW) return 0;
+    if (SUB == kConvex) return imax(g + j * e, q + j * c);
+    if (SUB == kAffine) return g + j * e;
+    return g + j * g;
+  };
+#pragma unroll 1
+  for (int sg = 0; sg < SEGS; ++sg) {
+    const uint32_t s0 = first_col(sg);
+    const uint64_t w0 = 2 * (uint64_t)(sg * nt + t);
+#pragma unroll
+    for (int k = 0; k < HP; k += 2) {
+      const P h0 = Lx::make(ramp((int32_t)(s0 + k)), ramp((int32_t)(s0 + HP + k)));
+      const P h1 = Lx::make(ramp((int32_t)(s0 + k + 1)), ramp((int32_t)(s0 + HP + k + 1)));
+      const uint64_t wk = w0 + (k / 2) * st2;
+      Lx::store2(H, wk, h0, h1);
+      if (SUB >= kAffine) Lx::store2(F, wk, NEG2, NEG2);
+      if (SUB == kConvex) Lx::store2(O, wk, NEG2, NEG2);
+    }
+  }
+  if (t == 0) {
+    D.fc[0] = 0;
+    D.fcF[0] = 0;
+    D.fcO[0] = 0;
+  }
+  int32_t bval = type == kSW ? 0 : (type == kOV ? kNegBig : NEGW);
+  int32_t brow = -1;
+  int32_t first_sink = -1;
+  // the strip holding column L-1 (NW selection)
+  const uint32_t tv_last = (L - 1) / CPT;
+  const int32_t last_k = (int32_t)(((L - 1) % CPT) % HP), last_hi = (int32_t)(((L - 1) % CPT) / HP);
+  __syncthreads();
+  for (uint32_t i = 1; i <= V; ++i) {
+    const uint4 rec = D.rowrec[i];
+    const uint32_t rflags = (rec.y >> 16) & 0xFFu;
+    const L16::P rc2 = L16::splat(rec.y >> 24);
+    const uint32_t pb = rec.x, pe = D.pred_ptr[i + 1];
+    // first column (thread 0): NW takes the best predecessor's plus a gap
+    int32_t fci = 0;
+    if (t == 0) {
+      int32_t fl = kNegBig, fa = kNegBig, fo = kNegBig;
+      for (uint32_t pi = pb; pi < pe; ++pi) {
+        const uint32_t p = D.preds[pi];
+        fl = imax(fl, D.fc[p]);
+        if (SUB >= kAffine) fa = imax(fa, D.fcF[p]);
+        if (SUB == kConvex) fo = imax(fo, D.fcO[p]);
+      }
+      const bool source = (rflags & kRowSource) != 0;
+      if (type == kNW) {
+        if (SUB == kLinear) {
+          fci = (source ? 0 : fl) + g;
+        } else {
+          const int32_t vF = (source ? g - e : fa) + e;
+          D.fcF[i] = vF;
+          if (SUB == kConvex) {
+            const int32_t vO = (source ? q - c : fo) + c;
+            D.fcO[i] = vO;
+            fci = imax(vF, vO);
+          } else {
+            fci = vF;
+          }
+        }
+      }
+      D.fc[i] = fci;
+    }
+    // scan carries from the previous strip (thread 0)
+    int32_t carry_q = 0, carry_e = 0, carry_h = 0;
+#pragma unroll 1
+    for (int sg = 0; sg < SEGS; ++sg) {
+      const uint32_t tv = sg * nt + t;
+      const uint32_t s0 = tv * CPT;
+      const uint64_t w0 = 2 * (uint64_t)tv;
+      uint32_t c8[(HP + 3) / 4], ch8[(HP + 3) / 4];
+#pragma unroll
+      for (int k4 = 0; k4 < (HP + 3) / 4; ++k4) {
+        uint32_t lo = 0, hi = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const uint32_t k = k4 * 4 + b;
+          const uint32_t jl = s0 + k, jh = s0 + HP + k;
+          lo |= (k < HP && jl < L ? (uint32_t)seq[jl] : 0xFFu) << (8 * b);
+          hi |= (k < HP && jh < L ? (uint32_t)seq[jh] : 0xFFu) << (8 * b);
+        }
+        c8[k4] = lo;
+        ch8[k4] = hi;
+      }
+      // every predecessor, the previous row included, from memory
+      P hd[HP], f[HP], o[HP];
+      bool first = true;
+      for (uint32_t pi = pb; pi < pe; ++pi) {
+        const uint32_t p = D.preds[pi];
+        P hp[HP], fp[HP], op[HP];
+        const uint64_t rwp = (uint64_t)p * wrow + w0;
+#pragma unroll
+        for (int k = 0; k < HP; k += 2) {
+          const uint64_t wk = rwp + (k / 2) * st2;
+          Lx::load2(H, wk, hp[k], hp[k + 1]);
+          if (SUB >= kAffine) Lx::load2(F, wk, fp[k], fp[k + 1]);
+          if (SUB == kConvex) Lx::load2(O, wk, op[k], op[k + 1]);
+        }
+        const int32_t hleft = tv == 0 ? D.fc[p]
+                                      : Lx::elem(H, (uint64_t)p * ld + 2 * ((HP / 2 - 1) * st2 + w0 - 1) + 1);
+#pragma unroll
+        for (int k = 0; k < HP; ++k) {
+          const P left = k == 0 ? Lx::make(hleft, Lx::lo(hp[HP - 1])) : hp[k - 1];
+          hd[k] = first ? left : Lx::max(hd[k], left, NZ);
+          if (SUB == kLinear) {
+            f[k] = first ? hp[k] : Lx::max(f[k], hp[k], NZ);
+          } else {
+            f[k] = first ? Lx::addmax(hp[k], ge2, fp[k]) : Lx::max3(f[k], Lx::add(hp[k], ge2), fp[k]);
+            if (SUB == kConvex)
+              o[k] = first ? Lx::addmax(hp[k], qc2, op[k]) : Lx::max3(o[k], Lx::add(hp[k], qc2), op[k]);
+          }
+        }
+        first = false;
+      }
+      const uint64_t rw = (uint64_t)i * wrow + w0;
+      P h[HP];
+#pragma unroll
+      for (int k = 0; k < HP; ++k) {
+        const uint32_t chars = __byte_perm(c8[k / 4], ch8[k / 4], (uint32_t)(k % 4) | (0x4u + k % 4) << 8) &
+                               0x00FF00FFu;
+        const P d = Lx::add(hd[k], Lx::profile(chars, rc2.v, m2, n2));
+        if (SUB == kLinear) {
+          h[k] = Lx::addmax(f[k], g2, d);
+        } else {
+          f[k] = Lx::add(f[k], e2);
+          if (SUB == kConvex) {
+            o[k] = Lx::add(o[k], c2);
+            h[k] = Lx::max3(d, f[k], o[k]);
+          } else {
+            h[k] = Lx::max(d, f[k], NZ);
+          }
+        }
+      }
+      if (SUB >= kAffine) {
+#pragma unroll
+        for (int k = 0; k < HP; k += 2) {
+          Lx::store2(F, rw + (k / 2) * st2, f[k], f[k + 1]);
+          if (SUB == kConvex) Lx::store2(O, rw + (k / 2) * st2, o[k], o[k + 1]);
+        }
+      }
+      P hs[HP], ee[HP], qq[HP];
+      int32_t out_q = 0, out_e = 0, out_h = 0;  // this strip's carries (its last column)
+      if (SUB == kLinear) {
+#pragma unroll
+        for (int k = 0; k < HP; ++k) hs[k] = h[k];
+        pair_scan<CPT, Lx>(hs, sg == 0 ? fci : carry_h, g, sh);
+        out_h = Lx::hi(hs[HP - 1]);
+        if (type == kSW) {
+          const P z = Lx::splat(0);
+#pragma unroll
+          for (int k = 0; k < HP; ++k) hs[k] = Lx::max(hs[k], z, NZ);
+        }
+      } else {
+        if (SUB == kConvex) {
+          P x[HP];
+#pragma unroll
+          for (int k = 0; k < HP; ++k) x[k] = Lx::add(h[k], q2);
+          const int32_t qin = pair_scan<CPT, Lx>(x, sg == 0 ? fci + q : carry_q, c, sh);
+          out_q = Lx::hi(x[HP - 1]);
+          qq[0] = Lx::make(qin, Lx::lo(x[HP - 1]));
+#pragma unroll
+          for (int k = 1; k < HP; ++k) qq[k] = x[k - 1];
+        }
+        {
+          uint32_t bmap = 0;
+          if (SUB == kConvex) {
+#pragma unroll
+            for (int k = 0; k < HP; ++k) {
+              if ((s0 + k + 1) % (uint32_t)lanes == 0) bmap |= 1u << k;
+              if ((s0 + HP + k + 1) % (uint32_t)lanes == 0) bmap |= 1u << (16 + k);
+            }
+          }
+          P x[HP];
+#pragma unroll
+          for (int k = 0; k < HP; ++k) {
+            if (SUB == kConvex) {
+              const uint32_t bm = (((bmap >> k) & 1u) ? 0x0000FFFFu : 0u) |
+                                  (((bmap >> (16 + k)) & 1u) ? 0xFFFF0000u : 0u);
+              x[k] = Lx::addmax(h[k], g2, Lx::select(bm, Lx::add(qq[k], g2), NEG2));
+            } else {
+              x[k] = Lx::add(h[k], g2);
+            }
+          }
+          const int32_t ein = pair_scan<CPT, Lx>(x, sg == 0 ? fci + g : carry_e, e, sh);
+          out_e = Lx::hi(x[HP - 1]);
+          ee[0] = Lx::make(ein, Lx::lo(x[HP - 1]));
+#pragma unroll
+          for (int k = 1; k < HP; ++k) ee[k] = x[k - 1];
+        }
+#pragma unroll
+        for (int k = 0; k < HP; ++k) {
+          if (SUB == kConvex)
+            hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], qq[k]) : Lx::max3(h[k], ee[k], qq[k]);
+          else
+            hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], ee[k]) : Lx::max(h[k], ee[k], NZ);
+        }
+      }
+      if (SUB >= kAffine) {
+#pragma unroll
+        for (int k = 0; k < HP; k += 2) {
+          Lx::store2(E, rw + (k / 2) * st2, ee[k], ee[k + 1]);
+          if (SUB == kConvex) Lx::store2(Q, rw + (k / 2) * st2, qq[k], qq[k + 1]);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < HP; k += 2) Lx::store2(H, rw + (k / 2) * st2, hs[k], hs[k + 1]);
+      // row selection (strict <: the earliest row wins a tie)
+      if (type == kNW) {
+        if ((rflags & kRowSink) && tv == tv_last) {
+          int32_t v = kNegBig;
+#pragma unroll
+          for (int k = 0; k < HP; ++k)
+            if (k == last_k) v = last_hi ? Lx::hi(hs[k]) : Lx::lo(hs[k]);
+          if (v > bval) {
+            bval = v;
+            brow = (int32_t)i;
+          }
+        }
+      } else if ((type == kSW || (rflags & kRowSink)) && s0 < L) {
+        P mx = NEG2;
+#pragma unroll
+        for (int k = 0; k < HP; ++k) {
+          const uint32_t vm = (s0 + k < L ? 0x0000FFFFu : 0u) | (s0 + HP + k < L ? 0xFFFF0000u : 0u);
+          mx = Lx::max(mx, Lx::select(vm, hs[k], NEG2), NZ);
+        }
+        const int32_t tm = imax(Lx::lo(mx), Lx::hi(mx));
+        if (tm > bval) {
+          bval = tm;
+          brow = (int32_t)i;
+        }
+      }
+      // hand this strip's carries to thread 0 for the next strip
+      if (SEGS > 1 && sg + 1 < SEGS) {
+        if (t == nt - 1) {
+          sh.bcast[0] = out_q;
+          sh.bcast[1] = out_e;
+          sh.bcast[2] = out_h;
+        }
+        __syncthreads();
+        carry_q = sh.bcast[0];
+        carry_e = sh.bcast[1];
+        carry_h = sh.bcast[2];
+        __syncthreads();
+      }
+    }
+    if (type == kOV && (rflags & kRowSink) && first_sink < 0) first_sink = (int32_t)i;
+    __syncthreads();
+  }
+
+  // global selection: best value, then the earliest row reaching it
+  const int32_t B = block_max(bval, sh);
+  const int32_t R = block_min(bval == B && brow >= 0 ? brow : 0x7fffffff, sh);
+  int64_t max_i = -1;
+  int32_t score = 0;
+  if (type == kSW) {
+    if (B > 0 && R != 0x7fffffff) {
+      max_i = R;
+      score = B;
+    }
+  } else if (type == kOV) {
+    if (B > 0) {
+      max_i = R;
+      score = B;
+    } else {
+      max_i = first_sink;
+      score = 0;
+    }
+  } else {
+    if (R != 0x7fffffff && B > NEGW) {
+      max_i = R;
+      score = B;
+    }
+  }
+  int64_t max_j = -1;
+  if (max_i >= 0) {
+    if (type == kNW) {
+      max_j = (int64_t)L - 1;
+    } else {
+      const uint64_t base = (uint64_t)max_i * ld;
+      int32_t jj = 0x7fffffff;
+      for (int sg = 0; sg < SEGS && jj == 0x7fffffff; ++sg)
+        for (int r = 0; r < CPT && jj == 0x7fffffff; ++r) {
+          const uint32_t j = first_col(sg) + r;
+          if (j < L && Lx::elem(H, base + colmap<CPT>(j, ntv)) == score) jj = (int32_t)j;
+        }
+      jj = block_min(jj, sh);
+      max_j = jj == 0x7fffffff ? -1 : jj;
+    }
+  }
+  *out_max_i = max_i;
+  *out_max_j = max_j;
+  *out_score = score;
+}
 // Traceback from (max_i, max_j) (implementation.hpp:955-1124, 1324-1574,
 // 1826-2121), thread 0.  Every move is re-derived from the stored
 // H/F/O/E/Q rows with the reference's tests in the reference's order.
@@ -781,7 +1113,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
 template <int SUB, int CPT, typename T>
 static __device__ __noinline__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphView& G,
                                 const uint8_t* seq, uint32_t L, uint32_t V, int64_t max_i,
-                                int64_t max_j, int32_t* out, uint32_t* n_out) {
+                                int64_t max_j, int32_t* out, uint32_t* n_out, uint32_t ntv) {
   using Lx = Lanes<T>;
   const uint64_t ld = D.caps.ld;
   const int32_t type = S.type;
@@ -791,7 +1123,7 @@ static __device__ __noinline__ int32_t dp_traceback(const Scoring& S, const DpVi
   const void* O = D.O;
   const void* E = D.E;
   const void* Q = D.Q;
-  const uint64_t nt = blockDim.x;  // the forward pass's CTA width
+  const uint64_t nt = ntv;  // the forward pass's row width in strips
   auto at = [&](const void* M, int64_t row, int64_t col) -> int32_t {
     return Lx::elem(M, (uint64_t)row * ld + colmap<CPT>((uint64_t)col, nt));
   };

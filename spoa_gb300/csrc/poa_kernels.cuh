@@ -35,21 +35,25 @@ struct SharedState {
 // int32 otherwise.  An int32 kernel runs int16-width reads with the 16-lane
 // semantics (vector starts of the convex E recurrence, -infinity of the NW
 // row selection), which gives the same results.
-template <int SUB, int CPT, typename T>
+template <int SUB, int CPT, typename T, int SEGS = 1>
 __device__ void read_align(const Scoring& S, const GraphView& G, DpView& D, BlockScratch& sh,
                            SharedState& ss, const uint8_t* seq, uint32_t L, int32_t lanes,
                            int32_t* pairs, int32_t* has, int32_t* score, uint32_t* np) {
   int64_t mi, mj;
   int32_t sc;
   const uint32_t V = G.hdr->n_nodes;
-  dp_forward<SUB, CPT, T>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
+  if constexpr (SEGS == 1)
+    dp_forward<SUB, CPT, T>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
+  else
+    dp_forward_seg<SUB, CPT, T, SEGS>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
   if (threadIdx.x == 0) {
     *np = 0;
     *has = 0;
     if (mi >= 0) {
       *has = 1;
       *score = sc;
-      const int32_t st = dp_traceback<SUB, CPT, T>(S, D, G, seq, L, V, mi, mj, pairs, np);
+      const int32_t st =
+          dp_traceback<SUB, CPT, T>(S, D, G, seq, L, V, mi, mj, pairs, np, blockDim.x * SEGS);
       if (st != kOk) ss.status = st;
     }
   }
@@ -136,12 +140,12 @@ __global__ void k_add(GraphView G, const int32_t* pairs, uint32_t n_pairs, const
 
 
 // One read of a window: align (both strands when asked), choose, add.
-template <int SUB, int CPT, typename T>
+template <int SUB, int CPT, typename T, int SEGS = 1>
 __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScratch& sh,
                             SharedState& ss, const uint8_t* seq, uint32_t L,
                             const uint8_t* qual, bool strand, int32_t* out_score,
                             int32_t* out_rev, const int32_t** out_pairs, uint32_t* out_np) {
-  if (threadIdx.x == 0) read_prologue(S, G, D, L, blockDim.x * CPT, sizeof(T) == 4, ss);
+  if (threadIdx.x == 0) read_prologue(S, G, D, L, blockDim.x * CPT * SEGS, sizeof(T) == 4, ss);
   __syncthreads();
   if (ss.status != kOk) return;
   const bool dp = ss.mode == 1;
@@ -152,7 +156,7 @@ __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScra
   }
   if (dp) {
     dp_build_rows(G, D, sh);
-    read_align<SUB, CPT, T>(S, G, D, sh, ss, seq, L, ss.lanes, D.aln_a, &ss.has_f, &ss.score_f,
+    read_align<SUB, CPT, T, SEGS>(S, G, D, sh, ss, seq, L, ss.lanes, D.aln_a, &ss.has_f, &ss.score_f,
                             &ss.np_f);
   }
   if (strand) {
@@ -160,7 +164,7 @@ __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScra
       D.seq_rc[j] = complement_base(seq[L - 1 - j]);
     __syncthreads();
     if (dp && ss.status == kOk)
-      read_align<SUB, CPT, T>(S, G, D, sh, ss, D.seq_rc, L, ss.lanes, D.aln_b, &ss.has_r,
+      read_align<SUB, CPT, T, SEGS>(S, G, D, sh, ss, D.seq_rc, L, ss.lanes, D.aln_b, &ss.has_r,
                               &ss.score_r, &ss.np_r);
   }
   if (threadIdx.x == 0 && ss.status == kOk) {
@@ -384,7 +388,7 @@ struct BatchArgs {
 template <typename T>
 constexpr int kBatchMaxRegs = sizeof(T) == 2 ? 96 : 128;
 
-template <int SUB, int CPT, typename T>
+template <int SUB, int CPT, typename T, int SEGS = 1>
 __global__ void __maxnreg__(kBatchMaxRegs<T>) k_batch(BatchArgs a) {
   __shared__ BlockScratch sh;
   __shared__ SharedState ss;
@@ -425,7 +429,7 @@ __global__ void __maxnreg__(kBatchMaxRegs<T>) k_batch(BatchArgs a) {
       // for each source node; known once the rows are built
       const uint64_t npred_before = V0 ? 1 : 0;
       cells += (unsigned long long)V0 * L * (strand ? 2u : 1u);
-      window_read<SUB, CPT, T>(S, G, D, sh, ss, a.seqs + off, L,
+      window_read<SUB, CPT, T, SEGS>(S, G, D, sh, ss, a.seqs + off, L,
                                a.quals ? a.quals + off : nullptr, strand, &s_score, &s_rev,
                                &s_pairs, &s_np);
       if (ss.status != kOk) {
@@ -534,6 +538,39 @@ int32_t launch_batch(int cpt, int nt, int grid, const BatchArgs& a, cudaStream_t
   return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
 }
 
+// Segmented kernels (dp_forward_seg) for rows wider than one strip per
+// thread can hold in registers: 12 columns per strip, 2, 4 or 8 strips per
+// thread.  Instantiated for int32 pairs only: the scores of such long rows
+// pass the int16 width rule only under the smallest penalties, and those
+// windows keep the single-strip int16 kernels (up to 32 x 512 columns).
+constexpr int kSegCpt = 12;
+template <int SUB, typename T>
+int32_t launch_batch_seg(int segs, int nt, int grid, const BatchArgs& a, cudaStream_t s) {
+  switch (segs) {
+    case 2: k_batch<SUB, kSegCpt, T, 2><<<grid, nt, 0, s>>>(a); break;
+    case 4: k_batch<SUB, kSegCpt, T, 4><<<grid, nt, 0, s>>>(a); break;
+    case 8: k_batch<SUB, kSegCpt, T, 8><<<grid, nt, 0, s>>>(a); break;
+    default: return kInvalidArgument;
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
+}
+
+template <int SUB, typename T>
+int32_t occupancy_batch_seg(int segs, int nt, int* blocks) {
+  cudaError_t err = cudaSuccess;
+  switch (segs) {
+    case 2: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch<SUB, kSegCpt, T, 2>, nt, 0); break;
+    case 4: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch<SUB, kSegCpt, T, 4>, nt, 0); break;
+    case 8: err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch<SUB, kSegCpt, T, 8>, nt, 0); break;
+    default: return kInvalidArgument;
+  }
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    return kCuda;
+  }
+  return kOk;
+}
+
 template <int SUB, typename T>
 int32_t occupancy_batch(int cpt, int nt, int* blocks) {
   cudaError_t err = cudaSuccess;
@@ -556,5 +593,9 @@ int32_t occupancy_batch(int cpt, int nt, int* blocks) {
                                             cudaStream_t);                                      \
   template int32_t launch_batch<SUB, T>(int, int, int, const BatchArgs&, cudaStream_t);         \
   template int32_t occupancy_batch<SUB, T>(int, int, int*);
+
+#define SPOA_GB300_INSTANTIATE_SEG(SUB)                                                         \
+  template int32_t launch_batch_seg<SUB, int32_t>(int, int, int, const BatchArgs&, cudaStream_t); \
+  template int32_t occupancy_batch_seg<SUB, int32_t>(int, int, int*);
 
 }  // namespace spoa_gb300

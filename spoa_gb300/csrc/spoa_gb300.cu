@@ -54,6 +54,14 @@ SPOA_EXTERN(kLinear, int32_t)
 SPOA_EXTERN(kAffine, int32_t)
 SPOA_EXTERN(kConvex, int32_t)
 #undef SPOA_EXTERN
+#define SPOA_EXTERN_SEG(SUB)                                                                     \
+  extern template int32_t launch_batch_seg<SUB, int32_t>(int, int, int, const BatchArgs&,        \
+                                                         cudaStream_t);                          \
+  extern template int32_t occupancy_batch_seg<SUB, int32_t>(int, int, int*);
+SPOA_EXTERN_SEG(kLinear)
+SPOA_EXTERN_SEG(kAffine)
+SPOA_EXTERN_SEG(kConvex)
+#undef SPOA_EXTERN_SEG
 }  // namespace spoa_gb300
 
 // ===========================================================================
@@ -82,6 +90,13 @@ constexpr int kCpts32[] = {8, 12, 16, 24, 32};
              : (sub) == kAffine ? fn<kAffine, int16_t>(__VA_ARGS__)                      \
              : (sub) == kConvex ? fn<kConvex, int16_t>(__VA_ARGS__)                      \
                                 : (int32_t)kInvalidArgument))
+
+// fn<gap model, int32_t>(...) for the kernels built for 32-bit lanes only
+#define SPOA_BY_SUB32(sub, fn, ...)                                                      \
+  ((sub) == kLinear   ? fn<kLinear, int32_t>(__VA_ARGS__)                                \
+   : (sub) == kAffine ? fn<kAffine, int32_t>(__VA_ARGS__)                                \
+   : (sub) == kConvex ? fn<kConvex, int32_t>(__VA_ARGS__)                                \
+                      : (int32_t)kInvalidArgument)
 
 // Latency tile: the smallest strip (most threads) that covers L.
 bool latency_tile(uint32_t L, bool wide, int* cpt, int* nt) {
@@ -118,6 +133,24 @@ bool throughput_tile(uint32_t L, bool wide, int* cpt, int* nt) {
     }
   }
   return best != ~0ull;
+}
+
+// Segmented tile for 32-bit rows wider than one 12-column strip per thread
+// covers (12 x 512): strips of 12 columns, the fewest strips per thread (2,
+// 4 or 8) that keep the CTA at 512 threads or fewer.  Each thread then holds
+// 12 columns in registers at a time instead of 16-32, which spill.
+bool seg_tile(uint32_t L, int* cpt, int* nt, int* segs) {
+  for (int s = 2; s <= 8; s *= 2) {
+    const uint64_t per = (uint64_t)kSegCpt * s;
+    const uint64_t t = std::max<uint64_t>(32, ((uint64_t)(L + per - 1) / per + 31) / 32 * 32);
+    if (t <= 512) {
+      *cpt = kSegCpt;
+      *nt = (int)t;
+      *segs = s;
+      return true;
+    }
+  }
+  return false;
 }
 
 struct DeviceBuf {
@@ -694,6 +727,7 @@ struct Pass {
   GraphCaps gcaps{};
   DpCaps dcaps{};
   int cpt = 0, nt = 0, ctas = 0;
+  int segs = 1;             // strips per thread (dp_forward_seg when > 1)
   uint64_t stride = 0;
   int tuned_cpt = 0, tuned_nt = 0;  // tile chosen by the tuner (0: the default)
   int cls = 0;              // length class
@@ -787,14 +821,20 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
     wnodes = std::max(wnodes, wp[w].nodes);
     many_aligned = many_aligned || wp[w].many_aligned;
   }
-  int cpt = d.columns_per_thread, nt = d.threads_per_window;
+  int cpt = d.columns_per_thread, nt = d.threads_per_window, segs = 1;
   if (p->tuned_cpt > 0 && (uint64_t)p->tuned_cpt * p->tuned_nt >= L) {
     cpt = p->tuned_cpt;
     nt = p->tuned_nt;
   }
   if (cpt <= 0 || nt <= 0 || (p->wide && !cpt_supported<int32_t>(cpt)) ||
       (!p->wide && !cpt_supported<int16_t>(cpt))) {
-    if (!throughput_tile(L, p->wide, &cpt, &nt)) return kTooLarge;
+    // default tile; 32-bit rows past one 12-column strip per thread go to
+    // the segmented kernel
+    if (p->wide && L > (uint32_t)kSegCpt * 512) {
+      if (!seg_tile(L, &cpt, &nt, &segs)) return kTooLarge;
+    } else if (!throughput_tile(L, p->wide, &cpt, &nt)) {
+      return kTooLarge;
+    }
   } else if ((uint64_t)cpt * nt < L) {
     return kTooLarge;
   }
@@ -802,9 +842,12 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
   GraphCaps gc;
   DpCaps dc;
   const uint64_t stride =
-      arena_caps(b->base.sub, p->wide, cpt, nt, nodes, maxsum, maxreads, many_aligned, &gc, &dc);
+      arena_caps(b->base.sub, p->wide, cpt * segs, nt, nodes, maxsum, maxreads, many_aligned, &gc,
+                 &dc);
   int blocks = 1;
-  if (SPOA_BY_SUB(b->base.sub, p->wide, occupancy_batch, cpt, nt, &blocks)) return kCuda;
+  if (segs > 1 ? SPOA_BY_SUB32(b->base.sub, occupancy_batch_seg, segs, nt, &blocks)
+               : SPOA_BY_SUB(b->base.sub, p->wide, occupancy_batch, cpt, nt, &blocks))
+    return kCuda;
   blocks = std::max(blocks, 1);
   uint64_t by_mem = std::max<uint64_t>(1, b->budget / stride);
   uint64_t ctas = d.ctas > 0 ? (uint64_t)d.ctas : (uint64_t)b->sm_count * blocks;
@@ -814,6 +857,7 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
   p->dcaps = dc;
   p->cpt = cpt;
   p->nt = nt;
+  p->segs = segs;
   p->ctas = (int)std::max<uint64_t>(ctas, 1);
   p->stride = stride;
   return kOk;
@@ -858,6 +902,13 @@ BatchArgs make_args(spoa_gb300_batch* b, const Pass& p, uint8_t* cons, const uin
   return a;
 }
 
+int32_t launch_pass(spoa_gb300_batch* b, const Pass& p, int ctas, const BatchArgs& a,
+                    cudaStream_t s) {
+  ++b->launches;
+  if (p.segs > 1) return SPOA_BY_SUB32(b->base.sub, launch_batch_seg, p.segs, p.nt, ctas, a, s);
+  return SPOA_BY_SUB(b->base.sub, p.wide, launch_batch, p.cpt, p.nt, ctas, a, s);
+}
+
 int32_t run_pass(spoa_gb300_batch* b, const Pass& p, cudaStream_t s, bool plain, uint8_t* cons,
                  const uint64_t* cons_off) {
   if (p.windows.empty()) return kOk;
@@ -865,17 +916,13 @@ int32_t run_pass(spoa_gb300_batch* b, const Pass& p, cudaStream_t s, bool plain,
                      p.windows.size() * 4, cudaMemcpyHostToDevice, s));
   CU(cudaMemsetAsync(b->d_queue.as<uint32_t>() + p.work_off, 0, 4 * p.windows.size(), s));
   BatchArgs a = make_args(b, p, cons, cons_off);
-  if (!plain) {
-    ++b->launches;
-    return SPOA_BY_SUB(b->base.sub, p.wide, launch_batch, p.cpt, p.nt, p.ctas, a, s);
-  }
+  if (!plain) return launch_pass(b, p, p.ctas, a, s);
   for (size_t k = 0; k < p.windows.size(); ++k) {
     BatchArgs one = a;
     one.work = a.work + k;
     one.n_work = 1;
     one.queue = a.queue + k;
-    ++b->launches;
-    int32_t st = SPOA_BY_SUB(b->base.sub, p.wide, launch_batch, p.cpt, p.nt, 1, one, s);
+    int32_t st = launch_pass(b, p, 1, one, s);
     if (st) return st;
   }
   return kOk;
@@ -1032,7 +1079,7 @@ int32_t autotune(spoa_gb300_batch* b, cudaStream_t s) {
   CU(cudaEventCreate(&e1));
   for (const Pass& p : b->passes) {
     int c0, n0;
-    if (tuned_tile(b->base.sub, p.wide, p.cls, &c0, &n0)) continue;
+    if (p.segs > 1 || tuned_tile(b->base.sub, p.wide, p.cls, &c0, &n0)) continue;
     uint32_t L = 1;
     for (uint32_t w : p.windows) L = std::max(L, b->lmax[w]);
     const auto cands = tile_candidates(L, p.wide);

@@ -45,3 +45,34 @@ def test_long_window_full_vs_oracle():
     assert res.cells > 3e9  # the int32 path over graphs of ~20k nodes
     ref = po.run_window(typ, *params, w.reads, with_msa=False)
     _check(res, ref)
+
+
+GAPS = {"linear": (5, -4, -8, -8, -8, -8), "affine": (5, -4, -8, -6, -8, -6),
+        "convex": (5, -4, -8, -6, -10, -4)}
+
+
+@pytest.mark.timeout(900)
+@pytest.mark.parametrize("gap", sorted(GAPS))
+def test_segmented_rows_vs_oracle(gap):
+    """Rows of 6.5-7.2k columns on the int32 width: past 12 x 512 columns,
+    where each thread holds two 12-column strips of the row; NW, SW and OV,
+    every score and alignment and the consensus."""
+    w = synth.long_10k(11, n_reads=3, tpl_len=7200, min_len=6500)
+    params = GAPS[gap]
+    for typ in (0, 1, 2):
+        ref = po.run_window(typ, *params, w.reads, with_msa=False)
+        res = sg.batch_poa([w.reads], typ, *params, want_alignments=True)
+        assert (res.status == 0).all()
+        _check(res, ref)
+
+
+@pytest.mark.timeout(900)
+def test_rows_past_16k_columns_vs_oracle():
+    """Reads of 16.5-17k columns (four 12-column strips per thread; no
+    single strip per thread covers them), SW convex."""
+    w = synth.long_10k(12, n_reads=2, tpl_len=17000, min_len=16500)
+    typ, params = synth.SCORING["long_10k"]
+    ref = po.run_window(typ, *params, w.reads, with_msa=False)
+    res = sg.batch_poa([w.reads], typ, *params, want_alignments=True)
+    assert (res.status == 0).all()
+    _check(res, ref)
