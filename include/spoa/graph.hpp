@@ -5,9 +5,11 @@
 // AddAlignment overloads and consensus / MSA calls.  The graph lives in
 // device memory (libspoa_gb300.so); AddAlignment, GenerateConsensus and
 // GenerateMultipleSequenceAlignment run there.  The host views returned by
-// nodes(), edges(), rank_to_node(), sequences() and consensus() are rebuilt
-// from a device export the first time one is read after a change; pointers
-// into them stay valid until the next change of the graph.
+// nodes(), edges(), rank_to_node(), sequences() and consensus() are brought
+// up to date from a device export the first time one is read after a
+// change.  Nodes and edges are only appended until Clear, and the Node and
+// Edge objects of a view are kept and updated by the next one, so pointers
+// to them stay valid until Clear, as the reference's do.
 #ifndef SPOA_GRAPH_HPP_
 #define SPOA_GRAPH_HPP_
 
@@ -101,6 +103,21 @@ class Graph {
   // graph.cpp:377-431: per consensus base the coverage of its column
   // (verbose: per code and gap row counts)
   std::string GenerateConsensus(std::vector<std::uint32_t>* summary, bool verbose = false);
+
+  // graph.cpp:541-595: the part of the graph that reaches node `end` over
+  // in-edges and aligned nodes without going below node id `begin`, as a
+  // new graph (sorted, no sequences); subgraph_to_graph gets one entry per
+  // node of this graph: this graph's node for each subgraph node, then
+  // nullptr.  Throws std::invalid_argument for a null subgraph_to_graph
+  // (the reference's message) and for node ids past the graph (which the
+  // reference does not check).
+  Graph Subgraph(std::uint32_t begin, std::uint32_t end,
+                 std::vector<const Node*>* subgraph_to_graph) const;
+
+  // graph.cpp:597-605: maps the node ids of an alignment against a
+  // subgraph to this graph's
+  void UpdateAlignment(const std::vector<const Node*>& subgraph_to_graph,
+                       Alignment* alignment) const;
 
   // graph.cpp:607-647: Graphviz text of the graph (consensus nodes coloured)
   void PrintDot(const std::string& path) const;

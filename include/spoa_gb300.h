@@ -149,6 +149,20 @@ int32_t spoa_gb300_graph_export(const spoa_gb300_graph* graph, uint8_t* chars, u
                                 uint32_t* labels, uint32_t* rank_to_node, uint32_t* seq_begin,
                                 uint32_t* consensus, int32_t* coder256, int32_t* decoder256);
 
+/* Replaces Graph::Subgraph (src/graph.cpp:518-595): `out` (an existing
+ * graph, emptied first) receives the part of `graph` reachable from node
+ * `end` over in-edges and aligned nodes, not below node id `begin`,
+ * renumbered in id order and topologically sorted; subgraph_to_graph
+ * (map_len >= number of nodes of `graph`, the size the reference gives its
+ * vector) receives the id in `graph` of every node of `out` and UINT32_MAX
+ * after them (the reference's nullptr).  begin and end must be node ids of
+ * `graph` (the reference does not check them).  Graph::UpdateAlignment
+ * (graph.cpp:597-605) is the host-side map of an alignment's node ids
+ * through subgraph_to_graph. */
+int32_t spoa_gb300_graph_subgraph(const spoa_gb300_graph* graph, uint32_t begin, uint32_t end,
+                                  spoa_gb300_graph* out, uint32_t* subgraph_to_graph,
+                                  uint32_t map_len);
+
 /* ---- Batched windows (no counterpart in the reference) ------------------- *
  * Many independent windows (each one Graph driven by the per-read loop of
  * src/main.cpp:275-314, then GenerateConsensus) in one persistent kernel:

@@ -75,6 +75,9 @@ def lib():
             f.argtypes = [P]
             f.restype = C.c_uint32
         L.oracle_graph_export.argtypes = [P] * 8
+        L.oracle_graph_export_ids.argtypes = [P] * 6
+        L.oracle_graph_export_ids.restype = C.c_uint32
+        L.oracle_subgraph.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
         L.oracle_graph_path.argtypes = [P, C.c_uint32, P, C.c_uint32]
         L.oracle_graph_path.restype = C.c_uint32
         L.oracle_window_run.argtypes = [C.POINTER(WindowParams), P, C.c_uint32, C.c_char_p,
@@ -265,9 +268,120 @@ def parse_reference_output(text: str) -> list:
             cur["summary" if tag == "Y" else "summary_verbose"] = vals
         elif tag == "G":
             cur["gfa"].append(rest)
+        elif tag in ("U", "K", "O", "L", "A", "Q"):
+            if tag == "U":
+                cur.setdefault("slices", []).append({})
+            cur["slices"][-1][tag] = rest
         elif tag == "X":
             cur["error"] = rest
         elif tag == "E":
             wins.append(cur)
             cur = None
     return wins
+
+
+# ---- slices: Graph::Subgraph + UpdateAlignment (graph.cpp:518-605) ---------
+
+def format_slices(specs) -> str:
+    """specs: iterable of (type, (m, n, g, e, q, c), reads, slices) with one
+    (begin, end) per read after the first ((-1, -1): the whole graph)."""
+    out = []
+    for typ, (m, n, g, e, q, c), reads, slices in specs:
+        out.append(f"S {typ} {m} {n} {g} {e} {q} {c} {len(reads)}\n")
+        out.extend(r.decode() + "\n" for r in reads)
+        out.extend(f"{b} {e_} \n" for b, e_ in slices)
+    return "".join(out)
+
+
+def slice_lines(read: int, sub_to_graph, chars, rank, edge_tail, edge_head, edge_weight,
+                aligned_off, aligned, consensus: str) -> dict:
+    """The U/K/O/L/A/Q lines of the reference driver for one subgraph, from
+    its arrays (ids in subgraph numbering, edges in id order)."""
+    n = len(chars)
+    al = []
+    for v in range(n):
+        lst = aligned[aligned_off[v]:aligned_off[v + 1]]
+        if len(lst):
+            al.append(f"{v}:" + ",".join(str(int(x)) for x in lst))
+    return {
+        "U": f"{read} {n}" + "".join(f" {int(x)}" for x in sub_to_graph[:n]),
+        "K": bytes(np.asarray(chars, np.uint8)).decode(),
+        "O": " ".join(str(int(x)) for x in rank),
+        "L": " ".join(f"{int(t)},{int(h)},{int(w)}"
+                      for t, h, w in zip(edge_tail, edge_head, edge_weight)),
+        "A": " ".join(al),
+        "Q": consensus,
+    }
+
+
+def run_slices(type_: int, params, reads: list[bytes], slices) -> dict:
+    """The slice protocol of ref_driver.cpp on the C oracle: read 0 added
+    whole; every later read aligned to Subgraph(begin, end) (or the whole
+    graph), its alignment mapped back (UpdateAlignment) and added."""
+    L = lib()
+    st = C.c_int32()
+    en = L.oracle_engine_create(type_, *params, C.byref(st))
+    if not en:
+        raise RuntimeError(f"oracle engine: status {st.value}")
+    g = L.oracle_graph_create()
+    sub = L.oracle_graph_create()
+    res = {"scores": [], "alignments": [], "slices": [], "consensus": "", "msa": []}
+    try:
+        for r, seq in enumerate(reads):
+            w = np.ones(max(len(seq), 1), np.uint32)
+            pairs = np.zeros(2 * (L.oracle_graph_num_nodes(g) + len(seq) + 16), np.int32)
+            npairs = C.c_uint32(0)
+            score = C.c_int32(0)
+            if r > 0:
+                b, e_ = slices[r - 1]
+                target = g
+                if b >= 0:
+                    nn = L.oracle_graph_num_nodes(g)
+                    m = np.zeros(max(nn, 1), np.uint32)
+                    assert L.oracle_subgraph(g, b, e_, sub, _ptr(m)) == 0
+                    target = sub
+                assert L.oracle_align(en, seq, len(seq), target, C.byref(score), _ptr(pairs),
+                                      pairs.size // 2, C.byref(npairs)) == 0
+                aln = pairs[:2 * npairs.value].reshape(-1, 2).copy()
+                if b >= 0:
+                    sn = L.oracle_graph_num_nodes(sub)
+                    se = L.oracle_graph_num_edges(sub)
+                    chars = np.zeros(max(sn, 1), np.uint8)
+                    rank = np.zeros(max(sn, 1), np.uint32)
+                    L.oracle_graph_export(sub, _ptr(chars), _ptr(rank), None, None, None, None,
+                                          None)
+                    et, eh = np.zeros(max(se, 1), np.uint32), np.zeros(max(se, 1), np.uint32)
+                    ew = np.zeros(max(se, 1), np.int64)
+                    aoff = np.zeros(sn + 1, np.uint32)
+                    na = L.oracle_graph_export_ids(sub, None, None, None, _ptr(aoff), None)
+                    al = np.zeros(max(na, 1), np.uint32)
+                    L.oracle_graph_export_ids(sub, _ptr(et), _ptr(eh), _ptr(ew), _ptr(aoff),
+                                              _ptr(al))
+                    cb = C.create_string_buffer(sn + 1)
+                    k = L.oracle_consensus(sub, cb, sn + 1)
+                    res["slices"].append(slice_lines(r, m, chars[:sn], rank[:sn], et[:se],
+                                                     eh[:se], ew[:se], aoff, al,
+                                                     cb.raw[:k].decode()))
+                    hit = aln[:, 0] != -1
+                    aln[hit, 0] = m[aln[hit, 0]].astype(np.int32)
+                res["scores"].append(score.value)
+                res["alignments"].append(aln)
+            else:
+                aln = np.zeros((0, 2), np.int32)
+            assert L.oracle_add_alignment(g, _ptr(np.ascontiguousarray(aln)), aln.shape[0], seq,
+                                          len(seq), _ptr(w), len(seq)) == 0
+        nn = L.oracle_graph_num_nodes(g)
+        cb = C.create_string_buffer(nn + 1)
+        k = L.oracle_consensus(g, cb, nn + 1)
+        res["consensus"] = cb.raw[:k].decode()
+        rows, rl = C.c_uint32(), C.c_uint32()
+        mcap = (len(reads) + 1) * (nn + 1)
+        mb = C.create_string_buffer(mcap)
+        assert L.oracle_msa(g, 0, mb, mcap, C.byref(rows), C.byref(rl)) == 0
+        res["msa"] = [mb.raw[i * rl.value:(i + 1) * rl.value].decode()
+                      for i in range(rows.value)]
+        return res
+    finally:
+        L.oracle_graph_destroy(sub)
+        L.oracle_graph_destroy(g)
+        L.oracle_engine_destroy(en)

@@ -22,6 +22,22 @@
 //   G <gfa line>          GFA with the consensus path
 //   E
 // A window that throws prints "X <message>" and continues with the next.
+//
+// Slice windows (Graph::Subgraph + UpdateAlignment, src/graph.cpp:518-605,
+// the way polishers align a read to the part of the graph it spans):
+//   S <type> <m> <n> <g> <e> <q> <c> <reads>
+//   <sequence>            one line per read; read 0 is added whole
+//   <begin> <end>         one line per read after the first: node ids of
+//                         the slice (-1 -1: align to the whole graph)
+// Output, per read after the first:
+//   U <read> <subgraph nodes> <subgraph_to_graph ids ...>
+//   K <characters of the subgraph's nodes, in id order>
+//   O <subgraph rank_to_node ids>
+//   L <tail>,<head>,<weight> ...   subgraph edges in edge order
+//   A <node>:<aligned>,... ...     subgraph aligned lists (non-empty ones)
+//   Q <subgraph consensus>
+//   R <read> <score> 0 <pairs> <node>,<pos> ...   after UpdateAlignment
+// then C, M and E as above.
 #include <algorithm>
 #include <chrono>
 #include <cstdint>
@@ -117,6 +133,65 @@ int main(int argc, char** argv) {
   std::uint64_t cells = 0;
   double seconds = 0;
   while (std::cin >> tag) {
+    if (tag == "S") {
+      int type, m, n, g, e, q, c;
+      std::uint32_t reads;
+      std::cin >> type >> m >> n >> g >> e >> q >> c >> reads;
+      std::vector<std::string> data(reads);
+      for (std::uint32_t r = 0; r < reads; ++r) std::cin >> data[r];
+      std::vector<std::int64_t> lo(reads, -1), hi(reads, -1);
+      for (std::uint32_t r = 1; r < reads; ++r) std::cin >> lo[r] >> hi[r];
+      std::ostringstream os;
+      os << "W " << window++ << "\n";
+      try {
+        auto engine = spoa::AlignmentEngine::Create(
+            static_cast<spoa::AlignmentType>(type), m, n, g, e, q, c);
+        spoa::Graph graph{};
+        for (std::uint32_t r = 0; r < reads; ++r) {
+          std::int32_t score = 0;
+          spoa::Alignment alignment;
+          if (r > 0 && lo[r] >= 0) {
+            std::vector<const spoa::Graph::Node*> map;
+            auto sub = graph.Subgraph(static_cast<std::uint32_t>(lo[r]),
+                                      static_cast<std::uint32_t>(hi[r]), &map);
+            os << "U " << r << " " << sub.nodes().size();
+            for (std::size_t k = 0; k < sub.nodes().size(); ++k) os << " " << map[k]->id;
+            os << "\nK ";
+            for (const auto& it : sub.nodes()) os << static_cast<char>(sub.decoder(it->code));
+            os << "\nO";
+            for (const auto& it : sub.rank_to_node()) os << " " << it->id;
+            os << "\nL";
+            for (const auto& it : sub.edges())
+              os << " " << it->tail->id << "," << it->head->id << "," << it->weight;
+            os << "\nA";
+            for (const auto& it : sub.nodes()) {
+              if (it->aligned_nodes.empty()) continue;
+              os << " " << it->id << ":";
+              for (std::size_t k = 0; k < it->aligned_nodes.size(); ++k)
+                os << (k ? "," : "") << it->aligned_nodes[k]->id;
+            }
+            alignment = engine->Align(data[r], sub, &score);
+            os << "\nQ " << sub.GenerateConsensus() << "\n";
+            graph.UpdateAlignment(map, &alignment);
+          } else if (r > 0) {
+            alignment = engine->Align(data[r], graph, &score);
+          }
+          graph.AddAlignment(alignment, data[r]);
+          if (r > 0) {
+            os << "R " << r << " " << score << " 0 " << alignment.size();
+            for (const auto& it : alignment) os << " " << it.first << "," << it.second;
+            os << "\n";
+          }
+        }
+        os << "C " << graph.GenerateConsensus() << "\n";
+        for (const auto& row : graph.GenerateMultipleSequenceAlignment()) os << "M " << row << "\n";
+      } catch (std::exception& ex) {
+        os << "X " << ex.what() << "\n";
+      }
+      os << "E\n";
+      std::cout << os.str();
+      continue;
+    }
     if (tag != "W") return 2;
     int type, m, n, g, e, q, c, strand, has_quality;
     std::uint32_t reads;

@@ -539,6 +539,90 @@ void oracle_graph_export(const oracle_graph* g, uint8_t* chars,
     memcpy(consensus, g->consensus.a, (size_t)g->consensus.n * sizeof(uint32_t));
 }
 
+/* Edges in id order (Graph::edges()) and the aligned-node lists as CSR
+ * (aligned_off has n_nodes + 1 entries); any pointer may be NULL.
+ * Returns the total length of the aligned lists. */
+uint32_t oracle_graph_export_ids(const oracle_graph* g, uint32_t* edge_tail,
+                                 uint32_t* edge_head, int64_t* edge_weight,
+                                 uint32_t* aligned_off, uint32_t* aligned) {
+  for (uint32_t e = 0; e < g->n_edges; ++e) {
+    if (edge_tail) edge_tail[e] = g->edges[e].tail;
+    if (edge_head) edge_head[e] = g->edges[e].head;
+    if (edge_weight) edge_weight[e] = g->edges[e].weight;
+  }
+  uint32_t n = 0;
+  for (uint32_t v = 0; v < g->n_nodes; ++v) {
+    if (aligned_off) aligned_off[v] = n;
+    for (uint32_t k = 0; k < g->nodes[v].aligned.n; ++k, ++n)
+      if (aligned) aligned[n] = g->nodes[v].aligned.a[k];
+  }
+  if (aligned_off) aligned_off[g->n_nodes] = n;
+  return n;
+}
+
+/* Graph::Subgraph (graph.cpp:518-595).  ExtractSubgraph's depth-first
+ * walk from `end` over in-edge tails and aligned nodes, a node entering the
+ * set when its id is at least `begin`; the set's nodes are added to `out`
+ * in id order, then per node its in-edges from inside the set
+ * (AddEdge with the 32-bit weight, label = number of sequences = 0) and its
+ * aligned nodes inside the set, in list order; then TopologicalSort.
+ * sub_to_graph gets n_nodes(g) entries: graph id per subgraph node, then
+ * UINT32_MAX. */
+int32_t oracle_subgraph(const oracle_graph* g, uint32_t begin, uint32_t end,
+                        oracle_graph* out, uint32_t* sub_to_graph) {
+  const uint32_t nn = g->n_nodes;
+  if (begin >= nn || end >= nn || out == g) return ORACLE_ERR_INVALID_ARGUMENT;
+  oracle_graph_clear(out);
+  out->num_codes = g->num_codes;
+  memcpy(out->coder, g->coder, sizeof(g->coder));
+  memcpy(out->decoder, g->decoder, sizeof(g->decoder));
+  uint8_t* in_set = (uint8_t*)calloc(nn, 1);
+  uint32_t* to_sub = (uint32_t*)malloc((size_t)nn * sizeof(uint32_t));
+  vec_u32 stack = {0};
+  int32_t rc = ORACLE_OK;
+  if (!in_set || !to_sub || vu_push(&stack, end)) rc = ORACLE_ERR_NO_MEMORY;
+  while (rc == ORACLE_OK && stack.n) {
+    uint32_t curr = stack.a[--stack.n];
+    if (in_set[curr] || curr < begin) continue;
+    const onode* nd = &g->nodes[curr];
+    for (uint32_t k = 0; k < nd->in.n && rc == ORACLE_OK; ++k)
+      if (vu_push(&stack, g->edges[nd->in.a[k]].tail)) rc = ORACLE_ERR_NO_MEMORY;
+    for (uint32_t k = 0; k < nd->aligned.n && rc == ORACLE_OK; ++k)
+      if (vu_push(&stack, nd->aligned.a[k])) rc = ORACLE_ERR_NO_MEMORY;
+    in_set[curr] = 1;
+  }
+  for (uint32_t v = 0; v < nn && rc == ORACLE_OK; ++v) {
+    to_sub[v] = UINT32_MAX;
+    sub_to_graph[v] = UINT32_MAX;
+  }
+  for (uint32_t v = 0; v < nn && rc == ORACLE_OK; ++v) {
+    if (!in_set[v]) continue;
+    int64_t id = add_node(out, g->nodes[v].code);
+    if (id < 0) { rc = ORACLE_ERR_NO_MEMORY; break; }
+    to_sub[v] = (uint32_t)id;
+    sub_to_graph[id] = v;
+  }
+  for (uint32_t v = 0; v < nn && rc == ORACLE_OK; ++v) {
+    if (!in_set[v]) continue;
+    const onode* nd = &g->nodes[v];
+    for (uint32_t k = 0; k < nd->in.n && rc == ORACLE_OK; ++k) {
+      const oedge* ed = &g->edges[nd->in.a[k]];
+      if (to_sub[ed->tail] != UINT32_MAX &&
+          add_edge(out, to_sub[ed->tail], to_sub[v], (uint32_t)ed->weight))
+        rc = ORACLE_ERR_NO_MEMORY;
+    }
+    for (uint32_t k = 0; k < nd->aligned.n && rc == ORACLE_OK; ++k) {
+      uint32_t a = to_sub[nd->aligned.a[k]];
+      if (a != UINT32_MAX && vu_push(&out->nodes[to_sub[v]].aligned, a)) rc = ORACLE_ERR_NO_MEMORY;
+    }
+  }
+  if (rc == ORACLE_OK && topological_sort(out)) rc = ORACLE_ERR_NO_MEMORY;
+  vu_free(&stack);
+  free(in_set);
+  free(to_sub);
+  return rc;
+}
+
 uint32_t oracle_graph_path(const oracle_graph* g, uint32_t label,
                            uint32_t* out, uint32_t cap) {
   if (label >= g->sequences.n) return 0;

@@ -84,6 +84,20 @@ void oracle_graph_export(const oracle_graph* g, uint8_t* chars,
 uint32_t oracle_graph_path(const oracle_graph* g, uint32_t label,
                            uint32_t* out, uint32_t cap);
 
+/* Edges in id order (Graph::edges()) and the aligned-node lists as CSR
+ * (aligned_off: n_nodes + 1 entries); NULL skips an array.  Returns the
+ * total length of the aligned lists. */
+uint32_t oracle_graph_export_ids(const oracle_graph* g, uint32_t* edge_tail,
+                                 uint32_t* edge_head, int64_t* edge_weight,
+                                 uint32_t* aligned_off, uint32_t* aligned);
+
+/* Graph::Subgraph (graph.cpp:518-595) into `out` (cleared first);
+ * sub_to_graph receives n_nodes(g) entries: the id in g of every node of
+ * out, then UINT32_MAX.  Graph::UpdateAlignment (graph.cpp:597-605) is the
+ * map of an alignment's node ids through sub_to_graph. */
+int32_t oracle_subgraph(const oracle_graph* g, uint32_t begin, uint32_t end,
+                        oracle_graph* out, uint32_t* sub_to_graph);
+
 /* One whole window, the way spoa's CLI drives it (src/main.cpp:275-314):
  * reads are aligned in order and added; with strand_ambiguous both strands
  * are aligned and the forward strand kept if score >= score_rev.

@@ -44,6 +44,7 @@ class AlignmentSubtype:
 
 
 OK = 0
+NO_NODE = 0xFFFFFFFF  # subgraph_to_graph entry past the subgraph's nodes
 _MESSAGES = {
     1: "invalid argument",
     2: "too large sequence!",
@@ -109,7 +110,8 @@ EXPORTED = [
     "spoa_gb300_graph_add_alignment_quality", "spoa_gb300_align_add",
     "spoa_gb300_align_add_reads",
     "spoa_gb300_graph_consensus", "spoa_gb300_graph_msa", "spoa_gb300_graph_counts",
-    "spoa_gb300_graph_export", "spoa_gb300_batch_create", "spoa_gb300_batch_launch",
+    "spoa_gb300_graph_export", "spoa_gb300_graph_subgraph", "spoa_gb300_batch_create",
+    "spoa_gb300_batch_launch",
     "spoa_gb300_batch_launch_plain", "spoa_gb300_batch_fetch", "spoa_gb300_batch_destroy",
     "spoa_gb300_batch_run", "spoa_gb300_server_create", "spoa_gb300_server_submit",
     "spoa_gb300_server_wait", "spoa_gb300_server_stats", "spoa_gb300_server_destroy",
@@ -149,6 +151,7 @@ def lib():
         L.spoa_gb300_graph_msa.argtypes = [P, I32, C.c_char_p, U64, P, P]
         L.spoa_gb300_graph_counts.argtypes = [P] * 7
         L.spoa_gb300_graph_export.argtypes = [P] * 19
+        L.spoa_gb300_graph_subgraph.argtypes = [P, U32, U32, P, P, U32]
         L.spoa_gb300_batch_create.argtypes = [C.POINTER(_BatchDesc), P]
         L.spoa_gb300_batch_launch.argtypes = [P, P]
         L.spoa_gb300_batch_launch_plain.argtypes = [P, P]
@@ -328,6 +331,28 @@ class Graph:
                 "label_off": lab_off[:E + 1], "labels": labs[:Lb], "rank_to_node": rank[:N],
                 "seq_begin": sb[:S], "consensus": cons[:Cn], "coder": coder,
                 "decoder": decoder, "num_codes": cnt["num_codes"]}
+
+    def subgraph(self, begin: int, end: int):
+        """Graph::Subgraph (graph.cpp:518-595): the part of the graph that
+        reaches node `end` over in-edges and aligned nodes without going
+        below node id `begin`, as a new device graph, and subgraph_to_graph
+        (uint32, one entry per node of this graph: the id here of each
+        subgraph node, then NO_NODE)."""
+        sub = Graph()
+        m = np.zeros(max(self.num_nodes, 1), np.uint32)
+        _check("Graph::Subgraph", lib().spoa_gb300_graph_subgraph(
+            self._h, begin, end, sub._h, _ptr(m), m.size))
+        return sub, m[:self.num_nodes]
+
+    @staticmethod
+    def update_alignment(subgraph_to_graph, alignment):
+        """Graph::UpdateAlignment (graph.cpp:597-605): node ids of an
+        alignment against a subgraph mapped back to this graph's."""
+        a = np.array(alignment, np.int32).reshape(-1, 2)
+        m = np.asarray(subgraph_to_graph, np.uint32)
+        hit = a[:, 0] != -1
+        a[hit, 0] = m[a[hit, 0]].astype(np.int32)
+        return a
 
     def paths(self, ex: dict | None = None) -> list:
         """Node path of every sequence (Node::Successor walks, graph.cpp:22-30)."""

@@ -343,6 +343,77 @@ __global__ void k_export(GraphView G, ExportPtrs x) {
     if (x.decoder) x.decoder[k] = h->decoder[k];
   }
 }
+
+// Graph::Subgraph (graph.cpp:541-595) of S into the empty graph D.  The
+// node set is ExtractSubgraph's (graph.cpp:518-539): every node reachable
+// from `end` over in-edges and aligned nodes, not expanded below id
+// `begin`; it is a set, so thread 0 walks it with any order of the stack.
+// Its nodes are added in id order (map[k] = id in S of node k of D), then,
+// node by node, each in-edge whose tail is in the set with the edge's
+// weight (one label, sequence 0, as AddEdge gives it on a graph without
+// sequences) and the aligned nodes in the set, in list order; the whole CTA
+// then sorts D.  gid (one word per node of S) and stack are scratch.
+// *status: kOk, or kCapacity when D or the stack is too small.
+__global__ void k_subgraph(GraphView S, GraphView D, uint32_t begin, uint32_t end, uint32_t* gid,
+                           uint32_t* stack, uint64_t stack_cap, uint32_t* map, int32_t* status) {
+  __shared__ int s_st;
+  const uint32_t nn = S.hdr->n_nodes;
+  constexpr uint32_t kIn = 0xFFFFFFFEu;  // in the set, not numbered yet
+  for (uint32_t v = threadIdx.x; v < nn; v += blockDim.x) gid[v] = kNone;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int st = kOk;
+    g_reset(D);
+    D.hdr->num_codes = S.hdr->num_codes;
+    for (int k = 0; k < 256; ++k) {
+      D.hdr->coder[k] = S.hdr->coder[k];
+      D.hdr->decoder[k] = S.hdr->decoder[k];
+    }
+    const uint32_t KS = S.caps.aligned;
+    uint64_t sp = 0;
+    if (end < nn) stack[sp++] = end;
+    while (sp && st == kOk) {
+      const uint32_t v = stack[--sp];
+      if (gid[v] != kNone || v < begin) continue;
+      gid[v] = kIn;
+      for (uint32_t e = S.nlink[v].x; e != kNone; e = S.erec[e].z) {
+        if (sp >= stack_cap) { st = kCapacity; break; }
+        stack[sp++] = S.erec[e].x;
+      }
+      for (uint32_t k = 0; k < S.n_aligned[v] && st == kOk; ++k) {
+        if (sp >= stack_cap) { st = kCapacity; break; }
+        stack[sp++] = S.aligned[(uint64_t)v * KS + k];
+      }
+    }
+    for (uint32_t v = 0; v < nn && st == kOk; ++v) {
+      if (gid[v] != kIn) continue;
+      const int64_t id = g_add_node(D, S.code[v]);
+      if (id < 0) { st = kCapacity; break; }
+      gid[v] = (uint32_t)id;
+      map[id] = v;
+    }
+    for (uint32_t v = 0; v < nn && st == kOk; ++v) {
+      const uint32_t h = gid[v];
+      if (h == kNone) continue;
+      for (uint32_t e = S.nlink[v].x; e != kNone; e = S.erec[e].z) {
+        const uint32_t t = gid[S.erec[e].x];
+        // AddEdge takes a 32-bit weight (graph.cpp:81)
+        if (t != kNone && g_add_edge(D, t, h, (uint32_t)S.e_weight[e])) { st = kCapacity; break; }
+      }
+      for (uint32_t k = 0; k < S.n_aligned[v] && st == kOk; ++k) {
+        const uint32_t a = gid[S.aligned[(uint64_t)v * KS + k]];
+        if (a != kNone && g_link_aligned(D, h, a)) st = kCapacity;
+      }
+    }
+    s_st = st;
+  }
+  __syncthreads();
+  if (s_st == kOk && g_topo_sort_cta(D, &s_st) != 0) {
+    if (threadIdx.x == 0) s_st = kCapacity;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *status = s_st;
+}
 #endif
 
 // ---------------------------------------------------------------------------

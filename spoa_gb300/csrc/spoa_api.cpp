@@ -228,16 +228,31 @@ void Graph::Refresh() const {
                                 rank.data(), sb.data(), cons.data(), coder_.data(),
                                 decoder_.data()));
   num_codes_ = codes;
-  nodes_.clear();
-  edges_.clear();
+  // Nodes and edges are only appended until Clear: the objects of the last
+  // view are updated in place and new ones appended, so pointers to them
+  // survive the refresh.
+  if (nodes_.size() > N) nodes_.resize(N);
+  if (edges_.size() > E) edges_.resize(E);
   nodes_.reserve(N);
   edges_.reserve(E);
-  for (uint32_t v = 0; v < N; ++v) nodes_.emplace_back(new Node(v, code[v]));
+  for (uint32_t v = 0; v < N; ++v) {
+    if (v < nodes_.size()) {
+      Node* node = nodes_[v].get();
+      node->code = code[v];
+      node->inedges.clear();
+      node->outedges.clear();
+      node->aligned_nodes.clear();
+    } else {
+      nodes_.emplace_back(new Node(v, code[v]));
+    }
+  }
   for (uint32_t k = 0; k < E; ++k) {
-    Edge* ed = new Edge(nodes_[et[k]].get(), nodes_[eh[k]].get(), 0, 0);
+    if (k >= edges_.size()) edges_.emplace_back(new Edge(nullptr, nullptr, 0, 0));
+    Edge* ed = edges_[k].get();
+    ed->tail = nodes_[et[k]].get();
+    ed->head = nodes_[eh[k]].get();
     ed->labels.assign(labs.begin() + lab_off[k], labs.begin() + lab_off[k + 1]);
     ed->weight = ew[k];
-    edges_.emplace_back(ed);
   }
   for (uint32_t v = 0; v < N; ++v) {
     Node* node = nodes_[v].get();
@@ -418,6 +433,29 @@ std::string Graph::GenerateConsensus(std::vector<std::uint32_t>* summary, bool v
     }
   }
   return dst;
+}
+
+Graph Graph::Subgraph(std::uint32_t begin, std::uint32_t end,
+                      std::vector<const Node*>* subgraph_to_graph) const {
+  if (!subgraph_to_graph) Throw("Graph::Subgraph", "invalid ptr to subgraph_to_graph");
+  Refresh();
+  const std::size_t n = nodes_.size();
+  if (begin >= n || end >= n) Throw("Graph::Subgraph", "invalid node id");
+  Graph sub;
+  std::vector<uint32_t> map(n);
+  Check("Graph::Subgraph", spoa_gb300_graph_subgraph(handle_, begin, end, sub.handle_,
+                                                      map.data(), static_cast<uint32_t>(n)));
+  subgraph_to_graph->assign(n, nullptr);
+  for (std::size_t k = 0; k < n && map[k] != 0xFFFFFFFFu; ++k)
+    (*subgraph_to_graph)[k] = nodes_[map[k]].get();
+  sub.Invalidate();
+  return sub;
+}
+
+void Graph::UpdateAlignment(const std::vector<const Node*>& subgraph_to_graph,
+                            Alignment* alignment) const {
+  for (auto& it : *alignment)
+    if (it.first != -1) it.first = static_cast<std::int32_t>(subgraph_to_graph[it.first]->id);
 }
 
 void Graph::PrintDot(const std::string& path) const {

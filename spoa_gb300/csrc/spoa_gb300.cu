@@ -710,6 +710,42 @@ int32_t spoa_gb300_graph_export(const spoa_gb300_graph* g, uint8_t* chars, uint8
   return kOk;
 }
 
+int32_t spoa_gb300_graph_subgraph(const spoa_gb300_graph* g, uint32_t begin, uint32_t end,
+                                  spoa_gb300_graph* out, uint32_t* subgraph_to_graph,
+                                  uint32_t map_len) {
+  if (!g || !out || out == g || !subgraph_to_graph) return kInvalidArgument;
+  const uint32_t nn = g->h.n_nodes;
+  if (begin >= nn || end >= nn || map_len < nn) return kInvalidArgument;
+  int32_t st = spoa_gb300_graph_clear(out);
+  if (st) return st;
+  // room for all of g: the subgraph holds at most its nodes and edges
+  st = graph_reserve(out, std::max<uint64_t>(nn, g->h.n_edges), 1);
+  if (st) return st;
+  // each node of the set is expanded once and pushes its in-edge tails and
+  // aligned nodes
+  const uint64_t stack_cap = (uint64_t)g->h.n_edges + (uint64_t)nn * g->caps.aligned + 1;
+  DeviceBuf scratch;
+  if (scratch.ensure(4 * (2 * (uint64_t)nn + stack_cap))) return kNoMemory;
+  uint32_t* gid = scratch.as<uint32_t>();
+  uint32_t* map = gid + nn;
+  uint32_t* stack = map + nn;
+  k_subgraph<<<1, 256>>>(g->v, out->v, begin, end, gid, stack, stack_cap, map,
+                         out->stat.as<int32_t>());
+  CU(cudaGetLastError());
+  int32_t dst = kOk;
+  CU(cudaMemcpy(&dst, out->stat.p, sizeof(dst), cudaMemcpyDeviceToHost));
+  if (dst != kOk) {
+    spoa_gb300_graph_clear(out);
+    return dst;
+  }
+  st = graph_refresh(out);
+  if (st) return st;
+  const uint32_t ns = out->h.n_nodes;
+  if (ns) CU(cudaMemcpy(subgraph_to_graph, map, 4 * (uint64_t)ns, cudaMemcpyDeviceToHost));
+  for (uint32_t k = ns; k < nn; ++k) subgraph_to_graph[k] = 0xFFFFFFFFu;
+  return kOk;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -183,3 +183,31 @@ def random_window(rng: np.random.Generator, ln: int, depth: int, err: float = 0.
                 r = tpl[:1]
         reads.append(r.tobytes())
     return reads
+
+
+def slice_window(seed: int, base_seed: int = 6_000_000):
+    """A polishing window with a backbone, for Graph::Subgraph: read 0 is
+    the template (L ~ U[200, 600]) and is added whole, so its bases are graph
+    nodes 0..L-1; each later read (depth U[5, 25]) copies a random span of
+    U[30%, 100%] of the template with 3% sub / 2.5% ins / 2.5% del.  Returns
+    (reads, slices): per read after the first the backbone node range
+    (begin, end) its span covers, except every 7th read (-1, -1: align to the
+    whole graph), every 11th an inverted range (an empty subgraph) and every
+    13th a single node."""
+    rng = np.random.Generator(np.random.PCG64(base_seed + seed))
+    ln = int(rng.integers(200, 601))
+    tpl = ACGT[rng.integers(0, 4, size=ln)]
+    reads, slices = [tpl.tobytes()], []
+    for r in range(1, int(rng.integers(5, 26)) + 1):
+        span = int(ln * rng.uniform(0.3, 1.0))
+        st = int(rng.integers(0, ln - span + 1))
+        reads.append(_mutate(rng, tpl[st:st + span], 0.03, 0.025, 0.025))
+        if r % 7 == 0:
+            slices.append((-1, -1))
+        elif r % 11 == 0:
+            slices.append((st + span - 1, st))
+        elif r % 13 == 0:
+            slices.append((st, st))
+        else:
+            slices.append((st, st + span - 1))
+    return reads, slices

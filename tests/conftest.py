@@ -49,6 +49,24 @@ def ref_windows():
         return json.load(fh)
 
 
+@pytest.fixture(scope="session")
+def slice_windows():
+    with gzip.open(os.path.join(GOLDEN, "slice_windows.json.gz"), "rt") as fh:
+        return json.load(fh)
+
+
+def check_slices(expect, scores, alignments, subgraphs, consensus, msa):
+    """Compare one backbone window run through Subgraph/UpdateAlignment
+    against a recorded reference run (subgraphs: driver lines per slice)."""
+    assert list(scores) == expect["scores"]
+    assert [sha(canon_alignment(a)) for a in alignments] == expect["aln_sha"]
+    for got, want in zip(subgraphs, expect["subgraph_first"]):
+        assert got == want
+    assert [{k: sha(v) for k, v in x.items()} for x in subgraphs] == expect["subgraph_sha"]
+    assert consensus == expect["consensus"]
+    assert sha("\n".join(msa)) == expect["msa_sha"]
+
+
 def check_against_expect(expect, scores, reversed_, alignments, consensus, msa, gfa):
     """Compare one window's outputs against a recorded reference run."""
     assert list(scores) == expect["scores"]

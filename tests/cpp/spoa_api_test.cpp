@@ -5,9 +5,14 @@
 // spoa_gb300.build next to libspoa.so; run by tests/test_cpp_api.py, which
 // compares the printed consensus, MSA and summaries with the fixtures.
 //
-// usage: spoa_api_test <reads.tsv> <cases.txt>
+// usage: spoa_api_test <reads.tsv> <cases.txt> [slices.txt]
 //   reads.tsv: one read per line, "sequence<TAB>quality"
 //   cases.txt: one case per line, "name type m n g e q c quality(0|1)"
+//   slices.txt: backbone windows for Graph::Subgraph / UpdateAlignment,
+//     "S type m n g e q c reads", the reads, then "begin end" per read after
+//     the first (-1 -1: the whole graph); printed as "SLICE <window> R
+//     <read> <score> <node,pos ...>" per read and "SLICE <window> C
+//     <consensus>"
 // Output lines: "CONS <name> <consensus>", "MSA <name> <row>" per row,
 // "SUMMARY <name> <v0,v1,...>" and "VSUMMARY" (verbose), "CLEAR <name>
 // <ok|mismatch>", "FAIL <what>",
@@ -68,6 +73,61 @@ void CheckMsa(const std::string& name, const std::vector<std::string>& msa,
     s.erase(std::remove(s.begin(), s.end(), '-'), s.end());
     if (s != reads[i].data) return Fail(name + " msa row is not the read");
   }
+}
+
+// Read 0 added whole; each later read aligned to Subgraph(begin, end) (or
+// the whole graph), its alignment mapped back with UpdateAlignment, added.
+void RunSlices(const char* path) {
+  std::ifstream in(path);
+  std::string tag;
+  int window = 0;
+  while (in >> tag && tag == "S") {
+    int type, m, n, g, e, q, c;
+    std::uint32_t nr;
+    in >> type >> m >> n >> g >> e >> q >> c >> nr;
+    std::vector<std::string> reads(nr);
+    for (auto& r : reads) in >> r;
+    auto ae = spoa::AlignmentEngine::Create(static_cast<spoa::AlignmentType>(type), m, n, g, e,
+                                            q, c);
+    spoa::Graph gr{};
+    gr.AddAlignment(spoa::Alignment(), reads[0]);
+    for (std::uint32_t r = 1; r < nr; ++r) {
+      long long b, en;
+      in >> b >> en;
+      std::int32_t score = 0;
+      spoa::Alignment a;
+      if (b >= 0) {
+        std::vector<const spoa::Graph::Node*> map;
+        spoa::Graph sub = gr.Subgraph(static_cast<std::uint32_t>(b),
+                                      static_cast<std::uint32_t>(en), &map);
+        if (map.size() != gr.nodes().size()) Fail("subgraph_to_graph size");
+        for (std::size_t k = 0; k < map.size(); ++k)
+          if ((k < sub.nodes().size()) != (map[k] != nullptr)) Fail("subgraph_to_graph entry");
+        a = ae->Align(reads[r], sub, &score);
+        gr.UpdateAlignment(map, &a);
+      } else {
+        a = ae->Align(reads[r], gr, &score);
+      }
+      gr.AddAlignment(a, reads[r]);
+      std::cout << "SLICE " << window << " R " << r << " " << score;
+      for (const auto& it : a) std::cout << " " << it.first << "," << it.second;
+      std::cout << "\n";
+    }
+    std::cout << "SLICE " << window++ << " C " << gr.GenerateConsensus() << "\n";
+  }
+  // graph.cpp:544-548
+  spoa::Graph gr{};
+  gr.AddAlignment(spoa::Alignment(), "ACGT");
+  try {
+    gr.Subgraph(0, 3, nullptr);
+    Fail("Subgraph without a map did not throw");
+  } catch (std::invalid_argument& ex) {
+    std::cout << "ERR SubgraphNullMap " << ex.what() << "\n";
+  }
+  // node objects outlive later changes of the graph (graph.hpp:40-70)
+  const spoa::Graph::Node* first = gr.nodes()[0].get();
+  gr.AddAlignment(spoa::Alignment(), "TTTT");
+  if (gr.nodes()[0].get() != first || first->id != 0) Fail("node pointer after AddAlignment");
 }
 
 std::string Join(const std::vector<std::uint32_t>& v) {
@@ -171,6 +231,7 @@ int main(int argc, char** argv) {
                 << "\n";
     }
     ErrorChecks();
+    if (argc > 3) RunSlices(argv[3]);
   } catch (std::exception& ex) {
     Fail(std::string("exception: ") + ex.what());
   }

@@ -16,7 +16,14 @@ It writes
                            verbose form);
   ref_windows.json.gz      seeded synthetic windows (inputs verbatim) with the
                            reference's outputs: scores, strand flags,
-                           consensus, and sha256 of alignments, MSA and GFA.
+                           consensus, and sha256 of alignments, MSA and GFA;
+  slice_windows.json.gz    backbone windows run through Graph::Subgraph and
+                           UpdateAlignment (inputs and slice ranges verbatim)
+                           with the reference's outputs: every subgraph's
+                           driver lines (sha256 of each; the first three
+                           subgraphs also verbatim), scores, alignments
+                           (sha256), consensus and MSA (sha256).
+With --only slices only the last file is rewritten.
 """
 from __future__ import annotations
 
@@ -128,13 +135,44 @@ def synthetic_specs():
     return specs
 
 
+SLICE_PARAMS = [(5, -4, -8, -8, -8, -8), (5, -4, -8, -6, -8, -6), (5, -4, -8, -6, -10, -4)]
+
+
+def write_slices():
+    """12 backbone windows: every type x gap model, plus three more."""
+    specs = []
+    for k in range(12):
+        reads, sl = synth.slice_window(k)
+        specs.append((f"slice{k}", k % 3, SLICE_PARAMS[(k // 3) % 3], reads, sl))
+    outs = po.parse_reference_output(po.run_reference(po.format_slices(
+        [(t, p, r, sl) for _, t, p, r, sl in specs])))
+    recs = []
+    for (name, t, p, r, sl), o in zip(specs, outs):
+        assert o["error"] is None, (name, o["error"])
+        subs = o.get("slices", [])
+        recs.append({"name": name, "type": t, "params": list(p),
+                     "reads": [x.decode() for x in r], "slices": [list(x) for x in sl],
+                     "expect": {"scores": o["scores"],
+                                "aln_sha": [sha(canon_alignment(a)) for a in o["alignments"]],
+                                "consensus": o["consensus"], "msa_sha": sha("\n".join(o["msa"])),
+                                "subgraph_sha": [{k: sha(v) for k, v in x.items()} for x in subs],
+                                "subgraph_first": subs[:3]}})
+    with gzip.open(os.path.join(HERE, "slice_windows.json.gz"), "wt") as fh:
+        json.dump(recs, fh)
+    print(f"wrote {len(recs)} slice windows")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", choices=["slices"], default=None)
     args = ap.parse_args()
     os.environ["SPOA_REFERENCE_TREE"] = args.reference
     if po.build_reference() is None:
         raise SystemExit("reference driver could not be built")
+    if args.only == "slices":
+        write_slices()
+        return
 
     reads = parse_fastq_gz(os.path.join(args.reference, "test/data/sample.fastq.gz"))
     assert len(reads) == 55, len(reads)
@@ -178,6 +216,7 @@ def main():
     with gzip.open(os.path.join(HERE, "ref_windows.json.gz"), "wt") as fh:
         json.dump(recs, fh)
     print(f"wrote {len(cases)} known-answer cases and {len(recs)} reference windows")
+    write_slices()
 
 
 if __name__ == "__main__":

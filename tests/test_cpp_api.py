@@ -20,15 +20,22 @@ def _driver():
     return DRIVER
 
 
-def _run(tmp_path, sample_reads, cases):
+def _run(tmp_path, sample_reads, cases, slices=None):
     reads = tmp_path / "reads.tsv"
     reads.write_text("".join(f"{s.decode()}\t{q.decode()}\n" for s, q in sample_reads))
     cf = tmp_path / "cases.txt"
     cf.write_text("".join(
         f"{c['name']} {c['type']} {' '.join(str(x) for x in c['params'])} {int(c['quality'])}\n"
         for c in cases))
-    r = subprocess.run([_driver(), str(reads), str(cf)], capture_output=True, text=True,
-                       timeout=1200)
+    args = [_driver(), str(reads), str(cf)]
+    if slices is not None:
+        sf = tmp_path / "slices.txt"
+        sf.write_text("".join(
+            f"S {w['type']} {' '.join(str(x) for x in w['params'])} {len(w['reads'])}\n"
+            + "".join(r + "\n" for r in w["reads"])
+            + "".join(f"{b} {e}\n" for b, e in w["slices"]) for w in slices))
+        args.append(str(sf))
+    r = subprocess.run(args, capture_output=True, text=True, timeout=1200)
     return r
 
 
@@ -50,7 +57,9 @@ def test_library_exports_the_spoa_api():
                 "spoa::Graph::nodes() const", "spoa::Graph::edges() const",
                 "spoa::Graph::rank_to_node() const", "spoa::Graph::sequences() const",
                 "spoa::Graph::consensus() const", "spoa::Graph::Node::Successor(unsigned int) const",
-                "spoa::Graph::Node::Coverage() const"]:
+                "spoa::Graph::Node::Coverage() const",
+                "spoa::Graph::Subgraph(unsigned int, unsigned int, std::vector<spoa::Graph::Node const*",
+                "spoa::Graph::UpdateAlignment(std::vector<spoa::Graph::Node const*"]:
         assert sym in out, sym
     assert out.count("spoa::Graph::AddAlignment(") == 6
 
@@ -63,8 +72,9 @@ def test_cpp_api_fails_loudly_without_a_gpu(tmp_path, sample_reads, spoa_test_ca
 
 
 @pytest.mark.gpu
-def test_cpp_api_known_answers(tmp_path, sample_reads, spoa_test_cases, spoa_test_outputs):
-    r = _run(tmp_path, sample_reads, spoa_test_cases)
+def test_cpp_api_known_answers(tmp_path, sample_reads, spoa_test_cases, spoa_test_outputs,
+                               slice_windows):
+    r = _run(tmp_path, sample_reads, spoa_test_cases, slice_windows)
     lines = r.stdout.splitlines()
     assert lines and lines[-1] == "DONE 0", "\n".join(ln for ln in lines if ln.startswith("FAIL"))
     assert r.returncode == 0
@@ -85,5 +95,15 @@ def test_cpp_api_known_answers(tmp_path, sample_reads, spoa_test_cases, spoa_tes
     assert by[("ERR", "EmptyInput")] == ["empty"]
     assert by[("ERR", "LargeInput1")] == ["AlignmentEngine::Prealloc] error: too large sequence!"]
     assert by[("ERR", "LargeInput2")] == ["no-throw"]
+    # graph.cpp:518-605 through Graph::Subgraph / UpdateAlignment
+    assert by[("ERR", "SubgraphNullMap")] == [
+        "[spoa::Graph::Subgraph] error: invalid ptr to subgraph_to_graph"]
+    for w, rec in enumerate(slice_windows):
+        rows = [v for (tag, name), vals in by.items() if tag == "SLICE" and name == str(w)
+                for v in vals]
+        reads = [x for x in rows if x.startswith("R ")]
+        assert [int(x.split(" ")[2]) for x in reads] == rec["expect"]["scores"]
+        assert [sha(" ".join(x.split(" ")[3:])) for x in reads] == rec["expect"]["aln_sha"]
+        assert [x[2:] for x in rows if x.startswith("C ")] == [rec["expect"]["consensus"]]
     assert by[("ERR", "UnequalWeights")] == [
         "[spoa::Graph::AddAlignment] error: sequence and weights are of unequal size!"]

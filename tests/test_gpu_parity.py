@@ -240,3 +240,54 @@ def test_windows_that_outgrow_their_arena_and_the_int16_width():
         got = [sv.wait(t, timeout=600) for t in tickets]
     assert [g[0] for g in got] == [0] * len(wins)
     assert [g[1] for g in got] == res.consensus
+
+
+def run_slices_gpu(type_, params, reads, slices):
+    """The slice protocol (read 0 whole; each later read aligned to
+    Graph::Subgraph(begin, end) and mapped back by UpdateAlignment) through
+    the device graph and the per-call engine."""
+    engine = sg.AlignmentEngine.create(type_, *params)
+    graph = sg.Graph()
+    graph.add_alignment(np.zeros((0, 2), np.int32), reads[0])
+    scores, alns, subs = [], [], []
+    for r, (b, e) in enumerate(slices, start=1):
+        if b >= 0:
+            sub, m = graph.subgraph(b, e)
+            assert (m[sub.num_nodes:] == sg.NO_NODE).all()
+            ex = sub.export()
+            cons = sub.generate_consensus()
+            subs.append(po.slice_lines(r, m, ex["chars"], ex["rank_to_node"], ex["edge_tail"],
+                                       ex["edge_head"], ex["edge_weight"], ex["aligned_off"],
+                                       ex["aligned"], cons))
+            aln, score = engine.align(reads[r], sub)
+            aln = graph.update_alignment(m, aln)
+        else:
+            aln, score = engine.align(reads[r], graph)
+        scores.append(0 if score is None else score)
+        alns.append(aln)
+        graph.add_alignment(aln, reads[r])
+    return scores, alns, subs, graph.generate_consensus(), \
+        graph.generate_multiple_sequence_alignment()
+
+
+def test_subgraph_update_alignment(slice_windows):
+    """Graph::Subgraph + UpdateAlignment (graph.cpp:518-605) on the device
+    against recorded reference runs: every subgraph's nodes, order, edges,
+    aligned lists and consensus, each score and mapped alignment, the final
+    consensus and MSA; includes whole-graph, empty and single-node slices."""
+    from conftest import check_slices
+    for rec in slice_windows:
+        got = run_slices_gpu(rec["type"], tuple(rec["params"]),
+                             [r.encode() for r in rec["reads"]], rec["slices"])
+        check_slices(rec["expect"], *got)
+
+
+def test_subgraph_rejects_bad_node_ids():
+    graph = sg.Graph()
+    graph.add_alignment(np.zeros((0, 2), np.int32), b"ACGTACGT")
+    for b, e in ((8, 2), (0, 8)):
+        with pytest.raises(sg.SpoaError) as ex:
+            graph.subgraph(b, e)
+        assert ex.value.status == 1
+    sub, m = graph.subgraph(7, 0)  # inverted range: an empty subgraph
+    assert sub.num_nodes == 0 and (m == sg.NO_NODE).all()

@@ -63,6 +63,18 @@ def test_reference_windows(ref_windows):
                              res.consensus, res.msa, _gfa(res))
 
 
+def test_slice_windows(slice_windows):
+    """Graph::Subgraph + UpdateAlignment (graph.cpp:518-605) on backbone
+    windows: every subgraph (nodes, order, edges, aligned lists, consensus),
+    score, mapped alignment, consensus and MSA against the reference."""
+    from conftest import check_slices
+    for rec in slice_windows:
+        res = po.run_slices(rec["type"], tuple(rec["params"]),
+                            [r.encode() for r in rec["reads"]], rec["slices"])
+        check_slices(rec["expect"], res["scores"], res["alignments"], res["slices"],
+                     res["consensus"], res["msa"])
+
+
 def test_engine_errors():
     L = po.lib()
     import ctypes as C
