@@ -4,7 +4,8 @@
 
 Compiles the four translation units in parallel with nvcc and links
 spoa_gb300/libspoa_gb300.so (the C ABI of include/spoa_gb300.h), then the C++
-drop-in layer spoa_gb300/libspoa.so (include/spoa/*.hpp).
+drop-in layer spoa_gb300/libspoa.so (include/spoa/*.hpp) and the `spoa`
+command-line program spoa_gb300/spoa over it.
 """
 from __future__ import annotations
 
@@ -22,6 +23,7 @@ LIB = os.path.join(HERE, "libspoa_gb300.so")
 CPPLIB = os.path.join(HERE, "libspoa.so")
 PEAKLIB = os.path.join(HERE, "libspoa_peak.so")
 CPPTEST = os.path.join(OUT, "spoa_api_test")
+CLI = os.path.join(HERE, "spoa")
 
 TUS = ["spoa_gb300"] + [f"inst_{m}{w}" for m in ("linear", "affine", "convex") for w in (16, 32)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -89,6 +91,14 @@ def build(verbose: bool = False, force: bool = False) -> str:
             subprocess.run(["g++", "-std=c++11", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
                             test_src, "-o", CPPTEST, "-L", HERE, "-lspoa",
                             "-Wl,-rpath," + HERE], check=True)
+        # the spoa command-line program (gzip input where zlib is installed)
+        cli_src = os.path.join(CSRC, "spoa_cli.cpp")
+        if os.path.exists(cli_src) and (force or _stale(CLI, [cli_src, CPPLIB] + cpp_hdrs)):
+            zlib = subprocess.run(["g++", "-x", "c++", "-E", "-"], input="#include <zlib.h>\n",
+                                  capture_output=True, text=True).returncode == 0
+            subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+                            cli_src, "-o", CLI, "-L", HERE, "-lspoa", "-lspoa_gb300"]
+                           + (["-lz"] if zlib else []) + ["-Wl,-rpath,$ORIGIN"], check=True)
     return LIB
 
 

@@ -23,7 +23,12 @@ It writes
                            driver lines (sha256 of each; the first three
                            subgraphs also verbatim), scores, alignments
                            (sha256), consensus and MSA (sha256).
-With --only slices only the last file is rewritten.
+  cli_outputs.json         what the reference CLI (its src/main.cpp, built
+                           by oracle/Makefile) prints for the cases of
+                           cli_inputs.py: exit code, stdout (sha256 and
+                           size; verbatim when short), stderr, DOT file
+                           (sha256); plus the names of the sample reads.
+With --only slices or --only cli only that file is rewritten.
 """
 from __future__ import annotations
 
@@ -40,6 +45,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
 
 from oracle import pyoracle as po  # noqa: E402
 from spoa_gb300 import synth  # noqa: E402
@@ -162,16 +168,52 @@ def write_slices():
     print(f"wrote {len(recs)} slice windows")
 
 
+def write_cli(reference: str):
+    """Runs the reference CLI on the inputs of cli_inputs.py."""
+    import subprocess
+    import tempfile
+    import cli_inputs
+    cli = os.path.join(ROOT, "oracle", "_ref", "spoa_ref_cli")
+    with gzip.open(os.path.join(reference, "test/data/sample.fastq.gz"), "rt") as fh:
+        lines = [ln.rstrip("\n") for ln in fh]
+    names = [lines[k][1:].split()[0] for k in range(0, len(lines) - 3, 4)]
+    with gzip.open(os.path.join(HERE, "sample_reads.tsv.gz"), "rt") as fh:
+        sample = [tuple(x.encode() for x in ln.rstrip("\n").split("\t")) for ln in fh if ln.strip()]
+    out = {"sample_names": names, "cases": [], "errors": []}
+    with tempfile.TemporaryDirectory() as d:
+        paths = cli_inputs.write_inputs(d, sample, names)
+        dot = os.path.join(d, "graph.dot")
+        for key, argv in cli_inputs.CASES + cli_inputs.ERROR_CASES:
+            if os.path.exists(dot):
+                os.remove(dot)
+            cmd = [cli] + [dot if a == "{dot}" else a for a in argv] + [paths[key]]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            rec = {"input": key, "args": argv, "rc": r.returncode, "stdout_sha": sha(r.stdout),
+                   "stdout_len": len(r.stdout), "stderr": r.stderr}
+            if len(r.stdout) < 4096:
+                rec["stdout"] = r.stdout
+            if "{dot}" in argv:
+                rec["dot_sha"] = sha(open(dot).read())
+            out["errors" if (key, argv) in cli_inputs.ERROR_CASES else "cases"].append(rec)
+            assert (r.returncode == 0) == ((key, argv) in cli_inputs.CASES), (argv, r.stderr)
+    with open(os.path.join(HERE, "cli_outputs.json"), "w") as fh:
+        json.dump(out, fh, indent=1)
+    print(f"wrote {len(out['cases'])} CLI cases and {len(out['errors'])} error cases")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["slices"], default=None)
+    ap.add_argument("--only", choices=["slices", "cli"], default=None)
     args = ap.parse_args()
     os.environ["SPOA_REFERENCE_TREE"] = args.reference
     if po.build_reference() is None:
         raise SystemExit("reference driver could not be built")
     if args.only == "slices":
         write_slices()
+        return
+    if args.only == "cli":
+        write_cli(args.reference)
         return
 
     reads = parse_fastq_gz(os.path.join(args.reference, "test/data/sample.fastq.gz"))
@@ -217,6 +259,7 @@ def main():
         json.dump(recs, fh)
     print(f"wrote {len(cases)} known-answer cases and {len(recs)} reference windows")
     write_slices()
+    write_cli(args.reference)
 
 
 if __name__ == "__main__":
