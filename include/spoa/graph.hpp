@@ -19,6 +19,11 @@
 #include <utility>
 #include <vector>
 
+#ifdef SPOA_USE_CEREAL
+#include "cereal/access.hpp"
+#include "cereal/types/vector.hpp"
+#endif
+
 struct spoa_gb300_graph;
 
 namespace spoa {
@@ -124,6 +129,28 @@ class Graph {
 
   // graph.cpp:649-658
   void Clear();
+
+  // Persistence.  The reference archives a Graph with cereal
+  // (graph.hpp:187-276); here Serialize gives the same fields (coder
+  // tables, nodes, edges with labels and weights, sequence starts, aligned
+  // pairs, rank order, last consensus) in this library's own byte layout,
+  // and Deserialize rebuilds a graph from them the way the reference's load
+  // does.  With SPOA_USE_CEREAL, save/load put those bytes into any cereal
+  // archive, so archive(graph) works as with the reference.
+  std::vector<std::uint8_t> Serialize() const;
+  void Deserialize(const std::vector<std::uint8_t>& bytes);
+#ifdef SPOA_USE_CEREAL
+  template <class Archive>
+  void save(Archive& archive) const {  // NOLINT
+    archive(Serialize());
+  }
+  template <class Archive>
+  void load(Archive& archive) {  // NOLINT
+    std::vector<std::uint8_t> bytes;
+    archive(bytes);
+    Deserialize(bytes);
+  }
+#endif
 
   // The device graph behind this object (for the C ABI and the fused
   // align-and-add call of libspoa_gb300).

@@ -163,6 +163,19 @@ int32_t spoa_gb300_graph_subgraph(const spoa_gb300_graph* graph, uint32_t begin,
                                   spoa_gb300_graph* out, uint32_t* subgraph_to_graph,
                                   uint32_t map_len);
 
+/* Graph persistence (the reference archives a Graph with cereal,
+ * include/spoa/graph.hpp:187-276; cereal is not used here).  save writes
+ * the fields the reference archives (coder tables, nodes, edges with labels
+ * and weights, sequence starts, aligned pairs, rank order, last consensus)
+ * in this library's own layout: *size gets the byte count, and `out` (when
+ * not NULL) the bytes if cap is large enough (SPOA_GB300_ERR_CAPACITY
+ * otherwise).  load rebuilds a graph from such bytes into `graph` (its
+ * previous contents are dropped) the way the reference's Graph::load
+ * rebuilds it; malformed input gives SPOA_GB300_ERR_INVALID_ARGUMENT. */
+int32_t spoa_gb300_graph_save(const spoa_gb300_graph* graph, uint8_t* out, uint64_t cap,
+                              uint64_t* size);
+int32_t spoa_gb300_graph_load(spoa_gb300_graph* graph, const uint8_t* in, uint64_t size);
+
 /* ---- Batched windows (no counterpart in the reference) ------------------- *
  * Many independent windows (each one Graph driven by the per-read loop of
  * src/main.cpp:275-314, then GenerateConsensus) in one persistent kernel:

@@ -268,10 +268,15 @@ def parse_reference_output(text: str) -> list:
             cur["summary" if tag == "Y" else "summary_verbose"] = vals
         elif tag == "G":
             cur["gfa"].append(rest)
-        elif tag in ("U", "K", "O", "L", "A", "Q"):
-            if tag == "U":
-                cur.setdefault("slices", []).append({})
-            cur["slices"][-1][tag] = rest
+        elif tag == "U":
+            cur.setdefault("slices", []).append({"U": rest})
+        elif tag in ("K", "O", "L", "A", "Q", "S"):
+            # lines of the last subgraph (after a U line), else of the graph
+            # as loaded (persisted windows)
+            if cur.get("slices") and tag not in cur["slices"][-1] and tag != "S":
+                cur["slices"][-1][tag] = rest
+            else:
+                cur.setdefault("loaded", {})[tag] = rest
         elif tag == "X":
             cur["error"] = rest
         elif tag == "E":
@@ -385,3 +390,37 @@ def run_slices(type_: int, params, reads: list[bytes], slices) -> dict:
         L.oracle_graph_destroy(sub)
         L.oracle_graph_destroy(g)
         L.oracle_engine_destroy(en)
+
+
+# ---- persisted windows: Graph::save / Graph::load (graph.hpp:187-276) -------
+
+def format_persist(specs) -> str:
+    """specs: iterable of (type, (m, n, g, e, q, c), reads, quals|None, split)."""
+    out = []
+    for typ, (m, n, g, e, q, c), reads, quals, split in specs:
+        hq = 1 if quals is not None else 0
+        out.append(f"P {typ} {m} {n} {g} {e} {q} {c} {hq} {len(reads)} {split}\n")
+        for k, r in enumerate(reads):
+            out.append(r.decode() + "\n")
+            if hq:
+                out.append(quals[k].decode() + "\n")
+    return "".join(out)
+
+
+def loaded_lines(chars, rank, seq_begin, consensus, edge_tail, edge_head, edge_weight,
+                 label_off, labels, aligned_off, aligned) -> dict:
+    """The K/O/S/Q/L/A lines of the reference driver for a loaded graph."""
+    al = []
+    for v in range(len(chars)):
+        lst = aligned[aligned_off[v]:aligned_off[v + 1]]
+        if len(lst):
+            al.append(f"{v}:" + ",".join(str(int(x)) for x in lst))
+    edges = []
+    for e in range(len(edge_tail)):
+        lab = "|".join(str(int(x)) for x in labels[label_off[e]:label_off[e + 1]])
+        edges.append(f"{int(edge_tail[e])},{int(edge_head[e])},{int(edge_weight[e])},{lab}")
+    return {"K": bytes(np.asarray(chars, np.uint8)).decode(),
+            "O": " ".join(str(int(x)) for x in rank),
+            "S": " ".join(str(int(x)) for x in seq_begin),
+            "Q": " ".join(str(int(x)) for x in consensus),
+            "L": " ".join(edges), "A": " ".join(al)}

@@ -38,6 +38,17 @@
 //   Q <subgraph consensus>
 //   R <read> <score> 0 <pairs> <node>,<pos> ...   after UpdateAlignment
 // then C, M and E as above.
+//
+// Persisted windows (Graph::save / Graph::load, include/spoa/graph.hpp:
+// 187-276, through the archives of ref_shim/cereal):
+//   P <type> <m> <n> <g> <e> <q> <c> <has_quality> <reads> <split>
+//   <sequence> [<quality>]  per read
+// Reads before `split` go into a graph (then GenerateConsensus); it is
+// saved and loaded into a second graph, which is printed as loaded
+//   K <node characters>   O <rank_to_node ids>   S <sequence start ids>
+//   Q <consensus ids>     L <tail>,<head>,<weight>,<label>|<label>... per edge
+//   A <node>:<aligned>,... per node with aligned nodes
+// and then takes the remaining reads: R lines for them, C, M, G and E.
 #include <algorithm>
 #include <chrono>
 #include <cstdint>
@@ -133,6 +144,76 @@ int main(int argc, char** argv) {
   std::uint64_t cells = 0;
   double seconds = 0;
   while (std::cin >> tag) {
+    if (tag == "P") {
+      int type, m, n, g, e, q, c, has_quality;
+      std::uint32_t reads, split;
+      std::cin >> type >> m >> n >> g >> e >> q >> c >> has_quality >> reads >> split;
+      std::vector<std::string> data(reads), quality(reads);
+      for (std::uint32_t r = 0; r < reads; ++r) {
+        std::cin >> data[r];
+        if (has_quality) std::cin >> quality[r];
+      }
+      std::ostringstream os;
+      os << "W " << window++ << "\n";
+      try {
+        auto engine = spoa::AlignmentEngine::Create(
+            static_cast<spoa::AlignmentType>(type), m, n, g, e, q, c);
+        auto add = [&](spoa::Graph& graph, std::uint32_t r) {
+          std::int32_t score = 0;
+          auto alignment = engine->Align(data[r], graph, &score);
+          if (quality[r].empty()) {
+            graph.AddAlignment(alignment, data[r]);
+          } else {
+            graph.AddAlignment(alignment, data[r], quality[r]);
+          }
+          return std::make_pair(score, alignment);
+        };
+        spoa::Graph first{};
+        for (std::uint32_t r = 0; r < split; ++r) add(first, r);
+        if (split > 0) first.GenerateConsensus();
+        std::string bytes;
+        cereal::BinaryOutputArchive out(&bytes);
+        out(first);
+        spoa::Graph graph{};
+        cereal::BinaryInputArchive in(bytes);
+        in(graph);
+        os << "K ";
+        for (const auto& it : graph.nodes()) os << static_cast<char>(graph.decoder(it->code));
+        os << "\nO";
+        for (const auto& it : graph.rank_to_node()) os << " " << it->id;
+        os << "\nS";
+        for (const auto& it : graph.sequences()) os << " " << it->id;
+        os << "\nQ";
+        for (const auto& it : graph.consensus()) os << " " << it->id;
+        os << "\nL";
+        for (const auto& it : graph.edges()) {
+          os << " " << it->tail->id << "," << it->head->id << "," << it->weight << ",";
+          for (std::size_t k = 0; k < it->labels.size(); ++k) os << (k ? "|" : "") << it->labels[k];
+        }
+        os << "\nA";
+        for (const auto& it : graph.nodes()) {
+          if (it->aligned_nodes.empty()) continue;
+          os << " " << it->id << ":";
+          for (std::size_t k = 0; k < it->aligned_nodes.size(); ++k)
+            os << (k ? "," : "") << it->aligned_nodes[k]->id;
+        }
+        os << "\n";
+        for (std::uint32_t r = split; r < reads; ++r) {
+          auto res = add(graph, r);
+          os << "R " << r << " " << res.first << " 0 " << res.second.size();
+          for (const auto& it : res.second) os << " " << it.first << "," << it.second;
+          os << "\n";
+        }
+        os << "C " << graph.GenerateConsensus() << "\n";
+        for (const auto& row : graph.GenerateMultipleSequenceAlignment()) os << "M " << row << "\n";
+        WriteGfa(graph, std::vector<bool>(), os);
+      } catch (std::exception& ex) {
+        os << "X " << ex.what() << "\n";
+      }
+      os << "E\n";
+      std::cout << os.str();
+      continue;
+    }
     if (tag == "S") {
       int type, m, n, g, e, q, c;
       std::uint32_t reads;

@@ -1,0 +1,2 @@
+// cereal/types/memory.hpp - see cereal/access.hpp (test infrastructure only).
+#include "cereal/access.hpp"

@@ -110,7 +110,8 @@ EXPORTED = [
     "spoa_gb300_graph_add_alignment_quality", "spoa_gb300_align_add",
     "spoa_gb300_align_add_reads",
     "spoa_gb300_graph_consensus", "spoa_gb300_graph_msa", "spoa_gb300_graph_counts",
-    "spoa_gb300_graph_export", "spoa_gb300_graph_subgraph", "spoa_gb300_batch_create",
+    "spoa_gb300_graph_export", "spoa_gb300_graph_subgraph", "spoa_gb300_graph_save",
+    "spoa_gb300_graph_load", "spoa_gb300_batch_create",
     "spoa_gb300_batch_launch",
     "spoa_gb300_batch_launch_plain", "spoa_gb300_batch_fetch", "spoa_gb300_batch_destroy",
     "spoa_gb300_batch_run", "spoa_gb300_server_create", "spoa_gb300_server_submit",
@@ -152,6 +153,8 @@ def lib():
         L.spoa_gb300_graph_counts.argtypes = [P] * 7
         L.spoa_gb300_graph_export.argtypes = [P] * 19
         L.spoa_gb300_graph_subgraph.argtypes = [P, U32, U32, P, P, U32]
+        L.spoa_gb300_graph_save.argtypes = [P, P, U64, P]
+        L.spoa_gb300_graph_load.argtypes = [P, P, U64]
         L.spoa_gb300_batch_create.argtypes = [C.POINTER(_BatchDesc), P]
         L.spoa_gb300_batch_launch.argtypes = [P, P]
         L.spoa_gb300_batch_launch_plain.argtypes = [P, P]
@@ -343,6 +346,25 @@ class Graph:
         _check("Graph::Subgraph", lib().spoa_gb300_graph_subgraph(
             self._h, begin, end, sub._h, _ptr(m), m.size))
         return sub, m[:self.num_nodes]
+
+    def save(self) -> bytes:
+        """The graph as bytes (the fields the reference's cereal
+        serialisation archives, include/spoa/graph.hpp:187-233, in this
+        library's own layout)."""
+        n = C.c_uint64()
+        _check("Graph::save", lib().spoa_gb300_graph_save(self._h, None, 0, C.byref(n)))
+        buf = np.zeros(max(n.value, 1), np.uint8)
+        _check("Graph::save", lib().spoa_gb300_graph_save(self._h, _ptr(buf), buf.size,
+                                                          C.byref(n)))
+        return buf[:n.value].tobytes()
+
+    def load(self, data: bytes) -> "Graph":
+        """Replaces this graph by one saved with save(), rebuilt the way the
+        reference's Graph::load rebuilds it (graph.hpp:236-275)."""
+        buf = np.frombuffer(bytes(data), np.uint8)
+        _check("Graph::load", lib().spoa_gb300_graph_load(
+            self._h, _ptr(np.ascontiguousarray(buf)) if buf.size else None, buf.size))
+        return self
 
     @staticmethod
     def update_alignment(subgraph_to_graph, alignment):

@@ -311,24 +311,15 @@ __device__ inline int g_add_label(GraphView& G, uint32_t e) {
   return 0;
 }
 
-// Graph::AddEdge (graph.cpp:81-91)
-__device__ inline int g_add_edge(GraphView& G, uint32_t tail, uint32_t head, uint32_t w) {
-  for (uint32_t e = G.nlink[tail].z; e != kNone;) {
-    const uint4 er = G.erec[e];
-    if (er.y == head) {
-      if (g_add_label(G, e)) return -1;
-      G.e_weight[e] += w;
-      return 0;
-    }
-    e = er.w;
-  }
+// A new edge tail -> head with weight w and no labels, appended to the
+// tail's out-edge list and the head's in-edge list; -1 when full.
+__device__ inline int64_t g_new_edge(GraphView& G, uint32_t tail, uint32_t head, int64_t w) {
   GraphHeader* h = G.hdr;
   if (h->n_edges >= G.caps.edges) return -1;
   uint32_t e = h->n_edges++;
   G.erec[e] = make_uint4(tail, head, kNone, kNone);
   G.e_weight[e] = w;
   G.e_lab_first[e] = G.e_lab_last[e] = kNone;
-  if (g_add_label(G, e)) return -1;
   const uint4 lt = G.nlink[tail];
   if (lt.w != kNone) G.erec[lt.w].w = e; else G.nlink[tail].z = e;
   G.nlink[tail].w = e;
@@ -343,6 +334,22 @@ __device__ inline int g_add_edge(GraphView& G, uint32_t tail, uint32_t head, uin
   if (d == 1) r.z = tail;
   if (d == 2) r.w = tail;
   G.nrec[head] = r;
+  return e;
+}
+
+// Graph::AddEdge (graph.cpp:81-91)
+__device__ inline int g_add_edge(GraphView& G, uint32_t tail, uint32_t head, uint32_t w) {
+  for (uint32_t e = G.nlink[tail].z; e != kNone;) {
+    const uint4 er = G.erec[e];
+    if (er.y == head) {
+      if (g_add_label(G, e)) return -1;
+      G.e_weight[e] += w;
+      return 0;
+    }
+    e = er.w;
+  }
+  const int64_t e = g_new_edge(G, tail, head, w);
+  if (e < 0 || g_add_label(G, (uint32_t)e)) return -1;
   return 0;
 }
 

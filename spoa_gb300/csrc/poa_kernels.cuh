@@ -414,6 +414,73 @@ __global__ void k_subgraph(GraphView S, GraphView D, uint32_t begin, uint32_t en
   __syncthreads();
   if (threadIdx.x == 0) *status = s_st;
 }
+
+// A saved graph (arrays checked by the host: every id in range, one rank
+// per node, at most caps.aligned aligned nodes per node).
+struct ImportArgs {
+  uint32_t n_nodes, n_edges, n_seqs, n_pairs, n_consensus, num_codes;
+  const uint8_t* codes;
+  const uint32_t *e_tail, *e_head;
+  const int64_t* e_weight;
+  const uint32_t *lab_off, *labels;  // labels of edge e: lab_off[e] .. lab_off[e + 1]
+  const uint32_t *seq_begin, *pairs, *rank, *consensus;
+  const int32_t *coder, *decoder;
+};
+
+// Rebuilds a saved graph in the empty graph G the way the reference's
+// Graph::load (include/spoa/graph.hpp:236-275) rebuilds it: nodes in id
+// order; edges in id order, each appended to its tail's out-edge list and
+// its head's in-edge list, with its labels and weight; for every aligned
+// pair (a, b) in order, b appended to a's list and a to b's (which can
+// reorder a node's aligned list against the saved graph, as the
+// reference's load does); rank order, sequence starts and the last
+// consensus as saved.  Thread 0; *status kOk or kCapacity.
+__global__ void k_import(GraphView G, ImportArgs a, int32_t* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int32_t st = kOk;
+  GraphHeader* h = G.hdr;
+  g_reset(G);
+  h->num_codes = a.num_codes;
+  for (int k = 0; k < 256; ++k) {
+    h->coder[k] = a.coder[k];
+    h->decoder[k] = a.decoder[k];
+  }
+  for (uint32_t v = 0; v < a.n_nodes && st == kOk; ++v)
+    if (g_add_node(G, a.codes[v]) < 0) st = kCapacity;
+  for (uint32_t e = 0; e < a.n_edges && st == kOk; ++e) {
+    const int64_t id = g_new_edge(G, a.e_tail[e], a.e_head[e], a.e_weight[e]);
+    if (id < 0) {
+      st = kCapacity;
+      break;
+    }
+    for (uint32_t k = a.lab_off[e]; k < a.lab_off[e + 1]; ++k) {
+      if (h->n_labels >= G.caps.labels) {
+        st = kCapacity;
+        break;
+      }
+      const uint32_t l = h->n_labels++;
+      G.lab_seq[l] = a.labels[k];
+      G.lab_next[l] = kNone;
+      if (G.e_lab_last[id] != kNone) G.lab_next[G.e_lab_last[id]] = l; else G.e_lab_first[id] = l;
+      G.e_lab_last[id] = l;
+    }
+  }
+  for (uint32_t k = 0; k < a.n_pairs && st == kOk; ++k) {
+    const uint32_t x = a.pairs[2 * k], y = a.pairs[2 * k + 1];
+    if (g_link_aligned(G, x, y) || g_link_aligned(G, y, x)) st = kCapacity;
+  }
+  if (st == kOk) {
+    for (uint32_t r = 0; r < a.n_nodes; ++r) {
+      G.rank_to_node[r] = a.rank[r];
+      G.node_to_rank[a.rank[r]] = r;
+    }
+    for (uint32_t s = 0; s < a.n_seqs; ++s) G.seq_begin[s] = a.seq_begin[s];
+    h->n_seqs = a.n_seqs;
+    for (uint32_t k = 0; k < a.n_consensus; ++k) G.consensus[k] = a.consensus[k];
+    h->n_consensus = a.n_consensus;
+  }
+  *status = st;
+}
 #endif
 
 // ---------------------------------------------------------------------------

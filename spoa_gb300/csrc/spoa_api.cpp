@@ -488,4 +488,20 @@ void Graph::Clear() {
   Check("Graph::Clear", spoa_gb300_graph_clear(handle_));
 }
 
+std::vector<std::uint8_t> Graph::Serialize() const {
+  uint64_t n = 0;
+  Check("Graph::save", spoa_gb300_graph_save(handle_, nullptr, 0, &n));
+  std::vector<std::uint8_t> bytes(n);
+  Check("Graph::save", spoa_gb300_graph_save(handle_, bytes.data(), n, &n));
+  return bytes;
+}
+
+void Graph::Deserialize(const std::vector<std::uint8_t>& bytes) {
+  Invalidate();
+  // a fresh view: node and edge objects of the old graph are not reused
+  nodes_.clear();
+  edges_.clear();
+  Check("Graph::load", spoa_gb300_graph_load(handle_, bytes.data(), bytes.size()));
+}
+
 }  // namespace spoa

@@ -746,6 +746,221 @@ int32_t spoa_gb300_graph_subgraph(const spoa_gb300_graph* g, uint32_t begin, uin
   return kOk;
 }
 
+// ---- graph persistence -----------------------------------------------------
+// The fields the reference's Graph::save archives (include/spoa/graph.hpp:
+// 188-233), in this library's own little-endian layout:
+//   "SPOAGB01"                       magic and version
+//   u32 num_codes, i32 coder[256], i32 decoder[256]
+//   u32 N, u8 code[N]                nodes in id order
+//   u32 E, E x {u32 tail, u32 head, i64 weight, u32 n, u32 label[n]}
+//   u32 S, u32 seq_begin[S]
+//   u32 P, P x {u32 a, u32 b}        aligned pairs, a < b, in node order
+//   u32 R, u32 rank_to_node[R]
+//   u32 C, u32 consensus[C]
+}  // extern "C"
+
+namespace {
+
+constexpr char kGraphMagic[8] = {'S', 'P', 'O', 'A', 'G', 'B', '0', '1'};
+
+struct Writer {
+  uint8_t* out;
+  uint64_t cap, n = 0;
+  void raw(const void* p, uint64_t bytes) {
+    if (out && bytes && n + bytes <= cap) std::memcpy(out + n, p, bytes);
+    n += bytes;
+  }
+  template <typename T> void put(T v) { raw(&v, sizeof(v)); }
+};
+
+struct Reader {
+  const uint8_t* p;
+  uint64_t size, n = 0;
+  bool ok = true;
+  bool raw(void* dst, uint64_t bytes) {
+    if (!ok || bytes > size - n) return ok = false;
+    if (!bytes) return true;
+    std::memcpy(dst, p + n, bytes);
+    n += bytes;
+    return true;
+  }
+  template <typename T> T get() {
+    T v{};
+    raw(&v, sizeof(v));
+    return v;
+  }
+  // a count of items of `bytes` each that the rest of the buffer can hold
+  uint32_t count(uint64_t bytes) {
+    const uint32_t c = get<uint32_t>();
+    if (ok && (uint64_t)c * bytes > size - n) ok = false;
+    return ok ? c : 0;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int32_t spoa_gb300_graph_save(const spoa_gb300_graph* g, uint8_t* out, uint64_t cap,
+                              uint64_t* size) {
+  if (!g || !size) return kInvalidArgument;
+  const GraphHeader& h = g->h;
+  const uint32_t N = h.n_nodes, E = h.n_edges, S = h.n_seqs, C = h.n_consensus;
+  std::vector<uint8_t> codes(N + 1);
+  std::vector<uint32_t> al_off(N + 1), al((uint64_t)N * g->caps.aligned + 1), tail(E + 1),
+      head(E + 1), lab_off(E + 1), labels(h.n_labels + 1), rank(N + 1), sb(S + 1), cons(C + 1);
+  std::vector<int64_t> weight(E + 1);
+  std::vector<int32_t> coder(256), decoder(256);
+  int32_t st = spoa_gb300_graph_export(g, nullptr, codes.data(), nullptr, nullptr, nullptr, nullptr,
+                                       al_off.data(), al.data(), tail.data(), head.data(),
+                                       weight.data(), lab_off.data(), labels.data(), rank.data(),
+                                       sb.data(), cons.data(), coder.data(), decoder.data());
+  if (st) return st;
+  Writer w{out, out ? cap : 0};
+  w.raw(kGraphMagic, sizeof(kGraphMagic));
+  w.put<uint32_t>(h.num_codes);
+  w.raw(coder.data(), 1024);
+  w.raw(decoder.data(), 1024);
+  w.put<uint32_t>(N);
+  w.raw(codes.data(), N);
+  w.put<uint32_t>(E);
+  for (uint32_t e = 0; e < E; ++e) {
+    w.put<uint32_t>(tail[e]);
+    w.put<uint32_t>(head[e]);
+    w.put<int64_t>(weight[e]);
+    w.put<uint32_t>(lab_off[e + 1] - lab_off[e]);
+    w.raw(labels.data() + lab_off[e], 4ull * (lab_off[e + 1] - lab_off[e]));
+  }
+  w.put<uint32_t>(S);
+  w.raw(sb.data(), 4ull * S);
+  uint32_t P = 0;
+  for (uint32_t v = 0; v < N; ++v)
+    for (uint32_t k = al_off[v]; k < al_off[v + 1]; ++k) P += v < al[k];
+  w.put<uint32_t>(P);
+  for (uint32_t v = 0; v < N; ++v)
+    for (uint32_t k = al_off[v]; k < al_off[v + 1]; ++k)
+      if (v < al[k]) {
+        w.put<uint32_t>(v);
+        w.put<uint32_t>(al[k]);
+      }
+  w.put<uint32_t>(N);
+  w.raw(rank.data(), 4ull * N);
+  w.put<uint32_t>(C);
+  w.raw(cons.data(), 4ull * C);
+  *size = w.n;
+  return out && w.n > cap ? kCapacity : kOk;
+}
+
+int32_t spoa_gb300_graph_load(spoa_gb300_graph* g, const uint8_t* in, uint64_t size) {
+  if (!g || (!in && size)) return kInvalidArgument;
+  Reader r{in, size};
+  char magic[8];
+  if (!r.raw(magic, 8) || std::memcmp(magic, kGraphMagic, 8) != 0) return kInvalidArgument;
+  const uint32_t num_codes = r.get<uint32_t>();
+  std::vector<int32_t> coder(256), decoder(256);
+  r.raw(coder.data(), 1024);
+  r.raw(decoder.data(), 1024);
+  const uint32_t N = r.count(1);
+  std::vector<uint8_t> codes(N + 1);
+  r.raw(codes.data(), N);
+  const uint32_t E = r.count(20);
+  std::vector<uint32_t> tail(E + 1), head(E + 1), lab_off(E + 1, 0), labels;
+  std::vector<int64_t> weight(E + 1);
+  for (uint32_t e = 0; e < E && r.ok; ++e) {
+    tail[e] = r.get<uint32_t>();
+    head[e] = r.get<uint32_t>();
+    weight[e] = r.get<int64_t>();
+    const uint32_t nl = r.count(4);
+    labels.resize(labels.size() + nl);
+    r.raw(labels.data() + labels.size() - nl, 4ull * nl);
+    lab_off[e + 1] = (uint32_t)labels.size();
+    if (tail[e] >= N || head[e] >= N) r.ok = false;
+  }
+  const uint32_t S = r.count(4);
+  std::vector<uint32_t> sb(S + 1);
+  r.raw(sb.data(), 4ull * S);
+  const uint32_t P = r.count(8);
+  std::vector<uint32_t> pairs(2ull * P + 1);
+  r.raw(pairs.data(), 8ull * P);
+  const uint32_t R = r.count(4);
+  std::vector<uint32_t> rank(R + 1);
+  r.raw(rank.data(), 4ull * R);
+  const uint32_t C = r.count(4);
+  std::vector<uint32_t> cons(C + 1);
+  r.raw(cons.data(), 4ull * C);
+  if (!r.ok || r.n != size || R != N || C > N || labels.size() >= 0xFFFFFFF0ull)
+    return kInvalidArgument;
+  // every id in range, ranks a permutation, aligned lists within capacity
+  std::vector<uint8_t> seen(N + 1, 0);
+  std::vector<uint32_t> deg(N + 1, 0);
+  for (uint32_t k = 0; k < R; ++k) {
+    if (rank[k] >= N || seen[rank[k]]) return kInvalidArgument;
+    seen[rank[k]] = 1;
+  }
+  for (uint32_t k = 0; k < S; ++k)
+    if (sb[k] >= N) return kInvalidArgument;
+  for (uint32_t k = 0; k < C; ++k)
+    if (cons[k] >= N) return kInvalidArgument;
+  for (uint32_t k = 0; k < 2 * P; ++k) {
+    if (pairs[k] >= N) return kInvalidArgument;
+    if (++deg[pairs[k]] > g->caps.aligned) return kCapacity;
+  }
+  for (uint32_t k = 0; k < P; ++k)
+    if (pairs[2 * k] == pairs[2 * k + 1]) return kInvalidArgument;
+  for (int k = 0; k < 256; ++k)
+    if (coder[k] < -1 || coder[k] > 255 || decoder[k] < -1 || decoder[k] > 255)
+      return kInvalidArgument;
+  int32_t st = spoa_gb300_graph_clear(g);
+  if (st) return st;
+  const uint64_t Lb = labels.size();
+  st = graph_reserve(g, std::max<uint64_t>({N, E, Lb}), std::max<uint32_t>(S, 1));
+  if (st) return st;
+  // one device buffer for every array
+  const uint64_t items[] = {N, 4ull * E, 4ull * E, 8ull * E, 4ull * (E + 1), 4 * Lb, 4ull * S,
+                            8ull * P, 4ull * N, 4ull * C, 1024, 1024};
+  const void* src[] = {codes.data(), tail.data(), head.data(), weight.data(), lab_off.data(),
+                       labels.data(), sb.data(), pairs.data(), rank.data(), cons.data(),
+                       coder.data(), decoder.data()};
+  uint64_t offs[12], total = 0;
+  for (int k = 0; k < 12; ++k) {
+    offs[k] = total;
+    total = align_up(total + std::max<uint64_t>(items[k], 8), 256);
+  }
+  DeviceBuf buf;
+  if (buf.ensure(total)) return kNoMemory;
+  uint8_t* b = buf.as<uint8_t>();
+  for (int k = 0; k < 12; ++k)
+    if (items[k]) CU(cudaMemcpy(b + offs[k], src[k], items[k], cudaMemcpyHostToDevice));
+  ImportArgs a;
+  a.n_nodes = N;
+  a.n_edges = E;
+  a.n_seqs = S;
+  a.n_pairs = P;
+  a.n_consensus = C;
+  a.num_codes = num_codes;
+  a.codes = b + offs[0];
+  a.e_tail = reinterpret_cast<const uint32_t*>(b + offs[1]);
+  a.e_head = reinterpret_cast<const uint32_t*>(b + offs[2]);
+  a.e_weight = reinterpret_cast<const int64_t*>(b + offs[3]);
+  a.lab_off = reinterpret_cast<const uint32_t*>(b + offs[4]);
+  a.labels = reinterpret_cast<const uint32_t*>(b + offs[5]);
+  a.seq_begin = reinterpret_cast<const uint32_t*>(b + offs[6]);
+  a.pairs = reinterpret_cast<const uint32_t*>(b + offs[7]);
+  a.rank = reinterpret_cast<const uint32_t*>(b + offs[8]);
+  a.consensus = reinterpret_cast<const uint32_t*>(b + offs[9]);
+  a.coder = reinterpret_cast<const int32_t*>(b + offs[10]);
+  a.decoder = reinterpret_cast<const int32_t*>(b + offs[11]);
+  k_import<<<1, 32>>>(g->v, a, g->stat.as<int32_t>());
+  CU(cudaGetLastError());
+  int32_t dst = kOk;
+  CU(cudaMemcpy(&dst, g->stat.p, sizeof(dst), cudaMemcpyDeviceToHost));
+  if (dst != kOk) {
+    spoa_gb300_graph_clear(g);
+    return dst;
+  }
+  return graph_refresh(g);
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

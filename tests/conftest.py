@@ -55,6 +55,12 @@ def slice_windows():
         return json.load(fh)
 
 
+@pytest.fixture(scope="session")
+def persist_windows():
+    with gzip.open(os.path.join(GOLDEN, "persist_windows.json.gz"), "rt") as fh:
+        return json.load(fh)
+
+
 def check_slices(expect, scores, alignments, subgraphs, consensus, msa):
     """Compare one backbone window run through Subgraph/UpdateAlignment
     against a recorded reference run (subgraphs: driver lines per slice)."""

@@ -128,6 +128,16 @@ void RunSlices(const char* path) {
   const spoa::Graph::Node* first = gr.nodes()[0].get();
   gr.AddAlignment(spoa::Alignment(), "TTTT");
   if (gr.nodes()[0].get() != first || first->id != 0) Fail("node pointer after AddAlignment");
+  // persistence: Serialize / Deserialize round trip (graph.hpp:187-276)
+  const std::string cons = gr.GenerateConsensus();
+  const auto bytes = gr.Serialize();
+  spoa::Graph back{};
+  back.Deserialize(bytes);
+  if (back.nodes().size() != gr.nodes().size() || back.edges().size() != gr.edges().size() ||
+      back.sequences().size() != 2 || back.consensus().size() != cons.size() ||
+      back.Serialize() != bytes || back.GenerateConsensus() != cons)
+    Fail("Serialize / Deserialize round trip");
+  std::cout << "ERR Persist ok\n";
 }
 
 std::string Join(const std::vector<std::uint32_t>& v) {

@@ -28,7 +28,15 @@ It writes
                            cli_inputs.py: exit code, stdout (sha256 and
                            size; verbatim when short), stderr, DOT file
                            (sha256); plus the names of the sample reads.
-With --only slices or --only cli only that file is rewritten.
+  persist_windows.json.gz  windows saved after some reads and loaded again
+                           with the reference's own Graph::save/load (through
+                           the archive stand-ins of oracle/ref_shim/cereal),
+                           then given the remaining reads: the graph as
+                           loaded (driver lines, sha256; verbatim for the
+                           first windows), scores, alignments, consensus, MSA
+                           and GFA after.
+With --only slices, --only cli or --only persist only that file is
+rewritten.
 """
 from __future__ import annotations
 
@@ -168,6 +176,37 @@ def write_slices():
     print(f"wrote {len(recs)} slice windows")
 
 
+def write_persist():
+    """Windows of every type and gap model, with and without qualities,
+    saved after 0, 1, some or all of their reads."""
+    specs = []
+    rng = np.random.default_rng(4242)
+    for k in range(12):
+        w = synth.batch_window(100 + k)
+        reads = w.reads[:12]
+        quals = ([bytes(rng.integers(33, 75, size=len(r)).astype(np.uint8)) for r in reads]
+                 if k % 2 else None)
+        split = [0, 1, 5, len(reads)][k % 4]
+        specs.append((f"persist{k}", k % 3, SLICE_PARAMS[(k // 3) % 3], reads, quals, split))
+    outs = po.parse_reference_output(po.run_reference(po.format_persist(
+        [(t, p, r, q, sp) for _, t, p, r, q, sp in specs])))
+    recs = []
+    for (name, t, p, r, q, sp), o in zip(specs, outs):
+        assert o["error"] is None, (name, o["error"])
+        recs.append({"name": name, "type": t, "params": list(p),
+                     "reads": [x.decode() for x in r],
+                     "quals": [x.decode() for x in q] if q is not None else None, "split": sp,
+                     "expect": {"loaded_sha": {k: sha(v) for k, v in o["loaded"].items()},
+                                "loaded": o["loaded"] if len(recs) < 2 else None,
+                                "scores": o["scores"],
+                                "aln_sha": [sha(canon_alignment(a)) for a in o["alignments"]],
+                                "consensus": o["consensus"], "msa_sha": sha("\n".join(o["msa"])),
+                                "gfa_sha": sha("\n".join(o["gfa"]))}})
+    with gzip.open(os.path.join(HERE, "persist_windows.json.gz"), "wt") as fh:
+        json.dump(recs, fh)
+    print(f"wrote {len(recs)} persisted windows")
+
+
 def write_cli(reference: str):
     """Runs the reference CLI on the inputs of cli_inputs.py."""
     import subprocess
@@ -204,7 +243,7 @@ def write_cli(reference: str):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["slices", "cli"], default=None)
+    ap.add_argument("--only", choices=["slices", "cli", "persist"], default=None)
     args = ap.parse_args()
     os.environ["SPOA_REFERENCE_TREE"] = args.reference
     if po.build_reference() is None:
@@ -214,6 +253,9 @@ def main():
         return
     if args.only == "cli":
         write_cli(args.reference)
+        return
+    if args.only == "persist":
+        write_persist()
         return
 
     reads = parse_fastq_gz(os.path.join(args.reference, "test/data/sample.fastq.gz"))
@@ -260,6 +302,7 @@ def main():
     print(f"wrote {len(cases)} known-answer cases and {len(recs)} reference windows")
     write_slices()
     write_cli(args.reference)
+    write_persist()
 
 
 if __name__ == "__main__":

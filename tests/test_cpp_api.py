@@ -96,6 +96,7 @@ def test_cpp_api_known_answers(tmp_path, sample_reads, spoa_test_cases, spoa_tes
     assert by[("ERR", "LargeInput1")] == ["AlignmentEngine::Prealloc] error: too large sequence!"]
     assert by[("ERR", "LargeInput2")] == ["no-throw"]
     # graph.cpp:518-605 through Graph::Subgraph / UpdateAlignment
+    assert by[("ERR", "Persist")] == ["ok"]
     assert by[("ERR", "SubgraphNullMap")] == [
         "[spoa::Graph::Subgraph] error: invalid ptr to subgraph_to_graph"]
     for w, rec in enumerate(slice_windows):

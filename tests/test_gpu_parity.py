@@ -291,3 +291,61 @@ def test_subgraph_rejects_bad_node_ids():
         assert ex.value.status == 1
     sub, m = graph.subgraph(7, 0)  # inverted range: an empty subgraph
     assert sub.num_nodes == 0 and (m == sg.NO_NODE).all()
+
+
+def _loaded_lines(graph):
+    ex = graph.export()
+    return po.loaded_lines(ex["chars"], ex["rank_to_node"], ex["seq_begin"], ex["consensus"],
+                           ex["edge_tail"], ex["edge_head"], ex["edge_weight"], ex["label_off"],
+                           ex["labels"], ex["aligned_off"], ex["aligned"])
+
+
+def test_save_load_matches_the_reference(persist_windows):
+    """Graph persistence: a window saved after 0, 1, some or all reads and
+    loaded again holds what the reference's own Graph::load rebuilds
+    (nodes, edges with labels and weights, aligned lists in the order load
+    gives them, rank order, sequence starts, consensus), and the remaining
+    reads then give the reference's scores, alignments, consensus, MSA and
+    GFA."""
+    from conftest import canon_alignment, sha
+    for rec in persist_windows:
+        reads = [r.encode() for r in rec["reads"]]
+        quals = [q.encode() for q in rec["quals"]] if rec["quals"] else None
+        engine = sg.AlignmentEngine.create(rec["type"], *rec["params"])
+        first = sg.Graph()
+        for k in range(rec["split"]):
+            aln, _ = engine.align(reads[k], first)
+            first.add_alignment(aln, reads[k], quals[k] if quals else 1)
+        if rec["split"]:
+            first.generate_consensus()
+        blob = first.save()
+        graph = sg.Graph().load(blob)
+        got = _loaded_lines(graph)
+        exp = rec["expect"]
+        if exp["loaded"]:
+            assert got == exp["loaded"], rec["name"]
+        assert {k: sha(v) for k, v in got.items()} == exp["loaded_sha"], rec["name"]
+        assert graph.save() == blob  # a loaded graph saves to the same bytes
+        scores, alns = [], []
+        for k in range(rec["split"], len(reads)):
+            aln, score = engine.align(reads[k], graph)
+            scores.append(0 if score is None else score)
+            alns.append(aln)
+            graph.add_alignment(aln, reads[k], quals[k] if quals else 1)
+        assert scores == exp["scores"], rec["name"]
+        assert [sha(canon_alignment(a)) for a in alns] == exp["aln_sha"], rec["name"]
+        assert graph.generate_consensus() == exp["consensus"], rec["name"]
+        assert sha("\n".join(graph.generate_multiple_sequence_alignment())) == exp["msa_sha"]
+        assert sha("\n".join(graph.gfa())) == exp["gfa_sha"], rec["name"]
+
+
+def test_load_rejects_malformed_bytes():
+    graph = sg.Graph()
+    graph.add_alignment(np.zeros((0, 2), np.int32), b"ACGTACGT")
+    graph.generate_consensus()
+    blob = graph.save()
+    for bad in (b"", b"XXXXXXXX" + blob[8:], blob[:-1], blob + b"\0"):
+        with pytest.raises(sg.SpoaError) as ex:
+            sg.Graph().load(bad)
+        assert ex.value.status == 1
+    assert sg.Graph().load(blob).generate_consensus() == "ACGTACGT"
