@@ -48,6 +48,9 @@ os.environ.setdefault("SPOA_GB300_TILE_CACHE",
                       os.path.join(ROOT, "spoa_gb300", "_build", "tile_cache.txt"))
 
 OPS = {0: (2, 1), 1: (3, 3), 2: (5, 4)}  # per cell: a * preds + b (SW adds 1)
+# score width the kernels compute in (the reference's width rule, per read)
+DTYPES = {"batch_10k": "int16", "single_500": "int16", "long_10k": "int32",
+          "uneven_2k": "int16/int32"}
 TRACEBACK_BYTES_PER_CELL = 0.5          # 4-bit traceback code per DP cell
 
 
@@ -365,7 +368,8 @@ def main():
     line = {
         "metric": "windows/s", "value": value, "unit": "windows/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": DTYPES.get(args.workload, "int16/int32"),
         "data": "synthetic (seeded; see spoa_gb300/synth.py)",
         "config": dict(cfg, parallelism=f"windows sharded over {world} GPU(s), no collective",
                        l2="inputs and per-CTA arenas larger than L2 (129 MB)",

@@ -1357,25 +1357,31 @@ int32_t autotune(spoa_gb300_batch* b, cudaStream_t s) {
       for (size_t k = 0; k < p.windows.size() && sample.size() < n; k += step)
         sample.push_back(p.windows[k]);
       q.windows = sample;
-      float best_ms = 0;
-      for (const auto& c : cands) {
-        q.tuned_cpt = c.first;
-        q.tuned_nt = c.second;
-        int32_t st = plan_pass(b, &q, b->plan0);
-        if (st) return st;
-        if (b->arena.ensure(q.stride * (uint64_t)q.ctas)) return kNoMemory;
-        CU(cudaEventRecord(e0, s));
-        st = run_pass(b, q, s, false, b->d_cons.as<uint8_t>(), b->d_cons_off.as<uint64_t>());
-        if (st) return st;
-        CU(cudaEventRecord(e1, s));
-        CU(cudaEventSynchronize(e1));
-        float ms = 0;
-        CU(cudaEventElapsedTime(&ms, e0, e1));
-        if (best_ms == 0 || ms < best_ms) {
-          best_ms = ms;
-          best = c;
+      // two rounds over the candidates, each keeping its faster time: the
+      // first launch of a kernel (module loading) and a GPU still raising
+      // its clocks must not count against whichever candidate runs first
+      std::vector<float> ms_of(cands.size(), 0.f);
+      for (int round = 0; round < 2; ++round) {
+        for (size_t k = 0; k < cands.size(); ++k) {
+          q.tuned_cpt = cands[k].first;
+          q.tuned_nt = cands[k].second;
+          int32_t st = plan_pass(b, &q, b->plan0);
+          if (st) return st;
+          if (b->arena.ensure(q.stride * (uint64_t)q.ctas)) return kNoMemory;
+          CU(cudaEventRecord(e0, s));
+          st = run_pass(b, q, s, false, b->d_cons.as<uint8_t>(), b->d_cons_off.as<uint64_t>());
+          if (st) return st;
+          CU(cudaEventRecord(e1, s));
+          CU(cudaEventSynchronize(e1));
+          float ms = 0;
+          CU(cudaEventElapsedTime(&ms, e0, e1));
+          if (round == 0 || ms < ms_of[k]) ms_of[k] = ms;
         }
       }
+      size_t bi = 0;
+      for (size_t k = 1; k < cands.size(); ++k)
+        if (ms_of[k] < ms_of[bi]) bi = k;
+      best = cands[bi];
     }
     std::lock_guard<std::mutex> lk(g_tune_mu);
     save_tile((int)b->base.sub, p.wide, p.cls, best.first, best.second);
