@@ -78,6 +78,9 @@ def lib():
         L.oracle_graph_export_ids.argtypes = [P] * 6
         L.oracle_graph_export_ids.restype = C.c_uint32
         L.oracle_subgraph.argtypes = [P, C.c_uint32, C.c_uint32, P, P]
+        L.oracle_graph_edge_labels.argtypes = [P, P, P]
+        L.oracle_graph_edge_labels.restype = C.c_uint32
+        L.oracle_graph_reload.argtypes = [P, P]
         L.oracle_graph_path.argtypes = [P, C.c_uint32, P, C.c_uint32]
         L.oracle_graph_path.restype = C.c_uint32
         L.oracle_window_run.argtypes = [C.POINTER(WindowParams), P, C.c_uint32, C.c_char_p,
@@ -424,3 +427,77 @@ def loaded_lines(chars, rank, seq_begin, consensus, edge_tail, edge_head, edge_w
             "S": " ".join(str(int(x)) for x in seq_begin),
             "Q": " ".join(str(int(x)) for x in consensus),
             "L": " ".join(edges), "A": " ".join(al)}
+
+
+def run_persist(type_: int, params, reads: list[bytes], quals, split: int) -> dict:
+    """The persisted-window protocol of ref_driver.cpp on the C oracle:
+    reads before `split` added (then GenerateConsensus), the graph saved and
+    loaded (oracle_graph_reload), the rest added to the loaded graph."""
+    from spoa_gb300.gfa import gfa_lines
+    L = lib()
+    st = C.c_int32()
+    en = L.oracle_engine_create(type_, *params, C.byref(st))
+    if not en:
+        raise RuntimeError(f"oracle engine: status {st.value}")
+    first, g = L.oracle_graph_create(), L.oracle_graph_create()
+    res = {"scores": [], "alignments": []}
+
+    def add(graph, k):
+        seq = reads[k]
+        pairs = np.zeros(2 * (L.oracle_graph_num_nodes(graph) + len(seq) + 16), np.int32)
+        n, score = C.c_uint32(0), C.c_int32(0)
+        assert L.oracle_align(en, seq, len(seq), graph, C.byref(score), _ptr(pairs),
+                              pairs.size // 2, C.byref(n)) == 0
+        w = (np.frombuffer(quals[k], np.uint8).astype(np.uint32) - 33 if quals is not None
+             else np.ones(len(seq), np.uint32))
+        w = np.ascontiguousarray(w, np.uint32)
+        aln = pairs[:2 * n.value].reshape(-1, 2).copy()
+        assert L.oracle_add_alignment(graph, _ptr(np.ascontiguousarray(aln)), aln.shape[0], seq,
+                                      len(seq), _ptr(w), len(seq)) == 0
+        return score.value, aln
+
+    try:
+        for k in range(split):
+            add(first, k)
+        if split:
+            nn = L.oracle_graph_num_nodes(first)
+            L.oracle_consensus(first, C.create_string_buffer(nn + 1), nn + 1)
+        assert L.oracle_graph_reload(first, g) == 0
+        ex = export_graph(g)
+        ne = L.oracle_graph_num_edges(g)
+        nn = L.oracle_graph_num_nodes(g)
+        et, eh = np.zeros(max(ne, 1), np.uint32), np.zeros(max(ne, 1), np.uint32)
+        ew = np.zeros(max(ne, 1), np.int64)
+        aoff = np.zeros(nn + 1, np.uint32)
+        na = L.oracle_graph_export_ids(g, None, None, None, _ptr(aoff), None)
+        al = np.zeros(max(na, 1), np.uint32)
+        L.oracle_graph_export_ids(g, _ptr(et), _ptr(eh), _ptr(ew), _ptr(aoff), _ptr(al))
+        loff = np.zeros(ne + 1, np.uint32)
+        nl = L.oracle_graph_edge_labels(g, _ptr(loff), None)
+        labs = np.zeros(max(nl, 1), np.uint32)
+        L.oracle_graph_edge_labels(g, _ptr(loff), _ptr(labs))
+        res["loaded"] = loaded_lines(ex["chars"], ex["rank_to_node"], ex["seq_begin"],
+                                     ex["consensus"], et[:ne], eh[:ne], ew[:ne], loff, labs,
+                                     aoff, al)
+        for k in range(split, len(reads)):
+            score, aln = add(g, k)
+            res["scores"].append(score)
+            res["alignments"].append(aln)
+        nn = L.oracle_graph_num_nodes(g)
+        cb = C.create_string_buffer(nn + 1)
+        k = L.oracle_consensus(g, cb, nn + 1)
+        res["consensus"] = cb.raw[:k].decode()
+        rows, rl = C.c_uint32(), C.c_uint32()
+        mcap = (len(reads) + 1) * (nn + 1)
+        mb = C.create_string_buffer(mcap)
+        assert L.oracle_msa(g, 0, mb, mcap, C.byref(rows), C.byref(rl)) == 0
+        res["msa"] = [mb.raw[i * rl.value:(i + 1) * rl.value].decode()
+                      for i in range(rows.value)]
+        ex = export_graph(g)
+        res["gfa"] = gfa_lines(ex["chars"], ex["edge_tail"], ex["edge_head"], ex["edge_weight"],
+                               ex["paths"], ex["consensus"], None)
+        return res
+    finally:
+        L.oracle_graph_destroy(first)
+        L.oracle_graph_destroy(g)
+        L.oracle_engine_destroy(en)

@@ -560,6 +560,71 @@ uint32_t oracle_graph_export_ids(const oracle_graph* g, uint32_t* edge_tail,
   return n;
 }
 
+/* Labels of every edge in id order as CSR (label_off: n_edges + 1
+ * entries); NULL skips an array.  Returns the total number of labels. */
+uint32_t oracle_graph_edge_labels(const oracle_graph* g, uint32_t* label_off,
+                                  uint32_t* labels) {
+  uint32_t n = 0;
+  for (uint32_t e = 0; e < g->n_edges; ++e) {
+    if (label_off) label_off[e] = n;
+    for (uint32_t k = 0; k < g->edges[e].labels.n; ++k, ++n)
+      if (labels) labels[n] = g->edges[e].labels.a[k];
+  }
+  if (label_off) label_off[g->n_edges] = n;
+  return n;
+}
+
+/* Graph::save followed by Graph::load (include/spoa/graph.hpp:187-276):
+ * `out` becomes what the reference's load rebuilds from what its save
+ * archives of g.  Nodes (id, code), edges (labels, weight) and the coder
+ * tables are copied; each edge, in id order, is appended to its tail's
+ * out-edges and its head's in-edges; the aligned pairs (a, b), a < b, taken
+ * in node order and then list order, are appended to both lists in that
+ * order; sequence starts, rank order and consensus are copied. */
+int32_t oracle_graph_reload(const oracle_graph* g, oracle_graph* out) {
+  if (out == g) return ORACLE_ERR_INVALID_ARGUMENT;
+  oracle_graph_clear(out);
+  out->num_codes = g->num_codes;
+  memcpy(out->coder, g->coder, sizeof(g->coder));
+  memcpy(out->decoder, g->decoder, sizeof(g->decoder));
+  for (uint32_t v = 0; v < g->n_nodes; ++v)
+    if (add_node(out, g->nodes[v].code) < 0) return ORACLE_ERR_NO_MEMORY;
+  for (uint32_t e = 0; e < g->n_edges; ++e) {
+    if (out->n_edges == out->cap_edges) {
+      uint32_t nc = out->cap_edges ? out->cap_edges * 2 : 64;
+      oedge* ne = (oedge*)realloc(out->edges, (size_t)nc * sizeof(oedge));
+      if (!ne) return ORACLE_ERR_NO_MEMORY;
+      out->edges = ne;
+      out->cap_edges = nc;
+    }
+    const oedge* src = &g->edges[e];
+    oedge* ed = &out->edges[out->n_edges++];
+    memset(ed, 0, sizeof(*ed));
+    ed->tail = src->tail;
+    ed->head = src->head;
+    ed->weight = src->weight;
+    for (uint32_t k = 0; k < src->labels.n; ++k)
+      if (vu_push(&ed->labels, src->labels.a[k])) return ORACLE_ERR_NO_MEMORY;
+    if (vu_push(&out->nodes[src->tail].out, e) || vu_push(&out->nodes[src->head].in, e))
+      return ORACLE_ERR_NO_MEMORY;
+  }
+  for (uint32_t v = 0; v < g->n_nodes; ++v) {
+    const onode* nd = &g->nodes[v];
+    for (uint32_t k = 0; k < nd->aligned.n; ++k) {
+      const uint32_t b = nd->aligned.a[k];
+      if (v < b && (vu_push(&out->nodes[v].aligned, b) || vu_push(&out->nodes[b].aligned, v)))
+        return ORACLE_ERR_NO_MEMORY;
+    }
+  }
+  for (uint32_t k = 0; k < g->sequences.n; ++k)
+    if (vu_push(&out->sequences, g->sequences.a[k])) return ORACLE_ERR_NO_MEMORY;
+  for (uint32_t k = 0; k < g->rank_to_node.n; ++k)
+    if (vu_push(&out->rank_to_node, g->rank_to_node.a[k])) return ORACLE_ERR_NO_MEMORY;
+  for (uint32_t k = 0; k < g->consensus.n; ++k)
+    if (vu_push(&out->consensus, g->consensus.a[k])) return ORACLE_ERR_NO_MEMORY;
+  return ORACLE_OK;
+}
+
 /* Graph::Subgraph (graph.cpp:518-595).  ExtractSubgraph's depth-first
  * walk from `end` over in-edge tails and aligned nodes, a node entering the
  * set when its id is at least `begin`; the set's nodes are added to `out`

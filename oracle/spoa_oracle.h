@@ -91,6 +91,16 @@ uint32_t oracle_graph_export_ids(const oracle_graph* g, uint32_t* edge_tail,
                                  uint32_t* edge_head, int64_t* edge_weight,
                                  uint32_t* aligned_off, uint32_t* aligned);
 
+/* Labels of every edge in id order as CSR (label_off: n_edges + 1
+ * entries); NULL skips an array.  Returns the total number of labels. */
+uint32_t oracle_graph_edge_labels(const oracle_graph* g, uint32_t* label_off,
+                                  uint32_t* labels);
+
+/* Graph::save then Graph::load (include/spoa/graph.hpp:187-276) of g into
+ * `out` (cleared first), with the reference's load order of edge and
+ * aligned lists. */
+int32_t oracle_graph_reload(const oracle_graph* g, oracle_graph* out);
+
 /* Graph::Subgraph (graph.cpp:518-595) into `out` (cleared first);
  * sub_to_graph receives n_nodes(g) entries: the id in g of every node of
  * out, then UINT32_MAX.  Graph::UpdateAlignment (graph.cpp:597-605) is the

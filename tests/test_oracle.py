@@ -75,6 +75,26 @@ def test_slice_windows(slice_windows):
                      res["consensus"], res["msa"])
 
 
+def test_persist_windows(persist_windows):
+    """Graph::save then Graph::load (graph.hpp:187-276): the graph as the
+    reference's load rebuilds it, then the remaining reads, against the
+    reference's own save/load."""
+    from conftest import canon_alignment, sha
+    for rec in persist_windows:
+        quals = [q.encode() for q in rec["quals"]] if rec["quals"] else None
+        res = po.run_persist(rec["type"], tuple(rec["params"]), [r.encode() for r in rec["reads"]],
+                             quals, rec["split"])
+        exp = rec["expect"]
+        if exp["loaded"]:
+            assert res["loaded"] == exp["loaded"], rec["name"]
+        assert {k: sha(v) for k, v in res["loaded"].items()} == exp["loaded_sha"], rec["name"]
+        assert res["scores"] == exp["scores"], rec["name"]
+        assert [sha(canon_alignment(a)) for a in res["alignments"]] == exp["aln_sha"]
+        assert res["consensus"] == exp["consensus"], rec["name"]
+        assert sha("\n".join(res["msa"])) == exp["msa_sha"], rec["name"]
+        assert sha("\n".join(res["gfa"])) == exp["gfa_sha"], rec["name"]
+
+
 def test_engine_errors():
     L = po.lib()
     import ctypes as C
