@@ -1,8 +1,9 @@
 // spoa/graph.hpp - spoa's partial-order graph, resident on the GPU.
 //
-// Source-compatible with spoa v4's include/spoa/graph.hpp (without the
-// cereal serialisation): the same Node / Edge types, accessors,
-// AddAlignment overloads and consensus / MSA calls.  The graph lives in
+// Source-compatible with spoa v4's include/spoa/graph.hpp: the same Node /
+// Edge types, accessors, AddAlignment overloads, consensus / MSA calls,
+// Subgraph / UpdateAlignment and (under SPOA_USE_CEREAL) cereal save / load
+// hooks, whose bytes are this library's own layout.  The graph lives in
 // device memory (libspoa_gb300.so); AddAlignment, GenerateConsensus and
 // GenerateMultipleSequenceAlignment run there.  The host views returned by
 // nodes(), edges(), rank_to_node(), sequences() and consensus() are brought
