@@ -2051,8 +2051,13 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
       R += w.off.size() - 1;
       S += w.sumlen;
     }
-    int cpt = 0, nt = 0;
-    if (!throughput_tile(lmax, wide, &cpt, &nt)) {
+    // the batched kernel's tiles: 32-bit rows past 12 x 512 columns go to
+    // the segmented forward
+    int cpt = 0, nt = 0, segs = 1;
+    const bool tiled = wide && lmax > (uint32_t)kSegCpt * 512
+                           ? seg_tile(lmax, &cpt, &nt, &segs)
+                           : throughput_tile(lmax, wide, &cpt, &nt);
+    if (!tiled) {
       // a read longer than any tile: the window fails alone
       auto w = take.front();
       {
@@ -2065,7 +2070,7 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
     GraphCaps gc;
     DpCaps dc;
     const uint64_t stride =
-        arena_caps(sv->base.sub, wide, cpt, nt, nodes, maxsum, maxreads, many, &gc, &dc);
+        arena_caps(sv->base.sub, wide, cpt * segs, nt, nodes, maxsum, maxreads, many, &gc, &dc);
     // inputs: work, queue, window read offsets, read offsets, types, strands,
     // consensus offsets, reads; outputs: scores, strands, lengths, status,
     // cell counters, consensus; then the arenas
@@ -2172,7 +2177,9 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
     bool ok = cudaMemcpyAsync(d, h, in_bytes, cudaMemcpyHostToDevice, L.stream) == cudaSuccess &&
               cudaMemsetAsync(d + o_cells, 0, 16, L.stream) == cudaSuccess;
     if (ok)
-      ok = SPOA_BY_SUB(sv->base.sub, wide, launch_batch, cpt, nt, (int)n, a, L.stream) == kOk;
+      ok = (segs > 1 ? SPOA_BY_SUB32(sv->base.sub, launch_batch_seg, segs, nt, (int)n, a, L.stream)
+                     : SPOA_BY_SUB(sv->base.sub, wide, launch_batch, cpt, nt, (int)n, a, L.stream))
+           == kOk;
     if (ok)
       ok = cudaMemcpyAsync(h + o_scores, d + o_scores, arena_off - o_scores, cudaMemcpyDeviceToHost,
                            L.stream) == cudaSuccess &&

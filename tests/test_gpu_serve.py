@@ -79,3 +79,15 @@ def test_wait_timeout_and_unknown_ticket():
             sv.wait(t + 1000)
         st, cons, lat = sv.wait(t, timeout=120)
         assert st == 0 and cons
+
+
+@pytest.mark.gpu
+def test_long_window_served():
+    """A window of 6.5-7k-column int32 rows through the server (the
+    segmented kernel), against the oracle."""
+    w = synth.long_10k(11, n_reads=3, tpl_len=7200, min_len=6500)
+    with sg.Server(2, *PARAMS) as sv:
+        t = sv.submit(w.reads, 2, False)
+        st, cons, lat = sv.wait(t, timeout=600)
+    assert st == 0
+    assert cons == po.run_window(2, *PARAMS, w.reads, with_msa=False).consensus
