@@ -47,3 +47,16 @@ def test_no_gpu_fails_loudly():
     assert ei.value.status == 10
     with pytest.raises(sg.SpoaError):
         sg.Graph()
+
+
+def test_graph_entry_points_reject_null_handles():
+    """Argument checks of the graph entry points that need no device: null
+    handles and missing outputs are refused before any CUDA call."""
+    import ctypes as C
+    L = sg.lib()
+    n = C.c_uint64()
+    assert L.spoa_gb300_graph_save(None, None, 0, C.byref(n)) == 1
+    assert L.spoa_gb300_graph_load(None, None, 0) == 1
+    m = (C.c_uint32 * 4)()
+    assert L.spoa_gb300_graph_subgraph(None, 0, 0, None, m, 4) == 1
+    assert L.spoa_gb300_graph_export(None, *([None] * 18)) == 1
