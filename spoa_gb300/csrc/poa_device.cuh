@@ -381,7 +381,9 @@ static __device__ __noinline__ int g_topo_sort_cta(GraphView& G, int* s_ret) {
   const uint32_t words = 3 * ((nn + 31) / 32);
   for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) bits[w] = 0;
   for (uint32_t v = threadIdx.x * 8; v < nn; v += blockDim.x * 8)
+#ifdef __CUDA_ARCH__
     asm volatile("prefetch.global.L1 [%0];" ::"l"(G.nrec + v));
+#endif
   __syncthreads();
   if (threadIdx.x == 0) {
     auto bit = [&](uint32_t v, uint32_t kind) { return (bits[3 * (v >> 5) + kind] >> (v & 31)) & 1u; };
@@ -661,6 +663,137 @@ __device__ inline uint32_t g_msa_columns(GraphView& G) {
     }
   }
   return j;
+}
+
+
+// ---------------------------------------------------------------------------
+// Graph::Subgraph and graph loading (thread 0)
+// ---------------------------------------------------------------------------
+// Graph::Subgraph (graph.cpp:541-595) of S into the empty graph D, without
+// the final sort.  The node set is ExtractSubgraph's (graph.cpp:518-539):
+// every node reachable from `end` over in-edges and aligned nodes, not
+// expanded below id `begin`; it is a set, so the stack may visit it in any
+// order.  Its nodes are added in id order (map[k] = id in S of node k of
+// D), then, node by node, each in-edge whose tail is in the set with the
+// edge's weight (one label, sequence 0, as AddEdge gives it on a graph
+// without sequences) and the aligned nodes in the set, in list order.
+// gid (one word per node of S) must hold kNone on entry; stack is scratch.
+// Returns kOk, or kCapacity when D or the stack is too small.
+__device__ inline int32_t g_subgraph_build(const GraphView& S, GraphView& D, uint32_t begin,
+                                           uint32_t end, uint32_t* gid, uint32_t* stack,
+                                           uint64_t stack_cap, uint32_t* map) {
+  const uint32_t nn = S.hdr->n_nodes;
+  constexpr uint32_t kIn = 0xFFFFFFFEu;  // in the set, not numbered yet
+  int32_t st = kOk;
+  g_reset(D);
+  D.hdr->num_codes = S.hdr->num_codes;
+  for (int k = 0; k < 256; ++k) {
+    D.hdr->coder[k] = S.hdr->coder[k];
+    D.hdr->decoder[k] = S.hdr->decoder[k];
+  }
+  const uint32_t KS = S.caps.aligned;
+  uint64_t sp = 0;
+  if (end < nn) stack[sp++] = end;
+  while (sp && st == kOk) {
+    const uint32_t v = stack[--sp];
+    if (gid[v] != kNone || v < begin) continue;
+    gid[v] = kIn;
+    for (uint32_t e = S.nlink[v].x; e != kNone; e = S.erec[e].z) {
+      if (sp >= stack_cap) { st = kCapacity; break; }
+      stack[sp++] = S.erec[e].x;
+    }
+    for (uint32_t k = 0; k < S.n_aligned[v] && st == kOk; ++k) {
+      if (sp >= stack_cap) { st = kCapacity; break; }
+      stack[sp++] = S.aligned[(uint64_t)v * KS + k];
+    }
+  }
+  for (uint32_t v = 0; v < nn && st == kOk; ++v) {
+    if (gid[v] != kIn) continue;
+    const int64_t id = g_add_node(D, S.code[v]);
+    if (id < 0) { st = kCapacity; break; }
+    gid[v] = (uint32_t)id;
+    map[id] = v;
+  }
+  for (uint32_t v = 0; v < nn && st == kOk; ++v) {
+    const uint32_t h = gid[v];
+    if (h == kNone) continue;
+    for (uint32_t e = S.nlink[v].x; e != kNone; e = S.erec[e].z) {
+      const uint32_t t = gid[S.erec[e].x];
+      // AddEdge takes a 32-bit weight (graph.cpp:81)
+      if (t != kNone && g_add_edge(D, t, h, (uint32_t)S.e_weight[e])) { st = kCapacity; break; }
+    }
+    for (uint32_t k = 0; k < S.n_aligned[v] && st == kOk; ++k) {
+      const uint32_t a = gid[S.aligned[(uint64_t)v * KS + k]];
+      if (a != kNone && g_link_aligned(D, h, a)) st = kCapacity;
+    }
+  }
+  return st;
+}
+
+// A saved graph (arrays checked by the caller: every id in range, one rank
+// per node, at most caps.aligned aligned nodes per node).
+struct ImportArgs {
+  uint32_t n_nodes, n_edges, n_seqs, n_pairs, n_consensus, num_codes;
+  const uint8_t* codes;
+  const uint32_t *e_tail, *e_head;
+  const int64_t* e_weight;
+  const uint32_t *lab_off, *labels;  // labels of edge e: lab_off[e] .. lab_off[e + 1]
+  const uint32_t *seq_begin, *pairs, *rank, *consensus;
+  const int32_t *coder, *decoder;
+};
+
+// Rebuilds a saved graph in the empty graph G the way the reference's
+// Graph::load (include/spoa/graph.hpp:236-275) rebuilds it: nodes in id
+// order; edges in id order, each appended to its tail's out-edge list and
+// its head's in-edge list, with its labels and weight; for every aligned
+// pair (a, b) in order, b appended to a's list and a to b's (which can
+// reorder a node's aligned list against the saved graph, as the
+// reference's load does); rank order, sequence starts and the last
+// consensus as saved.  Returns kOk or kCapacity.
+__device__ inline int32_t g_import(GraphView& G, const ImportArgs& a) {
+  int32_t st = kOk;
+  GraphHeader* h = G.hdr;
+  g_reset(G);
+  h->num_codes = a.num_codes;
+  for (int k = 0; k < 256; ++k) {
+    h->coder[k] = a.coder[k];
+    h->decoder[k] = a.decoder[k];
+  }
+  for (uint32_t v = 0; v < a.n_nodes && st == kOk; ++v)
+    if (g_add_node(G, a.codes[v]) < 0) st = kCapacity;
+  for (uint32_t e = 0; e < a.n_edges && st == kOk; ++e) {
+    const int64_t id = g_new_edge(G, a.e_tail[e], a.e_head[e], a.e_weight[e]);
+    if (id < 0) {
+      st = kCapacity;
+      break;
+    }
+    for (uint32_t k = a.lab_off[e]; k < a.lab_off[e + 1]; ++k) {
+      if (h->n_labels >= G.caps.labels) {
+        st = kCapacity;
+        break;
+      }
+      const uint32_t l = h->n_labels++;
+      G.lab_seq[l] = a.labels[k];
+      G.lab_next[l] = kNone;
+      if (G.e_lab_last[id] != kNone) G.lab_next[G.e_lab_last[id]] = l; else G.e_lab_first[id] = l;
+      G.e_lab_last[id] = l;
+    }
+  }
+  for (uint32_t k = 0; k < a.n_pairs && st == kOk; ++k) {
+    const uint32_t x = a.pairs[2 * k], y = a.pairs[2 * k + 1];
+    if (g_link_aligned(G, x, y) || g_link_aligned(G, y, x)) st = kCapacity;
+  }
+  if (st == kOk) {
+    for (uint32_t r = 0; r < a.n_nodes; ++r) {
+      G.rank_to_node[r] = a.rank[r];
+      G.node_to_rank[a.rank[r]] = r;
+    }
+    for (uint32_t s = 0; s < a.n_seqs; ++s) G.seq_begin[s] = a.seq_begin[s];
+    h->n_seqs = a.n_seqs;
+    for (uint32_t k = 0; k < a.n_consensus; ++k) G.consensus[k] = a.consensus[k];
+    h->n_consensus = a.n_consensus;
+  }
+  return st;
 }
 
 }  // namespace spoa_gb300

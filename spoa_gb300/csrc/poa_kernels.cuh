@@ -344,69 +344,17 @@ __global__ void k_export(GraphView G, ExportPtrs x) {
   }
 }
 
-// Graph::Subgraph (graph.cpp:541-595) of S into the empty graph D.  The
-// node set is ExtractSubgraph's (graph.cpp:518-539): every node reachable
-// from `end` over in-edges and aligned nodes, not expanded below id
-// `begin`; it is a set, so thread 0 walks it with any order of the stack.
-// Its nodes are added in id order (map[k] = id in S of node k of D), then,
-// node by node, each in-edge whose tail is in the set with the edge's
-// weight (one label, sequence 0, as AddEdge gives it on a graph without
-// sequences) and the aligned nodes in the set, in list order; the whole CTA
-// then sorts D.  gid (one word per node of S) and stack are scratch.
-// *status: kOk, or kCapacity when D or the stack is too small.
+// Graph::Subgraph (graph.cpp:541-595) of S into the empty graph D
+// (g_subgraph_build), then the CTA sorts D.  gid (one word per node of S)
+// and stack are scratch.  *status: kOk, or kCapacity when D or the stack is
+// too small.
 __global__ void k_subgraph(GraphView S, GraphView D, uint32_t begin, uint32_t end, uint32_t* gid,
                            uint32_t* stack, uint64_t stack_cap, uint32_t* map, int32_t* status) {
   __shared__ int s_st;
   const uint32_t nn = S.hdr->n_nodes;
-  constexpr uint32_t kIn = 0xFFFFFFFEu;  // in the set, not numbered yet
   for (uint32_t v = threadIdx.x; v < nn; v += blockDim.x) gid[v] = kNone;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int st = kOk;
-    g_reset(D);
-    D.hdr->num_codes = S.hdr->num_codes;
-    for (int k = 0; k < 256; ++k) {
-      D.hdr->coder[k] = S.hdr->coder[k];
-      D.hdr->decoder[k] = S.hdr->decoder[k];
-    }
-    const uint32_t KS = S.caps.aligned;
-    uint64_t sp = 0;
-    if (end < nn) stack[sp++] = end;
-    while (sp && st == kOk) {
-      const uint32_t v = stack[--sp];
-      if (gid[v] != kNone || v < begin) continue;
-      gid[v] = kIn;
-      for (uint32_t e = S.nlink[v].x; e != kNone; e = S.erec[e].z) {
-        if (sp >= stack_cap) { st = kCapacity; break; }
-        stack[sp++] = S.erec[e].x;
-      }
-      for (uint32_t k = 0; k < S.n_aligned[v] && st == kOk; ++k) {
-        if (sp >= stack_cap) { st = kCapacity; break; }
-        stack[sp++] = S.aligned[(uint64_t)v * KS + k];
-      }
-    }
-    for (uint32_t v = 0; v < nn && st == kOk; ++v) {
-      if (gid[v] != kIn) continue;
-      const int64_t id = g_add_node(D, S.code[v]);
-      if (id < 0) { st = kCapacity; break; }
-      gid[v] = (uint32_t)id;
-      map[id] = v;
-    }
-    for (uint32_t v = 0; v < nn && st == kOk; ++v) {
-      const uint32_t h = gid[v];
-      if (h == kNone) continue;
-      for (uint32_t e = S.nlink[v].x; e != kNone; e = S.erec[e].z) {
-        const uint32_t t = gid[S.erec[e].x];
-        // AddEdge takes a 32-bit weight (graph.cpp:81)
-        if (t != kNone && g_add_edge(D, t, h, (uint32_t)S.e_weight[e])) { st = kCapacity; break; }
-      }
-      for (uint32_t k = 0; k < S.n_aligned[v] && st == kOk; ++k) {
-        const uint32_t a = gid[S.aligned[(uint64_t)v * KS + k]];
-        if (a != kNone && g_link_aligned(D, h, a)) st = kCapacity;
-      }
-    }
-    s_st = st;
-  }
+  if (threadIdx.x == 0) s_st = g_subgraph_build(S, D, begin, end, gid, stack, stack_cap, map);
   __syncthreads();
   if (s_st == kOk && g_topo_sort_cta(D, &s_st) != 0) {
     if (threadIdx.x == 0) s_st = kCapacity;
@@ -415,71 +363,10 @@ __global__ void k_subgraph(GraphView S, GraphView D, uint32_t begin, uint32_t en
   if (threadIdx.x == 0) *status = s_st;
 }
 
-// A saved graph (arrays checked by the host: every id in range, one rank
-// per node, at most caps.aligned aligned nodes per node).
-struct ImportArgs {
-  uint32_t n_nodes, n_edges, n_seqs, n_pairs, n_consensus, num_codes;
-  const uint8_t* codes;
-  const uint32_t *e_tail, *e_head;
-  const int64_t* e_weight;
-  const uint32_t *lab_off, *labels;  // labels of edge e: lab_off[e] .. lab_off[e + 1]
-  const uint32_t *seq_begin, *pairs, *rank, *consensus;
-  const int32_t *coder, *decoder;
-};
-
-// Rebuilds a saved graph in the empty graph G the way the reference's
-// Graph::load (include/spoa/graph.hpp:236-275) rebuilds it: nodes in id
-// order; edges in id order, each appended to its tail's out-edge list and
-// its head's in-edge list, with its labels and weight; for every aligned
-// pair (a, b) in order, b appended to a's list and a to b's (which can
-// reorder a node's aligned list against the saved graph, as the
-// reference's load does); rank order, sequence starts and the last
-// consensus as saved.  Thread 0; *status kOk or kCapacity.
+// A saved graph rebuilt in G (g_import), thread 0; *status kOk or kCapacity.
 __global__ void k_import(GraphView G, ImportArgs a, int32_t* status) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int32_t st = kOk;
-  GraphHeader* h = G.hdr;
-  g_reset(G);
-  h->num_codes = a.num_codes;
-  for (int k = 0; k < 256; ++k) {
-    h->coder[k] = a.coder[k];
-    h->decoder[k] = a.decoder[k];
-  }
-  for (uint32_t v = 0; v < a.n_nodes && st == kOk; ++v)
-    if (g_add_node(G, a.codes[v]) < 0) st = kCapacity;
-  for (uint32_t e = 0; e < a.n_edges && st == kOk; ++e) {
-    const int64_t id = g_new_edge(G, a.e_tail[e], a.e_head[e], a.e_weight[e]);
-    if (id < 0) {
-      st = kCapacity;
-      break;
-    }
-    for (uint32_t k = a.lab_off[e]; k < a.lab_off[e + 1]; ++k) {
-      if (h->n_labels >= G.caps.labels) {
-        st = kCapacity;
-        break;
-      }
-      const uint32_t l = h->n_labels++;
-      G.lab_seq[l] = a.labels[k];
-      G.lab_next[l] = kNone;
-      if (G.e_lab_last[id] != kNone) G.lab_next[G.e_lab_last[id]] = l; else G.e_lab_first[id] = l;
-      G.e_lab_last[id] = l;
-    }
-  }
-  for (uint32_t k = 0; k < a.n_pairs && st == kOk; ++k) {
-    const uint32_t x = a.pairs[2 * k], y = a.pairs[2 * k + 1];
-    if (g_link_aligned(G, x, y) || g_link_aligned(G, y, x)) st = kCapacity;
-  }
-  if (st == kOk) {
-    for (uint32_t r = 0; r < a.n_nodes; ++r) {
-      G.rank_to_node[r] = a.rank[r];
-      G.node_to_rank[a.rank[r]] = r;
-    }
-    for (uint32_t s = 0; s < a.n_seqs; ++s) G.seq_begin[s] = a.seq_begin[s];
-    h->n_seqs = a.n_seqs;
-    for (uint32_t k = 0; k < a.n_consensus; ++k) G.consensus[k] = a.consensus[k];
-    h->n_consensus = a.n_consensus;
-  }
-  *status = st;
+  *status = g_import(G, a);
 }
 #endif
 
