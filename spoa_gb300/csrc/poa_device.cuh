@@ -470,11 +470,74 @@ __device__ inline int g_link_aligned(GraphView& G, uint32_t a, uint32_t b) {
   return 0;
 }
 
+// Read-only part of Graph::AddAlignment, run by every thread of the CTA
+// before thread 0 adds (g_add_alignment with `pre`): for each aligned pair
+// k (position not -1), pre[2k] = the existing node the reference reuses
+// (the pair's node if its code matches, else an aligned node with the code)
+// or kNone for a new node, and pre[2k+1] = the existing edge from the
+// previous aligned pair's node to it, or kNone.  Exact because the read's
+// path holds each node, and so each tail's out-edge list, at most once, and
+// never two nodes of one aligned group: nothing the add changes is read
+// here.  Characters new to the graph have no code yet (coder -1) and match
+// no node.  Every thread must call it; ends with __syncthreads.
+static __device__ __noinline__ void g_add_prepass(const GraphView& G, const int32_t* pairs,
+                                                  uint32_t n_pairs, const uint8_t* seq,
+                                                  uint32_t len, uint32_t* pre) {
+  const GraphHeader* h = G.hdr;
+  const uint32_t K = G.caps.aligned;
+  for (uint32_t k = threadIdx.x; k < n_pairs; k += blockDim.x) {
+    const int32_t nid = pairs[2 * k], pos = pairs[2 * k + 1];
+    uint32_t node = kNone;
+    if (pos >= 0 && (uint32_t)pos < len && nid >= 0 && (uint32_t)nid < h->n_nodes) {
+      const uint32_t code = (uint32_t)h->coder[seq[pos]];
+      if (G.code[nid] == code) {
+        node = (uint32_t)nid;
+      } else {
+        const uint32_t na = G.n_aligned[nid];
+        const uint32_t* al = G.aligned + (uint64_t)nid * K;
+        for (uint32_t a = 0; a < na; ++a) {
+          if (G.code[al[a]] == code) {
+            node = al[a];
+            break;
+          }
+        }
+      }
+    }
+    pre[2 * k] = node;
+  }
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < n_pairs; k += blockDim.x) {
+    uint32_t edge = kNone;
+    const uint32_t head = pre[2 * k];
+    if (pairs[2 * k + 1] != -1 && head != kNone) {
+      // the previous aligned pair's node
+      uint32_t tail = kNone;
+      for (uint32_t b = k; b-- > 0;) {
+        if (pairs[2 * b + 1] != -1) {
+          tail = pre[2 * b];
+          break;
+        }
+      }
+      if (tail != kNone) {
+        for (uint32_t e = G.nlink[tail].z; e != kNone; e = G.erec[e].w) {
+          if (G.erec[e].y == head) {
+            edge = e;
+            break;
+          }
+        }
+      }
+    }
+    pre[2 * k + 1] = edge;
+  }
+  __syncthreads();
+}
+
 // Graph::AddAlignment (graph.cpp:155-247) without its final
 // TopologicalSort, which the caller runs with the whole CTA
 // (g_topo_sort_cta).  pairs: n (node id | -1, position | -1).
 static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32_t* pairs, uint32_t n_pairs,
-                                          const uint8_t* seq, uint32_t len, const WeightSrc& w) {
+                                          const uint8_t* seq, uint32_t len, const WeightSrc& w,
+                                          const uint32_t* pre = nullptr) {
   GraphHeader* h = G.hdr;
   if (len == 0) return kOk;
   // room for the worst case of this read
@@ -514,15 +577,16 @@ static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32
   int64_t last = g_add_sequence(G, seq, w, (uint32_t)last_valid + 1, len);
   if (last < -1) return kCapacity;
   const uint32_t K = G.caps.aligned;
+  bool prev_new = true;  // prev was created by this read (it has no edge to an old node)
   for (uint32_t k = 0; k < n_pairs; ++k) {
     int32_t nid = pairs[2 * k], pos = pairs[2 * k + 1];
     if (pos == -1) continue;
     uint32_t code = (uint32_t)h->coder[seq[pos]];
     int64_t curr = -1;
-    if (nid == -1) {
-      curr = g_add_node(G, code);
-      if (curr < 0) return kCapacity;
-    } else {
+    bool curr_new = false;
+    if (pre) {
+      if (pre[2 * k] != kNone) curr = pre[2 * k];
+    } else if (nid != -1) {
       if (G.code[nid] == code) {
         curr = nid;
       } else {
@@ -534,26 +598,42 @@ static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32
             break;
           }
         }
-        if (curr < 0) {
-          curr = g_add_node(G, code);
-          if (curr < 0) return kCapacity;
-          for (uint32_t a = 0; a < na; ++a) {
-            uint32_t kt = al[a];
-            if (g_link_aligned(G, kt, (uint32_t)curr) || g_link_aligned(G, (uint32_t)curr, kt))
-              return kCapacity;
-          }
-          if (g_link_aligned(G, (uint32_t)nid, (uint32_t)curr) ||
-              g_link_aligned(G, (uint32_t)curr, (uint32_t)nid))
+      }
+    }
+    if (curr < 0) {
+      curr = g_add_node(G, code);
+      if (curr < 0) return kCapacity;
+      curr_new = true;
+      if (nid != -1) {
+        const uint32_t na = G.n_aligned[nid];
+        const uint32_t* al = G.aligned + (uint64_t)nid * K;
+        for (uint32_t a = 0; a < na; ++a) {
+          uint32_t kt = al[a];
+          if (g_link_aligned(G, kt, (uint32_t)curr) || g_link_aligned(G, (uint32_t)curr, kt))
             return kCapacity;
         }
+        if (g_link_aligned(G, (uint32_t)nid, (uint32_t)curr) ||
+            g_link_aligned(G, (uint32_t)curr, (uint32_t)nid))
+          return kCapacity;
       }
     }
     if (begin < 0) begin = curr;
     if (prev >= 0) {
-      if (g_add_edge(G, (uint32_t)prev, (uint32_t)curr, w.at(pos - 1) + w.at(pos)))
-        return kCapacity;
+      const uint32_t wt = w.at(pos - 1) + w.at(pos);
+      if (!pre) {
+        if (g_add_edge(G, (uint32_t)prev, (uint32_t)curr, wt)) return kCapacity;
+      } else if (!prev_new && !curr_new && pre[2 * k + 1] != kNone) {
+        // AddEdge on an existing edge: one more label and the weight
+        const uint32_t e = pre[2 * k + 1];
+        if (g_add_label(G, e)) return kCapacity;
+        G.e_weight[e] += wt;
+      } else {
+        const int64_t e = g_new_edge(G, (uint32_t)prev, (uint32_t)curr, wt);
+        if (e < 0 || g_add_label(G, (uint32_t)e)) return kCapacity;
+      }
     }
     prev = curr;
+    prev_new = curr_new;
   }
   if (last >= 0) {
     if (g_add_edge(G, (uint32_t)prev, (uint32_t)last, w.at(last_valid) + w.at(last_valid + 1)))

@@ -52,11 +52,15 @@ DG* dg_create(uint32_t nodes, uint32_t edges, uint32_t labels, uint32_t seqs, ui
 
 void dg_destroy(DG* g) { delete g; }
 
-// Graph::AddAlignment, then the sort (graph.cpp:155-303)
+// Graph::AddAlignment, then the sort (graph.cpp:155-303); with_prepass runs
+// the read-only pre-pass first and lets the add use its results
 int32_t dg_add(DG* g, const int32_t* pairs, uint32_t n_pairs, const char* seq, uint32_t len,
-               const uint32_t* weights) {
+               const uint32_t* weights, int32_t with_prepass) {
   WeightSrc ws{weights, nullptr, len, 0u, 1u};
-  int32_t st = g_add_alignment(g->v, pairs, n_pairs, reinterpret_cast<const uint8_t*>(seq), len, ws);
+  const uint8_t* s = reinterpret_cast<const uint8_t*>(seq);
+  std::vector<uint32_t> pre(2 * (size_t)n_pairs + 2);
+  if (with_prepass) g_add_prepass(g->v, pairs, n_pairs, s, len, pre.data());
+  int32_t st = g_add_alignment(g->v, pairs, n_pairs, s, len, ws, with_prepass ? pre.data() : nullptr);
   if (st != kOk) return st;
   int ret = 0;
   if (len > 0 && g_topo_sort_cta(g->v, &ret) != 0) return kCapacity;

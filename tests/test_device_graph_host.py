@@ -32,7 +32,7 @@ def dg():
     L.dg_create.restype = P
     L.dg_create.argtypes = [U32] * 5
     L.dg_destroy.argtypes = [P]
-    L.dg_add.argtypes = [P, P, U32, C.c_char_p, U32, P]
+    L.dg_add.argtypes = [P, P, U32, C.c_char_p, U32, P, C.c_int32]
     L.dg_counts.argtypes = [P, P]
     L.dg_export.argtypes = [P] * 12
     L.dg_consensus.argtypes = [P, C.c_char_p, U32]
@@ -91,7 +91,7 @@ def oracle_state(g) -> dict:
             "seq_begin": ex["seq_begin"].tolist(), "consensus": ex["consensus"].tolist()}
 
 
-def _window(L, type_, params, reads, quals=None, check_every_read=True):
+def _window(L, type_, params, reads, quals=None, check_every_read=True, prepass=True):
     """Replays a window on the oracle and on the host-built device graph
     with the oracle's alignments; returns both graphs (caller frees)."""
     O = po.lib()
@@ -109,7 +109,7 @@ def _window(L, type_, params, reads, quals=None, check_every_read=True):
         w = np.ascontiguousarray(w, np.uint32)
         aln = np.ascontiguousarray(pairs[:2 * n.value])
         assert O.oracle_add_alignment(og, _ptr(aln), n.value, r, len(r), _ptr(w), len(r)) == 0
-        assert L.dg_add(g, _ptr(aln), n.value, r, len(r), _ptr(w)) == 0
+        assert L.dg_add(g, _ptr(aln), n.value, r, len(r), _ptr(w), 1 if prepass else 0) == 0
         if check_every_read or k == len(reads) - 1:
             assert dg_state(L, g) == oracle_state(og), k
     O.oracle_engine_destroy(en)
@@ -119,12 +119,14 @@ def _window(L, type_, params, reads, quals=None, check_every_read=True):
 def test_add_alignment_and_sort_match_the_oracle(dg, ref_windows):
     """Every read of 60 recorded windows (adversarial lengths, N bases,
     qualities, long insertions, polishing and uneven shapes): the graph after
-    each AddAlignment + sort, then the consensus."""
+    each AddAlignment + sort, then the consensus; half the windows add with
+    the read-only pre-pass (g_add_prepass), half without."""
     O = po.lib()
-    for rec in ref_windows[::3][:60]:
+    for i, rec in enumerate(ref_windows[::3][:60]):
         reads = [r.encode() for r in rec["reads"]]
         quals = [q.encode() for q in rec["quals"]] if rec["quals"] else None
-        og, g = _window(dg, rec["type"], tuple(rec["params"]), reads, quals)
+        # the add with and without its read-only pre-pass
+        og, g = _window(dg, rec["type"], tuple(rec["params"]), reads, quals, prepass=i % 2 == 0)
         n = O.oracle_graph_num_nodes(og)
         a, b = C.create_string_buffer(n + 1), C.create_string_buffer(n + 1)
         ka = O.oracle_consensus(og, a, n + 1)
