@@ -16,8 +16,10 @@ e2e       windows/s through the public batch API from pinned host buffers:
 plain     windows/s of the one-window-per-launch form on a sample.
 roofline  HBM view: algorithmic bytes (the 4-bit traceback state of every
           cell) per second against the measured copy bandwidth; int_roofline
-          is the integer-pipe view (the survey's per-cell max/add counts
-          against a measured max/add rate), the bound that applies.
+          is the integer-pipe view (max/add operations per cell: linear
+          2d+1, affine 3d+3, convex 5d+4, +1 for SW, d the row's
+          predecessors, against a measured max/add rate), the bound that
+          applies.
 cpu_baseline  the C oracle (the reference algorithm restated in C, one window
           per host thread) on a bounded sample of the same workload.
 
