@@ -64,6 +64,19 @@ def test_library_exports_the_spoa_api():
     assert out.count("spoa::Graph::AddAlignment(") == 6
 
 
+@pytest.mark.skipif(shutil.which("g++") is None, reason="g++ not available")
+def test_cereal_archives_compile_against_the_header():
+    """With SPOA_USE_CEREAL, `archive(graph)` compiles as with the reference
+    (the library's save/load hooks put its own bytes into the archive)."""
+    src = os.path.join(os.path.dirname(__file__), "cpp", "cereal_compile_check.cpp")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run(["g++", "-std=c++11", "-fsyntax-only", "-DSPOA_USE_CEREAL",
+                        "-I", os.path.join(root, "include"),
+                        "-I", os.path.join(root, "oracle", "ref_shim"), src],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 @pytest.mark.skipif(sg.lib().spoa_gb300_device_count() > 0, reason="a GPU is visible")
 def test_cpp_api_fails_loudly_without_a_gpu(tmp_path, sample_reads, spoa_test_cases):
     r = _run(tmp_path, sample_reads[:3], spoa_test_cases[:1])
