@@ -380,8 +380,8 @@ static __device__ __noinline__ int g_topo_sort_cta(GraphView& G, int* s_ret) {
   uint32_t* __restrict__ bits = G.sort_bits;
   const uint32_t words = 3 * ((nn + 31) / 32);
   for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) bits[w] = 0;
-  for (uint32_t v = threadIdx.x * 8; v < nn; v += blockDim.x * 8)
 #ifdef __CUDA_ARCH__
+  for (uint32_t v = threadIdx.x * 8; v < nn; v += blockDim.x * 8)
     asm volatile("prefetch.global.L1 [%0];" ::"l"(G.nrec + v));
 #endif
   __syncthreads();

@@ -1,0 +1,96 @@
+// window_host.cpp - one window through the device code of the batched
+// kernel (spoa_gb300/csrc/poa_window.cuh: forward pass with its CTA scans,
+// traceback, strand choice, AddAlignment, topological sort, consensus), run
+// on the host by the SIMT emulation of simt_host.h, one CTA of `nt` threads
+// per read.  TEST INFRASTRUCTURE ONLY (tests/test_window_host.py compares
+// it with the oracle); the product runs the same functions on the GPU.
+#include "simt_host.h"
+
+#include "../../spoa_gb300/csrc/poa_window.cuh"
+
+using namespace spoa_gb300;
+
+namespace {
+
+template <int SUB, int CPT, typename T>
+int32_t run(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t* off,
+            const char* quals, int32_t strand, uint32_t nt, int32_t* scores, int32_t* rev,
+            int32_t* aln, uint64_t aln_cap, uint64_t* aln_off, char* cons, uint32_t cons_cap,
+            uint32_t* cons_len) {
+  uint64_t sum = 0;
+  uint32_t lmax = 1;
+  for (uint32_t r = 0; r < n_reads; ++r) {
+    sum += off[r + 1] - off[r];
+    lmax = std::max<uint32_t>(lmax, (uint32_t)(off[r + 1] - off[r]));
+  }
+  GraphCaps gc{(uint32_t)sum + 2, 2 * (uint32_t)sum + n_reads + 8, (uint32_t)sum + n_reads + 8,
+               n_reads + 1, 31};
+  GraphView G;
+  std::vector<uint8_t> gbuf(graph_layout(nullptr, gc, &G) + 256);
+  graph_layout(gbuf.data(), gc, &G);
+  DpCaps dc{gc.nodes + 1, CPT * nt, gc.edges + gc.nodes + 2, S.sub, sizeof(T)};
+  DpView D;
+  std::vector<uint8_t> dbuf(dp_layout(nullptr, dc, &D) + 256);
+  dp_layout(dbuf.data(), dc, &D);
+  simt::launch(1, [&] { g_reset(G); });
+  BlockScratch sh;
+  SharedState ss;
+  uint64_t na = 0;
+  aln_off[0] = 0;
+  for (uint32_t r = 0; r < n_reads; ++r) {
+    const uint32_t L = (uint32_t)(off[r + 1] - off[r]);
+    const uint8_t* seq = reinterpret_cast<const uint8_t*>(seqs) + off[r];
+    const uint8_t* qual = quals ? reinterpret_cast<const uint8_t*>(quals) + off[r] : nullptr;
+    int32_t score = 0, rv = 0;
+    const int32_t* pairs = nullptr;
+    uint32_t np = 0;
+    simt::launch(nt, [&] {
+      window_read<SUB, CPT, T>(S, G, D, sh, ss, seq, L, qual, strand != 0, &score, &rv, &pairs,
+                               &np);
+    });
+    if (ss.status != kOk) return ss.status;
+    scores[r] = score;
+    rev[r] = rv;
+    if (na + np > aln_cap) return kCapacity;
+    for (uint32_t k = 0; k < 2 * np; ++k) aln[2 * na + k] = pairs[k];
+    na += np;
+    aln_off[r + 1] = na;
+  }
+  simt::launch(1, [&] { write_consensus(G, reinterpret_cast<uint8_t*>(cons), cons_cap, cons_len); });
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" int32_t wh_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t e, int32_t q,
+                          int32_t c, int32_t wide, int32_t cpt, uint32_t nt, uint32_t n_reads,
+                          const char* seqs, const uint64_t* off, const char* quals,
+                          int32_t strand, int32_t* scores, int32_t* rev, int32_t* aln,
+                          uint64_t aln_cap, uint64_t* aln_off, char* cons, uint32_t cons_cap,
+                          uint32_t* cons_len) {
+  // AlignmentEngine::Create's subtype and canonical penalties
+  // (alignment_engine.cpp:57-66)
+  const int32_t sub = g >= e ? kLinear : ((g <= q || e >= c) ? kAffine : kConvex);
+  if (sub == kLinear) {
+    e = g;
+  } else if (sub == kAffine) {
+    q = g;
+    c = e;
+  }
+  const Scoring S{type, sub, m, n, g, e, q, c};
+#define RUN(SUBV, C, TT)                                                                        \
+  return run<SUBV, C, TT>(S, n_reads, seqs, off, quals, strand, nt, scores, rev, aln, aln_cap, \
+                          aln_off, cons, cons_cap, cons_len)
+#define BY_SUB(C, TT)                   \
+  switch (sub) {                        \
+    case kLinear: RUN(kLinear, C, TT);  \
+    case kAffine: RUN(kAffine, C, TT);  \
+    default: RUN(kConvex, C, TT);       \
+  }
+  if (cpt == 8) {
+    if (wide) BY_SUB(8, int32_t) else BY_SUB(8, int16_t)
+  }
+  if (wide) BY_SUB(16, int32_t) else BY_SUB(16, int16_t)
+#undef BY_SUB
+#undef RUN
+}
