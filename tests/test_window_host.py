@@ -85,12 +85,14 @@ def test_window_device_code_matches_the_oracle(wh, ref_windows):
     """Recorded windows of every shape the fixture holds (adversarial
     lengths, N bases, qualities, both strands, long insertions) through the
     emulated CTA; reads up to 256 columns take one warp, longer ones two."""
-    nts = set()
-    for rec in ref_windows[::14]:
+    nts, strands = set(), 0
+    for i, rec in enumerate(ref_windows):
         if max(len(r) for r in rec["reads"]) > 512 or len(rec["reads"]) > 12:
             continue
-        nts.add(_check_window(wh, rec))
-    assert nts >= {32}
+        if i % 14 == 0 or (rec["strand_ambiguous"] and i % 12 == 1):
+            nts.add(_check_window(wh, rec))
+            strands += rec["strand_ambiguous"]
+    assert nts >= {32} and strands >= 4
 
 
 def test_two_warp_ctas_and_int32_rows(wh):
