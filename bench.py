@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--windows-per-cta", type=int, default=1, choices=[1, 2, 4],
+                    help="windows in flight per CTA (16-bit windows)")
     return ap.parse_args()
 
 
@@ -272,7 +274,8 @@ def main():
     def make_batch():
         return sg.Batch.from_arrays(seqs, off, wro, typ, *params, window_types=wtypes,
                                     window_strand=wstrand,
-                                    autotune=args.workload == "batch_10k")
+                                    autotune=args.workload == "batch_10k",
+                                    windows_per_cta=args.windows_per_cta)
 
     batch = make_batch()
     for _ in range(args.warmup):

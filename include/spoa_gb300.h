@@ -204,6 +204,9 @@ typedef struct {
                                       first launch and keep the fastest (cached
                                       per process, and per device model in the
                                       file named by SPOA_GB300_TILE_CACHE) */
+  int32_t windows_per_cta;         /* 2 or 4: windows of 16-bit width in flight
+                                      per CTA, their graph updates on parallel
+                                      lanes; otherwise 1 */
 } spoa_gb300_batch_desc;
 
 typedef struct {

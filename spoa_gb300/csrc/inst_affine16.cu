@@ -4,4 +4,5 @@
 
 namespace spoa_gb300 {
 SPOA_GB300_INSTANTIATE(kAffine, int16_t)
+SPOA_GB300_INSTANTIATE_MW(kAffine)
 }  // namespace spoa_gb300

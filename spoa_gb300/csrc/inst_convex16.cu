@@ -4,4 +4,5 @@
 
 namespace spoa_gb300 {
 SPOA_GB300_INSTANTIATE(kConvex, int16_t)
+SPOA_GB300_INSTANTIATE_MW(kConvex)
 }  // namespace spoa_gb300

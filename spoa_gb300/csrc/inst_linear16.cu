@@ -4,4 +4,5 @@
 
 namespace spoa_gb300 {
 SPOA_GB300_INSTANTIATE(kLinear, int16_t)
+SPOA_GB300_INSTANTIATE_MW(kLinear)
 }  // namespace spoa_gb300

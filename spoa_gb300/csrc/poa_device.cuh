@@ -375,6 +375,84 @@ __device__ inline int64_t g_add_sequence(GraphView& G, const uint8_t* seq, const
 // Every thread clears the bitmaps and prefetches the node records into L1,
 // then thread 0 runs the DFS.  Returns 0, or -1 when the stack or the guard
 // runs out (identical in every thread).
+// The DFS of g_topo_sort_cta on one thread, the mark bitmaps already
+// cleared: 0, or -1 when the stack or the guard runs out.
+__device__ __forceinline__ int g_topo_dfs(GraphView& G) {
+  const uint32_t nn = G.hdr->n_nodes;
+  uint32_t* __restrict__ bits = G.sort_bits;
+  auto bit = [&](uint32_t v, uint32_t kind) { return (bits[3 * (v >> 5) + kind] >> (v & 31)) & 1u; };
+  auto set = [&](uint32_t v, uint32_t kind) { bits[3 * (v >> 5) + kind] |= 1u << (v & 31); };
+  constexpr uint32_t kBusy = 0, kDone = 1, kIgn = 2;
+  uint32_t* __restrict__ stack = G.stack;
+  uint64_t sp = 0;
+  auto push = [&](uint32_t v) -> bool {
+    if (sp >= G.stack_cap) return false;
+    stack[sp++] = v;
+    return true;
+  };
+  uint32_t rank = 0;
+  const uint32_t K = G.caps.aligned;
+  // every iteration pops or pushes; pushes are bounded by the stack size
+  uint64_t guard = 0;
+  const uint64_t guard_max = 4 * G.stack_cap + 4 * (uint64_t)nn + 16;
+  int rc = 0;
+  for (uint32_t s = 0; s < nn && rc == 0; ++s) {
+    if (bit(s, kDone) || bit(s, kBusy)) continue;
+    push(s);
+    while (sp) {
+      if (++guard > guard_max) { rc = -1; break; }
+      const uint32_t curr = stack[sp - 1];
+      bool valid = true;
+      if (!bit(curr, kDone)) {
+        const uint4 r = G.nrec[curr];
+        const uint32_t deg = r.x & 0xFFFFu, na = r.x >> 16;
+        // in-edge tails in insertion order: three from the record, the
+        // rest from the edge list
+        if (deg > 0 && !bit(r.y, kDone)) { if (!push(r.y)) { rc = -1; break; } valid = false; }
+        if (deg > 1 && !bit(r.z, kDone)) { if (!push(r.z)) { rc = -1; break; } valid = false; }
+        if (deg > 2 && !bit(r.w, kDone)) { if (!push(r.w)) { rc = -1; break; } valid = false; }
+        if (deg > 3) {
+          uint32_t e = G.nlink[curr].x;
+          for (int k = 0; k < 3 && e != kNone; ++k) e = G.erec[e].z;
+          for (; e != kNone; e = G.erec[e].z) {
+            const uint32_t tl = G.erec[e].x;
+            if (!bit(tl, kDone)) { if (!push(tl)) { rc = -1; break; } valid = false; }
+          }
+          if (rc) break;
+        }
+        const uint32_t* al = G.aligned + (uint64_t)curr * K;
+        const bool ign = bit(curr, kIgn);
+        if (!ign) {
+          for (uint32_t k = 0; k < na; ++k) {
+            const uint32_t a = al[k];
+            if (!bit(a, kDone)) {
+              if (!push(a)) { rc = -1; break; }
+              set(a, kIgn);
+              valid = false;
+            }
+          }
+          if (rc) break;
+        }
+        if (valid) {
+          set(curr, kDone);
+          if (!ign) {
+            G.rank_to_node[rank] = curr;
+            G.node_to_rank[curr] = rank++;
+            for (uint32_t k = 0; k < na; ++k) {
+              G.rank_to_node[rank] = al[k];
+              G.node_to_rank[al[k]] = rank++;
+            }
+          }
+        } else {
+          set(curr, kBusy);
+        }
+      }
+      if (valid) --sp;
+    }
+  }
+  return (rc == 0 && rank == nn) ? 0 : -1;
+}
+
 static __device__ __noinline__ int g_topo_sort_cta(GraphView& G, int* s_ret) {
   const uint32_t nn = G.hdr->n_nodes;
   uint32_t* __restrict__ bits = G.sort_bits;
@@ -385,79 +463,7 @@ static __device__ __noinline__ int g_topo_sort_cta(GraphView& G, int* s_ret) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(G.nrec + v));
 #endif
   __syncthreads();
-  if (threadIdx.x == 0) {
-    auto bit = [&](uint32_t v, uint32_t kind) { return (bits[3 * (v >> 5) + kind] >> (v & 31)) & 1u; };
-    auto set = [&](uint32_t v, uint32_t kind) { bits[3 * (v >> 5) + kind] |= 1u << (v & 31); };
-    constexpr uint32_t kBusy = 0, kDone = 1, kIgn = 2;
-    uint32_t* __restrict__ stack = G.stack;
-    uint64_t sp = 0;
-    auto push = [&](uint32_t v) -> bool {
-      if (sp >= G.stack_cap) return false;
-      stack[sp++] = v;
-      return true;
-    };
-    uint32_t rank = 0;
-    const uint32_t K = G.caps.aligned;
-    // every iteration pops or pushes; pushes are bounded by the stack size
-    uint64_t guard = 0;
-    const uint64_t guard_max = 4 * G.stack_cap + 4 * (uint64_t)nn + 16;
-    int rc = 0;
-    for (uint32_t s = 0; s < nn && rc == 0; ++s) {
-      if (bit(s, kDone) || bit(s, kBusy)) continue;
-      push(s);
-      while (sp) {
-        if (++guard > guard_max) { rc = -1; break; }
-        const uint32_t curr = stack[sp - 1];
-        bool valid = true;
-        if (!bit(curr, kDone)) {
-          const uint4 r = G.nrec[curr];
-          const uint32_t deg = r.x & 0xFFFFu, na = r.x >> 16;
-          // in-edge tails in insertion order: three from the record, the
-          // rest from the edge list
-          if (deg > 0 && !bit(r.y, kDone)) { if (!push(r.y)) { rc = -1; break; } valid = false; }
-          if (deg > 1 && !bit(r.z, kDone)) { if (!push(r.z)) { rc = -1; break; } valid = false; }
-          if (deg > 2 && !bit(r.w, kDone)) { if (!push(r.w)) { rc = -1; break; } valid = false; }
-          if (deg > 3) {
-            uint32_t e = G.nlink[curr].x;
-            for (int k = 0; k < 3 && e != kNone; ++k) e = G.erec[e].z;
-            for (; e != kNone; e = G.erec[e].z) {
-              const uint32_t tl = G.erec[e].x;
-              if (!bit(tl, kDone)) { if (!push(tl)) { rc = -1; break; } valid = false; }
-            }
-            if (rc) break;
-          }
-          const uint32_t* al = G.aligned + (uint64_t)curr * K;
-          const bool ign = bit(curr, kIgn);
-          if (!ign) {
-            for (uint32_t k = 0; k < na; ++k) {
-              const uint32_t a = al[k];
-              if (!bit(a, kDone)) {
-                if (!push(a)) { rc = -1; break; }
-                set(a, kIgn);
-                valid = false;
-              }
-            }
-            if (rc) break;
-          }
-          if (valid) {
-            set(curr, kDone);
-            if (!ign) {
-              G.rank_to_node[rank] = curr;
-              G.node_to_rank[curr] = rank++;
-              for (uint32_t k = 0; k < na; ++k) {
-                G.rank_to_node[rank] = al[k];
-                G.node_to_rank[al[k]] = rank++;
-              }
-            }
-          } else {
-            set(curr, kBusy);
-          }
-        }
-        if (valid) --sp;
-      }
-    }
-    *s_ret = (rc == 0 && rank == nn) ? 0 : -1;
-  }
+  if (threadIdx.x == 0) *s_ret = g_topo_dfs(G);
   __syncthreads();
   return *s_ret;
 }

@@ -9,6 +9,7 @@
 #include "poa_device.cuh"
 #include "poa_dp.cuh"
 #include "poa_window.cuh"
+#include "poa_batch_mw.cuh"
 
 namespace spoa_gb300 {
 
@@ -203,38 +204,6 @@ __global__ void k_import(GraphView G, ImportArgs a, int32_t* status) {
 // ---------------------------------------------------------------------------
 // persistent batch kernel
 // ---------------------------------------------------------------------------
-struct BatchArgs {
-  Scoring base;
-  const int8_t* win_type;
-  const int8_t* win_strand;
-  uint32_t n_windows;
-  const uint32_t* win_read_off;
-  const uint8_t* seqs;
-  const uint64_t* seq_off;
-  const uint8_t* quals;
-  const uint32_t* work;     // window ids to process (queue order)
-  uint32_t n_work;
-  uint32_t* queue;          // atomic cursor into work
-  uint8_t* arena;
-  uint64_t arena_stride;
-  GraphCaps gcaps;
-  DpCaps dcaps;
-  int32_t* read_scores;
-  uint8_t* read_rev;
-  uint8_t* cons;
-  const uint64_t* cons_off;
-  uint32_t* cons_len;
-  int32_t* win_status;
-  int32_t* aln_out;         // optional
-  const uint64_t* aln_off;
-  uint32_t* aln_len;
-  uint8_t* msa_out;         // optional
-  const uint64_t* msa_off;
-  uint32_t* msa_rows;
-  uint32_t* msa_cols;
-  unsigned long long* cells;       // sum of read length x graph nodes
-  unsigned long long* pred_cells;  // sum of read length x predecessor entries
-};
 
 // Register cap: 96 for int16 pairs gives 5 single-warp windows per SM
 // sub-partition (20 per SM) and measured 6 % faster than 128 (16 per SM)
@@ -328,6 +297,24 @@ __global__ void __maxnreg__(kBatchMaxRegs<T>) k_batch(BatchArgs a) {
     }
     __syncthreads();
   }
+}
+
+// W windows per CTA (batch_cta_mw): the serial graph updates of the W
+// windows run on W lanes side by side.
+template <int SUB, int CPT, typename T, int W>
+__global__ void __maxnreg__(kBatchMaxRegs<T>) k_batch_mw(BatchArgs a) {
+  __shared__ BlockScratch sh;
+  __shared__ SharedState ss;
+  __shared__ MwSlot slot[W];
+  __shared__ GraphView Gs[W];
+  __shared__ DpView D;
+  __shared__ int32_t* pairs[W];
+  __shared__ uint8_t* reads[W];
+  __shared__ MwShared m;
+  if (threadIdx.x == 0)
+    mw_layout(a.arena + a.arena_stride * blockIdx.x, W, a.gcaps, a.dcaps, &D, Gs, pairs, reads);
+  __syncthreads();
+  batch_cta_mw<SUB, CPT, T, W>(a, sh, ss, slot, Gs, D, pairs, reads, m);
 }
 
 }  // namespace spoa_gb300
@@ -439,6 +426,38 @@ int32_t occupancy_batch(int cpt, int nt, int* blocks) {
   return kOk;
 }
 
+// W windows per CTA (2 or 4), 16-bit lanes
+template <int SUB>
+int32_t launch_batch_mw(int cpt, int nt, int W, int grid, const BatchArgs& a, cudaStream_t s) {
+  using T = int16_t;
+#define L_(C)                                                      \
+  if (W == 2)                                                      \
+    k_batch_mw<SUB, C, T, 2><<<grid, nt, 0, s>>>(a);              \
+  else                                                             \
+    k_batch_mw<SUB, C, T, 4><<<grid, nt, 0, s>>>(a)
+  SPOA_CPT_SWITCH(T, cpt, L_)
+#undef L_
+  return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
+}
+
+template <int SUB>
+int32_t occupancy_batch_mw(int cpt, int nt, int W, int* blocks) {
+  using T = int16_t;
+  cudaError_t err = cudaSuccess;
+#define L_(C)                                                                           \
+  err = W == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(                       \
+                     blocks, k_batch_mw<SUB, C, T, 2>, nt, 0)                          \
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(                       \
+                     blocks, k_batch_mw<SUB, C, T, 4>, nt, 0)
+  SPOA_CPT_SWITCH(T, cpt, L_)
+#undef L_
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    return kCuda;
+  }
+  return kOk;
+}
+
 #define SPOA_GB300_INSTANTIATE(SUB, T)                                                          \
   template int32_t launch_align<SUB, T>(int, int, const Scoring&, const GraphView&,             \
                                         const DpView&, const uint8_t*, uint32_t, ReadOut*);     \
@@ -448,6 +467,10 @@ int32_t occupancy_batch(int cpt, int nt, int* blocks) {
                                             cudaStream_t);                                      \
   template int32_t launch_batch<SUB, T>(int, int, int, const BatchArgs&, cudaStream_t);         \
   template int32_t occupancy_batch<SUB, T>(int, int, int*);
+
+#define SPOA_GB300_INSTANTIATE_MW(SUB)                                                          \
+  template int32_t launch_batch_mw<SUB>(int, int, int, int, const BatchArgs&, cudaStream_t);    \
+  template int32_t occupancy_batch_mw<SUB>(int, int, int, int*);
 
 #define SPOA_GB300_INSTANTIATE_SEG(SUB)                                                         \
   template int32_t launch_batch_seg<SUB, int32_t>(int, int, int, const BatchArgs&, cudaStream_t); \

@@ -185,4 +185,38 @@ static __device__ __noinline__ int32_t window_msa(GraphView& G, bool include_con
   return kOk;
 }
 
+// Arguments of the persistent batched kernels.
+struct BatchArgs {
+  Scoring base;
+  const int8_t* win_type;
+  const int8_t* win_strand;
+  uint32_t n_windows;
+  const uint32_t* win_read_off;
+  const uint8_t* seqs;
+  const uint64_t* seq_off;
+  const uint8_t* quals;
+  const uint32_t* work;     // window ids to process (queue order)
+  uint32_t n_work;
+  uint32_t* queue;          // atomic cursor into work
+  uint8_t* arena;
+  uint64_t arena_stride;
+  GraphCaps gcaps;
+  DpCaps dcaps;
+  int32_t* read_scores;
+  uint8_t* read_rev;
+  uint8_t* cons;
+  const uint64_t* cons_off;
+  uint32_t* cons_len;
+  int32_t* win_status;
+  int32_t* aln_out;         // optional
+  const uint64_t* aln_off;
+  uint32_t* aln_len;
+  uint8_t* msa_out;         // optional
+  const uint64_t* msa_off;
+  uint32_t* msa_rows;
+  uint32_t* msa_cols;
+  unsigned long long* cells;       // sum of read length x graph nodes
+  unsigned long long* pred_cells;  // sum of read length x predecessor entries
+};
+
 }  // namespace spoa_gb300

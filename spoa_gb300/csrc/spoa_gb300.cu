@@ -62,6 +62,14 @@ SPOA_EXTERN_SEG(kLinear)
 SPOA_EXTERN_SEG(kAffine)
 SPOA_EXTERN_SEG(kConvex)
 #undef SPOA_EXTERN_SEG
+#define SPOA_EXTERN_MW(SUB)                                                                      \
+  extern template int32_t launch_batch_mw<SUB>(int, int, int, int, const BatchArgs&,             \
+                                               cudaStream_t);                                    \
+  extern template int32_t occupancy_batch_mw<SUB>(int, int, int, int*);
+SPOA_EXTERN_MW(kLinear)
+SPOA_EXTERN_MW(kAffine)
+SPOA_EXTERN_MW(kConvex)
+#undef SPOA_EXTERN_MW
 }  // namespace spoa_gb300
 
 // ===========================================================================
@@ -96,6 +104,13 @@ constexpr int kCpts32[] = {8, 12, 16, 24, 32};
   ((sub) == kLinear   ? fn<kLinear, int32_t>(__VA_ARGS__)                                \
    : (sub) == kAffine ? fn<kAffine, int32_t>(__VA_ARGS__)                                \
    : (sub) == kConvex ? fn<kConvex, int32_t>(__VA_ARGS__)                                \
+                      : (int32_t)kInvalidArgument)
+
+// fn<gap model>(...) for the kernels built for 16-bit lanes only
+#define SPOA_BY_SUB16(sub, fn, ...)                                                      \
+  ((sub) == kLinear   ? fn<kLinear>(__VA_ARGS__)                                         \
+   : (sub) == kAffine ? fn<kAffine>(__VA_ARGS__)                                         \
+   : (sub) == kConvex ? fn<kConvex>(__VA_ARGS__)                                         \
                       : (int32_t)kInvalidArgument)
 
 // Latency tile: the smallest strip (most threads) that covers L.
@@ -979,6 +994,7 @@ struct Pass {
   DpCaps dcaps{};
   int cpt = 0, nt = 0, ctas = 0;
   int segs = 1;             // strips per thread (dp_forward_seg when > 1)
+  int wpc = 1;              // windows per CTA (batch_cta_mw when > 1)
   uint64_t stride = 0;
   int tuned_cpt = 0, tuned_nt = 0;  // tile chosen by the tuner (0: the default)
   int cls = 0;              // length class
@@ -1092,23 +1108,33 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
   uint64_t nodes = d.max_nodes ? std::max<uint64_t>(d.max_nodes, wnodes) : wnodes;
   GraphCaps gc;
   DpCaps dc;
-  const uint64_t stride =
+  uint64_t stride =
       arena_caps(b->base.sub, p->wide, cpt * segs, nt, nodes, maxsum, maxreads, many_aligned, &gc,
                  &dc);
+  // several windows per CTA: 16-bit lanes, single-strip tiles
+  const int wpc = (d.windows_per_cta == 2 || d.windows_per_cta == 4) && !p->wide && segs == 1
+                      ? d.windows_per_cta
+                      : 1;
+  if (wpc > 1) {
+    DpView dv;
+    stride = align_up(mw_layout(nullptr, wpc, gc, dc, &dv, nullptr, nullptr, nullptr), 256);
+  }
   int blocks = 1;
   if (segs > 1 ? SPOA_BY_SUB32(b->base.sub, occupancy_batch_seg, segs, nt, &blocks)
-               : SPOA_BY_SUB(b->base.sub, p->wide, occupancy_batch, cpt, nt, &blocks))
+      : wpc > 1 ? SPOA_BY_SUB16(b->base.sub, occupancy_batch_mw, cpt, nt, wpc, &blocks)
+                : SPOA_BY_SUB(b->base.sub, p->wide, occupancy_batch, cpt, nt, &blocks))
     return kCuda;
   blocks = std::max(blocks, 1);
   uint64_t by_mem = std::max<uint64_t>(1, b->budget / stride);
   uint64_t ctas = d.ctas > 0 ? (uint64_t)d.ctas : (uint64_t)b->sm_count * blocks;
   ctas = std::min<uint64_t>(ctas, by_mem);
-  ctas = std::min<uint64_t>(ctas, p->windows.size());
+  ctas = std::min<uint64_t>(ctas, (p->windows.size() + wpc - 1) / wpc);
   p->gcaps = gc;
   p->dcaps = dc;
   p->cpt = cpt;
   p->nt = nt;
   p->segs = segs;
+  p->wpc = wpc;
   p->ctas = (int)std::max<uint64_t>(ctas, 1);
   p->stride = stride;
   return kOk;
@@ -1157,6 +1183,8 @@ int32_t launch_pass(spoa_gb300_batch* b, const Pass& p, int ctas, const BatchArg
                     cudaStream_t s) {
   ++b->launches;
   if (p.segs > 1) return SPOA_BY_SUB32(b->base.sub, launch_batch_seg, p.segs, p.nt, ctas, a, s);
+  if (p.wpc > 1)
+    return SPOA_BY_SUB16(b->base.sub, launch_batch_mw, p.cpt, p.nt, p.wpc, ctas, a, s);
   return SPOA_BY_SUB(b->base.sub, p.wide, launch_batch, p.cpt, p.nt, ctas, a, s);
 }
 

@@ -11,6 +11,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <barrier>
 #include <cstdint>
 #include <cstring>
@@ -175,4 +176,10 @@ static inline uint32_t __byte_perm(uint32_t x, uint32_t y, uint32_t s) {
 template <typename T>
 static inline void __stcs(T* p, T v) {
   *p = v;
+}
+static inline uint32_t atomicAdd(uint32_t* p, uint32_t v) {
+  return std::atomic_ref<uint32_t>(*p).fetch_add(v);
+}
+static inline unsigned long long atomicAdd(unsigned long long* p, unsigned long long v) {
+  return std::atomic_ref<unsigned long long>(*p).fetch_add(v);
 }

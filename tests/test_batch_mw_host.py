@@ -1,0 +1,79 @@
+"""The batched loop with W windows per CTA (spoa_gb300/csrc/poa_batch_mw.cuh)
+run on the host by the SIMT emulation (tests/host/batch_mw_host.cpp): one
+CTA takes every window of a small batch from the queue; each window's read
+scores, strand choices and consensus must equal the oracle's, for W = 2
+(one strand) and W = 4 (strand-ambiguous).  (W = 1 is the one-window loop of
+the batched kernel; tests/test_window_host.py covers its device code.)"""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from oracle import pyoracle as po
+from spoa_gb300 import synth
+
+SRC = os.path.join(ROOT, "tests", "host", "batch_mw_host.cpp")
+OUT = os.path.join(ROOT, "tests", "host", "_build", "libbatch_mw_host.so")
+CSRC = os.path.join(ROOT, "spoa_gb300", "csrc")
+
+
+@pytest.fixture(scope="module")
+def mw():
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    os.makedirs(os.path.dirname(OUT), exist_ok=True)
+    deps = [SRC, os.path.join(ROOT, "tests", "host", "simt_host.h")] + [
+        os.path.join(CSRC, f) for f in ("poa_device.cuh", "poa_dp.cuh", "poa_window.cuh",
+                                        "poa_batch_mw.cuh")]
+    if not os.path.exists(OUT) or any(os.path.getmtime(d) > os.path.getmtime(OUT) for d in deps):
+        subprocess.run(["g++", "-std=c++20", "-O1", "-shared", "-fPIC", "-pthread", SRC, "-o",
+                        OUT], check=True)
+    L = C.CDLL(OUT)
+    I32, U32, P = C.c_int32, C.c_uint32, C.c_void_p
+    L.mw_run.argtypes = [I32] * 8 + [U32, P, C.c_char_p, P, P, P, P, C.c_char_p, P, P, P]
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def run_mw(L, windows, type_, params, W, strand):
+    reads = [r for w in windows for r in w]
+    wro = np.zeros(len(windows) + 1, np.uint32)
+    wro[1:] = np.cumsum([len(w) for w in windows])
+    off = np.zeros(len(reads) + 1, np.uint64)
+    off[1:] = np.cumsum([len(r) for r in reads])
+    st = np.full(len(windows), 1 if strand else 0, np.int8)
+    scores, rev = np.zeros(len(reads), np.int32), np.zeros(len(reads), np.uint8)
+    coff = np.zeros(len(windows) + 1, np.uint64)
+    coff[1:] = np.cumsum([4 * max(len(r) for r in w) + 64 for w in windows])
+    cons = C.create_string_buffer(int(coff[-1]) + 1)
+    clen = np.zeros(len(windows), np.uint32)
+    status = np.full(len(windows), -1, np.int32)
+    L.mw_run(type_, *params, W, len(windows), _ptr(wro), b"".join(reads), _ptr(off), _ptr(st),
+             _ptr(scores), _ptr(rev), cons, _ptr(coff), _ptr(clen), _ptr(status))
+    return (status.tolist(), scores.tolist(), rev.tolist(),
+            [cons.raw[int(coff[w]):int(coff[w]) + int(clen[w])].decode()
+             for w in range(len(windows))])
+
+
+@pytest.mark.parametrize("W,strand", [(2, False), (4, True)])
+def test_windows_per_cta_match_the_oracle(mw, W, strand):
+    rng = np.random.default_rng(77)
+    windows = [synth.random_window(rng, 50 + 9 * k, 2 + k % 5, err=0.12) for k in range(7)]
+    params = synth.SCORING["batch_10k"][1]
+    status, scores, rev, cons = run_mw(mw, windows, 2, params, W, strand)
+    assert status == [0] * len(windows)
+    r0 = 0
+    for w, win in enumerate(windows):
+        ref = po.run_window(2, *params, win, strand_ambiguous=strand, with_msa=False)
+        n = len(win)
+        assert scores[r0:r0 + n] == ref.scores, (W, strand, w)
+        assert rev[r0:r0 + n] == [int(x) for x in ref.reversed], (W, strand, w)
+        assert cons[w] == ref.consensus, (W, strand, w)
+        r0 += n
