@@ -12,7 +12,7 @@ using namespace spoa_gb300;
 
 namespace {
 
-template <int SUB, int CPT, typename T>
+template <int SUB, int CPT, typename T, int SEGS = 1>
 int32_t run(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t* off,
             const char* quals, int32_t strand, uint32_t nt, int32_t* scores, int32_t* rev,
             int32_t* aln, uint64_t aln_cap, uint64_t* aln_off, char* cons, uint32_t cons_cap,
@@ -28,7 +28,7 @@ int32_t run(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t
   GraphView G;
   std::vector<uint8_t> gbuf(graph_layout(nullptr, gc, &G) + 256);
   graph_layout(gbuf.data(), gc, &G);
-  DpCaps dc{gc.nodes + 1, CPT * nt, gc.edges + gc.nodes + 2, S.sub, sizeof(T)};
+  DpCaps dc{gc.nodes + 1, CPT * nt * SEGS, gc.edges + gc.nodes + 2, S.sub, sizeof(T)};
   DpView D;
   std::vector<uint8_t> dbuf(dp_layout(nullptr, dc, &D) + 256);
   dp_layout(dbuf.data(), dc, &D);
@@ -45,8 +45,8 @@ int32_t run(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t
     const int32_t* pairs = nullptr;
     uint32_t np = 0;
     simt::launch(nt, [&] {
-      window_read<SUB, CPT, T>(S, G, D, sh, ss, seq, L, qual, strand != 0, &score, &rv, &pairs,
-                               &np);
+      window_read<SUB, CPT, T, SEGS>(S, G, D, sh, ss, seq, L, qual, strand != 0, &score, &rv,
+                                     &pairs, &np);
     });
     if (ss.status != kOk) return ss.status;
     scores[r] = score;
@@ -78,9 +78,9 @@ extern "C" int32_t wh_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t
     c = e;
   }
   const Scoring S{type, sub, m, n, g, e, q, c};
-#define RUN(SUBV, C, TT)                                                                        \
-  return run<SUBV, C, TT>(S, n_reads, seqs, off, quals, strand, nt, scores, rev, aln, aln_cap, \
-                          aln_off, cons, cons_cap, cons_len)
+#define RUN(SUBV, C, TT, ...)                                                              \
+  return run<SUBV, C, TT, ##__VA_ARGS__>(S, n_reads, seqs, off, quals, strand, nt, scores, rev, \
+                                         aln, aln_cap, aln_off, cons, cons_cap, cons_len)
 #define BY_SUB(C, TT)                   \
   switch (sub) {                        \
     case kLinear: RUN(kLinear, C, TT);  \
@@ -89,6 +89,13 @@ extern "C" int32_t wh_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t
   }
   if (cpt == 8) {
     if (wide) BY_SUB(8, int32_t) else BY_SUB(8, int16_t)
+  }
+  if (cpt == -12) {  // the segmented forward: two 12-column strips per thread, 32-bit lanes
+    switch (sub) {
+      case kLinear: RUN(kLinear, 12, int32_t, 2);
+      case kAffine: RUN(kAffine, 12, int32_t, 2);
+      default: RUN(kConvex, 12, int32_t, 2);
+    }
   }
   if (wide) BY_SUB(16, int32_t) else BY_SUB(16, int16_t)
 #undef BY_SUB

@@ -108,3 +108,19 @@ def test_two_warp_ctas_and_int32_rows(wh):
                "params": list(params), "strand_ambiguous": False, "name": f"{k}{params}"}
         assert _check_window(wh, rec) == 64
         assert _check_window(wh, rec, wide=True) == 64
+
+
+def test_segmented_rows(wh):
+    """The segmented forward (dp_forward_seg: two 12-column strips per
+    thread, the scan carries handed from strip to strip) on 32-bit rows."""
+    from spoa_gb300 import synth
+    w = synth.long_10k(8, n_reads=3, tpl_len=560, min_len=500)
+    reads = list(w.reads)
+    for typ, params in ((0, (5, -4, -8, -6, -10, -4)), (1, (5, -4, -8, -6, -8, -6))):
+        st, scores, rev, alns, cons = run_host(wh, typ, params, reads, None, False, -12, 32, True)
+        assert st == 0
+        ref = po.run_window(typ, *params, reads, with_msa=False)
+        assert scores == ref.scores
+        for a, b in zip(alns, ref.alignments):
+            assert np.array_equal(a, b)
+        assert cons == ref.consensus
