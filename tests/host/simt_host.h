@@ -134,6 +134,28 @@ static inline T __shfl_xor_sync(unsigned, T v, unsigned m) {
   return out;
 }
 
+template <typename T>
+static inline T __shfl_sync(unsigned, T v, int src) {
+  int32_t bits;
+  std::memcpy(&bits, &v, sizeof(bits));
+  const int32_t r = simt::exchange(bits, (unsigned)src % 32);
+  T out;
+  std::memcpy(&out, &r, sizeof(out));
+  return out;
+}
+
+static inline unsigned __ballot_sync(unsigned, int pred) {
+  unsigned m = 0;
+  for (unsigned l = 0; l < 32; ++l) m |= (unsigned)(simt::exchange(pred ? 1 : 0, l) != 0) << l;
+  return m;
+}
+
+static inline int __ffs(unsigned x) { return x ? __builtin_ctz(x) + 1 : 0; }
+
+static inline void __syncwarp(unsigned = 0xffffffffu) {
+  if (simt::cta()) simt::cta()->warp[threadIdx.x / 32]->arrive_and_wait();
+}
+
 // ---- SIMD integer intrinsics, per their documented lane semantics ----
 namespace simt {
 inline int32_t lo16(uint32_t x) { return (int16_t)(x & 0xFFFFu); }
