@@ -149,6 +149,16 @@ int32_t spoa_gb300_graph_export(const spoa_gb300_graph* graph, uint8_t* chars, u
                                 uint32_t* labels, uint32_t* rank_to_node, uint32_t* seq_begin,
                                 uint32_t* consensus, int32_t* coder256, int32_t* decoder256);
 
+/* GFA 1.0 text of the graph in the layout of the reference CLI's PrintGfa
+ * (src/main.cpp:119-199): headers holds one name per sequence (NULL: read0,
+ * read1, ...), is_reversed one flag per sequence for reads kept on the
+ * reverse strand (NULL: none), and include_consensus adds the path of the
+ * last consensus.  *len gets the byte count; out (when not NULL) the text
+ * if cap is large enough (SPOA_GB300_ERR_CAPACITY otherwise). */
+int32_t spoa_gb300_graph_gfa(const spoa_gb300_graph* graph, const char* const* headers,
+                             const uint8_t* is_reversed, int32_t include_consensus, char* out,
+                             uint64_t cap, uint64_t* len);
+
 /* Replaces Graph::Subgraph (src/graph.cpp:518-595): `out` (an existing
  * graph, emptied first) receives the part of `graph` reachable from node
  * `end` over in-edges and aligned nodes, not below node id `begin`,

@@ -111,7 +111,8 @@ EXPORTED = [
     "spoa_gb300_graph_add_alignment_quality", "spoa_gb300_align_add",
     "spoa_gb300_align_add_reads",
     "spoa_gb300_graph_consensus", "spoa_gb300_graph_msa", "spoa_gb300_graph_counts",
-    "spoa_gb300_graph_export", "spoa_gb300_graph_subgraph", "spoa_gb300_graph_save",
+    "spoa_gb300_graph_export", "spoa_gb300_graph_gfa", "spoa_gb300_graph_subgraph",
+    "spoa_gb300_graph_save",
     "spoa_gb300_graph_load", "spoa_gb300_batch_create",
     "spoa_gb300_batch_launch",
     "spoa_gb300_batch_launch_plain", "spoa_gb300_batch_fetch", "spoa_gb300_batch_destroy",
@@ -154,6 +155,7 @@ def lib():
         L.spoa_gb300_graph_counts.argtypes = [P] * 7
         L.spoa_gb300_graph_export.argtypes = [P] * 19
         L.spoa_gb300_graph_subgraph.argtypes = [P, U32, U32, P, P, U32]
+        L.spoa_gb300_graph_gfa.argtypes = [P, P, P, I32, C.c_char_p, U64, P]
         L.spoa_gb300_graph_save.argtypes = [P, P, U64, P]
         L.spoa_gb300_graph_load.argtypes = [P, P, U64]
         L.spoa_gb300_batch_create.argtypes = [C.POINTER(_BatchDesc), P]
@@ -396,6 +398,23 @@ class Graph:
                 it = nxt
             res.append(np.array(path, np.uint32))
         return res
+
+    def gfa_text(self, is_reversed=None, headers=None, include_consensus=True) -> str:
+        """The same GFA as gfa(), written by the library
+        (spoa_gb300_graph_gfa) into one string."""
+        names = None
+        if headers is not None:
+            enc = [h.encode() if isinstance(h, str) else bytes(h) for h in headers]
+            names = (C.c_char_p * len(enc))(*enc)
+        rev = (np.ascontiguousarray(np.asarray(is_reversed, np.uint8))
+               if is_reversed is not None and len(is_reversed) else None)
+        n = C.c_uint64()
+        args = (self._h, names, _ptr(rev) if rev is not None else None,
+                1 if include_consensus else 0)
+        _check("Graph::gfa", lib().spoa_gb300_graph_gfa(*args, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(max(n.value, 1))
+        _check("Graph::gfa", lib().spoa_gb300_graph_gfa(*args, buf, n.value, C.byref(n)))
+        return buf.raw[:n.value].decode()
 
     def gfa(self, is_reversed=None, headers=None, include_consensus=True) -> list:
         """GFA lines in the layout of spoa's CLI writer (src/main.cpp:119-199);

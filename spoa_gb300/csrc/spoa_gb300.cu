@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "../../include/spoa_gb300.h"
+#include "gfa_text.h"
 #define SPOA_GB300_HOST_TU
 #include "poa_kernels.cuh"
 
@@ -722,6 +723,32 @@ int32_t spoa_gb300_graph_export(const spoa_gb300_graph* g, uint8_t* chars, uint8
   for (int k = 0; k < 18; ++k)
     if (items[k].host && items[k].bytes)
       CU(cudaMemcpy(items[k].host, b + offs[k], items[k].bytes, cudaMemcpyDeviceToHost));
+  return kOk;
+}
+
+int32_t spoa_gb300_graph_gfa(const spoa_gb300_graph* g, const char* const* headers,
+                             const uint8_t* is_reversed, int32_t include_consensus, char* out,
+                             uint64_t cap, uint64_t* len) {
+  if (!g || !len) return kInvalidArgument;
+  const GraphHeader& h = g->h;
+  const uint32_t N = h.n_nodes, E = h.n_edges;
+  std::vector<uint8_t> chars(N + 1);
+  std::vector<uint32_t> out_off(N + 2), out_e(E + 1), head(E + 1), lab_off(E + 2),
+      labels(h.n_labels + 1), sb(h.n_seqs + 1), cons(h.n_consensus + 1);
+  std::vector<int64_t> weight(E + 1);
+  const int32_t st = spoa_gb300_graph_export(g, chars.data(), nullptr, nullptr, nullptr,
+                                             out_off.data(), out_e.data(), nullptr, nullptr,
+                                             nullptr, head.data(), weight.data(), lab_off.data(),
+                                             labels.data(), nullptr, sb.data(), cons.data(),
+                                             nullptr, nullptr);
+  if (st) return st;
+  GfaGraph gg{N, h.n_seqs, h.n_consensus, chars.data(), out_off.data(), out_e.data(),
+              head.data(), weight.data(), lab_off.data(), labels.data(), sb.data(), cons.data()};
+  const std::string text = gfa_text(gg, headers, is_reversed, include_consensus != 0);
+  *len = text.size();
+  if (!out) return kOk;
+  if (text.size() > cap) return kCapacity;
+  std::memcpy(out, text.data(), text.size());
   return kOk;
 }
 

@@ -349,3 +349,21 @@ def test_load_rejects_malformed_bytes():
             sg.Graph().load(bad)
         assert ex.value.status == 1
     assert sg.Graph().load(blob).generate_consensus() == "ACGTACGT"
+
+
+def test_library_gfa_text(ref_windows):
+    """spoa_gb300_graph_gfa (GFA written by the library into a caller buffer)
+    equals the GFA pinned by the recorded reference runs."""
+    from conftest import sha
+    for rec in ref_windows[::21]:
+        engine = sg.AlignmentEngine.create(rec["type"], *rec["params"])
+        graph = sg.Graph()
+        rev = []
+        for k, r in enumerate(rec["reads"]):
+            q = rec["quals"][k] if rec["quals"] else None
+            _, rv = sg.align_add(engine, graph, r, q, rec["strand_ambiguous"])
+            rev.append(int(rv))
+        graph.generate_consensus()
+        text = graph.gfa_text(rev if rec["strand_ambiguous"] else None)
+        assert sha(text[:-1]) == rec["expect"]["gfa_sha"], rec["name"]
+        assert text == "\n".join(graph.gfa(rev if rec["strand_ambiguous"] else None)) + "\n"
