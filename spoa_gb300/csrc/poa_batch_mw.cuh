@@ -27,16 +27,13 @@ struct MwSlot {
   unsigned long long cells, pred_cells;
 };
 
-// Bytes of one slot after its graph arena: the chosen alignment (aln_cap
-// pairs) and the chosen read (ld bytes).
-__host__ __device__ inline uint64_t mw_slot_bytes(const DpCaps& dc, uint64_t aln_cap) {
-  return align_up(8 * aln_cap, 256) + align_up(dc.ld, 256);
-}
-
-// The CTA's arena: the DP arena, then W x (graph arena, slot buffers).
+// The CTA's arena: the DP arena, then per slot its graph arena, the chosen
+// alignment (aln_cap pairs), the add's pre-pass results (two words per
+// pair, g_add_prepass) and the chosen read (ld bytes).
 __host__ __device__ inline uint64_t mw_layout(uint8_t* base, int W, const GraphCaps& gc,
                                               const DpCaps& dc, DpView* D, GraphView* Gs,
-                                              int32_t** pairs, uint8_t** reads) {
+                                              int32_t** pairs, uint8_t** reads,
+                                              uint32_t** pre = nullptr) {
   uint64_t off = align_up(dp_layout(base, dc, D), 256);
   for (int s = 0; s < W; ++s) {
     GraphView g;
@@ -44,6 +41,8 @@ __host__ __device__ inline uint64_t mw_layout(uint8_t* base, int W, const GraphC
     if (Gs) Gs[s] = g;
     off += gb;
     if (pairs) pairs[s] = base ? reinterpret_cast<int32_t*>(base + off) : nullptr;
+    off += align_up(8 * D->aln_cap, 256);
+    if (pre) pre[s] = base ? reinterpret_cast<uint32_t*>(base + off) : nullptr;
     off += align_up(8 * D->aln_cap, 256);
     if (reads) reads[s] = base ? base + off : nullptr;
     off += align_up(dc.ld, 256);
@@ -56,12 +55,12 @@ struct MwShared {
   uint32_t dims[2];
 };
 
-// Every thread calls; Gs, slot_pairs and slot_reads have W entries each
-// (shared memory), D is the CTA's DP view.
+// Every thread calls; Gs, slot_pairs, slot_reads and slot_pre have W
+// entries each (shared memory), D is the CTA's DP view.
 template <int SUB, int CPT, typename T, int W>
 __device__ void batch_cta_mw(const BatchArgs& a, BlockScratch& sh, SharedState& ss, MwSlot* slot,
                              GraphView* Gs, DpView& D, int32_t** slot_pairs, uint8_t** slot_reads,
-                             MwShared& m) {
+                             uint32_t** slot_pre, MwShared& m) {
   Scoring S = a.base;
   auto fill = [&](int s) {  // thread 0: the slot's next window
     const uint32_t k = atomicAdd(a.queue, 1u);
@@ -135,6 +134,8 @@ __device__ void batch_cta_mw(const BatchArgs& a, BlockScratch& sh, SharedState& 
         for (uint32_t k = threadIdx.x; k < L; k += blockDim.x) slot_reads[s][k] = chosen[k];
         if (threadIdx.x == 0 && V0 && ss.mode == 1)
           slot[s].pred_cells += (unsigned long long)D.pred_ptr[V0 + 1] * L * (strand ? 2u : 1u);
+        // the add's read-only half on the whole CTA, before the graph changes
+        g_add_prepass(G, pairs, np, chosen, L, slot_pre[s]);
       }
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -161,7 +162,7 @@ __device__ void batch_cta_mw(const BatchArgs& a, BlockScratch& sh, SharedState& 
         const uint8_t* qual = a.quals ? a.quals + a.seq_off[r] : nullptr;
         WeightSrc ws{nullptr, qual, q.L, q.rev ? 1u : 0u, 1u};
         int32_t st = g_add_alignment(G, slot_pairs[threadIdx.x], q.np, slot_reads[threadIdx.x],
-                                     q.L, ws);
+                                     q.L, ws, slot_pre[threadIdx.x]);
         if (st == kOk && q.L > 0) {
           const uint32_t words = 3 * ((G.hdr->n_nodes + 31) / 32);
           for (uint32_t k = 0; k < words; ++k) G.sort_bits[k] = 0;

@@ -310,11 +310,13 @@ __global__ void __maxnreg__(kBatchMaxRegs<T>) k_batch_mw(BatchArgs a) {
   __shared__ DpView D;
   __shared__ int32_t* pairs[W];
   __shared__ uint8_t* reads[W];
+  __shared__ uint32_t* pre[W];
   __shared__ MwShared m;
   if (threadIdx.x == 0)
-    mw_layout(a.arena + a.arena_stride * blockIdx.x, W, a.gcaps, a.dcaps, &D, Gs, pairs, reads);
+    mw_layout(a.arena + a.arena_stride * blockIdx.x, W, a.gcaps, a.dcaps, &D, Gs, pairs, reads,
+              pre);
   __syncthreads();
-  batch_cta_mw<SUB, CPT, T, W>(a, sh, ss, slot, Gs, D, pairs, reads, m);
+  batch_cta_mw<SUB, CPT, T, W>(a, sh, ss, slot, Gs, D, pairs, reads, pre, m);
 }
 
 }  // namespace spoa_gb300

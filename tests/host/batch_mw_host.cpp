@@ -15,7 +15,7 @@ template <int SUB, int W>
 int32_t run(const Scoring& S, uint32_t n_windows, const uint32_t* wro, const char* seqs,
             const uint64_t* off, int32_t* scores, uint8_t* rev, char* cons,
             const uint64_t* cons_off, uint32_t* cons_len, int32_t* win_status,
-            const int8_t* strands) {
+            const int8_t* strands, const char* quals) {
   constexpr int CPT = 8;
   const uint32_t n_reads = wro[n_windows];
   uint64_t maxsum = 1;
@@ -34,8 +34,9 @@ int32_t run(const Scoring& S, uint32_t n_windows, const uint32_t* wro, const cha
   GraphView Gs[W];
   int32_t* pairs[W];
   uint8_t* reads[W];
+  uint32_t* pre[W];
   std::vector<uint8_t> arena(mw_layout(nullptr, W, gc, dc, &D, nullptr, nullptr, nullptr) + 256);
-  mw_layout(arena.data(), W, gc, dc, &D, Gs, pairs, reads);
+  mw_layout(arena.data(), W, gc, dc, &D, Gs, pairs, reads, pre);
   std::vector<uint32_t> work(n_windows);
   for (uint32_t w = 0; w < n_windows; ++w) work[w] = w;
   uint32_t queue = 0;
@@ -47,6 +48,7 @@ int32_t run(const Scoring& S, uint32_t n_windows, const uint32_t* wro, const cha
   a.win_read_off = wro;
   a.seqs = reinterpret_cast<const uint8_t*>(seqs);
   a.seq_off = off;
+  a.quals = reinterpret_cast<const uint8_t*>(quals);
   a.work = work.data();
   a.n_work = n_windows;
   a.queue = &queue;
@@ -62,7 +64,7 @@ int32_t run(const Scoring& S, uint32_t n_windows, const uint32_t* wro, const cha
   SharedState ss;
   MwSlot slot[W];
   MwShared m;
-  simt::launch(nt, [&] { batch_cta_mw<SUB, CPT, int16_t, W>(a, sh, ss, slot, Gs, D, pairs, reads, m); });
+  simt::launch(nt, [&] { batch_cta_mw<SUB, CPT, int16_t, W>(a, sh, ss, slot, Gs, D, pairs, reads, pre, m); });
   (void)n_reads;
   return kOk;
 }
@@ -73,7 +75,7 @@ extern "C" int32_t mw_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t
                           int32_t c, int32_t W, uint32_t n_windows, const uint32_t* wro,
                           const char* seqs, const uint64_t* off, const int8_t* strands,
                           int32_t* scores, uint8_t* rev, char* cons, const uint64_t* cons_off,
-                          uint32_t* cons_len, int32_t* win_status) {
+                          uint32_t* cons_len, int32_t* win_status, const char* quals) {
   const int32_t sub = g >= e ? kLinear : ((g <= q || e >= c) ? kAffine : kConvex);
   if (sub == kLinear) {
     e = g;
@@ -84,7 +86,7 @@ extern "C" int32_t mw_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t
   const Scoring S{type, sub, m, n, g, e, q, c};
 #define RUN(SUBV, WV) \
   return run<SUBV, WV>(S, n_windows, wro, seqs, off, scores, rev, cons, cons_off, cons_len, \
-                       win_status, strands)
+                       win_status, strands, quals)
 #define BY_SUB(WV)                    \
   switch (sub) {                      \
     case kLinear: RUN(kLinear, WV);   \

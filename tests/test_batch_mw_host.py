@@ -2,7 +2,7 @@
 run on the host by the SIMT emulation (tests/host/batch_mw_host.cpp): one
 CTA takes every window of a small batch from the queue; each window's read
 scores, strand choices and consensus must equal the oracle's, for W = 2
-(one strand) and W = 4 (strand-ambiguous).  (W = 1 is the one-window loop of
+(one strand, quality weights) and W = 4 (strand-ambiguous).  (W = 1 is the one-window loop of
 the batched kernel; tests/test_window_host.py covers its device code.)"""
 import ctypes as C
 import os
@@ -34,7 +34,8 @@ def mw():
                         OUT], check=True)
     L = C.CDLL(OUT)
     I32, U32, P = C.c_int32, C.c_uint32, C.c_void_p
-    L.mw_run.argtypes = [I32] * 8 + [U32, P, C.c_char_p, P, P, P, P, C.c_char_p, P, P, P]
+    L.mw_run.argtypes = [I32] * 8 + [U32, P, C.c_char_p, P, P, P, P, C.c_char_p, P, P, P,
+                                     C.c_char_p]
     return L
 
 
@@ -42,7 +43,7 @@ def _ptr(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
-def run_mw(L, windows, type_, params, W, strand):
+def run_mw(L, windows, type_, params, W, strand, quals=None):
     reads = [r for w in windows for r in w]
     wro = np.zeros(len(windows) + 1, np.uint32)
     wro[1:] = np.cumsum([len(w) for w in windows])
@@ -56,22 +57,26 @@ def run_mw(L, windows, type_, params, W, strand):
     clen = np.zeros(len(windows), np.uint32)
     status = np.full(len(windows), -1, np.int32)
     L.mw_run(type_, *params, W, len(windows), _ptr(wro), b"".join(reads), _ptr(off), _ptr(st),
-             _ptr(scores), _ptr(rev), cons, _ptr(coff), _ptr(clen), _ptr(status))
+             _ptr(scores), _ptr(rev), cons, _ptr(coff), _ptr(clen), _ptr(status),
+             b"".join(q for w in quals for q in w) if quals else None)
     return (status.tolist(), scores.tolist(), rev.tolist(),
             [cons.raw[int(coff[w]):int(coff[w]) + int(clen[w])].decode()
              for w in range(len(windows))])
 
 
-@pytest.mark.parametrize("W,strand", [(2, False), (4, True)])
-def test_windows_per_cta_match_the_oracle(mw, W, strand):
+@pytest.mark.parametrize("W,strand,with_quals", [(2, False, True), (4, True, False)])
+def test_windows_per_cta_match_the_oracle(mw, W, strand, with_quals):
     rng = np.random.default_rng(77)
     windows = [synth.random_window(rng, 50 + 9 * k, 2 + k % 5, err=0.12) for k in range(7)]
+    quals = ([[bytes(rng.integers(33, 75, size=len(r)).astype(np.uint8)) for r in w]
+              for w in windows] if with_quals else None)
     params = synth.SCORING["batch_10k"][1]
-    status, scores, rev, cons = run_mw(mw, windows, 2, params, W, strand)
+    status, scores, rev, cons = run_mw(mw, windows, 2, params, W, strand, quals)
     assert status == [0] * len(windows)
     r0 = 0
     for w, win in enumerate(windows):
-        ref = po.run_window(2, *params, win, strand_ambiguous=strand, with_msa=False)
+        ref = po.run_window(2, *params, win, quals[w] if quals else None,
+                            strand_ambiguous=strand, with_msa=False)
         n = len(win)
         assert scores[r0:r0 + n] == ref.scores, (W, strand, w)
         assert rev[r0:r0 + n] == [int(x) for x in ref.reversed], (W, strand, w)
