@@ -17,7 +17,6 @@ int32_t run(const Scoring& S, uint32_t n_windows, const uint32_t* wro, const cha
             const uint64_t* cons_off, uint32_t* cons_len, int32_t* win_status,
             const int8_t* strands, const char* quals) {
   constexpr int CPT = 8;
-  const uint32_t n_reads = wro[n_windows];
   uint64_t maxsum = 1;
   uint32_t lmax = 1, maxreads = 1;
   for (uint32_t w = 0; w < n_windows; ++w) {
@@ -65,7 +64,6 @@ int32_t run(const Scoring& S, uint32_t n_windows, const uint32_t* wro, const cha
   MwSlot slot[W];
   MwShared m;
   simt::launch(nt, [&] { batch_cta_mw<SUB, CPT, int16_t, W>(a, sh, ss, slot, Gs, D, pairs, reads, pre, m); });
-  (void)n_reads;
   return kOk;
 }
 
