@@ -196,17 +196,23 @@ def cpu_baseline(wins, typ, params, wtypes, wstrand, seconds):
     per_window = dt / max(len(probe), 1) * threads
     n = int(min(len(wins), max(len(probe), seconds / per_window * threads)))
     sample = wins[:n]
+    secs = []
     t0 = time.perf_counter()
-    cons, cells = _run_oracle(po, sample, typ, params, wtypes, wstrand, threads)
+    cons, cells = _run_oracle(po, sample, typ, params, wtypes, wstrand, threads, secs)
     dt = time.perf_counter() - t0
+    secs.sort()
+    pct = lambda f: secs[min(len(secs) - 1, int(f * len(secs)))] if secs else None  # noqa: E731
     return {"value": n / dt, "unit": "windows/s", "cores": threads, "kind": "port",
             "sample": f"first {n} windows of the workload, {dt:.1f} s, {cells / dt / 1e9:.3f} GCUPS",
+            "window_seconds_p50": pct(0.50), "window_seconds_p99": pct(0.99),
             "consensus": cons, "n": n}
 
 
-def _run_oracle(po, wins, typ, params, wtypes, wstrand, threads):
+def _run_oracle(po, wins, typ, params, wtypes, wstrand, threads, secs=None):
+    """The oracle on host threads; secs (a list) gets per-window wall times."""
     if wtypes is None:
-        return po.batch_run(typ, *params, [w.reads for w in wins], n_threads=threads)
+        return po.batch_run(typ, *params, [w.reads for w in wins], n_threads=threads,
+                            window_seconds=secs)
     # per-window type/strand: group by (type, strand)
     cons = [None] * len(wins)
     cells = 0
@@ -215,7 +221,7 @@ def _run_oracle(po, wins, typ, params, wtypes, wstrand, threads):
         groups.setdefault((wtypes[k], wstrand[k]), []).append(k)
     for (t, s), idx in groups.items():
         c, ce = po.batch_run(t, *params, [wins[k].reads for k in idx], strand_ambiguous=bool(s),
-                             n_threads=threads)
+                             n_threads=threads, window_seconds=secs)
         cells += ce
         for k, cc in zip(idx, c):
             cons[k] = cc

@@ -87,7 +87,7 @@ def lib():
                                         P, C.c_char_p, P, P, P, C.c_uint64, P]
         L.oracle_batch_run.argtypes = [C.POINTER(WindowParams), C.c_uint32, P, C.c_char_p,
                                        P, C.c_char_p, C.c_int32, C.c_char_p, C.c_uint64,
-                                       P, P, P]
+                                       P, P, P, P]
         _lib = L
     return _lib
 
@@ -187,9 +187,10 @@ def run_window(type_: int, m: int, n: int, g: int, e: int, q: int, c: int,
 
 def batch_run(type_: int, m: int, n: int, g: int, e: int, q: int, c: int,
               windows: list[list[bytes]], strand_ambiguous: bool = False,
-              n_threads: int | None = None):
+              n_threads: int | None = None, window_seconds: list | None = None):
     """Many windows on host threads (one window per task).  Returns
-    (consensus list, matrix cells)."""
+    (consensus list, matrix cells); window_seconds, when a list, gets each
+    window's wall time on its thread."""
     L = lib()
     p = WindowParams(type_, m, n, g, e, q, c, 1 if strand_ambiguous else 0)
     reads = [r for w in windows for r in w]
@@ -206,9 +207,12 @@ def batch_run(type_: int, m: int, n: int, g: int, e: int, q: int, c: int,
     cons = C.create_string_buffer(int(coff[-1]) + 1)
     cells = C.c_uint64()
     scores = np.zeros(max(len(reads), 1), np.int32)
+    secs = np.zeros(max(len(windows), 1), np.float64)
     st = L.oracle_batch_run(C.byref(p), len(windows), _ptr(wro), seqs, _ptr(off), None,
                             n_threads or os.cpu_count() or 1, cons, int(coff[-1]),
-                            _ptr(coff), _ptr(scores), C.byref(cells))
+                            _ptr(coff), _ptr(scores), C.byref(cells), _ptr(secs))
+    if window_seconds is not None:
+        window_seconds.extend(secs[:len(windows)].tolist())
     if st != 0:
         raise RuntimeError(f"oracle batch failed with status {st}")
     raw = cons.raw

@@ -26,6 +26,7 @@
  * (padding score <= every gap-open penalty), so they change neither row
  * maxima nor first-index searches and are not materialised.
  */
+#define _POSIX_C_SOURCE 199309L  /* clock_gettime */
 #include "spoa_oracle.h"
 
 #include <limits.h>
@@ -33,6 +34,7 @@
 #include <stdatomic.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 /* ------------------------------------------------------------------ */
 /* small growable vector                                               */
@@ -1363,10 +1365,17 @@ typedef struct {
   uint64_t cons_cap;
   uint64_t* cons_off; /* per window, fixed stride region start */
   int32_t* read_scores;
+  double* win_seconds; /* per window, wall time of its thread, or NULL */
   atomic_uint next;
   atomic_int status;
   atomic_ullong cells;
 } batch_ctx;
+
+static double now_seconds(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
 
 static void* batch_worker(void* arg) {
   batch_ctx* bc = (batch_ctx*)arg;
@@ -1378,6 +1387,7 @@ static void* batch_worker(void* arg) {
   for (;;) {
     uint32_t w = atomic_fetch_add(&bc->next, 1);
     if (w >= bc->n_windows) break;
+    const double t0 = bc->win_seconds ? now_seconds() : 0.0;
     oracle_graph_clear(g);
     uint32_t r0 = bc->win_read_off[w], r1 = bc->win_read_off[w + 1];
     uint64_t cells = 0;
@@ -1394,6 +1404,7 @@ static void* batch_worker(void* arg) {
       uint32_t n = oracle_consensus(g, bc->cons + a, (uint32_t)cap);
       if (n < cap) bc->cons[a + n] = 0;
     }
+    if (bc->win_seconds) bc->win_seconds[w] = now_seconds() - t0;
   }
   oracle_graph_destroy(g);
   return NULL;
@@ -1404,7 +1415,7 @@ int32_t oracle_batch_run(const oracle_window_params* p, uint32_t n_windows,
                          const uint64_t* seq_off, const char* quals,
                          int32_t n_threads, char* cons, uint64_t cons_cap,
                          uint64_t* cons_off, int32_t* read_scores,
-                         uint64_t* cells) {
+                         uint64_t* cells, double* win_seconds) {
   (void)cons_cap;
   batch_ctx bc;
   bc.p = p;
@@ -1417,6 +1428,7 @@ int32_t oracle_batch_run(const oracle_window_params* p, uint32_t n_windows,
   bc.cons_cap = cons_cap;
   bc.cons_off = cons_off;
   bc.read_scores = read_scores;
+  bc.win_seconds = win_seconds;
   atomic_init(&bc.next, 0);
   atomic_init(&bc.status, 0);
   atomic_init(&bc.cells, 0);

@@ -130,13 +130,14 @@ int32_t oracle_window_run(const oracle_window_params* p, oracle_graph* g,
 /* Many independent windows on a pool of host threads, one window per task
  * (each with its own engine and graph, the way spoa's callers scale it).
  * Writes per-window consensus (cons_off[w]..) and returns the number of
- * matrix cells (sum over reads of len x nodes) through *cells. */
+ * matrix cells (sum over reads of len x nodes) through *cells; win_seconds
+ * (NULL to skip) gets each window's wall time on its thread. */
 int32_t oracle_batch_run(const oracle_window_params* p, uint32_t n_windows,
                          const uint32_t* win_read_off, const char* seqs,
                          const uint64_t* seq_off, const char* quals,
                          int32_t n_threads, char* cons, uint64_t cons_cap,
                          uint64_t* cons_off, int32_t* read_scores,
-                         uint64_t* cells);
+                         uint64_t* cells, double* win_seconds);
 
 #ifdef __cplusplus
 }
