@@ -65,6 +65,7 @@ __device__ void batch_cta_mw(const BatchArgs& a, BlockScratch& sh, SharedState& 
   auto fill = [&](int s) {  // thread 0: the slot's next window
     const uint32_t k = atomicAdd(a.queue, 1u);
     MwSlot& q = slot[s];
+    q.pending = 0;  // shared memory starts undefined: an empty slot must not add
     q.w = k < a.n_work ? a.work[k] : kNone;
     if (q.w == kNone) return;
     q.r = a.win_read_off[q.w];

@@ -61,8 +61,11 @@ int32_t run(const Scoring& S, uint32_t n_windows, const uint32_t* wro, const cha
   a.pred_cells = cells + 1;
   BlockScratch sh;
   SharedState ss;
+  // shared memory starts with arbitrary contents: so does the emulation
   MwSlot slot[W];
   MwShared m;
+  std::memset(static_cast<void*>(slot), 0xAB, sizeof(slot));
+  std::memset(static_cast<void*>(&m), 0xAB, sizeof(m));
   simt::launch(nt, [&] { batch_cta_mw<SUB, CPT, int16_t, W>(a, sh, ss, slot, Gs, D, pairs, reads, pre, m); });
   return kOk;
 }

@@ -82,3 +82,13 @@ def test_windows_per_cta_match_the_oracle(mw, W, strand, with_quals):
         assert rev[r0:r0 + n] == [int(x) for x in ref.reversed], (W, strand, w)
         assert cons[w] == ref.consensus, (W, strand, w)
         r0 += n
+
+
+def test_fewer_windows_than_slots(mw):
+    """One window on a CTA of four slots: the empty slots stay idle."""
+    rng = np.random.default_rng(5)
+    windows = [synth.random_window(rng, 70, 4, err=0.1)]
+    params = synth.SCORING["batch_10k"][1]
+    status, scores, rev, cons = run_mw(mw, windows, 2, params, 4, False)
+    ref = po.run_window(2, *params, windows[0], with_msa=False)
+    assert status == [0] and scores == ref.scores and cons == [ref.consensus]
