@@ -20,8 +20,15 @@ roofline  HBM view: algorithmic bytes (the 4-bit traceback state of every
           2d+1, affine 3d+3, convex 5d+4, +1 for SW, d the row's
           predecessors, against a measured max/add rate), the bound that
           applies.
-cpu_baseline  the C oracle (the reference algorithm restated in C, one window
-          per host thread) on a bounded sample of the same workload.
+cpu_baseline  the reference's own library (oracle/ref_bench.cpp over the
+          reference sources: its SimdAlignmentEngine on an AVX2 host, its
+          SisdAlignmentEngine elsewhere), one window per host thread, on a
+          bounded sample of the same workload; the C oracle (the reference
+          algorithm restated in C) timed beside it.  Where the reference
+          sources are not staged, the C oracle alone.
+parity    a sample of the timed workload rerun with alignments returned,
+          every read's score and alignment and every consensus compared with
+          the oracle.
 
 Under torchrun every rank runs its own batch (weak scaling: windows are
 independent and are sharded with no collective); value is the sum of the
@@ -75,6 +82,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--windows-per-cta", type=int, default=1, choices=[1, 2, 4],
                     help="windows in flight per CTA (16-bit windows)")
+    ap.add_argument("--parity-windows", type=int, default=256,
+                    help="windows rerun with alignments and checked against the oracle")
     return ap.parse_args()
 
 
@@ -92,6 +101,12 @@ def max_over_ranks(value: float, dist, device: str) -> float:
     t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def common_config(cfg: dict, world: int) -> dict:
+    """The config keys both arms print (the workload, not the GPU's tile)."""
+    return dict(cfg, parallelism=f"windows sharded over {world} GPU(s), no collective",
+                l2="inputs and per-CTA arenas larger than L2 (129 MB)")
 
 
 def workload(name: str, n_override: int, rank: int):
@@ -184,17 +199,47 @@ def traffic_per_cell():
     return None
 
 
+def _types_strands(wins, typ, wtypes, wstrand):
+    types = wtypes if wtypes is not None else [typ] * len(wins)
+    strands = wstrand if wstrand is not None else [0] * len(wins)
+    return types, strands
+
+
+def _sample_size(wins, seconds, per_window, threads, floor):
+    return int(min(len(wins), max(floor, seconds / max(per_window, 1e-6) * threads)))
+
+
+def reference_cpu(wins, typ, params, wtypes, wstrand, seconds, threads, want_consensus=False):
+    """The reference's own library on `threads` host threads over a sample of
+    the workload sized to about `seconds`; None when it is not built."""
+    from oracle import pyoracle as po
+    if po.reference_bench() is None:
+        return None
+    types, strands = _types_strands(wins, typ, wtypes, wstrand)
+    k = min(len(wins), threads)
+    probe = po.run_reference_bench([w.reads for w in wins[:k]], types[:k], strands[:k], params,
+                                   threads)
+    per_window = probe["seconds"] / max(k, 1) * threads
+    n = _sample_size(wins, seconds, per_window, threads, k)
+    rec = po.run_reference_bench([w.reads for w in wins[:n]], types[:n], strands[:n], params,
+                                 threads, want_consensus=want_consensus)
+    rec["n"] = n
+    return rec
+
+
 def cpu_baseline(wins, typ, params, wtypes, wstrand, seconds):
+    """The reference library (kind "reference") and the C oracle (kind
+    "port") on all host threads, each on a bounded sample of the workload."""
     from oracle import pyoracle as po
     threads = os.cpu_count() or 1
     po.lib()
-    # estimate the cost of one window per thread, then size the sample
+    # the port: estimate the cost of one window per thread, then size the sample
     probe = wins[:threads]
     t0 = time.perf_counter()
     _run_oracle(po, probe, typ, params, wtypes, wstrand, threads)
     dt = max(time.perf_counter() - t0, 1e-3)
     per_window = dt / max(len(probe), 1) * threads
-    n = int(min(len(wins), max(len(probe), seconds / per_window * threads)))
+    n = _sample_size(wins, seconds, per_window, threads, len(probe))
     sample = wins[:n]
     secs = []
     t0 = time.perf_counter()
@@ -202,10 +247,29 @@ def cpu_baseline(wins, typ, params, wtypes, wstrand, seconds):
     dt = time.perf_counter() - t0
     secs.sort()
     pct = lambda f: secs[min(len(secs) - 1, int(f * len(secs)))] if secs else None  # noqa: E731
-    return {"value": n / dt, "unit": "windows/s", "cores": threads, "kind": "port",
-            "sample": f"first {n} windows of the workload, {dt:.1f} s, {cells / dt / 1e9:.3f} GCUPS",
+    port = {"value": n / dt, "unit": "windows/s", "cores": threads, "kind": "port",
+            "sample": f"first {n} windows of the workload, {dt:.1f} s, "
+                      f"{cells / dt / 1e9:.3f} GCUPS",
             "window_seconds_p50": pct(0.50), "window_seconds_p99": pct(0.99),
             "consensus": cons, "n": n}
+    ref = reference_cpu(wins, typ, params, wtypes, wstrand, seconds, threads,
+                        want_consensus=True)
+    if ref is None:
+        return port
+    rn = ref.pop("n")
+    rcons = ref.pop("consensus")
+    out = {"value": rn / ref["seconds"], "unit": "windows/s", "cores": ref["threads"],
+           "kind": "reference",
+           "engine": "spoa " + ("SimdAlignmentEngine" if ref["engine"] == "simd"
+                                else "SisdAlignmentEngine") + " (the reference's own library, "
+                                "built from its sources on this host)",
+           "sample": f"first {rn} windows of the workload, {ref['seconds']:.1f} s, "
+                     f"{ref['cells'] / ref['seconds'] / 1e9:.3f} GCUPS",
+           "window_seconds_p50": ref["window_seconds_p50"],
+           "window_seconds_p99": ref["window_seconds_p99"],
+           "reference_consensus": rcons, "reference_n": rn,
+           "consensus": port.pop("consensus"), "n": port.pop("n"), "port": port}
+    return out
 
 
 def _run_oracle(po, wins, typ, params, wtypes, wstrand, threads, secs=None):
@@ -250,6 +314,53 @@ def flatten(wins, pinned: bool):
     return seqs, off, wro
 
 
+def int_peaks():
+    """Integer max/add rates measured in this run: the 32-bit forms and the
+    16x2 forms (lane-operations per second), or (None, None)."""
+    try:
+        import ctypes as C
+        pl = C.CDLL(os.path.join(ROOT, "spoa_gb300", "libspoa_peak.so"))
+        pl.spoa_gb300_int_peak_ops.restype = C.c_double
+        pl.spoa_gb300_int_peak_ops16x2.restype = C.c_double
+        p32 = pl.spoa_gb300_int_peak_ops(4096)
+        p16 = pl.spoa_gb300_int_peak_ops16x2(4096)
+        return (p32 if p32 > 0 else None), (p16 if p16 > 0 else None)
+    except (OSError, AttributeError):
+        return None, None
+
+
+def parity_sample(sg, wins, typ, params, wtypes, wstrand, k, device):
+    """The first k windows rerun with alignments returned; every read's
+    score, strand and alignment and every consensus compared with the
+    oracle (run on host threads: the ctypes calls release the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import pyoracle as po
+    k = min(k, len(wins))
+    if k <= 0:
+        return None
+    types, strands = _types_strands(wins, typ, wtypes, wstrand)
+    res = sg.batch_poa([w.reads for w in wins[:k]], typ, *params, window_types=types[:k],
+                       window_strand=strands[:k], want_alignments=True, device=device)
+    po.lib()
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        refs = list(ex.map(lambda j: po.run_window(types[j], *params, wins[j].reads,
+                                                   strand_ambiguous=bool(strands[j]),
+                                                   with_msa=False), range(k)))
+    scores = aligns = cons = True
+    r0 = 0
+    for j, ref in enumerate(refs):
+        n = len(wins[j].reads)
+        scores &= res.scores[r0:r0 + n].tolist() == ref.scores and \
+            res.reversed[r0:r0 + n].tolist() == ref.reversed
+        aligns &= all(np.array_equal(a, b) for a, b in zip(res.alignments[r0:r0 + n],
+                                                           ref.alignments))
+        cons &= res.consensus[j] == ref.consensus
+        r0 += n
+    return {"windows": k, "reads": r0, "scores_equal": bool(scores),
+            "alignments_equal": bool(aligns), "consensus_equal": bool(cons)}
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -270,8 +381,10 @@ def main():
     import spoa_gb300 as sg
     if sg.lib().spoa_gb300_device_count() <= 0:
         raise SystemExit("no CUDA device visible")
+    # the library links its own CUDA runtime: name the rank's device to it
+    device = local if world > 1 else None
     if args.workload == "serve":
-        return serve(args, sg, rank, world, dist)
+        return serve(args, sg, rank, world, dist, device)
 
     wins, typ, params, wtypes, wstrand, cfg = workload(args.workload, args.windows, rank)
     n_windows = len(wins)
@@ -281,7 +394,7 @@ def main():
         return sg.Batch.from_arrays(seqs, off, wro, typ, *params, window_types=wtypes,
                                     window_strand=wstrand,
                                     autotune=args.workload == "batch_10k",
-                                    windows_per_cta=args.windows_per_cta)
+                                    windows_per_cta=args.windows_per_cta, device=device)
 
     batch = make_batch()
     for _ in range(args.warmup):
@@ -339,7 +452,7 @@ def main():
         ps, po_, pw = flatten(wins[:k], pinned=False)
         pb = sg.Batch.from_arrays(ps, po_, pw, typ, *params,
                                   window_types=wtypes[:k] if wtypes else None,
-                                  window_strand=wstrand[:k] if wstrand else None)
+                                  window_strand=wstrand[:k] if wstrand else None, device=device)
         pb.launch_plain()
         pr = pb.fetch()
         plain = {"value": k / (pr.kernel_ms / 1e3), "unit": "windows/s", "sample_windows": k,
@@ -353,20 +466,24 @@ def main():
     sub = batch.subtype
     a_, b_ = OPS[sub]
     ops = a_ * pred_cells + b_ * cells + (cells if typ == 0 else 0)
-    int_peak = None
-    try:
-        import ctypes as C
-        pl = C.CDLL(os.path.join(ROOT, "spoa_gb300", "libspoa_peak.so"))
-        pl.spoa_gb300_int_peak_ops.restype = C.c_double
-        int_peak = pl.spoa_gb300_int_peak_ops(4096)
-    except OSError:
-        pass
+    p32, p16 = int_peaks()
+    # the 16-bit kernels issue the 16x2 forms, the 32-bit ones the 32-bit forms
+    int_peak = p16 if DTYPES.get(args.workload) == "int16" else p32
     int_roof = None
-    if int_peak and int_peak > 0:
+    if int_peak:
         int_roof = {"achieved": ops / step_s / 1e9, "peak": int_peak / 1e9, "unit": "Gop/s",
                     "frac": ops / step_s / int_peak,
                     "ops_per_cell": ops / max(cells, 1),
-                    "peak_kind": "measured in this run (max/add probe)"}
+                    "peak_kind": "measured in this run: " + (
+                        "__viaddmax_s16x2 / __vimax3_s16x2 / __vadd2 chains, two lane-ops each"
+                        if int_peak is p16 else "__viaddmax_s32 / __vimax3_s32 / add chains"),
+                    "peak_s32": p32 / 1e9 if p32 else None,
+                    "peak_s16x2": p16 / 1e9 if p16 else None}
+
+    parity = None
+    if rank == 0 and args.parity_windows > 0:
+        parity = parity_sample(sg, wins, typ, params, wtypes, wstrand, args.parity_windows,
+                               device)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -375,6 +492,11 @@ def main():
         cons = cpu.pop("consensus")
         cpu["parity_sample_windows"] = k
         cpu["parity_sample_equal"] = bool(cons == res.consensus[:k])
+        if "reference_consensus" in cpu:
+            rc, rn = cpu.pop("reference_consensus"), cpu.pop("reference_n")
+            cpu["reference_consensus_equal_windows"] = int(
+                sum(a == b for a, b in zip(rc, res.consensus[:rn])))
+            cpu["reference_windows"] = rn
 
     line = {
         "metric": "windows/s", "value": value, "unit": "windows/s", "n_gpus": world,
@@ -382,10 +504,10 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": DTYPES.get(args.workload, "int16/int32"),
         "data": "synthetic (seeded; see spoa_gb300/synth.py)",
-        "config": dict(cfg, parallelism=f"windows sharded over {world} GPU(s), no collective",
-                       l2="inputs and per-CTA arenas larger than L2 (129 MB)",
-                       threads_per_window=res.threads_per_window,
-                       columns_per_thread=res.columns_per_thread, ctas=res.ctas),
+        "config": common_config(cfg, world),
+        "tile": {"threads_per_window": res.threads_per_window,
+                 "columns_per_thread": res.columns_per_thread, "ctas": res.ctas,
+                 "windows_per_cta": args.windows_per_cta},
         "gcups": gcups, "cells_per_step": cells * world,
         "e2e": e2e, "plain": plain,
         "gpu_launches": launches,
@@ -393,8 +515,11 @@ def main():
                      "frac": achieved_gbs / hbm_peak,
                      "traffic": (tpc * cells) if tpc else None,
                      "peak_kind": peak_kind,
-                     "algorithmic_bytes": "0.5 B per DP cell (4-bit traceback state)"},
+                     "algorithmic_bytes": "0.5 B per DP cell (4-bit traceback state)",
+                     "binding": "the integer max/add pipe (int_roofline); HBM is not the "
+                                "bound of this path"},
         "int_roofline": int_roof,
+        "parity": parity,
         "cpu_baseline": cpu,
         "clocks": clk,
         "wall_s": wall,
@@ -423,7 +548,7 @@ def serve_stream(n: int, rate: float, seed: int):
     return out
 
 
-def serve(args, sg, rank, world, dist):
+def serve(args, sg, rank, world, dist, device=None):
     """Served form: windows arrive over time (Poisson, at each offered load
     of --rates) and go through the continuous-batching server; reports the
     completed windows/s and the latency (completion minus arrival)
@@ -437,11 +562,11 @@ def serve(args, sg, rank, world, dist):
     for i, rate in enumerate(rates):
         stream = serve_stream(args.serve_windows, rate, seed=rank * 101 + i)
         # warm-up: the kernels of every width and class once
-        with sg.Server(2, *params) as sv:
+        with sg.Server(2, *params, device=device) as sv:
             for reads, typ, strand, _ in stream[:8]:
                 sv.wait(sv.submit(reads, typ, strand), timeout=600)
         cells = 0
-        with sg.Server(2, *params, gather_seconds=0.0005) as sv:
+        with sg.Server(2, *params, gather_seconds=0.0005, device=device) as sv:
             t0 = time.perf_counter()
             tickets = [sv.submit(r, t, s, a) for r, t, s, a in stream]
             res = [sv.wait(t, timeout=3600) for t in tickets]
@@ -474,34 +599,59 @@ def serve(args, sg, rank, world, dist):
 
 
 def reference_arm(args):
-    """The reference algorithm on the host cores (the C oracle: the
-    reference's own build is x86-only and its tree is not on the GPU machine)."""
+    """The reference's CPU implementation on all host cores: its own library
+    built from its sources (oracle/ref_bench.cpp; the SisdAlignmentEngine on
+    the aarch64 GPU machine, where the reference has no SIMD path), else the C
+    oracle.  Each step times a bounded sample of the same workload."""
     from oracle import pyoracle as po
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     wins, typ, params, wtypes, wstrand, cfg = workload(args.workload, args.windows, 0)
     threads = os.cpu_count() or 1
-    po.lib()
-    probe = wins[:threads]
-    t0 = time.perf_counter()
-    _run_oracle(po, probe, typ, params, wtypes, wstrand, threads)
-    per_window = max(time.perf_counter() - t0, 1e-3) / max(len(probe), 1) * threads
+    types, strands = _types_strands(wins, typ, wtypes, wstrand)
     total_steps = args.steps + args.warmup
     budget = 150.0 / max(total_steps, 1)
-    n = int(min(len(wins), max(len(probe), budget / per_window * threads)))
+    use_ref = po.reference_bench() is not None
+    if use_ref:
+        k = min(len(wins), threads)
+        probe = po.run_reference_bench([w.reads for w in wins[:k]], types[:k], strands[:k],
+                                       params, threads)
+        per_window = probe["seconds"] / max(k, 1) * threads
+        engine = probe["engine"]
+    else:
+        po.lib()
+        probe = wins[:threads]
+        t0 = time.perf_counter()
+        _run_oracle(po, probe, typ, params, wtypes, wstrand, threads)
+        per_window = max(time.perf_counter() - t0, 1e-3) / max(len(probe), 1) * threads
+    n = _sample_size(wins, budget, per_window, threads, min(len(wins), threads))
     sample = wins[:n]
+
+    def step():
+        if use_ref:
+            return po.run_reference_bench([w.reads for w in sample], types[:n], strands[:n],
+                                          params, threads)["seconds"]
+        t0 = time.perf_counter()
+        _run_oracle(po, sample, typ, params, wtypes, wstrand, threads)
+        return time.perf_counter() - t0
+
     for _ in range(args.warmup):
-        _run_oracle(po, sample, typ, params, wtypes, wstrand, threads)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        _run_oracle(po, sample, typ, params, wtypes, wstrand, threads)
-    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+        step()
+    dt = sum(step() for _ in range(args.steps)) / max(args.steps, 1)
     value = n / dt
+    kind = "reference" if use_ref else "port"
+    what = (("spoa SisdAlignmentEngine" if engine == "sisd" else "spoa SimdAlignmentEngine") +
+            " (the reference's own library, built from its sources on this host)"
+            if use_ref else "the C oracle (the reference algorithm restated in C)")
     line = {"impl": "reference", "metric": "windows/s", "value": value, "unit": "windows/s",
             "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic (seeded; see spoa_gb300/synth.py)", "config": cfg,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": DTYPES.get(args.workload, "int16/int32"),
+            "data": "synthetic (seeded; see spoa_gb300/synth.py)",
+            "config": common_config(cfg, world),
             "cpu_baseline": {"value": value, "unit": "windows/s", "cores": threads,
-                             "kind": "port",
-                             "sample": f"first {n} windows of the workload per step"},
+                             "kind": kind, "engine": what,
+                             "sample": f"first {n} windows of the workload per step "
+                                       f"(of {len(wins)}), one window per host thread"},
             "e2e": {"value": value, "unit": "windows/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

@@ -217,6 +217,11 @@ typedef struct {
   int32_t windows_per_cta;         /* 2 or 4: windows of 16-bit width in flight
                                       per CTA, their graph updates on parallel
                                       lanes; otherwise 1 */
+  int32_t device_set;              /* nonzero: the batch lives on `device`;
+                                      0: on the calling thread's current device
+                                      at batch_create.  Every later call on the
+                                      batch switches to that device and back. */
+  int32_t device;
 } spoa_gb300_batch_desc;
 
 typedef struct {
@@ -273,6 +278,9 @@ typedef struct {
   int32_t max_windows_per_launch; /* (0: 4096) */
   double gather_seconds;        /* wait this long after the oldest arrival to gather
                                    more windows into one launch (0: none) */
+  int32_t device_set;           /* nonzero: serve on `device`; 0: on the calling
+                                   thread's current device at server_create */
+  int32_t device;
 } spoa_gb300_server_desc;
 
 int32_t spoa_gb300_server_create(const spoa_gb300_server_desc* desc, spoa_gb300_server** out);
@@ -317,12 +325,19 @@ void spoa_gb300_server_destroy(spoa_gb300_server* server);
  * offsets, or NULL for weight 1), d_consensus (consensus_cap bytes),
  * d_consensus_len (1 value), d_read_scores (n_reads values, or NULL),
  * d_status (1 value: SPOA_GB300_OK, SPOA_GB300_ERR_CAPACITY when the window
- * outgrew the limits below, SPOA_GB300_ERR_OVERFLOW, or
+ * outgrew the device-checked limits below, SPOA_GB300_ERR_OVERFLOW, or
  * SPOA_GB300_ERR_NEEDS_INT32 when a read needs 32-bit scores).
- * Limits: n_reads <= SPOA_GB300_NOALLOC_MAX_READS, every read at most
- * max_read_len <= SPOA_GB300_NOALLOC_MAX_READ_LEN bases, at most
- * SPOA_GB300_NOALLOC_MAX_NODES graph nodes; larger sizes are rejected with
- * SPOA_GB300_ERR_TOO_LARGE before anything is launched.
+ * Limits checked on the host, before anything is launched (larger values
+ * return SPOA_GB300_ERR_TOO_LARGE): n_reads <= SPOA_GB300_NOALLOC_MAX_READS
+ * and max_read_len <= SPOA_GB300_NOALLOC_MAX_READ_LEN.
+ * Limits checked on the device, reported in *d_status as
+ * SPOA_GB300_ERR_CAPACITY (the host cannot see device-resident reads or the
+ * graph): every read at most as long as the max_read_len passed in (more
+ * precisely, the column tile chosen for it), at most
+ * SPOA_GB300_NOALLOC_MAX_NODES graph nodes, at most
+ * SPOA_GB300_NOALLOC_MAX_ALIGNED nodes aligned to any node (one column of
+ * the MSA holds at most that many + 1 different letters), a consensus of at
+ * most consensus_cap bases.
  * The first call on a device looks up the array's device address; make it
  * before any stream capture.  All calls share the one array, so calls that
  * overlap on the GPU (other streams, other host threads) race with each
@@ -331,6 +346,7 @@ void spoa_gb300_server_destroy(spoa_gb300_server* server);
 #define SPOA_GB300_NOALLOC_MAX_READS 256
 #define SPOA_GB300_NOALLOC_MAX_READ_LEN 640
 #define SPOA_GB300_NOALLOC_MAX_NODES 4096
+#define SPOA_GB300_NOALLOC_MAX_ALIGNED 63
 #define SPOA_GB300_ERR_NEEDS_INT32 11
 int32_t spoa_gb300_window_poa_noalloc(int32_t type, int8_t m, int8_t n, int8_t g, int8_t e,
                                       int8_t q, int8_t c, int32_t strand_ambiguous,

@@ -15,6 +15,10 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 _REF_DRIVER = os.path.join(_HERE, "_ref", "spoa_ref_driver")
+_REF_BENCH = os.path.join(_HERE, "_ref", "spoa_ref_bench")
+# the reference's library sources, staged (unmodified, git-ignored) so they
+# travel to machines without the reference tree
+_STAGED = os.path.join(os.path.dirname(_HERE), "baseline", "_ref", "spoa")
 _lib = None
 
 TYPES = {"SW": 0, "NW": 1, "OV": 2}
@@ -29,18 +33,71 @@ def build(force: bool = False) -> str:
     return _LIB_PATH
 
 
+def reference_tree() -> str:
+    """The reference source tree: $SPOA_REFERENCE_TREE, else the directory
+    `reference` beside this repository."""
+    return os.environ.get("SPOA_REFERENCE_TREE",
+                          os.path.join(os.path.dirname(os.path.dirname(_HERE)), "reference"))
+
+
 def build_reference() -> str | None:
-    """Compile the reference driver (needs the reference source tree)."""
-    ref = os.environ.get("SPOA_REFERENCE_TREE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src")):
-        return None
-    subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={ref}"], check=True,
-                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    """Where the reference tree is present: compile the reference driver and
+    stage the reference's library sources for the CPU baseline.  Wherever a
+    staged copy exists (here, or on a machine the repository was copied to):
+    compile the baseline timer from it.  Returns the driver or None."""
+    ref = reference_tree()
+    if os.path.isdir(os.path.join(ref, "src")):
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", "stage", f"REF={ref}"], check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    if os.path.isdir(os.path.join(_STAGED, "src")):
+        subprocess.run(["make", "-s", "-C", _HERE, "bench"], check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     return _REF_DRIVER if os.path.exists(_REF_DRIVER) else None
 
 
 def reference_driver() -> str | None:
     return _REF_DRIVER if os.path.exists(_REF_DRIVER) else None
+
+
+def reference_bench() -> str | None:
+    """The timer of the reference's own library (oracle/ref_bench.cpp)."""
+    return _REF_BENCH if os.path.exists(_REF_BENCH) else None
+
+
+def write_windows_file(path: str, windows, types, strands) -> None:
+    """Windows in the input format of ref_bench.cpp."""
+    import struct
+    with open(path, "wb") as fh:
+        fh.write(b"SPWB" + struct.pack("<I", len(windows)))
+        for reads, t, s in zip(windows, types, strands):
+            fh.write(struct.pack("<bbHI", int(t), 1 if s else 0, 0, len(reads)))
+            fh.write(np.asarray([len(r) for r in reads], np.uint32).tobytes())
+            fh.write(b"".join(reads))
+
+
+def run_reference_bench(windows, types, strands, params, threads: int,
+                        want_consensus: bool = False) -> dict:
+    """Times the reference library on `threads` host threads over the
+    windows (one window per task).  Returns the timer's JSON record, plus
+    the consensus list when asked."""
+    import json
+    import tempfile
+    exe = reference_bench()
+    if exe is None:
+        raise FileNotFoundError("reference timer not built")
+    with tempfile.TemporaryDirectory() as tmp:
+        inp = os.path.join(tmp, "windows.bin")
+        write_windows_file(inp, windows, types, strands)
+        out = os.path.join(tmp, "consensus.txt")
+        cmd = [exe, inp] + [str(int(x)) for x in params] + [str(threads)]
+        if want_consensus:
+            cmd.append(out)
+        r = subprocess.run(cmd, capture_output=True, text=True, check=True)
+        rec = json.loads(r.stdout.strip().splitlines()[-1])
+        if want_consensus:
+            with open(out) as fh:
+                rec["consensus"] = fh.read().split("\n")[:len(windows)]
+    return rec
 
 
 class WindowParams(C.Structure):

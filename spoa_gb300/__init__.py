@@ -80,7 +80,8 @@ class _BatchDesc(C.Structure):
                 ("columns_per_thread", C.c_int32), ("ctas", C.c_int32),
                 ("memory_budget", C.c_uint64), ("want_alignments", C.c_int32),
                 ("want_msa", C.c_int32), ("autotune", C.c_int32),
-                ("windows_per_cta", C.c_int32)]
+                ("windows_per_cta", C.c_int32), ("device_set", C.c_int32),
+                ("device", C.c_int32)]
 
 
 class _BatchResult(C.Structure):
@@ -99,7 +100,8 @@ class _ServerDesc(C.Structure):
     _fields_ = [("type", C.c_int32), ("m", C.c_int8), ("n", C.c_int8), ("g", C.c_int8),
                 ("e", C.c_int8), ("q", C.c_int8), ("c", C.c_int8), ("pad", C.c_int8),
                 ("memory_budget", C.c_uint64), ("max_streams", C.c_int32),
-                ("max_windows_per_launch", C.c_int32), ("gather_seconds", C.c_double)]
+                ("max_windows_per_launch", C.c_int32), ("gather_seconds", C.c_double),
+                ("device_set", C.c_int32), ("device", C.c_int32)]
 
 
 # Every symbol of include/spoa_gb300.h
@@ -505,7 +507,7 @@ class Batch:
     def _create(self, seqs, off, wro, type_, m, n, g, e, q, c, window_types, window_strand,
                 quals, want_alignments=False, want_msa=False, threads_per_window=0,
                 columns_per_thread=0, ctas=0, max_nodes=0, memory_budget=0, autotune=False,
-                windows_per_cta=1):
+                windows_per_cta=1, device=None):
         self._seqs = np.ascontiguousarray(seqs, np.uint8)
         self._off = np.ascontiguousarray(off, np.uint64)
         self._wro = np.ascontiguousarray(wro, np.uint32)
@@ -537,6 +539,8 @@ class Batch:
         d.want_msa = 1 if want_msa else 0
         d.autotune = 1 if autotune else 0
         d.windows_per_cta = windows_per_cta
+        d.device_set = 1 if device is not None else 0
+        d.device = int(device) if device is not None else 0
         self._desc = d
         h = C.c_void_p()
         _check("batch_create", lib().spoa_gb300_batch_create(C.byref(d), C.byref(h)))
@@ -616,12 +620,13 @@ class Server:
     def __init__(self, type_: int, m: int, n: int, g: int, e: int | None = None,
                  q: int | None = None, c: int | None = None, memory_budget: int = 0,
                  max_streams: int = 0, max_windows_per_launch: int = 0,
-                 gather_seconds: float = 0.0):
+                 gather_seconds: float = 0.0, device: int | None = None):
         e = g if e is None else e
         if q is None or c is None:
             q, c = g, e
         d = _ServerDesc(type_, m, n, g, e, q, c, 0, memory_budget, max_streams,
-                        max_windows_per_launch, gather_seconds)
+                        max_windows_per_launch, gather_seconds,
+                        1 if device is not None else 0, int(device or 0))
         h = C.c_void_p()
         _check("Server::Create", lib().spoa_gb300_server_create(C.byref(d), C.byref(h)))
         self._h = h

@@ -70,6 +70,12 @@ __device__ inline void read_prologue(const Scoring& S, const GraphView& G, const
   ss.status = kOk;
   ss.mode = 0;
   ss.lanes = 16;
+  // every read is staged in buffers of caps.ld bytes (the reverse
+  // complement, the multi-window slots), the first one too
+  if (L > nthreads_cols || L > D.caps.ld) {
+    ss.status = kCapacity;
+    return;
+  }
   if (V == 0 || L == 0) return;
   int32_t lanes = lanes_for(S, L, V);
   if (!lanes) {
@@ -80,8 +86,7 @@ __device__ inline void read_prologue(const Scoring& S, const GraphView& G, const
     ss.status = kNeedWide;  // rerun the window with the int32 kernel
     return;
   }
-  if (L > nthreads_cols || L > D.caps.ld || V + 1 > D.caps.rows ||
-      (uint64_t)G.hdr->n_edges + V + 1 > D.caps.preds) {
+  if (V + 1 > D.caps.rows || (uint64_t)G.hdr->n_edges + V + 1 > D.caps.preds) {
     ss.status = kCapacity;
     return;
   }

@@ -169,6 +169,45 @@ bool seg_tile(uint32_t L, int* cpt, int* nt, int* segs) {
   return false;
 }
 
+// Makes `dev` the calling thread's current device while the guard lives and
+// restores the previous current device afterwards.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = true;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+      ok = false;
+      return;
+    }
+    if (prev != dev && cudaSetDevice(dev) != cudaSuccess) {
+      cudaGetLastError();
+      ok = false;
+    }
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// The device a batch or server runs on: the requested ordinal, or the
+// calling thread's current device; -1 when the ordinal does not exist.
+int resolve_device(int32_t set, int32_t ordinal) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  if (set) return ordinal >= 0 && ordinal < n ? ordinal : -1;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return dev;
+}
+
 struct DeviceBuf {
   void* p = nullptr;
   size_t n = 0;
@@ -1081,6 +1120,7 @@ struct spoa_gb300_batch {
   int launches = 0;
   uint64_t cells = 0;
   int sm_count = 0;
+  int device = 0;
 };
 
 namespace {
@@ -1567,6 +1607,10 @@ int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* d, spoa_gb300_batch
     return kInvalidArgument;
   *out = nullptr;
   if (d->type != kSW && d->type != kNW && d->type != kOV) return kInvalidArgument;
+  const int dev = resolve_device(d->device_set, d->device);
+  if (dev < 0) return d->device_set ? kInvalidArgument : kCuda;
+  DeviceGuard guard(dev);
+  if (!guard.ok) return kCuda;
   spoa_gb300_engine* en = nullptr;
   int32_t st = spoa_gb300_engine_create(d->type, d->m, d->n, d->g, d->e, d->q, d->c, &en);
   if (st) return st;
@@ -1575,6 +1619,7 @@ int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* d, spoa_gb300_batch
   auto* b = new (std::nothrow) spoa_gb300_batch();
   if (!b) return kNoMemory;
   b->desc = *d;
+  b->device = dev;
   b->base = base;
   b->n_windows = d->n_windows;
   b->wro.assign(d->window_read_off, d->window_read_off + d->n_windows + 1);
@@ -1584,8 +1629,6 @@ int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* d, spoa_gb300_batch
     return kInvalidArgument;
   }
   b->seq_off.assign(d->seq_off, d->seq_off + b->n_reads + 1);
-  int dev = 0;
-  cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
   b->lmax.assign(b->n_windows, 1);
   b->sumlen.assign(b->n_windows, 0);
@@ -1694,17 +1737,23 @@ int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* d, spoa_gb300_batch
 int32_t spoa_gb300_batch_launch(spoa_gb300_batch* b, void* stream) {
   if (!b) return kInvalidArgument;
   if (!b->n_windows) return kOk;
+  DeviceGuard guard(b->device);
+  if (!guard.ok) return kCuda;
   return launch_all(b, stream, false);
 }
 
 int32_t spoa_gb300_batch_launch_plain(spoa_gb300_batch* b, void* stream) {
   if (!b) return kInvalidArgument;
   if (!b->n_windows) return kOk;
+  DeviceGuard guard(b->device);
+  if (!guard.ok) return kCuda;
   return launch_all(b, stream, true);
 }
 
 int32_t spoa_gb300_batch_fetch(spoa_gb300_batch* b, spoa_gb300_batch_result* r) {
   if (!b || !r) return kInvalidArgument;
+  DeviceGuard guard(b->device);
+  if (!guard.ok) return kCuda;
   std::memset(r, 0, sizeof(*r));
   const uint32_t W = b->n_windows, R = b->n_reads;
   b->h_scores.resize(R + 1);
@@ -1787,7 +1836,11 @@ int32_t spoa_gb300_batch_fetch(spoa_gb300_batch* b, spoa_gb300_batch_result* r) 
   return kOk;
 }
 
-void spoa_gb300_batch_destroy(spoa_gb300_batch* b) { delete b; }
+void spoa_gb300_batch_destroy(spoa_gb300_batch* b) {
+  if (!b) return;
+  DeviceGuard guard(b->device);
+  delete b;
+}
 
 int32_t spoa_gb300_batch_run(const spoa_gb300_batch_desc* d, spoa_gb300_batch** out,
                              spoa_gb300_batch_result* r) {
@@ -1892,7 +1945,7 @@ extern "C" int32_t spoa_gb300_window_poa_noalloc(
   gc.edges = 4 * SPOA_GB300_NOALLOC_MAX_NODES + 64;
   gc.labels = SPOA_GB300_NOALLOC_MAX_READS * SPOA_GB300_NOALLOC_MAX_READ_LEN + 2;
   gc.seqs = n_reads + 1;
-  gc.aligned = 15;
+  gc.aligned = SPOA_GB300_NOALLOC_MAX_ALIGNED;
   DpCaps dc{gc.nodes + 1, (uint32_t)(cpt * nt), gc.edges + gc.nodes + 2, sub, 2};  // int16 only
   GraphView gv;
   DpView dv;
@@ -2366,8 +2419,13 @@ int32_t spoa_gb300_server_create(const spoa_gb300_server_desc* d, spoa_gb300_ser
   sv->desc = *d;
   if (sv->desc.max_streams <= 0) sv->desc.max_streams = 32;
   if (sv->desc.max_windows_per_launch <= 0) sv->desc.max_windows_per_launch = 4096;
-  if (cudaGetDevice(&sv->device) != cudaSuccess) {
-    cudaGetLastError();
+  sv->device = resolve_device(d->device_set, d->device);
+  if (sv->device < 0) {
+    delete sv;
+    return d->device_set ? kInvalidArgument : kCuda;
+  }
+  DeviceGuard guard(sv->device);
+  if (!guard.ok) {
     delete sv;
     return kCuda;
   }
@@ -2465,6 +2523,7 @@ void spoa_gb300_server_destroy(spoa_gb300_server* sv) {
   if (!sv) return;
   sv->stop = true;
   if (sv->loop.joinable()) sv->loop.join();
+  DeviceGuard guard(sv->device);
   for (ServedLaunch& L : sv->slots) {
     if (L.stream) cudaStreamDestroy(L.stream);
     if (L.done) cudaEventDestroy(L.done);

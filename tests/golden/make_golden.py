@@ -1,7 +1,7 @@
 """Regenerates the golden fixtures in this directory.
 
 Run here, where the reference tree and its compiled driver exist:
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py [--reference <reference tree>]
 
 It writes
   sample_reads.tsv.gz      the 55 reads of test/data/sample.fastq.gz
@@ -242,7 +242,7 @@ def write_cli(reference: str):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=po.reference_tree())
     ap.add_argument("--only", choices=["slices", "cli", "persist"], default=None)
     args = ap.parse_args()
     os.environ["SPOA_REFERENCE_TREE"] = args.reference
