@@ -84,6 +84,8 @@ def parse():
                     help="windows in flight per CTA (16-bit windows)")
     ap.add_argument("--parity-windows", type=int, default=256,
                     help="windows rerun with alignments and checked against the oracle")
+    ap.add_argument("--tile", default="",
+                    help="CPTxTHREADS: force the tile of every pass (no tuner)")
     return ap.parse_args()
 
 
@@ -390,10 +392,13 @@ def main():
     n_windows = len(wins)
     seqs, off, wro = flatten(wins, pinned=True)
 
+    cpt, nt = (int(x) for x in args.tile.split("x")) if args.tile else (0, 0)
+
     def make_batch():
         return sg.Batch.from_arrays(seqs, off, wro, typ, *params, window_types=wtypes,
                                     window_strand=wstrand,
-                                    autotune=args.workload == "batch_10k",
+                                    autotune=args.workload == "batch_10k" and not args.tile,
+                                    columns_per_thread=cpt, threads_per_window=nt,
                                     windows_per_cta=args.windows_per_cta, device=device)
 
     batch = make_batch()

@@ -47,15 +47,20 @@ __device__ void read_align(const Scoring& S, const GraphView& G, DpView& D, Bloc
     dp_forward<SUB, CPT, T>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
   else
     dp_forward_seg<SUB, CPT, T, SEGS>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
-  if (threadIdx.x == 0) {
-    *np = 0;
-    *has = 0;
+  // mi is the same in every thread: warp 0 runs the traceback
+  if (threadIdx.x < 32) {
+    if (threadIdx.x == 0) {
+      *np = 0;
+      *has = 0;
+    }
     if (mi >= 0) {
-      *has = 1;
-      *score = sc;
-      const int32_t st =
-          dp_traceback<SUB, CPT, T>(S, D, G, seq, L, V, mi, mj, pairs, np, blockDim.x * SEGS);
-      if (st != kOk) ss.status = st;
+      if (threadIdx.x == 0) {
+        *has = 1;
+        *score = sc;
+      }
+      const int32_t st = dp_traceback<SUB, CPT, T>(S, D, G, seq, L, V, mi, mj, pairs, np,
+                                                   blockDim.x * SEGS, sh.tb);
+      if (threadIdx.x == 0 && st != kOk) ss.status = st;
     }
   }
   __syncthreads();
@@ -122,20 +127,28 @@ __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScra
       read_align<SUB, CPT, T, SEGS>(S, G, D, sh, ss, D.seq_rc, L, ss.lanes, D.aln_b, &ss.has_r,
                               &ss.score_r, &ss.np_r);
   }
-  if (threadIdx.x == 0 && ss.status == kOk) {
+  __syncthreads();
+  if (ss.status == kOk) {
     // main.cpp:276-301: scores start at 0; keep forward if score >= score_rev
     const int32_t sf = ss.has_f ? ss.score_f : 0;
     const int32_t sr = ss.has_r ? ss.score_r : 0;
     const bool rev = strand && !(sf >= sr);
     const int32_t* pairs = rev ? D.aln_b : D.aln_a;
     const uint32_t np = rev ? ss.np_r : ss.np_f;
-    WeightSrc ws{nullptr, qual, L, rev ? 1u : 0u, 1u};
-    int32_t st = g_add_alignment(G, pairs, np, rev ? D.seq_rc : seq, L, ws);
-    if (st != kOk) ss.status = st;
-    *out_score = rev ? sr : sf;
-    *out_rev = rev ? 1 : 0;
-    *out_pairs = pairs;
-    *out_np = np;
+    const uint8_t* chosen = rev ? D.seq_rc : seq;
+    // AddAlignment's read-only lookups on every thread, into the alignment
+    // buffer the strand choice left unused (two words per pair fit it)
+    uint32_t* pre = reinterpret_cast<uint32_t*>(rev ? D.aln_a : D.aln_b);
+    g_add_prepass(G, pairs, np, chosen, L, pre);
+    if (threadIdx.x == 0) {
+      WeightSrc ws{nullptr, qual, L, rev ? 1u : 0u, 1u};
+      int32_t st = g_add_alignment(G, pairs, np, chosen, L, ws, pre);
+      if (st != kOk) ss.status = st;
+      *out_score = rev ? sr : sf;
+      *out_rev = rev ? 1 : 0;
+      *out_pairs = pairs;
+      *out_np = np;
+    }
   }
   __syncthreads();
   if (ss.status == kOk && L > 0) {
