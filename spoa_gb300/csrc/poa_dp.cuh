@@ -41,36 +41,11 @@ __device__ __forceinline__ int32_t addmax(int32_t a, int32_t b, int32_t c) {
   return __viaddmax_s32(a, b, c);
 }
 
-// The traceback's band (dp_traceback): the cells a run of traceback steps
-// reads, loaded by the 32 lanes of warp 0 in one round of independent loads
-// and then read by lane 0 from shared memory.  Band row d is DP row i0 - d;
-// its kTbCols columns are j0 - d - kTbHalf .. j0 - d + kTbHalf, a diagonal
-// strip that follows a path of matches and mismatches through the previous
-// ranks.  Rows per band: 32 for 16-bit cells, 16 for 32-bit ones (the same
-// bytes).
-constexpr int kTbHalf = 3, kTbCols = 2 * kTbHalf + 1, kTbRowsMax = 32;
-constexpr int kTbCellBytes = 5 * kTbRowsMax * kTbCols * 2;
-struct TbBand {
-  int64_t i0, j0;        // anchor of the band
-  int64_t i, j;          // walk position, handed between the lanes
-  uint64_t np, guard;
-  int32_t status, done;
-  // per band row: node of the rank, first predecessor entry and count,
-  // first two predecessors in the reference's order, first-column value,
-  // row character, source flag
-  uint32_t node[kTbRowsMax], pb[kTbRowsMax], cnt[kTbRowsMax], p0[kTbRowsMax], p1[kTbRowsMax];
-  int32_t fc[kTbRowsMax];
-  uint8_t ch[kTbRowsMax], src[kTbRowsMax];
-  uint8_t seq[64];  // read characters of columns j0 + kTbHalf - k, k < 64
-  alignas(16) uint8_t cells[kTbCellBytes];  // [matrix][row][column] of the cell type
-};
-
 struct BlockScratch {
   int32_t wv[32];
   int32_t wv2[32];
   int32_t edge[32];
   int32_t bcast[8];
-  TbBand tb;
 };
 
 // Exclusive prefix-max of v over the CTA's threads (kNegBig for thread 0).
@@ -1146,330 +1121,221 @@ __device__ __noinline__ void dp_forward_seg(const Scoring& S, DpView& D,
   *out_score = score;
 }
 // Traceback from (max_i, max_j) (implementation.hpp:955-1124, 1324-1574,
-// 1826-2121).  Every move is re-derived from the stored H/F/O/E/Q rows with
-// the reference's tests in the reference's order, by lane 0 of warp 0.  The
-// 32 lanes of warp 0 call it together: they load the band of cells and row
-// data around the current position (TbBand) in one round of independent
-// loads, lane 0 walks while the next step's tests stay inside the band
-// (reading anything outside it from global memory), and the lanes reload
-// the band around the position where lane 0 stopped.  Pairs are written to
-// `out` in forward order; every lane returns the status.
+// 1826-2121), thread 0.  Every move is re-derived from the stored
+// H/F/O/E/Q rows with the reference's tests in the reference's order.
+// Pairs are written to `out` in forward order.
 template <int SUB, int CPT, typename T>
 static __device__ __noinline__ int32_t dp_traceback(const Scoring& S, const DpView& D, const GraphView& G,
                                 const uint8_t* seq, uint32_t L, uint32_t V, int64_t max_i,
-                                int64_t max_j, int32_t* out, uint32_t* n_out, uint32_t ntv,
-                                TbBand& B) {
+                                int64_t max_j, int32_t* out, uint32_t* n_out, uint32_t ntv) {
   using Lx = Lanes<T>;
-  constexpr int R = sizeof(T) == 2 ? kTbRowsMax : kTbRowsMax / 2;  // band rows
-  constexpr int NM = SUB == kConvex ? 5 : (SUB == kAffine ? 3 : 1);  // matrices
-  const uint32_t lane = threadIdx.x & 31;
   const uint64_t ld = D.caps.ld;
   const int32_t type = S.type;
   const int32_t m = S.m, n = S.n, g = S.g, e = S.e, q = S.q, c = S.c;
-  // matrices in band order: H, F, E (affine, convex), O, Q (convex)
-  const void* M[5] = {D.H, D.F, D.E, D.O, D.Q};
-  enum { mH = 0, mF = 1, mE = 2, mO = 3, mQ = 4 };
+  const void* H = D.H;
+  const void* F = D.F;
+  const void* O = D.O;
+  const void* E = D.E;
+  const void* Q = D.Q;
   const uint64_t nt = ntv;  // the forward pass's row width in strips
-  T* cells = reinterpret_cast<T*>(B.cells);
-  auto gat = [&](int mi, int64_t row, int64_t col) -> int32_t {
-    return Lx::elem(M[mi], (uint64_t)row * ld + colmap<CPT>((uint64_t)col, nt));
+  auto at = [&](const void* M, int64_t row, int64_t col) -> int32_t {
+    return Lx::elem(M, (uint64_t)row * ld + colmap<CPT>((uint64_t)col, nt));
   };
-
-  if (lane == 0) {
-    B.i = max_i;
-    B.j = max_j;
-    B.np = 0;
-    B.guard = 0;
-    B.status = kOk;
-    B.done = 0;
-  }
+  // H, E or Q of column col, where column -1 is the first column: the
+  // forward pass starts all three in-row recurrences from it
+  auto left = [&](const void* M, int64_t row, int64_t col) -> int32_t {
+    return col < 0 ? D.fc[row] : at(M, row, col);
+  };
+  // extend_left continues past column cc (implementation.hpp:2031-2035):
+  // E (and Q, convex) of cc extend the values of column cc-1
+  auto run = [&](int64_t row, int64_t cc) -> bool {
+    bool r = at(E, row, cc) == left(E, row, cc - 1) + e;
+    if (SUB == kConvex) r = r && at(Q, row, cc) == left(Q, row, cc - 1) + c;
+    return r;
+  };
+  int32_t* tb = out;  // written back to front, reversed at the end
+  uint64_t np = 0;
   const uint64_t cap = D.aln_cap;
+  int64_t i = max_i, j = max_j, prev_i = 0, prev_j = 0;
+  uint64_t guard = 0;
   const uint64_t guard_max = 4 * ((uint64_t)V + L) + 64;
+#define EMIT(a, b)                    \
+  do {                                \
+    if (np >= cap) return kTraceback; \
+    tb[2 * np] = (a);                 \
+    tb[2 * np + 1] = (b);             \
+    ++np;                             \
+  } while (0)
   while (true) {
-    __syncwarp();
-    if (B.done) break;
-    // (re)load the band around the current position
-    const int64_t i0 = B.i, j0 = B.j;
-    {
-      const int64_t d = lane, r = i0 - d;
-      if (d < R && r >= 0) {
-        if (r >= 1) {
-          const uint4 rec = D.rowrec[r];
-          const uint32_t pb = rec.x;
-          uint32_t cnt = rec.y & 0xFFFFu;
-          if (cnt == 0xFFFFu) cnt = D.pred_ptr[r + 1] - pb;
-          B.pb[d] = pb;
-          B.cnt[d] = cnt;
-          B.ch[d] = (uint8_t)(rec.y >> 24);
-          B.src[d] = (rec.y >> 16) & kRowSource ? 1 : 0;
-          B.node[d] = G.rank_to_node[r - 1];
-          B.p0[d] = D.preds[pb];
-          B.p1[d] = cnt > 1 ? D.preds[pb + 1] : kNone;
-        }
-        B.fc[d] = D.fc[r];
-        for (int mi = 0; mi < NM; ++mi) {
-          for (int k = 0; k < kTbCols; ++k) {
-            const int64_t col = j0 - d - kTbHalf + k;
-            if (col >= 0 && col < (int64_t)L) cells[(mi * R + d) * kTbCols + k] = (T)gat(mi, r, col);
-          }
-        }
-      }
-      for (int k = lane; k < 64; k += 32) {
-        const int64_t col = j0 + kTbHalf - k;
-        if (col >= 0 && col < (int64_t)L) B.seq[k] = seq[col];
+    if (++guard > guard_max) return kTraceback;
+    if (j == -1 || i == 0) break;
+    const uint32_t node = G.rank_to_node[i - 1];
+    const int32_t h = at(H, i, j);
+    if (type == kSW && h == 0) break;
+    const uint32_t pb = D.pred_ptr[i], pe = D.pred_ptr[i + 1];
+    const int32_t prf = D.row_char[i] == seq[j] ? m : n;
+    bool found = false, ext_left = false, ext_up = false;
+    for (uint32_t pi = pb; pi < pe; ++pi) {
+      const int64_t p = D.preds[pi];
+      const int32_t hd = j ? at(H, p, j - 1) : D.fc[p];
+      if (h == hd + prf) {
+        prev_i = p;
+        prev_j = j - 1;
+        found = true;
+        break;
       }
     }
-    __syncwarp();
-    if (lane == 0) {
-      // accessors: the band where it holds the cell, global memory elsewhere
-      auto at = [&](int mi, int64_t row, int64_t col) -> int32_t {
-        const int64_t d = i0 - row, k = col - (j0 - d) + kTbHalf;
-        if (d >= 0 && d < R && k >= 0 && k < kTbCols) return cells[(mi * R + d) * kTbCols + k];
-        return gat(mi, row, col);
-      };
-      auto fcv = [&](int64_t row) -> int32_t {
-        const int64_t d = i0 - row;
-        return d >= 0 && d < R ? B.fc[d] : D.fc[row];
-      };
-      // H, E or Q of column col, where column -1 is the first column: the
-      // forward pass starts all three in-row recurrences from it
-      auto left = [&](int mi, int64_t row, int64_t col) -> int32_t {
-        return col < 0 ? fcv(row) : at(mi, row, col);
-      };
-      auto seq_at = [&](int64_t col) -> uint8_t {
-        const int64_t k = j0 + kTbHalf - col;
-        return k >= 0 && k < 64 ? B.seq[k] : seq[col];
-      };
-      struct Row {
-        uint32_t node, pb, cnt, p0, p1;
-        uint8_t ch, src;
-      };
-      auto row_of = [&](int64_t r) -> Row {
-        const int64_t d = i0 - r;
-        if (d >= 0 && d < R)
-          return Row{B.node[d], B.pb[d], B.cnt[d], B.p0[d], B.p1[d], B.ch[d], B.src[d]};
-        Row x;
-        x.node = G.rank_to_node[r - 1];
-        x.pb = D.pred_ptr[r];
-        x.cnt = D.pred_ptr[r + 1] - x.pb;
-        x.p0 = D.preds[x.pb];
-        x.p1 = x.cnt > 1 ? D.preds[x.pb + 1] : kNone;
-        x.ch = D.row_char[r];
-        x.src = D.row_indeg[r] == 0 ? 1 : 0;
-        return x;
-      };
-      auto pred = [&](const Row& x, uint32_t k) -> int64_t {
-        return k == 0 ? x.p0 : k == 1 ? x.p1 : D.preds[x.pb + k];
-      };
-      // extend_left continues past column cc (implementation.hpp:2031-2035):
-      // E (and Q, convex) of cc extend the values of column cc-1
-      auto run = [&](int64_t row, int64_t cc) -> bool {
-        bool r = at(mE, row, cc) == left(mE, row, cc - 1) + e;
-        if (SUB == kConvex) r = r && at(mQ, row, cc) == left(mQ, row, cc - 1) + c;
-        return r;
-      };
-      int32_t* tb = out;  // written back to front, reversed at the end
-      uint64_t np = B.np, guard = B.guard;
-      int64_t i = B.i, j = B.j, prev_i = 0, prev_j = 0;
-      int32_t st = kOk;
-      bool done = false;
-#define EMIT(a, b)                                 \
-  do {                                             \
-    if (np >= cap) { st = kTraceback; goto out_; } \
-    tb[2 * np] = (a);                              \
-    tb[2 * np + 1] = (b);                          \
-    ++np;                                          \
-  } while (0)
-      while (true) {
-        if (j == -1 || i == 0) { done = true; break; }
-        {
-          // stop for a new band when this step's tests would leave it: the
-          // row and the predecessor row i-1, columns j-1 .. j
-          const int64_t d = i0 - i, k = j - (j0 - d) + kTbHalf;
-          if (d < 0 || d + 1 >= R || k < 1 || k + 1 >= kTbCols) break;
-        }
-        if (++guard > guard_max) { st = kTraceback; goto out_; }
-        const Row x = row_of(i);
-        const uint32_t node = x.node;
-        const int32_t h = at(mH, i, j);
-        if (type == kSW && h == 0) { done = true; break; }
-        const int32_t prf = x.ch == seq_at(j) ? m : n;
-        bool found = false, ext_left = false, ext_up = false;
-        for (uint32_t k = 0; k < x.cnt; ++k) {
-          const int64_t p = pred(x, k);
-          const int32_t hd = j ? at(mH, p, j - 1) : fcv(p);
-          if (h == hd + prf) {
-            prev_i = p;
-            prev_j = j - 1;
-            found = true;
-            break;
+    if (!found) {
+      for (uint32_t pi = pb; pi < pe; ++pi) {
+        const int64_t p = D.preds[pi];
+        const int32_t hp = at(H, p, j);
+        bool take;
+        if (SUB == kLinear) {
+          take = h == hp + g;
+        } else if (SUB == kAffine) {
+          ext_up = h == at(F, p, j) + e;
+          take = ext_up || h == hp + g;
+        } else {
+          ext_up = h == at(F, p, j) + e;
+          if (ext_up) {
+            take = true;
+          } else if (h == hp + g) {
+            take = true;
+          } else {
+            ext_up = h == at(O, p, j) + c;
+            take = ext_up || h == hp + q;
           }
         }
-        if (!found) {
-          for (uint32_t k = 0; k < x.cnt; ++k) {
-            const int64_t p = pred(x, k);
-            const int32_t hp = at(mH, p, j);
-            bool take;
-            if (SUB == kLinear) {
-              take = h == hp + g;
-            } else if (SUB == kAffine) {
-              ext_up = h == at(mF, p, j) + e;
-              take = ext_up || h == hp + g;
-            } else {
-              ext_up = h == at(mF, p, j) + e;
-              if (ext_up) {
-                take = true;
-              } else if (h == hp + g) {
-                take = true;
-              } else {
-                ext_up = h == at(mO, p, j) + c;
-                take = ext_up || h == hp + q;
-              }
-            }
-            if (take) {
+        if (take) {
+          prev_i = p;
+          prev_j = j;
+          found = true;
+          break;
+        }
+      }
+    }
+    if (!found) {
+      // horizontal tests in the reference's order (implementation.hpp
+      // 1977-1990): E extension, H + g, Q extension, H + q
+      const int32_t hl = left(H, i, j - 1);
+      bool any;
+      if (SUB == kLinear) {
+        any = h == hl + g;
+      } else {
+        const bool mA = h == left(E, i, j - 1) + e;
+        const bool mB = h == hl + g;
+        any = mA || mB;
+        ext_left = mA;
+        if (SUB == kConvex && !any) {
+          const bool mC = h == left(Q, i, j - 1) + c;
+          any = mC || h == hl + q;
+          ext_left = mC;
+        }
+      }
+      if (any) {
+        prev_i = i;
+        prev_j = j - 1;
+        found = true;
+      }
+    }
+    EMIT(i == prev_i ? -1 : (int32_t)node, j == prev_j ? -1 : (int32_t)j);
+    i = prev_i;
+    j = prev_j;
+    if (SUB >= kAffine && ext_left) {
+      while (true) {
+        if (++guard > guard_max) return kTraceback;
+        EMIT(-1, (int32_t)j);
+        --j;
+        if (j == -1) break;
+        if (!run(i, j + 1)) break;
+      }
+    } else if (SUB >= kAffine && ext_up) {
+      while (true) {
+        if (++guard > guard_max) return kTraceback;
+        const uint32_t un = G.rank_to_node[i - 1];
+        const int32_t fv = at(F, i, j);
+        const uint32_t pb2 = D.pred_ptr[i];
+        const uint32_t pe2 = D.row_indeg[i] ? D.pred_ptr[i + 1] : pb2;  // sources: none
+        bool stop;
+        prev_i = 0;
+        if (SUB == kAffine) {
+          stop = false;
+          for (uint32_t pi = pb2; pi < pe2; ++pi) {
+            const int64_t p = D.preds[pi];
+            stop = fv == at(H, p, j) + g;
+            if (stop || fv == at(F, p, j) + e) {
               prev_i = p;
-              prev_j = j;
-              found = true;
               break;
             }
           }
-        }
-        if (!found) {
-          // horizontal tests in the reference's order (implementation.hpp
-          // 1977-1990): E extension, H + g, Q extension, H + q
-          const int32_t hl = left(mH, i, j - 1);
-          bool any;
-          if (SUB == kLinear) {
-            any = h == hl + g;
-          } else {
-            const bool mA = h == left(mE, i, j - 1) + e;
-            const bool mB = h == hl + g;
-            any = mA || mB;
-            ext_left = mA;
-            if (SUB == kConvex && !any) {
-              const bool mC = h == left(mQ, i, j - 1) + c;
-              any = mC || h == hl + q;
-              ext_left = mC;
-            }
-          }
-          if (any) {
-            prev_i = i;
-            prev_j = j - 1;
-            found = true;
-          }
-        }
-        EMIT(i == prev_i ? -1 : (int32_t)node, j == prev_j ? -1 : (int32_t)j);
-        i = prev_i;
-        j = prev_j;
-        if (SUB >= kAffine && ext_left) {
-          while (true) {
-            if (++guard > guard_max) { st = kTraceback; goto out_; }
-            EMIT(-1, (int32_t)j);
-            --j;
-            if (j == -1) break;
-            if (!run(i, j + 1)) break;
-          }
-        } else if (SUB >= kAffine && ext_up) {
-          while (true) {
-            if (++guard > guard_max) { st = kTraceback; goto out_; }
-            const Row y = row_of(i);
-            const int32_t fv = at(mF, i, j);
-            const uint32_t npred = y.src ? 0 : y.cnt;  // sources: none
-            bool stop;
-            prev_i = 0;
-            if (SUB == kAffine) {
+        } else {
+          const int32_t ov = at(O, i, j);
+          stop = true;
+          for (uint32_t pi = pb2; pi < pe2; ++pi) {
+            const int64_t p = D.preds[pi];
+            if (fv == at(F, p, j) + e || ov == at(O, p, j) + c) {
+              prev_i = p;
               stop = false;
-              for (uint32_t k = 0; k < npred; ++k) {
-                const int64_t p = pred(y, k);
-                stop = fv == at(mH, p, j) + g;
-                if (stop || fv == at(mF, p, j) + e) {
-                  prev_i = p;
-                  break;
-                }
-              }
-            } else {
-              const int32_t ov = at(mO, i, j);
-              stop = true;
-              for (uint32_t k = 0; k < npred; ++k) {
-                const int64_t p = pred(y, k);
-                if (fv == at(mF, p, j) + e || ov == at(mO, p, j) + c) {
-                  prev_i = p;
-                  stop = false;
-                  break;
-                }
-              }
-              if (stop) {
-                for (uint32_t k = 0; k < npred; ++k) {
-                  const int64_t p = pred(y, k);
-                  const int32_t hp = at(mH, p, j);
-                  if (fv == hp + g || ov == hp + q) {
-                    prev_i = p;
-                    break;
-                  }
-                }
-              }
+              break;
             }
-            EMIT((int32_t)y.node, -1);
-            i = prev_i;
-            if (stop || i == 0) break;
           }
-        }
-      }
-      if (done && type == kNW) {
-        while (i == 0 && j != -1) {
-          EMIT(-1, (int32_t)j);
-          --j;
-        }
-        while (i != 0 && j == -1) {
-          if (++guard > guard_max) { st = kTraceback; goto out_; }
-          EMIT((int32_t)G.rank_to_node[i - 1], -1);
-          if (D.row_indeg[i] == 0) {
-            i = 0;
-          } else {
-            for (uint32_t pi = D.pred_ptr[i]; pi < D.pred_ptr[i + 1]; ++pi) {
+          if (stop) {
+            for (uint32_t pi = pb2; pi < pe2; ++pi) {
               const int64_t p = D.preds[pi];
-              bool hit;
-              if (SUB == kLinear) {
-                hit = D.fc[i] == D.fc[p] + g;
-              } else if (SUB == kAffine) {
-                hit = D.fcF[i] == D.fcF[p] + e;
-              } else {
-                hit = D.fcF[i] == D.fcF[p] + e || D.fcO[i] == D.fcO[p] + c;
-              }
-              if (hit) {
-                i = p;
+              const int32_t hp = at(H, p, j);
+              if (fv == hp + g || ov == hp + q) {
+                prev_i = p;
                 break;
               }
             }
           }
         }
+        EMIT((int32_t)un, -1);
+        i = prev_i;
+        if (stop || i == 0) break;
       }
+    }
+  }
+  if (type == kNW) {
+    while (i == 0 && j != -1) {
+      EMIT(-1, (int32_t)j);
+      --j;
+    }
+    while (i != 0 && j == -1) {
+      if (++guard > guard_max) return kTraceback;
+      const uint32_t un = G.rank_to_node[i - 1];
+      EMIT((int32_t)un, -1);
+      if (D.row_indeg[i] == 0) {
+        i = 0;
+      } else {
+        for (uint32_t pi = D.pred_ptr[i]; pi < D.pred_ptr[i + 1]; ++pi) {
+          const int64_t p = D.preds[pi];
+          bool hit;
+          if (SUB == kLinear) {
+            hit = D.fc[i] == D.fc[p] + g;
+          } else if (SUB == kAffine) {
+            hit = D.fcF[i] == D.fcF[p] + e;
+          } else {
+            hit = D.fcF[i] == D.fcF[p] + e || D.fcO[i] == D.fcO[p] + c;
+          }
+          if (hit) {
+            i = p;
+            break;
+          }
+        }
+      }
+    }
+  }
 #undef EMIT
-    out_:
-      B.i = i;
-      B.j = j;
-      B.np = np;
-      B.guard = guard;
-      B.status = st;
-      B.done = done || st != kOk;
-    }
+  for (uint64_t a = 0, b = np ? np - 1 : 0; a < b; ++a, --b) {
+    const int32_t x0 = tb[2 * a], x1 = tb[2 * a + 1];
+    tb[2 * a] = tb[2 * b];
+    tb[2 * a + 1] = tb[2 * b + 1];
+    tb[2 * b] = x0;
+    tb[2 * b + 1] = x1;
   }
-  const int32_t st = B.status;
-  const uint64_t np = B.np;
-  if (st == kOk) {
-    // reverse the pairs (written back to front) across the lanes
-    for (uint64_t a = lane; a < np / 2; a += 32) {
-      const uint64_t b = np - 1 - a;
-      const int32_t x0 = out[2 * a], x1 = out[2 * a + 1];
-      out[2 * a] = out[2 * b];
-      out[2 * a + 1] = out[2 * b + 1];
-      out[2 * b] = x0;
-      out[2 * b + 1] = x1;
-    }
-    __syncwarp();
-    if (lane == 0) *n_out = (uint32_t)np;
-  }
-  return st;
+  *n_out = (uint32_t)np;
+  return kOk;
 }
 
 }  // namespace spoa_gb300

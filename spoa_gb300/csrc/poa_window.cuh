@@ -47,20 +47,15 @@ __device__ void read_align(const Scoring& S, const GraphView& G, DpView& D, Bloc
     dp_forward<SUB, CPT, T>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
   else
     dp_forward_seg<SUB, CPT, T, SEGS>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
-  // mi is the same in every thread: warp 0 runs the traceback
-  if (threadIdx.x < 32) {
-    if (threadIdx.x == 0) {
-      *np = 0;
-      *has = 0;
-    }
+  if (threadIdx.x == 0) {
+    *np = 0;
+    *has = 0;
     if (mi >= 0) {
-      if (threadIdx.x == 0) {
-        *has = 1;
-        *score = sc;
-      }
-      const int32_t st = dp_traceback<SUB, CPT, T>(S, D, G, seq, L, V, mi, mj, pairs, np,
-                                                   blockDim.x * SEGS, sh.tb);
-      if (threadIdx.x == 0 && st != kOk) ss.status = st;
+      *has = 1;
+      *score = sc;
+      const int32_t st =
+          dp_traceback<SUB, CPT, T>(S, D, G, seq, L, V, mi, mj, pairs, np, blockDim.x * SEGS);
+      if (st != kOk) ss.status = st;
     }
   }
   __syncthreads();
