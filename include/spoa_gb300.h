@@ -281,6 +281,20 @@ typedef struct {
   int32_t device_set;           /* nonzero: serve on `device`; 0: on the calling
                                    thread's current device at server_create */
   int32_t device;
+  int32_t resident;             /* nonzero: polishing-sized windows (16-bit scores,
+                                   reads of at most 640 bases, at most 255 reads
+                                   and 65,534 bases) go to one persistent kernel
+                                   that keeps running while work arrives: each
+                                   window takes a slot of a ring in host-mapped
+                                   memory, its reads are copied to the device,
+                                   the slot is published, and a CTA of the
+                                   running kernel claims it and writes the
+                                   consensus back; the kernel's CTAs leave after
+                                   20 ms without work (a bounded wait) and the
+                                   server starts it again when work arrives.
+                                   Other windows, and windows that outgrow the
+                                   resident kernel's arenas, are launched as
+                                   above. */
 } spoa_gb300_server_desc;
 
 int32_t spoa_gb300_server_create(const spoa_gb300_server_desc* desc, spoa_gb300_server** out);
@@ -305,6 +319,10 @@ int32_t spoa_gb300_server_wait(spoa_gb300_server* server, uint64_t ticket,
 /* Launches issued and windows completed so far. */
 int32_t spoa_gb300_server_stats(const spoa_gb300_server* server, uint64_t* launches,
                                 uint64_t* completed);
+/* Windows the resident kernel finished (or handed back to the launch path)
+ * and launches of the resident kernel so far. */
+int32_t spoa_gb300_server_resident_stats(const spoa_gb300_server* server, uint64_t* windows,
+                                         uint64_t* launches);
 /* Stops the server once every submitted window has finished. */
 void spoa_gb300_server_destroy(spoa_gb300_server* server);
 

@@ -101,7 +101,7 @@ class _ServerDesc(C.Structure):
                 ("e", C.c_int8), ("q", C.c_int8), ("c", C.c_int8), ("pad", C.c_int8),
                 ("memory_budget", C.c_uint64), ("max_streams", C.c_int32),
                 ("max_windows_per_launch", C.c_int32), ("gather_seconds", C.c_double),
-                ("device_set", C.c_int32), ("device", C.c_int32)]
+                ("device_set", C.c_int32), ("device", C.c_int32), ("resident", C.c_int32)]
 
 
 # Every symbol of include/spoa_gb300.h
@@ -119,7 +119,8 @@ EXPORTED = [
     "spoa_gb300_batch_launch",
     "spoa_gb300_batch_launch_plain", "spoa_gb300_batch_fetch", "spoa_gb300_batch_destroy",
     "spoa_gb300_batch_run", "spoa_gb300_server_create", "spoa_gb300_server_submit",
-    "spoa_gb300_server_wait", "spoa_gb300_server_stats", "spoa_gb300_server_destroy",
+    "spoa_gb300_server_wait", "spoa_gb300_server_stats", "spoa_gb300_server_resident_stats",
+    "spoa_gb300_server_destroy",
     "spoa_gb300_window_poa_noalloc",
 ]
 
@@ -173,6 +174,7 @@ def lib():
         L.spoa_gb300_server_submit.argtypes = [P, C.c_char_p, P, U32, I32, I32, C.c_double, P]
         L.spoa_gb300_server_wait.argtypes = [P, U64, C.c_double, C.c_char_p, U32, P, P, P]
         L.spoa_gb300_server_stats.argtypes = [P, P, P]
+        L.spoa_gb300_server_resident_stats.argtypes = [P, P, P]
         L.spoa_gb300_server_destroy.argtypes = [P]
         L.spoa_gb300_server_destroy.restype = None
         _lib = L
@@ -620,13 +622,14 @@ class Server:
     def __init__(self, type_: int, m: int, n: int, g: int, e: int | None = None,
                  q: int | None = None, c: int | None = None, memory_budget: int = 0,
                  max_streams: int = 0, max_windows_per_launch: int = 0,
-                 gather_seconds: float = 0.0, device: int | None = None):
+                 gather_seconds: float = 0.0, device: int | None = None,
+                 resident: bool = False):
         e = g if e is None else e
         if q is None or c is None:
             q, c = g, e
         d = _ServerDesc(type_, m, n, g, e, q, c, 0, memory_budget, max_streams,
                         max_windows_per_launch, gather_seconds,
-                        1 if device is not None else 0, int(device or 0))
+                        1 if device is not None else 0, int(device or 0), 1 if resident else 0)
         h = C.c_void_p()
         _check("Server::Create", lib().spoa_gb300_server_create(C.byref(d), C.byref(h)))
         self._h = h
@@ -659,7 +662,11 @@ class Server:
     def stats(self):
         la, co = C.c_uint64(), C.c_uint64()
         _check("Server::Stats", lib().spoa_gb300_server_stats(self._h, C.byref(la), C.byref(co)))
-        return {"launches": la.value, "completed": co.value}
+        rw, rl = C.c_uint64(), C.c_uint64()
+        _check("Server::Stats",
+               lib().spoa_gb300_server_resident_stats(self._h, C.byref(rw), C.byref(rl)))
+        return {"launches": la.value, "completed": co.value, "resident_windows": rw.value,
+                "resident_launches": rl.value}
 
     def close(self):
         if getattr(self, "_h", None):

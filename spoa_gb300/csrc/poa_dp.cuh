@@ -49,9 +49,11 @@ struct BlockScratch {
 };
 
 // Exclusive prefix-max of v over the CTA's threads (kNegBig for thread 0).
+// NW: warps of the CTA when known at compile time (0: blockDim.x / 32).
+template <int NW = 0>
 __device__ __forceinline__ int32_t block_excl_max(int32_t v, BlockScratch& sh) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t nw = blockDim.x >> 5;
+  const uint32_t nw = NW ? NW : blockDim.x >> 5;
   int32_t x = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -71,9 +73,10 @@ __device__ __forceinline__ int32_t block_excl_max(int32_t v, BlockScratch& sh) {
   return ex;
 }
 
+template <int NW = 0>
 __device__ __forceinline__ int32_t block_max(int32_t v, BlockScratch& sh) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t nw = blockDim.x >> 5;
+  const uint32_t nw = NW ? NW : blockDim.x >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = imax(v, __shfl_xor_sync(0xffffffffu, v, o));
   if (nw > 1) {
@@ -87,9 +90,10 @@ __device__ __forceinline__ int32_t block_max(int32_t v, BlockScratch& sh) {
   return v;
 }
 
+template <int NW = 0>
 __device__ __forceinline__ int32_t block_min(int32_t v, BlockScratch& sh) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t nw = blockDim.x >> 5;
+  const uint32_t nw = NW ? NW : blockDim.x >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
   if (nw > 1) {
@@ -110,13 +114,13 @@ __device__ __forceinline__ int32_t block_min(int32_t v, BlockScratch& sh) {
 // With b_t = agg_t - t*CPT*pen this is a plain prefix-max.  Only thread 0
 // knows `init`; it folds it into its own aggregate (its strip end is then
 // exactly X[CPT-1]), so the other threads never need it.
-template <int CPT>
+template <int CPT, int NW = 0>
 __device__ __forceinline__ int32_t scan_carry(int32_t agg, int32_t init, int32_t pen,
                                               BlockScratch& sh) {
   const int32_t t = (int32_t)threadIdx.x;
   const int32_t D = CPT * pen;
   int32_t v = t == 0 ? imax(agg, init + D) : agg;
-  int32_t ex = block_excl_max(v - t * D, sh);
+  int32_t ex = block_excl_max<NW>(v - t * D, sh);
   return t == 0 ? init : ex + (t - 1) * D;
 }
 
@@ -327,6 +331,19 @@ struct Lanes<int32_t> {
   }
 };
 
+// Lane masks of a pair from two bits: 0xFFFF in the low lane when bit 15 of
+// y is set, in the high lane when bit 31 is (one byte permute replicating
+// the sign bits of bytes 1 and 3).
+__device__ __forceinline__ uint32_t sign_lanes(uint32_t y) {
+  uint32_t mask;
+#ifdef __CUDA_ARCH__
+  asm("prmt.b32 %0, %1, 0, 0xBB99;" : "=r"(mask) : "r"(y));
+#else  // host builds of this header (test harness): the same lane masks
+  mask = ((y & 0x8000u) ? 0x0000FFFFu : 0u) | ((y & 0x80000000u) ? 0xFFFF0000u : 0u);
+#endif
+  return mask;
+}
+
 // Element index of column j in a row of a CTA of nt threads (see DpView):
 // column j is lane r / (CPT/2) of pair k = r % (CPT/2) of thread t = j / CPT
 // (r = j % CPT), and pair k of thread t is pair word
@@ -338,10 +355,11 @@ __host__ __device__ __forceinline__ uint64_t colmap(uint64_t j, uint64_t nt) {
 }
 
 // Value of thread t-1 (thread 0 gets `fill`).
+template <int NW = 0>
 __device__ __forceinline__ int32_t from_left(int32_t a, int32_t fill, BlockScratch& sh) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int32_t x = __shfl_up_sync(0xffffffffu, a, 1);
-  if ((blockDim.x >> 5) > 1) {
+  if ((NW ? NW : blockDim.x >> 5) > 1) {
     if (lane == 31) sh.wv[warp] = a;
     __syncthreads();
     if (lane == 0 && warp > 0) x = sh.wv[warp - 1];
@@ -353,17 +371,18 @@ __device__ __forceinline__ int32_t from_left(int32_t a, int32_t fill, BlockScrat
 // Strip scan of X[j] = max(a[j], X[j-1] + pen) over this thread's pairs with
 // the CTA carry.  On return x[k] holds X at the columns of pair k; returns
 // X[s-1], the value carried into the strip (init for thread 0).
-template <int CPT, typename Lx>
+template <int CPT, typename Lx, int NW = 0>
 __device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, int32_t pen,
                                              BlockScratch& sh) {
   constexpr int HP = CPT / 2;
+  static_assert(HP <= 16, "pair masks hold at most 16 pairs per strip");
   using P = typename Lx::P;
   const P pen2 = Lx::splat(pen);
 #pragma unroll
   for (int k = 1; k < HP; ++k) x[k] = Lx::addmax(x[k - 1], pen2, x[k]);
   const int32_t lo_agg = Lx::lo(x[HP - 1]), hi_agg = Lx::hi(x[HP - 1]);
   const int32_t agg = imax(hi_agg, lo_agg + HP * pen);
-  const int32_t c = scan_carry<CPT>(agg, init, pen, sh);  // X[s-1]
+  const int32_t c = scan_carry<CPT, NW>(agg, init, pen, sh);  // X[s-1]
   const int32_t c_hi = imax(lo_agg, c + HP * pen);          // X[s+HP-1]
   const P carry = Lx::make(c, c_hi);
 #pragma unroll
@@ -374,7 +393,10 @@ __device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, in
 
 // Forward pass + row selection + max_j (identical in every thread on
 // return).  T = int16_t for the 16-lane width, int32_t for the 8-lane one.
-template <int SUB, int CPT, typename T>
+// NT: the CTA's threads when known at compile time (0: blockDim.x); with it
+// every row offset of a load or store is a constant of the instruction and
+// the scans of a one-warp CTA take no shared-memory path.
+template <int SUB, int CPT, typename T, int NT = 0>
 __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restrict__ seq,
                            uint32_t L, uint32_t V, int32_t lanes, BlockScratch& sh,
                            int64_t* out_max_i, int64_t* out_max_j, int32_t* out_score) {
@@ -382,6 +404,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
   using P = typename Lx::P;
   using L16 = Lanes<int16_t>;
   constexpr int HP = CPT / 2;
+  static_assert(HP <= 16, "pair masks hold at most 16 pairs per strip");
   const uint32_t t = threadIdx.x;
   const uint32_t s0 = t * CPT;
   const uint64_t ld = D.caps.ld;        // elements per row
@@ -389,7 +412,8 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
   // pairs k and k+1 (k even) of this thread: pair words w0 + (k/2) * st2
   // and the next; the warp's accesses to them are contiguous
   const uint64_t w0 = 2 * (uint64_t)t;
-  const uint64_t st2 = 2 * (uint64_t)blockDim.x;
+  constexpr int NW = NT / 32;
+  const uint64_t st2 = 2 * (uint64_t)(NT ? NT : blockDim.x);
   const int32_t type = S.type;
   const int32_t m = S.m, n = S.n, g = S.g, e = S.e, q = S.q, c = S.c;
   const int32_t NEGW = lanes == 8 ? (INT32_MIN + 1024) : (INT16_MIN + 1024);
@@ -643,7 +667,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
     if (SUB == kLinear) {
 #pragma unroll
       for (int k = 0; k < HP; ++k) hs[k] = h[k];
-      pair_scan<CPT, Lx>(hs, fci, g, sh);
+      pair_scan<CPT, Lx, NW>(hs, fci, g, sh);
       if (type == kSW) {
         const P z = Lx::splat(0);
 #pragma unroll
@@ -655,7 +679,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
 #pragma unroll
         for (int k = 0; k < HP; ++k) x[k] = Lx::add(h[k], q2);
         // x = Q' (Q of the next column); Q[s0] = Q'[s0-1] is the carry
-        const int32_t qin = pair_scan<CPT, Lx>(x, fci + q, c, sh);
+        const int32_t qin = pair_scan<CPT, Lx, NW>(x, fci + q, c, sh);
         qq[0] = Lx::make(qin, Lx::lo(x[HP - 1]));
 #pragma unroll
         for (int k = 1; k < HP; ++k) qq[k] = x[k - 1];
@@ -665,14 +689,15 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
 #pragma unroll
         for (int k = 0; k < HP; ++k) {
           if (SUB == kConvex) {
-            const uint32_t bm = (((bmap >> k) & 1u) ? 0x0000FFFFu : 0u) |
-                                (((bmap >> (16 + k)) & 1u) ? 0xFFFF0000u : 0u);
-            x[k] = Lx::addmax(h[k], g2, Lx::select(bm, Lx::add(qq[k], g2), NEG2));
+            // max(H1, Q at vector starts) + g: bits k and 16 + k of bmap
+            // moved to bits 15 and 31 give the pair's lane masks
+            const uint32_t bm = sign_lanes(bmap << (15 - k));
+            x[k] = Lx::add(Lx::max(h[k], Lx::select(bm, qq[k], NEG2), NZ), g2);
           } else {
             x[k] = Lx::add(h[k], g2);
           }
         }
-        const int32_t ein = pair_scan<CPT, Lx>(x, fci + g, e, sh);  // x = E'
+        const int32_t ein = pair_scan<CPT, Lx, NW>(x, fci + g, e, sh);  // x = E'
         ee[0] = Lx::make(ein, Lx::lo(x[HP - 1]));
 #pragma unroll
         for (int k = 1; k < HP; ++k) ee[k] = x[k - 1];
@@ -686,7 +711,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
       }
     }
     // column s0-1 of this row (thread 0: the first column fc)
-    const int32_t lH = from_left(Lx::hi(hs[HP - 1]), fci, sh);
+    const int32_t lH = from_left<NW>(Lx::hi(hs[HP - 1]), fci, sh);
     // the gap rows E and Q as the recurrences computed them: the traceback
     // re-derives its horizontal tests from them
     if (SUB >= kAffine) {
@@ -743,8 +768,8 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
   }
 
   // global selection: best value, then the earliest row reaching it
-  const int32_t B = block_max(bval, sh);
-  const int32_t R = block_min(bval == B && brow >= 0 ? brow : 0x7fffffff, sh);
+  const int32_t B = block_max<NW>(bval, sh);
+  const int32_t R = block_min<NW>(bval == B && brow >= 0 ? brow : 0x7fffffff, sh);
   int64_t max_i = -1;
   int32_t score = 0;
   if (type == kSW) {
@@ -777,9 +802,9 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
       int32_t jj = 0x7fffffff;
       for (int r = 0; r < CPT && jj == 0x7fffffff; ++r) {
         const uint32_t j = s0 + r;
-        if (j < L && Lx::elem(H, base + colmap<CPT>(j, blockDim.x)) == score) jj = (int32_t)j;
+        if (j < L && Lx::elem(H, base + colmap<CPT>(j, NT ? NT : blockDim.x)) == score) jj = (int32_t)j;
       }
-      jj = block_min(jj, sh);
+      jj = block_min<NW>(jj, sh);
       max_j = jj == 0x7fffffff ? -1 : jj;
     }
   }
@@ -806,6 +831,7 @@ __device__ __noinline__ void dp_forward_seg(const Scoring& S, DpView& D,
   using P = typename Lx::P;
   using L16 = Lanes<int16_t>;
   constexpr int HP = CPT / 2;
+  static_assert(HP <= 16, "pair masks hold at most 16 pairs per strip");
   const uint32_t t = threadIdx.x, nt = blockDim.x, ntv = nt * SEGS;
   const uint64_t ld = D.caps.ld;
   const uint64_t wrow = ld / 2;
@@ -1003,9 +1029,8 @@ __device__ __noinline__ void dp_forward_seg(const Scoring& S, DpView& D,
 #pragma unroll
           for (int k = 0; k < HP; ++k) {
             if (SUB == kConvex) {
-              const uint32_t bm = (((bmap >> k) & 1u) ? 0x0000FFFFu : 0u) |
-                                  (((bmap >> (16 + k)) & 1u) ? 0xFFFF0000u : 0u);
-              x[k] = Lx::addmax(h[k], g2, Lx::select(bm, Lx::add(qq[k], g2), NEG2));
+              const uint32_t bm = sign_lanes(bmap << (15 - k));
+              x[k] = Lx::add(Lx::max(h[k], Lx::select(bm, qq[k], NEG2), NZ), g2);
             } else {
               x[k] = Lx::add(h[k], g2);
             }
@@ -1166,9 +1191,28 @@ static __device__ __noinline__ int32_t dp_traceback(const Scoring& S, const DpVi
     tb[2 * np + 1] = (b);             \
     ++np;                             \
   } while (0)
+  // The path mostly steps diagonally through the previous ranks: the H
+  // cells kTbAhead steps ahead on the current diagonal and on the diagonal
+  // one row up (where it continues after a vertical move) are prefetched
+  // into L1 while this step is tested, so the walk rarely waits for DRAM.
+  constexpr int64_t kTbAhead = 8;
+  auto prefetch = [&](int64_t row, int64_t col) {
+#ifdef __CUDA_ARCH__
+    const char* p = static_cast<const char*>(H) +
+                    sizeof(T) * ((uint64_t)row * ld + colmap<CPT>((uint64_t)col, nt));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+#else
+    (void)row;
+    (void)col;
+#endif
+  };
   while (true) {
     if (++guard > guard_max) return kTraceback;
     if (j == -1 || i == 0) break;
+    if (i > kTbAhead + 1 && j >= kTbAhead) {
+      prefetch(i - kTbAhead, j - kTbAhead);
+      prefetch(i - kTbAhead - 1, j - kTbAhead);
+    }
     const uint32_t node = G.rank_to_node[i - 1];
     const int32_t h = at(H, i, j);
     if (type == kSW && h == 0) break;

@@ -212,7 +212,7 @@ __global__ void k_import(GraphView G, ImportArgs a, int32_t* status) {
 template <typename T>
 constexpr int kBatchMaxRegs = sizeof(T) == 2 ? 96 : 128;
 
-template <int SUB, int CPT, typename T, int SEGS = 1>
+template <int SUB, int CPT, typename T, int SEGS = 1, int NT = 0>
 __global__ void __maxnreg__(kBatchMaxRegs<T>) k_batch(BatchArgs a) {
   __shared__ BlockScratch sh;
   __shared__ SharedState ss;
@@ -253,9 +253,9 @@ __global__ void __maxnreg__(kBatchMaxRegs<T>) k_batch(BatchArgs a) {
       // for each source node; known once the rows are built
       const uint64_t npred_before = V0 ? 1 : 0;
       cells += (unsigned long long)V0 * L * (strand ? 2u : 1u);
-      window_read<SUB, CPT, T, SEGS>(S, G, D, sh, ss, a.seqs + off, L,
-                               a.quals ? a.quals + off : nullptr, strand, &s_score, &s_rev,
-                               &s_pairs, &s_np);
+      window_read<SUB, CPT, T, SEGS, NT>(S, G, D, sh, ss, a.seqs + off, L,
+                                         a.quals ? a.quals + off : nullptr, strand, &s_score,
+                                         &s_rev, &s_pairs, &s_np);
       if (ss.status != kOk) {
         status = ss.status;
         break;
@@ -294,6 +294,154 @@ __global__ void __maxnreg__(kBatchMaxRegs<T>) k_batch(BatchArgs a) {
       a.win_status[w] = status;
       if (a.cells) atomicAdd(a.cells, cells);
       if (a.pred_cells) atomicAdd(a.pred_cells, pred_cells);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// resident kernel of the served form
+// ---------------------------------------------------------------------------
+// Windows handed to a running kernel: the host appends one slot per window
+// to a ring in host-mapped memory and then raises `tail`; every CTA of the
+// resident kernel claims the next published slot (CAS on `head`, device
+// memory), runs the window in its own arena (the per-read loop of
+// src/main.cpp:275-314, then GenerateConsensus) and writes the consensus
+// and status back into host-mapped memory, `seq` last.  A CTA that finds no
+// work polls with a back-off and leaves after `idle_ns` nanoseconds without
+// any (a bounded wait: the kernel never spins forever; the host launches it
+// again when new work arrives and it has ended).
+struct ServeSlot {
+  const uint8_t* seqs;      // device: the window's reads back to back
+  const uint64_t* seq_off;  // device: n_reads + 1 offsets into seqs
+  uint8_t* cons;            // host-mapped: consensus output, cons_cap bytes
+  uint32_t n_reads, cons_cap;
+  int32_t type, strand;
+};
+struct ServeDone {
+  int32_t status;
+  uint32_t cons_len;
+  unsigned long long cells;
+  unsigned long long seq;  // slot index + 1 of the finished window, written last
+};
+struct ServeArgs {
+  Scoring base;
+  const ServeSlot* ring;  // host-mapped, `cap` slots
+  ServeDone* done;        // host-mapped, `cap` entries
+  uint32_t cap;
+  const unsigned long long* tail;  // host-mapped: slots published
+  unsigned long long* head;        // device: slots claimed
+  uint8_t* arena;
+  uint64_t arena_stride;
+  GraphCaps gcaps;
+  DpCaps dcaps;
+  unsigned long long idle_ns;
+};
+
+__device__ __forceinline__ unsigned long long serve_clock_ns() {
+  unsigned long long t = 0;
+#ifdef __CUDA_ARCH__
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+#endif
+  return t;
+}
+
+__device__ __forceinline__ unsigned long long load_acquire_sys(const unsigned long long* p) {
+  unsigned long long v = 0;
+#ifdef __CUDA_ARCH__
+  asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+#endif
+  return v;
+}
+
+__device__ __forceinline__ void store_release_sys(unsigned long long* p, unsigned long long v) {
+#ifdef __CUDA_ARCH__
+  asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+#endif
+}
+
+template <int SUB, int CPT, typename T, int NT = 0>
+__global__ void __maxnreg__(kBatchMaxRegs<T>) k_serve(ServeArgs a) {
+  __shared__ BlockScratch sh;
+  __shared__ SharedState ss;
+  __shared__ unsigned long long s_k;
+  __shared__ ServeSlot slot;
+  __shared__ const int32_t* s_pairs;
+  __shared__ int32_t s_score, s_rev;
+  __shared__ uint32_t s_np;
+  __shared__ GraphView G;
+  __shared__ DpView D;
+  if (threadIdx.x == 0) {
+    uint8_t* base = a.arena + a.arena_stride * blockIdx.x;
+    const uint64_t gbytes = graph_layout(base, a.gcaps, &G);
+    dp_layout(base + gbytes, a.dcaps, &D);
+  }
+  __syncthreads();
+  Scoring S = a.base;
+  while (true) {
+    if (threadIdx.x == 0) {
+      // claim the next published slot, waiting at most idle_ns for one
+      s_k = ~0ull;
+      const unsigned long long t0 = serve_clock_ns();
+      unsigned int nap = 256;
+      while (true) {
+        const unsigned long long t = load_acquire_sys(a.tail);
+        const unsigned long long h = *(volatile unsigned long long*)a.head;
+        if (h < t) {
+          if (atomicCAS(a.head, h, h + 1) == h) {
+            s_k = h;
+            break;
+          }
+          continue;
+        }
+        if (serve_clock_ns() - t0 > a.idle_ns) break;
+#ifdef __CUDA_ARCH__
+        __nanosleep(nap);
+#endif
+        if (nap < 65536) nap *= 2;
+      }
+      if (s_k != ~0ull) {
+        const volatile ServeSlot* v = a.ring + (s_k % a.cap);
+        slot.seqs = v->seqs;
+        slot.seq_off = v->seq_off;
+        slot.cons = v->cons;
+        slot.n_reads = v->n_reads;
+        slot.cons_cap = v->cons_cap;
+        slot.type = v->type;
+        slot.strand = v->strand;
+        g_reset(G);
+      }
+    }
+    __syncthreads();
+    const unsigned long long k = s_k;
+    if (k == ~0ull) break;
+    S.type = slot.type;
+    const bool strand = slot.strand != 0;
+    int32_t status = kOk;
+    unsigned long long cells = 0;
+    for (uint32_t r = 0; r < slot.n_reads; ++r) {
+      const uint64_t off = slot.seq_off[r];
+      const uint32_t L = (uint32_t)(slot.seq_off[r + 1] - off);
+      cells += (unsigned long long)G.hdr->n_nodes * L * (strand ? 2u : 1u);
+      window_read<SUB, CPT, T, 1, NT>(S, G, D, sh, ss, slot.seqs + off, L, nullptr, strand,
+                                      &s_score, &s_rev, &s_pairs, &s_np);
+      if (ss.status != kOk) {
+        status = ss.status;
+        break;
+      }
+    }
+    if (threadIdx.x == 0) {
+      uint32_t len = 0;
+      if (status == kOk) {
+        write_consensus(G, slot.cons, slot.cons_cap, &len);
+        if (len > slot.cons_cap) status = kCapacity;
+      }
+      ServeDone* d = a.done + (k % a.cap);
+      d->status = status;
+      d->cons_len = len;
+      d->cells = cells;
+      __threadfence_system();
+      store_release_sys(&d->seq, k + 1);
     }
     __syncthreads();
   }
@@ -374,9 +522,15 @@ int32_t launch_align_add(int cpt, int nt, const Scoring& S, const GraphView& G,
   return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
 }
 
+// One-warp tiles (every polishing-sized window) run the kernels built for
+// exactly 32 threads (NT = 32 in dp_forward); other tiles the general ones.
 template <int SUB, typename T>
 int32_t launch_batch(int cpt, int nt, int grid, const BatchArgs& a, cudaStream_t s) {
-#define L_(C) k_batch<SUB, C, T><<<grid, nt, 0, s>>>(a)
+#define L_(C)                                          \
+  if (nt == 32)                                        \
+    k_batch<SUB, C, T, 1, 32><<<grid, nt, 0, s>>>(a);  \
+  else                                                 \
+    k_batch<SUB, C, T><<<grid, nt, 0, s>>>(a)
   SPOA_CPT_SWITCH(T, cpt, L_)
 #undef L_
   return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
@@ -418,7 +572,10 @@ int32_t occupancy_batch_seg(int segs, int nt, int* blocks) {
 template <int SUB, typename T>
 int32_t occupancy_batch(int cpt, int nt, int* blocks) {
   cudaError_t err = cudaSuccess;
-#define L_(C) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch<SUB, C, T>, nt, 0)
+#define L_(C)                                                                                 \
+  err = nt == 32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch<SUB, C, T, 1, 32>, \
+                                                                 nt, 0)                       \
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch<SUB, C, T>, nt, 0)
   SPOA_CPT_SWITCH(T, cpt, L_)
 #undef L_
   if (err != cudaSuccess) {
@@ -460,6 +617,33 @@ int32_t occupancy_batch_mw(int cpt, int nt, int W, int* blocks) {
   return kOk;
 }
 
+template <int SUB, typename T>
+int32_t launch_serve(int cpt, int nt, int grid, const ServeArgs& a, cudaStream_t s) {
+#define L_(C)                                          \
+  if (nt == 32)                                        \
+    k_serve<SUB, C, T, 32><<<grid, nt, 0, s>>>(a);     \
+  else                                                 \
+    k_serve<SUB, C, T><<<grid, nt, 0, s>>>(a)
+  SPOA_CPT_SWITCH(T, cpt, L_)
+#undef L_
+  return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
+}
+
+template <int SUB, typename T>
+int32_t occupancy_serve(int cpt, int nt, int* blocks) {
+  cudaError_t err = cudaSuccess;
+#define L_(C)                                                                                  \
+  err = nt == 32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_serve<SUB, C, T, 32>, nt, 0) \
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_serve<SUB, C, T>, nt, 0)
+  SPOA_CPT_SWITCH(T, cpt, L_)
+#undef L_
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    return kCuda;
+  }
+  return kOk;
+}
+
 #define SPOA_GB300_INSTANTIATE(SUB, T)                                                          \
   template int32_t launch_align<SUB, T>(int, int, const Scoring&, const GraphView&,             \
                                         const DpView&, const uint8_t*, uint32_t, ReadOut*);     \
@@ -468,7 +652,9 @@ int32_t occupancy_batch_mw(int cpt, int nt, int W, int* blocks) {
                                             const uint8_t*, int32_t, ReadOut*, const ReadOut*,  \
                                             cudaStream_t);                                      \
   template int32_t launch_batch<SUB, T>(int, int, int, const BatchArgs&, cudaStream_t);         \
-  template int32_t occupancy_batch<SUB, T>(int, int, int*);
+  template int32_t occupancy_batch<SUB, T>(int, int, int*);                                      \
+  template int32_t launch_serve<SUB, T>(int, int, int, const ServeArgs&, cudaStream_t);         \
+  template int32_t occupancy_serve<SUB, T>(int, int, int*);
 
 #define SPOA_GB300_INSTANTIATE_MW(SUB)                                                          \
   template int32_t launch_batch_mw<SUB>(int, int, int, int, const BatchArgs&, cudaStream_t);    \

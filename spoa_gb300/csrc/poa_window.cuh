@@ -36,7 +36,7 @@ struct SharedState {
 // int32 otherwise.  An int32 kernel runs int16-width reads with the 16-lane
 // semantics (vector starts of the convex E recurrence, -infinity of the NW
 // row selection), which gives the same results.
-template <int SUB, int CPT, typename T, int SEGS = 1>
+template <int SUB, int CPT, typename T, int SEGS = 1, int NT = 0>
 __device__ void read_align(const Scoring& S, const GraphView& G, DpView& D, BlockScratch& sh,
                            SharedState& ss, const uint8_t* seq, uint32_t L, int32_t lanes,
                            int32_t* pairs, int32_t* has, int32_t* score, uint32_t* np) {
@@ -44,7 +44,7 @@ __device__ void read_align(const Scoring& S, const GraphView& G, DpView& D, Bloc
   int32_t sc;
   const uint32_t V = G.hdr->n_nodes;
   if constexpr (SEGS == 1)
-    dp_forward<SUB, CPT, T>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
+    dp_forward<SUB, CPT, T, NT>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
   else
     dp_forward_seg<SUB, CPT, T, SEGS>(S, D, seq, L, V, lanes, sh, &mi, &mj, &sc);
   if (threadIdx.x == 0) {
@@ -95,7 +95,8 @@ __device__ inline void read_prologue(const Scoring& S, const GraphView& G, const
 }
 
 // One read of a window: align (both strands when asked), choose, add.
-template <int SUB, int CPT, typename T, int SEGS = 1>
+// NT: the CTA's threads when known at compile time (dp_forward).
+template <int SUB, int CPT, typename T, int SEGS = 1, int NT = 0>
 __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScratch& sh,
                             SharedState& ss, const uint8_t* seq, uint32_t L,
                             const uint8_t* qual, bool strand, int32_t* out_score,
@@ -111,16 +112,16 @@ __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScra
   }
   if (dp) {
     dp_build_rows(G, D, sh);
-    read_align<SUB, CPT, T, SEGS>(S, G, D, sh, ss, seq, L, ss.lanes, D.aln_a, &ss.has_f, &ss.score_f,
-                            &ss.np_f);
+    read_align<SUB, CPT, T, SEGS, NT>(S, G, D, sh, ss, seq, L, ss.lanes, D.aln_a, &ss.has_f,
+                                      &ss.score_f, &ss.np_f);
   }
   if (strand) {
     for (uint32_t j = threadIdx.x; j < L; j += blockDim.x)
       D.seq_rc[j] = complement_base(seq[L - 1 - j]);
     __syncthreads();
     if (dp && ss.status == kOk)
-      read_align<SUB, CPT, T, SEGS>(S, G, D, sh, ss, D.seq_rc, L, ss.lanes, D.aln_b, &ss.has_r,
-                              &ss.score_r, &ss.np_r);
+      read_align<SUB, CPT, T, SEGS, NT>(S, G, D, sh, ss, D.seq_rc, L, ss.lanes, D.aln_b,
+                                        &ss.has_r, &ss.score_r, &ss.np_r);
   }
   __syncthreads();
   if (ss.status == kOk) {

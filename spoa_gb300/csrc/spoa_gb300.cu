@@ -47,7 +47,9 @@ namespace spoa_gb300 {
                                                    const uint8_t*, int32_t, ReadOut*,           \
                                                    const ReadOut*, cudaStream_t);               \
   extern template int32_t launch_batch<SUB, T>(int, int, int, const BatchArgs&, cudaStream_t);  \
-  extern template int32_t occupancy_batch<SUB, T>(int, int, int*);
+  extern template int32_t occupancy_batch<SUB, T>(int, int, int*);                               \
+  extern template int32_t launch_serve<SUB, T>(int, int, int, const ServeArgs&, cudaStream_t);  \
+  extern template int32_t occupancy_serve<SUB, T>(int, int, int*);
 SPOA_EXTERN(kLinear, int16_t)
 SPOA_EXTERN(kAffine, int16_t)
 SPOA_EXTERN(kConvex, int16_t)
@@ -2084,6 +2086,7 @@ struct ServedWindow {
   uint32_t lmax = 1;
   uint64_t sumlen = 0;
   WindowPlan plan;
+  bool resident_failed = false;  // the resident kernel could not hold it
   Clock::time_point arrival;
   // results
   bool done = false;
@@ -2107,6 +2110,61 @@ struct ServedLaunch {
   bool busy = false;
 };
 
+// The resident form of the server: polishing-sized windows (16-bit
+// scores, reads of at most 640 bases) go to one persistent kernel (k_serve)
+// that keeps running while work keeps arriving.  Each window takes a slot of
+// a ring in host-mapped memory; its reads are copied to the device in
+// batches, and a batch is published (ring slots filled, `tail` raised)
+// once its copy has completed.  The kernel's CTAs claim published slots and
+// write each consensus and status back into host-mapped memory.
+constexpr uint32_t kResidentMaxLen = 640;  // one warp of 20 columns per thread
+constexpr uint32_t kResidentMaxReads = 255;
+constexpr uint64_t kResidentMaxBases = 65534;
+constexpr uint32_t kResidentRing = 8192;
+constexpr uint32_t kResidentConsCap = 2 * kResidentMaxLen + 64;
+constexpr unsigned long long kResidentIdleNs = 20ull * 1000 * 1000;  // 20 ms without work
+
+struct ResidentStage {  // one batch of windows on its way to the device
+  uint8_t* pinned = nullptr;
+  uint64_t cap = 0;
+  cudaEvent_t copied = nullptr;
+  std::vector<uint64_t> ks;  // ring slots of the batch, in order
+};
+
+struct Resident {
+  bool ready = false;
+  bool failed = false;  // set-up failed: the launch path serves every window
+  int cpt = 0, nt = 0, ctas = 0;
+  GraphCaps gc{};
+  DpCaps dc{};
+  uint64_t stride = 0, arena_off = ~0ull;
+  void* host = nullptr;  // the mapped block: ring, done, tail, consensus
+  ptrdiff_t host_to_dev = 0;  // device address of the mapped block minus its host address
+  ServeSlot* ring = nullptr;
+  ServeDone* done = nullptr;
+  unsigned long long* tail = nullptr;
+  uint8_t* cons = nullptr;
+  DeviceBuf head;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ended = nullptr;
+  bool launched = false;
+  uint64_t next = 0, published = 0, head_seen = 0;
+  struct Entry {
+    std::shared_ptr<ServedWindow> w;
+    uint64_t in_off = ~0ull;
+    bool live = false;
+  };
+  std::vector<Entry> entries;      // per ring slot
+  std::deque<uint64_t> in_flight;  // published slots not yet finished
+  std::deque<ResidentStage> staging;
+  std::vector<ResidentStage> spare;
+  std::atomic<uint64_t> windows{0}, launches{0};
+  template <typename X>
+  X* dev(X* host_ptr) const {
+    return reinterpret_cast<X*>(reinterpret_cast<uint8_t*>(host_ptr) + host_to_dev);
+  }
+};
+
 }  // namespace
 
 struct spoa_gb300_server {
@@ -2114,6 +2172,7 @@ struct spoa_gb300_server {
   Scoring base{};
   int device = 0;
   DevicePool pool;
+  Resident res;
   std::vector<ServedLaunch> slots;
   std::mutex mu;
   std::condition_variable cv;  // completions, for wait()
@@ -2150,6 +2209,8 @@ void finish_window(spoa_gb300_server* sv, const std::shared_ptr<ServedWindow>& w
   sv->cv.notify_all();
 }
 
+bool resident_eligible(const spoa_gb300_server* sv, const ServedWindow& w);
+
 // Takes arrived windows of the front window's class and width (in arrival
 // order) into a free slot while their footprint fits the pool; false when
 // nothing could be admitted.
@@ -2157,13 +2218,20 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
   std::vector<std::shared_ptr<ServedWindow>> take;
   {
     std::lock_guard<std::mutex> lk(sv->mu);
-    if (sv->pending.empty()) return false;
-    const auto& f = sv->pending.front();
+    // windows the resident kernel takes are not launched
+    auto first = std::find_if(sv->pending.begin(), sv->pending.end(),
+                              [&](const std::shared_ptr<ServedWindow>& w) {
+                                return !resident_eligible(sv, *w);
+                              });
+    if (first == sv->pending.end()) return false;
+    const auto& f = *first;
     const bool wide = f->plan.wide;
     const int cls = length_class(f->lmax);
     const size_t cap = (size_t)std::max(1, sv->desc.max_windows_per_launch);
-    for (auto it = sv->pending.begin(); it != sv->pending.end() && take.size() < cap; ++it)
-      if ((*it)->plan.wide == wide && length_class((*it)->lmax) == cls) take.push_back(*it);
+    for (auto it = first; it != sv->pending.end() && take.size() < cap; ++it)
+      if (!resident_eligible(sv, **it) && (*it)->plan.wide == wide &&
+          length_class((*it)->lmax) == cls)
+        take.push_back(*it);
   }
   const bool wide = take.front()->plan.wide;
   // footprint of the first k windows; halve k until it fits the pool
@@ -2377,6 +2445,266 @@ void complete(spoa_gb300_server* sv, ServedLaunch& L, bool ok) {
   L.busy = false;
 }
 
+// Sets up the resident kernel's ring, arenas and stream (first use).
+bool resident_setup_once(spoa_gb300_server* sv);
+bool resident_setup(spoa_gb300_server* sv) {
+  Resident& R = sv->res;
+  if (R.ready) return true;
+  if (R.failed) return false;
+  if (!resident_setup_once(sv)) R.failed = true;
+  return R.ready;
+}
+
+bool resident_setup_once(spoa_gb300_server* sv) {
+  Resident& R = sv->res;
+  if (!throughput_tile(kResidentMaxLen, false, &R.cpt, &R.nt)) return false;
+  int blocks = 1;
+  if (SPOA_BY_SUB(sv->base.sub, false, occupancy_serve, R.cpt, R.nt, &blocks)) return false;
+  int sms = 1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sv->device);
+  // three quarters of the CTA slots: launches of other windows share the GPU
+  uint64_t ctas = std::max<uint64_t>(1, (uint64_t)sms * std::max(blocks, 1) * 3 / 4);
+  R.gc.nodes = 4096;
+  R.gc.edges = 4 * R.gc.nodes + 64;
+  R.gc.labels = (uint32_t)kResidentMaxBases + 2;
+  R.gc.seqs = kResidentMaxReads + 1;
+  R.gc.aligned = 4;
+  R.dc = DpCaps{R.gc.nodes + 1, (uint32_t)(R.cpt * R.nt), R.gc.edges + R.gc.nodes + 2,
+                sv->base.sub, 2};
+  GraphView gv;
+  DpView dv;
+  R.stride = align_up(graph_layout(nullptr, R.gc, &gv), 256) +
+             align_up(dp_layout(nullptr, R.dc, &dv), 256);
+  // at most half of the budget for the resident arenas
+  ctas = std::min<uint64_t>(ctas, std::max<uint64_t>(1, sv->pool.size() / 2 / R.stride));
+  R.arena_off = sv->pool.alloc(R.stride * ctas);
+  if (R.arena_off == ~0ull) return false;
+  R.ctas = (int)ctas;
+  const uint64_t bytes = a16(sizeof(ServeSlot) * kResidentRing) +
+                         a16(sizeof(ServeDone) * kResidentRing) + a16(sizeof(unsigned long long)) +
+                         (uint64_t)kResidentConsCap * kResidentRing;
+  if (cudaHostAlloc(&R.host, bytes, cudaHostAllocMapped) != cudaSuccess) {
+    cudaGetLastError();
+    R.host = nullptr;
+    return false;
+  }
+  std::memset(R.host, 0, bytes);
+  void* dev = nullptr;
+  if (cudaHostGetDevicePointer(&dev, R.host, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  R.host_to_dev = static_cast<uint8_t*>(dev) - static_cast<uint8_t*>(R.host);
+  uint8_t* h = static_cast<uint8_t*>(R.host);
+  R.ring = reinterpret_cast<ServeSlot*>(h);
+  h += a16(sizeof(ServeSlot) * kResidentRing);
+  R.done = reinterpret_cast<ServeDone*>(h);
+  h += a16(sizeof(ServeDone) * kResidentRing);
+  R.tail = reinterpret_cast<unsigned long long*>(h);
+  h += a16(sizeof(unsigned long long));
+  R.cons = h;
+  if (R.head.ensure(8) || cudaMemset(R.head.p, 0, 8) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&R.ended, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  R.entries.resize(kResidentRing);
+  R.ready = true;
+  return true;
+}
+
+bool resident_eligible(const spoa_gb300_server* sv, const ServedWindow& w) {
+  return sv->desc.resident && !sv->res.failed && !w.plan.wide && !w.plan.many_aligned && !w.resident_failed &&
+         w.off.size() > 1 && w.lmax <= kResidentMaxLen && w.off.size() - 1 <= kResidentMaxReads &&
+         w.sumlen <= kResidentMaxBases;
+}
+
+// Moves arrived resident-eligible windows into one staging batch (ring
+// slots, device input memory from the pool, one copy); false when nothing
+// moved.
+bool resident_admit(spoa_gb300_server* sv) {
+  Resident& R = sv->res;
+  std::vector<std::shared_ptr<ServedWindow>> take;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    for (const auto& w : sv->pending)
+      if (resident_eligible(sv, *w)) take.push_back(w);
+  }
+  if (take.empty() || !resident_setup(sv)) return false;
+  ResidentStage st;
+  if (!R.spare.empty()) {
+    st = std::move(R.spare.back());
+    R.spare.pop_back();
+  } else if (cudaEventCreateWithFlags(&st.copied, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  st.ks.clear();
+  // inputs of the batch: per window its read offsets, then its reads
+  std::vector<std::pair<uint64_t, uint64_t>> parts;  // (pool offset, bytes)
+  uint64_t total = 0;
+  size_t n = 0;
+  for (; n < take.size(); ++n) {
+    const ServedWindow& w = *take[n];
+    const uint64_t k = R.next + n;
+    if (R.entries[k % kResidentRing].live) break;  // ring full
+    const uint64_t bytes = a16(8 * w.off.size()) + a16(w.sumlen);
+    const uint64_t off = sv->pool.alloc(bytes);
+    if (off == ~0ull) break;  // no memory now: the rest waits
+    parts.emplace_back(off, bytes);
+    total += bytes;
+  }
+  if (n == 0) {
+    R.spare.push_back(std::move(st));
+    return false;
+  }
+  if (st.cap < total) {
+    if (st.pinned) cudaFreeHost(st.pinned);
+    st.pinned = nullptr;
+    st.cap = 0;
+    if (cudaHostAlloc(&st.pinned, total, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      st.pinned = nullptr;
+      for (auto& p : parts) sv->pool.release(p.first);
+      R.spare.push_back(std::move(st));
+      return false;
+    }
+    st.cap = total;
+  }
+  uint64_t o = 0;
+  bool ok = true;
+  for (size_t i = 0; i < n; ++i) {
+    const ServedWindow& w = *take[i];
+    uint8_t* dst = st.pinned + o;
+    std::memcpy(dst, w.off.data(), 8 * w.off.size());
+    std::memcpy(dst + a16(8 * w.off.size()), w.seqs.data(), w.sumlen);
+    ok = ok && cudaMemcpyAsync(sv->pool.ptr(parts[i].first), dst, parts[i].second,
+                               cudaMemcpyHostToDevice, R.stream) == cudaSuccess;
+    o += parts[i].second;
+    const uint64_t k = R.next++;
+    Resident::Entry& e = R.entries[k % kResidentRing];
+    e.w = take[i];
+    e.in_off = parts[i].first;
+    e.live = true;
+    st.ks.push_back(k);
+    ServeSlot& slot = R.ring[k % kResidentRing];
+    slot.seqs = sv->pool.ptr(parts[i].first) + a16(8 * w.off.size());
+    slot.seq_off = reinterpret_cast<const uint64_t*>(sv->pool.ptr(parts[i].first));
+    slot.cons = R.dev(R.cons + (uint64_t)(k % kResidentRing) * kResidentConsCap);
+    slot.n_reads = (uint32_t)(w.off.size() - 1);
+    slot.cons_cap = kResidentConsCap;
+    slot.type = w.type;
+    slot.strand = w.strand;
+  }
+  ok = ok && cudaEventRecord(st.copied, R.stream) == cudaSuccess;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    for (size_t i = 0; i < n; ++i)
+      sv->pending.erase(std::find(sv->pending.begin(), sv->pending.end(), take[i]));
+  }
+  if (!ok) cudaGetLastError();  // the batch is published and reported after its event
+  R.staging.push_back(std::move(st));
+  return true;
+}
+
+// Publishes staged batches whose copy completed (in order), starts the
+// kernel when it is not running and published work is unclaimed, and
+// hands out finished windows.  Returns true when anything happened; sets
+// *busy when windows are still in flight.
+bool resident_progress(spoa_gb300_server* sv, bool* busy) {
+  Resident& R = sv->res;
+  *busy = false;
+  if (!R.ready) return false;
+  bool progress = false;
+  while (!R.staging.empty()) {
+    ResidentStage& st = R.staging.front();
+    const cudaError_t q = cudaEventQuery(st.copied);
+    if (q == cudaErrorNotReady) break;
+    if (q != cudaSuccess) cudaGetLastError();
+    for (uint64_t k : st.ks) R.in_flight.push_back(k);
+    R.published = st.ks.back() + 1;
+    std::atomic_thread_fence(std::memory_order_release);
+    reinterpret_cast<std::atomic<unsigned long long>*>(R.tail)->store(R.published,
+                                                                      std::memory_order_release);
+    R.spare.push_back(std::move(st));
+    R.staging.pop_front();
+    progress = true;
+  }
+  // the kernel: (re)started when it has ended and published work is unclaimed
+  if (R.published > R.head_seen) {
+    const bool running = R.launched && cudaEventQuery(R.ended) == cudaErrorNotReady;
+    if (!running) {
+      cudaGetLastError();
+      unsigned long long head = 0;
+      if (cudaMemcpy(&head, R.head.p, 8, cudaMemcpyDeviceToHost) == cudaSuccess)
+        R.head_seen = head;
+      else
+        cudaGetLastError();
+      if (R.head_seen < R.published) {
+        ServeArgs a{};
+        a.base = sv->base;
+        a.ring = R.dev(R.ring);
+        a.done = R.dev(R.done);
+        a.cap = kResidentRing;
+        a.tail = R.dev(R.tail);
+        a.head = R.head.as<unsigned long long>();
+        a.arena = sv->pool.ptr(R.arena_off);
+        a.arena_stride = R.stride;
+        a.gcaps = R.gc;
+        a.dcaps = R.dc;
+        a.idle_ns = kResidentIdleNs;
+        if (SPOA_BY_SUB(sv->base.sub, false, launch_serve, R.cpt, R.nt, R.ctas, a, R.stream) ==
+                kOk &&
+            cudaEventRecord(R.ended, R.stream) == cudaSuccess) {
+          R.launched = true;
+          ++R.launches;
+          ++sv->launches;
+          progress = true;
+        } else {
+          cudaGetLastError();
+        }
+      }
+    }
+  }
+  // finished windows
+  for (size_t i = 0; i < R.in_flight.size();) {
+    const uint64_t k = R.in_flight[i];
+    ServeDone& d = R.done[k % kResidentRing];
+    const unsigned long long seq =
+        reinterpret_cast<std::atomic<unsigned long long>*>(&d.seq)->load(std::memory_order_acquire);
+    if (seq != k + 1) {
+      ++i;
+      continue;
+    }
+    Resident::Entry& e = R.entries[k % kResidentRing];
+    std::shared_ptr<ServedWindow> w = std::move(e.w);
+    const int32_t status = d.status;
+    const uint32_t len = d.cons_len;
+    sv->pool.release(e.in_off);
+    e.live = false;
+    R.in_flight.erase(R.in_flight.begin() + (long)i);
+    progress = true;
+    ++R.windows;
+    if (status == kNeedWide || status == kCapacity) {
+      // outside the resident kernel's limits: the launch path runs it again
+      w->resident_failed = true;
+      if (status == kNeedWide) w->plan.wide = true;
+      std::lock_guard<std::mutex> lk(sv->mu);
+      sv->pending.push_front(w);
+      continue;
+    }
+    std::string cons;
+    if (status == kOk)
+      cons.assign(reinterpret_cast<const char*>(R.cons + (uint64_t)(k % kResidentRing) *
+                                                             kResidentConsCap),
+                  std::min<uint32_t>(len, kResidentConsCap));
+    finish_window(sv, w, status, std::move(cons));
+  }
+  *busy = !R.in_flight.empty() || !R.staging.empty();
+  return progress;
+}
+
 void serve_loop(spoa_gb300_server* sv) {
   cudaSetDevice(sv->device);
   const auto gather = std::chrono::duration<double>(std::max(0.0, sv->desc.gather_seconds));
@@ -2401,6 +2729,15 @@ void serve_loop(spoa_gb300_server* sv) {
         sv->pending.push_back(sv->incoming.begin()->second);
         sv->incoming.erase(sv->incoming.begin());
       }
+    }
+    if (sv->desc.resident) {
+      if (resident_admit(sv)) progress = true;
+      bool busy = false;
+      if (resident_progress(sv, &busy)) progress = true;
+      if (busy) in_flight = true;
+    }
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
       waiting = !sv->pending.empty() || !sv->incoming.empty();
     }
     for (ServedLaunch& L : sv->slots) {
@@ -2542,11 +2879,35 @@ int32_t spoa_gb300_server_stats(const spoa_gb300_server* sv, uint64_t* launches,
   return kOk;
 }
 
+int32_t spoa_gb300_server_resident_stats(const spoa_gb300_server* sv, uint64_t* windows,
+                                         uint64_t* launches) {
+  if (!sv) return kInvalidArgument;
+  if (windows) *windows = sv->res.windows;
+  if (launches) *launches = sv->res.launches;
+  return kOk;
+}
+
 void spoa_gb300_server_destroy(spoa_gb300_server* sv) {
   if (!sv) return;
   sv->stop = true;
   if (sv->loop.joinable()) sv->loop.join();
   DeviceGuard guard(sv->device);
+  if (sv->res.ready) {
+    cudaStreamSynchronize(sv->res.stream);
+    for (auto* v : {&sv->res.staging}) {
+      for (auto& st : *v) {
+        if (st.pinned) cudaFreeHost(st.pinned);
+        if (st.copied) cudaEventDestroy(st.copied);
+      }
+    }
+    for (auto& st : sv->res.spare) {
+      if (st.pinned) cudaFreeHost(st.pinned);
+      if (st.copied) cudaEventDestroy(st.copied);
+    }
+  }
+  if (sv->res.ended) cudaEventDestroy(sv->res.ended);
+  if (sv->res.stream) cudaStreamDestroy(sv->res.stream);
+  if (sv->res.host) cudaFreeHost(sv->res.host);
   for (ServedLaunch& L : sv->slots) {
     if (L.stream) cudaStreamDestroy(L.stream);
     if (L.done) cudaEventDestroy(L.done);

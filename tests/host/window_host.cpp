@@ -12,7 +12,7 @@ using namespace spoa_gb300;
 
 namespace {
 
-template <int SUB, int CPT, typename T, int SEGS = 1>
+template <int SUB, int CPT, typename T, int SEGS = 1, int NT = 0>
 int32_t run(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t* off,
             const char* quals, int32_t strand, uint32_t nt, int32_t* scores, int32_t* rev,
             int32_t* aln, uint64_t aln_cap, uint64_t* aln_off, char* cons, uint32_t cons_cap,
@@ -45,8 +45,8 @@ int32_t run(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t
     const int32_t* pairs = nullptr;
     uint32_t np = 0;
     simt::launch(nt, [&] {
-      window_read<SUB, CPT, T, SEGS>(S, G, D, sh, ss, seq, L, qual, strand != 0, &score, &rv,
-                                     &pairs, &np);
+      window_read<SUB, CPT, T, SEGS, NT>(S, G, D, sh, ss, seq, L, qual, strand != 0, &score,
+                                         &rv, &pairs, &np);
     });
     if (ss.status != kOk) return ss.status;
     scores[r] = score;
@@ -89,6 +89,13 @@ extern "C" int32_t wh_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t
   }
   if (cpt == 8) {
     if (wide) BY_SUB(8, int32_t) else BY_SUB(8, int16_t)
+  }
+  if (cpt == 16 && nt == 32 && !wide) {  // the one-warp build of the forward pass (NT = 32)
+    switch (sub) {
+      case kLinear: RUN(kLinear, 16, int16_t, 1, 32);
+      case kAffine: RUN(kAffine, 16, int16_t, 1, 32);
+      default: RUN(kConvex, 16, int16_t, 1, 32);
+    }
   }
   if (cpt == -12) {  // the segmented forward: two 12-column strips per thread, 32-bit lanes
     switch (sub) {

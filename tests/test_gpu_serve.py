@@ -91,3 +91,45 @@ def test_long_window_served():
         st, cons, lat = sv.wait(t, timeout=600)
     assert st == 0
     assert cons == po.run_window(2, *PARAMS, w.reads, with_msa=False).consensus
+
+
+@pytest.mark.gpu
+def test_resident_kernel_results_alone_and_in_the_mix():
+    """Resident mode: polishing-sized windows go to one persistent kernel fed
+    through a ring while it runs, the others are launched; every window's
+    consensus equals the same window run alone, arrivals spread over time.
+    Two windows that outgrow the resident kernel's arenas (20-letter noisy
+    reads) come back from it and finish through the launch path."""
+    wins = _mix(40, 5)
+    rng = np.random.Generator(np.random.PCG64(79))
+    big = [synth.random_window(rng, 300, 40, err=0.6, alphabet=b"ACDEFGHIKLMNPQRSTVWY")
+           for _ in range(2)]
+    wins = wins[:10] + [(big[0], 2, False)] + wins[10:30] + [(big[1], 2, False)] + wins[30:]
+    delays = np.sort(np.random.Generator(np.random.PCG64(6)).uniform(0, 0.05, len(wins)))
+    with sg.Server(2, *PARAMS, max_streams=4, resident=True) as sv:
+        tickets = [sv.submit(r, t, s, d) for (r, t, s), d in zip(wins, delays)]
+        got = [sv.wait(t, timeout=600) for t in tickets]
+        stats = sv.stats()
+    assert stats["completed"] == len(wins)
+    resident = sum(1 for r, _, s in wins if max(len(x) for x in r) <= 640 and not s)
+    assert stats["resident_windows"] >= resident
+    assert stats["resident_launches"] >= 1
+    for (reads, typ, strand), (st, cons, lat) in zip(wins, got):
+        assert st == 0
+        alone = sg.batch_poa([reads], typ, *PARAMS, window_strand=[1 if strand else 0])
+        assert alone.consensus[0] == cons
+
+
+@pytest.mark.gpu
+def test_resident_kernel_leaves_when_idle_and_starts_again():
+    """The resident kernel's CTAs leave after 20 ms without work (a bounded
+    wait); windows arriving later start it again."""
+    wins = [synth.batch_window(30_000 + k).reads for k in range(6)]
+    with sg.Server(2, *PARAMS, resident=True) as sv:
+        tickets = [sv.submit(w, delay=0.2 * k) for k, w in enumerate(wins)]
+        got = [sv.wait(t, timeout=600) for t in tickets]
+        stats = sv.stats()
+    assert stats["resident_windows"] == len(wins)
+    assert stats["resident_launches"] >= 2
+    ref = sg.batch_poa(wins, 2, *PARAMS)
+    assert [g[1] for g in got] == ref.consensus and all(g[0] == 0 for g in got)

@@ -124,3 +124,18 @@ def test_segmented_rows(wh):
         for a, b in zip(alns, ref.alignments):
             assert np.array_equal(a, b)
         assert cons == ref.consensus
+
+
+def test_one_warp_build_of_the_forward(wh, ref_windows):
+    """The forward pass built for exactly 32 threads (row offsets fixed at
+    compile time, scans without the cross-warp path), as the batched kernel
+    runs every polishing-sized window, on recorded windows of up to 512
+    columns (16 columns per thread), both strands included."""
+    done = 0
+    for i, rec in enumerate(ref_windows):
+        if max(len(r) for r in rec["reads"]) > 512 or len(rec["reads"]) > 12:
+            continue
+        if i % 9 == 0 or (rec["strand_ambiguous"] and i % 10 == 3):
+            assert _check_window(wh, rec, cpt=16) == 32
+            done += 1
+    assert done >= 8
