@@ -212,8 +212,10 @@ __global__ void k_import(GraphView G, ImportArgs a, int32_t* status) {
 template <typename T>
 constexpr int kBatchMaxRegs = sizeof(T) == 2 ? 96 : 128;
 
-template <int SUB, int CPT, typename T, int SEGS = 1, int NT = 0>
-__global__ void __maxnreg__(kBatchMaxRegs<T>) k_batch(BatchArgs a) {
+// MR: the register cap (the tile tuner also tries 128 for one-warp 16-bit
+// tiles: fewer resident windows, no spills).
+template <int SUB, int CPT, typename T, int SEGS = 1, int NT = 0, int MR = kBatchMaxRegs<T>>
+__global__ void __maxnreg__(MR) k_batch(BatchArgs a) {
   __shared__ BlockScratch sh;
   __shared__ SharedState ss;
   __shared__ uint32_t s_w, s_dims[2];
@@ -585,6 +587,31 @@ int32_t occupancy_batch(int cpt, int nt, int* blocks) {
   return kOk;
 }
 
+// One-warp 16-bit tiles with 128 registers per thread (a tuner candidate)
+template <int SUB>
+int32_t launch_batch_r128(int cpt, int grid, const BatchArgs& a, cudaStream_t s) {
+  using T = int16_t;
+#define L_(C) k_batch<SUB, C, T, 1, 32, 128><<<grid, 32, 0, s>>>(a)
+  SPOA_CPT_SWITCH(T, cpt, L_)
+#undef L_
+  return cudaGetLastError() == cudaSuccess ? kOk : kCuda;
+}
+
+template <int SUB>
+int32_t occupancy_batch_r128(int cpt, int* blocks) {
+  using T = int16_t;
+  cudaError_t err = cudaSuccess;
+#define L_(C) \
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch<SUB, C, T, 1, 32, 128>, 32, 0)
+  SPOA_CPT_SWITCH(T, cpt, L_)
+#undef L_
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    return kCuda;
+  }
+  return kOk;
+}
+
 // W windows per CTA (2 or 4), 16-bit lanes
 template <int SUB>
 int32_t launch_batch_mw(int cpt, int nt, int W, int grid, const BatchArgs& a, cudaStream_t s) {
@@ -658,7 +685,9 @@ int32_t occupancy_serve(int cpt, int nt, int* blocks) {
 
 #define SPOA_GB300_INSTANTIATE_MW(SUB)                                                          \
   template int32_t launch_batch_mw<SUB>(int, int, int, int, const BatchArgs&, cudaStream_t);    \
-  template int32_t occupancy_batch_mw<SUB>(int, int, int, int*);
+  template int32_t occupancy_batch_mw<SUB>(int, int, int, int*);                                \
+  template int32_t launch_batch_r128<SUB>(int, int, const BatchArgs&, cudaStream_t);            \
+  template int32_t occupancy_batch_r128<SUB>(int, int*);
 
 #define SPOA_GB300_INSTANTIATE_SEG(SUB)                                                         \
   template int32_t launch_batch_seg<SUB, int32_t>(int, int, int, const BatchArgs&, cudaStream_t); \

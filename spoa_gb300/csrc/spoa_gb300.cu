@@ -68,7 +68,9 @@ SPOA_EXTERN_SEG(kConvex)
 #define SPOA_EXTERN_MW(SUB)                                                                      \
   extern template int32_t launch_batch_mw<SUB>(int, int, int, int, const BatchArgs&,             \
                                                cudaStream_t);                                    \
-  extern template int32_t occupancy_batch_mw<SUB>(int, int, int, int*);
+  extern template int32_t occupancy_batch_mw<SUB>(int, int, int, int*);                         \
+  extern template int32_t launch_batch_r128<SUB>(int, int, const BatchArgs&, cudaStream_t);     \
+  extern template int32_t occupancy_batch_r128<SUB>(int, int*);
 SPOA_EXTERN_MW(kLinear)
 SPOA_EXTERN_MW(kAffine)
 SPOA_EXTERN_MW(kConvex)
@@ -1065,6 +1067,8 @@ struct Pass {
   int wpc = 1;              // windows per CTA (batch_cta_mw when > 1)
   uint64_t stride = 0;
   int tuned_cpt = 0, tuned_nt = 0;  // tile chosen by the tuner (0: the default)
+  int tuned_wpc = 0, tuned_regs = 0;  // windows per CTA and register cap chosen by the tuner
+  int regs = 0;             // 128: the one-warp 16-bit kernel with 128 registers
   int cls = 0;              // length class
   double work = 0;          // estimated DP work (sum of read lengths x longest read)
   uint64_t arena_off = 0;   // byte offset of this pass's arenas in the batch arena
@@ -1180,17 +1184,20 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
   uint64_t stride =
       arena_caps(b->base.sub, p->wide, cpt * segs, nt, nodes, maxsum, maxreads, many_aligned, &gc,
                  &dc);
-  // several windows per CTA: 16-bit lanes, single-strip tiles
-  const int wpc = (d.windows_per_cta == 2 || d.windows_per_cta == 4) && !p->wide && segs == 1
-                      ? d.windows_per_cta
-                      : 1;
+  // several windows per CTA: 16-bit lanes, single-strip tiles (the tuner's
+  // choice for the class, else the descriptor's)
+  const int want_wpc = p->tuned_wpc > 0 ? p->tuned_wpc : d.windows_per_cta;
+  const int wpc = (want_wpc == 2 || want_wpc == 4) && !p->wide && segs == 1 ? want_wpc : 1;
   if (wpc > 1) {
     DpView dv;
     stride = align_up(mw_layout(nullptr, wpc, gc, dc, &dv, nullptr, nullptr, nullptr), 256);
   }
+  // 128 registers: one-warp 16-bit single-window tiles, when the tuner chose it
+  const int regs = p->tuned_regs == 128 && !p->wide && segs == 1 && wpc == 1 && nt == 32 ? 128 : 0;
   int blocks = 1;
   if (segs > 1 ? SPOA_BY_SUB32(b->base.sub, occupancy_batch_seg, segs, nt, &blocks)
       : wpc > 1 ? SPOA_BY_SUB16(b->base.sub, occupancy_batch_mw, cpt, nt, wpc, &blocks)
+      : regs ? SPOA_BY_SUB16(b->base.sub, occupancy_batch_r128, cpt, &blocks)
                 : SPOA_BY_SUB(b->base.sub, p->wide, occupancy_batch, cpt, nt, &blocks))
     return kCuda;
   blocks = std::max(blocks, 1);
@@ -1204,6 +1211,7 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
   p->nt = nt;
   p->segs = segs;
   p->wpc = wpc;
+  p->regs = regs;
   p->ctas = (int)std::max<uint64_t>(ctas, 1);
   p->stride = stride;
   return kOk;
@@ -1254,6 +1262,7 @@ int32_t launch_pass(spoa_gb300_batch* b, const Pass& p, int ctas, const BatchArg
   if (p.segs > 1) return SPOA_BY_SUB32(b->base.sub, launch_batch_seg, p.segs, p.nt, ctas, a, s);
   if (p.wpc > 1)
     return SPOA_BY_SUB16(b->base.sub, launch_batch_mw, p.cpt, p.nt, p.wpc, ctas, a, s);
+  if (p.regs == 128) return SPOA_BY_SUB16(b->base.sub, launch_batch_r128, p.cpt, ctas, a, s);
   return SPOA_BY_SUB(b->base.sub, p.wide, launch_batch, p.cpt, p.nt, ctas, a, s);
 }
 
@@ -1277,6 +1286,13 @@ int32_t run_pass(spoa_gb300_batch* b, const Pass& p, cudaStream_t s, bool plain,
 }
 
 // ---- tile tuner ------------------------------------------------------------
+// A tuner choice for one length class: columns per thread x threads, and for
+// 16-bit single-strip tiles windows per CTA (batch_cta_mw) and the register
+// cap of the one-warp kernel (0: the default).
+struct TileChoice {
+  int cpt = 0, nt = 0, wpc = 1, regs = 0;
+};
+
 // Candidate tiles for windows up to L columns: every columns-per-thread of
 // the width with its thread count (a multiple of 32, at most 512), kept when
 // its padded row is at most 1.5x the tightest; at most four, tightest first.
@@ -1301,7 +1317,7 @@ std::vector<std::pair<int, int>> tile_candidates(uint32_t L, bool wide) {
 // kept there (one "device sub wide class cpt nt" line each) and reused by
 // later processes on the same device model.
 std::mutex g_tune_mu;
-std::map<std::tuple<int, bool, int>, std::pair<int, int>> g_tuned;
+std::map<std::tuple<int, bool, int>, TileChoice> g_tuned;
 bool g_tune_loaded = false;
 
 std::string device_tag() {
@@ -1325,31 +1341,36 @@ void load_tile_cache() {  // under g_tune_mu
   FILE* f = std::fopen(path, "r");
   if (!f) return;
   const std::string tag = device_tag();
-  char dev[256];
-  int sub, wide, cls, cpt, nt;
-  while (std::fscanf(f, "%255s %d %d %d %d %d", dev, &sub, &wide, &cls, &cpt, &nt) == 6)
-    if (tag == dev && cpt > 0 && nt > 0)
-      g_tuned[std::make_tuple(sub, wide != 0, cls)] = std::make_pair(cpt, nt);
+  char line[512], dev[256];
+  while (std::fgets(line, sizeof line, f)) {
+    int sub, wide, cls;
+    TileChoice t;
+    const int got = std::sscanf(line, "%255s %d %d %d %d %d %d %d", dev, &sub, &wide, &cls,
+                                &t.cpt, &t.nt, &t.wpc, &t.regs);
+    if (got < 6) continue;
+    if (got < 8) t.wpc = 1, t.regs = 0;  // lines of the tile-only format
+    if (tag == dev && t.cpt > 0 && t.nt > 0) g_tuned[std::make_tuple(sub, wide != 0, cls)] = t;
+  }
   std::fclose(f);
 }
 
-void save_tile(int sub, bool wide, int cls, int cpt, int nt) {  // under g_tune_mu
-  g_tuned[std::make_tuple(sub, wide, cls)] = std::make_pair(cpt, nt);
+void save_tile(int sub, bool wide, int cls, const TileChoice& t) {  // under g_tune_mu
+  g_tuned[std::make_tuple(sub, wide, cls)] = t;
   const char* path = std::getenv("SPOA_GB300_TILE_CACHE");
   if (!path) return;
   if (FILE* f = std::fopen(path, "a")) {
-    std::fprintf(f, "%s %d %d %d %d %d\n", device_tag().c_str(), sub, wide ? 1 : 0, cls, cpt, nt);
+    std::fprintf(f, "%s %d %d %d %d %d %d %d\n", device_tag().c_str(), sub, wide ? 1 : 0, cls,
+                 t.cpt, t.nt, t.wpc, t.regs);
     std::fclose(f);
   }
 }
 
-bool tuned_tile(int sub, bool wide, int cls, int* cpt, int* nt) {
+bool tuned_tile(int sub, bool wide, int cls, TileChoice* t) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   load_tile_cache();
   auto it = g_tuned.find(std::make_tuple(sub, wide, cls));
   if (it == g_tuned.end()) return false;
-  *cpt = it->second.first;
-  *nt = it->second.second;
+  *t = it->second;
   return true;
 }
 
@@ -1378,7 +1399,13 @@ int32_t make_passes(spoa_gb300_batch* b, const std::vector<uint32_t>& windows,
     p.wide = std::get<0>(g.first);
     p.cls = std::get<1>(g.first);
     p.windows = std::move(g.second);
-    if (!forced) tuned_tile(b->base.sub, p.wide, p.cls, &p.tuned_cpt, &p.tuned_nt);
+    TileChoice tc;
+    if (!forced && tuned_tile(b->base.sub, p.wide, p.cls, &tc)) {
+      p.tuned_cpt = tc.cpt;
+      p.tuned_nt = tc.nt;
+      p.tuned_wpc = tc.wpc;
+      p.tuned_regs = tc.regs;
+    }
     std::stable_sort(p.windows.begin(), p.windows.end(),
                      [&](uint32_t x, uint32_t y) { return work(x) > work(y); });
     double total = 0;
@@ -1426,12 +1453,33 @@ int32_t autotune(spoa_gb300_batch* b, cudaStream_t s) {
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
   for (const Pass& p : b->passes) {
-    int c0, n0;
-    if (p.segs > 1 || tuned_tile(b->base.sub, p.wide, p.cls, &c0, &n0)) continue;
+    TileChoice known;
+    if (p.segs > 1 || tuned_tile(b->base.sub, p.wide, p.cls, &known)) continue;
     uint32_t L = 1;
     for (uint32_t w : p.windows) L = std::max(L, b->lmax[w]);
-    const auto cands = tile_candidates(L, p.wide);
-    std::pair<int, int> best = cands.empty() ? std::make_pair(0, 0) : cands.front();
+    std::vector<TileChoice> cands;
+    for (const auto& c : tile_candidates(L, p.wide)) {
+      TileChoice t;
+      t.cpt = c.first;
+      t.nt = c.second;
+      cands.push_back(t);
+    }
+    // The default tile (fewest padded columns, then fewest threads) comes
+    // first; for 16-bit one-warp defaults also two windows per CTA and the
+    // 128-register build of the one-warp kernel.
+    int dc = 0, dn = 0;
+    if (!throughput_tile(L, p.wide, &dc, &dn)) dc = dn = 0;
+    std::stable_partition(cands.begin(), cands.end(),
+                          [&](const TileChoice& t) { return t.cpt == dc && t.nt == dn; });
+    if (!cands.empty() && !p.wide && cands.front().cpt == dc && dn == 32) {
+      TileChoice t = cands.front();
+      t.wpc = 2;
+      cands.push_back(t);
+      t.wpc = 1;
+      t.regs = 128;
+      cands.push_back(t);
+    }
+    TileChoice best = cands.empty() ? TileChoice{} : cands.front();
     if (cands.size() > 1) {
       // one sample for every candidate: at least four windows per CTA of the
       // candidate with the most CTAs, so the pass's tail does not decide
@@ -1439,13 +1487,18 @@ int32_t autotune(spoa_gb300_batch* b, cudaStream_t s) {
       q.wide = p.wide;
       q.cls = p.cls;
       q.windows = p.windows;
+      auto take = [&](const TileChoice& t) {
+        q.tuned_cpt = t.cpt;
+        q.tuned_nt = t.nt;
+        q.tuned_wpc = t.wpc;
+        q.tuned_regs = t.regs;
+        return plan_pass(b, &q, b->plan0);
+      };
       size_t n = 1;
       for (const auto& c : cands) {
-        q.tuned_cpt = c.first;
-        q.tuned_nt = c.second;
-        int32_t st = plan_pass(b, &q, b->plan0);
+        int32_t st = take(c);
         if (st) return st;
-        n = std::max<size_t>(n, 4 * (size_t)q.ctas);
+        n = std::max<size_t>(n, 4 * (size_t)q.ctas * (size_t)q.wpc);
       }
       // evenly spaced over the pass (longest first), so the sample keeps
       // its mix of window sizes
@@ -1454,23 +1507,16 @@ int32_t autotune(spoa_gb300_batch* b, cudaStream_t s) {
       for (size_t k = 0; k < p.windows.size() && sample.size() < n; k += step)
         sample.push_back(p.windows[k]);
       q.windows = sample;
-      // The default tile (fewest padded columns, then fewest threads) stays
-      // unless another candidate is faster in every one of three rounds by
-      // more than 3 %: a single timing can be off (the first launch of a
-      // kernel loads its module, clocks still rising, another process), and
-      // a tile kept by mistake costs every later launch.
-      int dc = 0, dn = 0;
-      if (!throughput_tile(L, p.wide, &dc, &dn)) dc = dn = 0;
-      size_t di = 0;
-      for (size_t k = 0; k < cands.size(); ++k)
-        if (cands[k].first == dc && cands[k].second == dn) di = k;
+      // The default (index 0) stays unless another candidate is faster in
+      // every one of three rounds by more than 3 %: a single timing can be
+      // off (the first launch of a kernel loads its module, clocks still
+      // rising, another process), and a choice kept by mistake costs every
+      // later launch.
       constexpr int kRounds = 3;
       std::vector<std::vector<float>> ms_of(cands.size());
       for (int round = 0; round < kRounds; ++round) {
         for (size_t k = 0; k < cands.size(); ++k) {
-          q.tuned_cpt = cands[k].first;
-          q.tuned_nt = cands[k].second;
-          int32_t st = plan_pass(b, &q, b->plan0);
+          int32_t st = take(cands[k]);
           if (st) return st;
           if (b->arena.ensure(q.stride * (uint64_t)q.ctas)) return kNoMemory;
           CU(cudaEventRecord(e0, s));
@@ -1483,20 +1529,21 @@ int32_t autotune(spoa_gb300_batch* b, cudaStream_t s) {
           ms_of[k].push_back(ms);
         }
       }
-      const float dmin = *std::min_element(ms_of[di].begin(), ms_of[di].end());
-      size_t bi = di;
+      const float dmin = *std::min_element(ms_of[0].begin(), ms_of[0].end());
+      size_t bi = 0;
       float bmax = dmin;
-      for (size_t k = 0; k < cands.size(); ++k) {
+      for (size_t k = 1; k < cands.size(); ++k) {
         const float kmax = *std::max_element(ms_of[k].begin(), ms_of[k].end());
-        if (k != di && kmax < 0.97f * dmin && kmax < bmax) {
+        if (kmax < 0.97f * dmin && kmax < bmax) {
           bi = k;
           bmax = kmax;
         }
       }
       if (std::getenv("SPOA_GB300_TUNE_LOG")) {
         for (size_t k = 0; k < cands.size(); ++k) {
-          std::fprintf(stderr, "tile tuner: sub %d wide %d class %d tile %dx%d ms", (int)b->base.sub,
-                       p.wide ? 1 : 0, p.cls, cands[k].first, cands[k].second);
+          std::fprintf(stderr, "tile tuner: sub %d wide %d class %d tile %dx%d wpc %d regs %d ms",
+                       (int)b->base.sub, p.wide ? 1 : 0, p.cls, cands[k].cpt, cands[k].nt,
+                       cands[k].wpc, cands[k].regs);
           for (float x : ms_of[k]) std::fprintf(stderr, " %.2f", x);
           std::fprintf(stderr, "%s\n", k == bi ? " (kept)" : "");
         }
@@ -1504,7 +1551,7 @@ int32_t autotune(spoa_gb300_batch* b, cudaStream_t s) {
       best = cands[bi];
     }
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    save_tile((int)b->base.sub, p.wide, p.cls, best.first, best.second);
+    save_tile((int)b->base.sub, p.wide, p.cls, best);
     changed = true;
   }
   cudaEventDestroy(e0);
