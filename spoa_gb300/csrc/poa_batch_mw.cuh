@@ -167,7 +167,7 @@ __device__ void batch_cta_mw(const BatchArgs& a, BlockScratch& sh, SharedState& 
         if (st == kOk && q.L > 0) {
           const uint32_t words = 3 * ((G.hdr->n_nodes + 31) / 32);
           for (uint32_t k = 0; k < words; ++k) G.sort_bits[k] = 0;
-          if (g_topo_dfs(G, G.sort_bits, G.stack, 0) != 0) st = kCapacity;
+          if (g_topo_dfs(G) != 0) st = kCapacity;
         }
         if (st != kOk) {
           q.status = st;

@@ -371,37 +371,23 @@ __device__ inline int64_t g_add_sequence(GraphView& G, const uint8_t* seq, const
 
 // Graph::TopologicalSort (graph.cpp:249-303): the reference's iterative DFS
 // over in-edges and aligned nodes, with its mark states (0 new, 1 in
-// progress, 2 done) and ignored flags held as bitmaps.  The bitmaps and the
-// bottom of the DFS stack can live in shared memory (TopoScratch): every
-// step reads and sets marks that the previous steps just wrote, and global
-// stores would send those reads to L2.
-
-// Shared-memory room of the sort: mark bitmaps for up to kTopoSmemNodes
-// nodes and the bottom kTopoSmemStack entries of the stack.
-constexpr uint32_t kTopoSmemNodes = 2048, kTopoSmemStack = 64;
-struct TopoScratch {
-  uint32_t bits[3 * (kTopoSmemNodes / 32)];
-  uint32_t stack[kTopoSmemStack];
-};
-
-// The DFS of g_topo_sort_cta on one thread, the mark bitmaps (`bits`, three
-// interleaved words per 32 nodes) already cleared; stack entries below
-// `scap` are held in `sstack`, the rest in the graph arena.  0, or -1 when
-// the stack or the guard runs out.
-__device__ __forceinline__ int g_topo_dfs(GraphView& G, uint32_t* __restrict__ bits,
-                                          uint32_t* __restrict__ sstack, uint32_t scap) {
+// progress, 2 done) and ignored flags held as bitmaps in the graph arena.
+// Every thread clears the bitmaps and prefetches the node records into L1,
+// then thread 0 runs the DFS.  Returns 0, or -1 when the stack or the guard
+// runs out (identical in every thread).
+// The DFS of g_topo_sort_cta on one thread, the mark bitmaps already
+// cleared: 0, or -1 when the stack or the guard runs out.
+__device__ __forceinline__ int g_topo_dfs(GraphView& G) {
   const uint32_t nn = G.hdr->n_nodes;
+  uint32_t* __restrict__ bits = G.sort_bits;
   auto bit = [&](uint32_t v, uint32_t kind) { return (bits[3 * (v >> 5) + kind] >> (v & 31)) & 1u; };
   auto set = [&](uint32_t v, uint32_t kind) { bits[3 * (v >> 5) + kind] |= 1u << (v & 31); };
   constexpr uint32_t kBusy = 0, kDone = 1, kIgn = 2;
-  uint32_t* __restrict__ gstack = G.stack;
+  uint32_t* __restrict__ stack = G.stack;
   uint64_t sp = 0;
-  uint32_t top = kNone;  // stack[sp - 1], kept in a register
   auto push = [&](uint32_t v) -> bool {
     if (sp >= G.stack_cap) return false;
-    if (sp < scap) sstack[sp] = v; else gstack[sp] = v;
-    ++sp;
-    top = v;
+    stack[sp++] = v;
     return true;
   };
   uint32_t rank = 0;
@@ -415,7 +401,7 @@ __device__ __forceinline__ int g_topo_dfs(GraphView& G, uint32_t* __restrict__ b
     push(s);
     while (sp) {
       if (++guard > guard_max) { rc = -1; break; }
-      const uint32_t curr = top;
+      const uint32_t curr = stack[sp - 1];
       bool valid = true;
       if (!bit(curr, kDone)) {
         const uint4 r = G.nrec[curr];
@@ -461,25 +447,15 @@ __device__ __forceinline__ int g_topo_dfs(GraphView& G, uint32_t* __restrict__ b
           set(curr, kBusy);
         }
       }
-      if (valid) {
-        --sp;
-        if (sp) top = sp - 1 < scap ? sstack[sp - 1] : gstack[sp - 1];
-      }
+      if (valid) --sp;
     }
   }
   return (rc == 0 && rank == nn) ? 0 : -1;
 }
 
-// The sort by a CTA: every thread clears the bitmaps and prefetches the
-// node records into L1, then thread 0 runs the DFS.  With `sm` (shared
-// memory of the caller) the bitmaps of graphs up to kTopoSmemNodes nodes
-// and the bottom of the stack live there.  Returns 0, or -1 when the stack
-// or the guard runs out (identical in every thread).
-static __device__ __noinline__ int g_topo_sort_cta(GraphView& G, int* s_ret,
-                                                   TopoScratch* sm = nullptr) {
+static __device__ __noinline__ int g_topo_sort_cta(GraphView& G, int* s_ret) {
   const uint32_t nn = G.hdr->n_nodes;
-  const bool smem = sm != nullptr && nn <= kTopoSmemNodes;
-  uint32_t* __restrict__ bits = smem ? sm->bits : G.sort_bits;
+  uint32_t* __restrict__ bits = G.sort_bits;
   const uint32_t words = 3 * ((nn + 31) / 32);
   for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) bits[w] = 0;
 #ifdef __CUDA_ARCH__
@@ -487,8 +463,7 @@ static __device__ __noinline__ int g_topo_sort_cta(GraphView& G, int* s_ret,
     asm volatile("prefetch.global.L1 [%0];" ::"l"(G.nrec + v));
 #endif
   __syncthreads();
-  if (threadIdx.x == 0)
-    *s_ret = g_topo_dfs(G, bits, sm ? sm->stack : G.stack, sm ? kTopoSmemStack : 0);
+  if (threadIdx.x == 0) *s_ret = g_topo_dfs(G);
   __syncthreads();
   return *s_ret;
 }

@@ -46,7 +46,6 @@ struct BlockScratch {
   int32_t wv2[32];
   int32_t edge[32];
   int32_t bcast[8];
-  TopoScratch topo;  // the topological sort's marks and stack bottom
 };
 
 // Exclusive prefix-max of v over the CTA's threads (kNegBig for thread 0).

@@ -149,7 +149,7 @@ __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScra
   __syncthreads();
   if (ss.status == kOk && L > 0) {
     int* ret = &ss.pad;
-    if (g_topo_sort_cta(G, ret, &sh.topo) != 0 && threadIdx.x == 0) ss.status = kCapacity;
+    if (g_topo_sort_cta(G, ret) != 0 && threadIdx.x == 0) ss.status = kCapacity;
     __syncthreads();
   }
 }
