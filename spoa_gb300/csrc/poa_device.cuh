@@ -284,10 +284,28 @@ __device__ inline void g_reset(GraphView& G) {
   for (int i = 0; i < 256; ++i) h->coder[i] = h->decoder[i] = -1;
 }
 
-__device__ inline int64_t g_add_node(GraphView& G, uint32_t code) {
+// The graph's element counters, kept in registers while AddAlignment
+// appends (thread 0 writes them back at the end): read back from the
+// header after every append, they would make each step wait for the store
+// of the step before.
+struct GraphCounts {
+  uint32_t nodes, edges, labels, seqs;
+};
+__device__ __forceinline__ GraphCounts g_counts(const GraphView& G) {
+  const GraphHeader* h = G.hdr;
+  return GraphCounts{h->n_nodes, h->n_edges, h->n_labels, h->n_seqs};
+}
+__device__ __forceinline__ void g_store_counts(GraphView& G, const GraphCounts& c) {
   GraphHeader* h = G.hdr;
-  if (h->n_nodes >= G.caps.nodes) return -1;
-  uint32_t id = h->n_nodes++;
+  h->n_nodes = c.nodes;
+  h->n_edges = c.edges;
+  h->n_labels = c.labels;
+  h->n_seqs = c.seqs;
+}
+
+__device__ inline int64_t g_add_node(GraphView& G, GraphCounts& c, uint32_t code) {
+  if (c.nodes >= G.caps.nodes) return -1;
+  uint32_t id = c.nodes++;
   G.code[id] = (uint8_t)code;
   G.nlink[id] = make_uint4(kNone, kNone, kNone, kNone);
   G.in_deg[id] = 0;
@@ -295,15 +313,21 @@ __device__ inline int64_t g_add_node(GraphView& G, uint32_t code) {
   G.nrec[id] = make_uint4(0, kNone, kNone, kNone);
   return id;
 }
+__device__ inline int64_t g_add_node(GraphView& G, uint32_t code) {
+  GraphCounts c = g_counts(G);
+  const int64_t id = g_add_node(G, c, code);
+  g_store_counts(G, c);
+  return id;
+}
 
-__device__ inline int g_add_label(GraphView& G, uint32_t e) {
-  GraphHeader* h = G.hdr;
-  if (h->n_labels >= G.caps.labels) return -1;
-  uint32_t l = h->n_labels++;
-  G.lab_seq[l] = h->n_seqs;
+__device__ inline int g_add_label(GraphView& G, GraphCounts& c, uint32_t e) {
+  if (c.labels >= G.caps.labels) return -1;
+  uint32_t l = c.labels++;
+  G.lab_seq[l] = c.seqs;
   G.lab_next[l] = kNone;
-  if (G.e_lab_last[e] != kNone) {
-    G.lab_next[G.e_lab_last[e]] = l;
+  const uint32_t last = G.e_lab_last[e];
+  if (last != kNone) {
+    G.lab_next[last] = l;
   } else {
     G.e_lab_first[e] = l;
   }
@@ -313,10 +337,10 @@ __device__ inline int g_add_label(GraphView& G, uint32_t e) {
 
 // A new edge tail -> head with weight w and no labels, appended to the
 // tail's out-edge list and the head's in-edge list; -1 when full.
-__device__ inline int64_t g_new_edge(GraphView& G, uint32_t tail, uint32_t head, int64_t w) {
-  GraphHeader* h = G.hdr;
-  if (h->n_edges >= G.caps.edges) return -1;
-  uint32_t e = h->n_edges++;
+__device__ inline int64_t g_new_edge(GraphView& G, GraphCounts& c, uint32_t tail, uint32_t head,
+                                     int64_t w) {
+  if (c.edges >= G.caps.edges) return -1;
+  uint32_t e = c.edges++;
   G.erec[e] = make_uint4(tail, head, kNone, kNone);
   G.e_weight[e] = w;
   G.e_lab_first[e] = G.e_lab_last[e] = kNone;
@@ -336,37 +360,52 @@ __device__ inline int64_t g_new_edge(GraphView& G, uint32_t tail, uint32_t head,
   G.nrec[head] = r;
   return e;
 }
+__device__ inline int64_t g_new_edge(GraphView& G, uint32_t tail, uint32_t head, int64_t w) {
+  GraphCounts c = g_counts(G);
+  const int64_t e = g_new_edge(G, c, tail, head, w);
+  g_store_counts(G, c);
+  return e;
+}
 
 // Graph::AddEdge (graph.cpp:81-91)
-__device__ inline int g_add_edge(GraphView& G, uint32_t tail, uint32_t head, uint32_t w) {
+__device__ inline int g_add_edge(GraphView& G, GraphCounts& c, uint32_t tail, uint32_t head,
+                                 uint32_t w) {
   for (uint32_t e = G.nlink[tail].z; e != kNone;) {
     const uint4 er = G.erec[e];
     if (er.y == head) {
-      if (g_add_label(G, e)) return -1;
+      if (g_add_label(G, c, e)) return -1;
       G.e_weight[e] += w;
       return 0;
     }
     e = er.w;
   }
-  const int64_t e = g_new_edge(G, tail, head, w);
-  if (e < 0 || g_add_label(G, (uint32_t)e)) return -1;
+  const int64_t e = g_new_edge(G, c, tail, head, w);
+  if (e < 0 || g_add_label(G, c, (uint32_t)e)) return -1;
   return 0;
+}
+__device__ inline int g_add_edge(GraphView& G, uint32_t tail, uint32_t head, uint32_t w) {
+  GraphCounts c = g_counts(G);
+  const int r = g_add_edge(G, c, tail, head, w);
+  g_store_counts(G, c);
+  return r;
 }
 
 // Graph::AddSequence (graph.cpp:93-110).  -1: empty range, -2: capacity.
-__device__ inline int64_t g_add_sequence(GraphView& G, const uint8_t* seq, const WeightSrc& w,
-                                         uint32_t begin, uint32_t end) {
+__device__ inline int64_t g_add_sequence(GraphView& G, GraphCounts& c, const uint8_t* seq,
+                                         const WeightSrc& w, uint32_t begin, uint32_t end) {
   if (begin == end) return -1;
   int64_t prev = -1;
   for (uint32_t i = begin; i < end; ++i) {
-    int64_t curr = g_add_node(G, (uint32_t)G.hdr->coder[seq[i]]);
+    int64_t curr = g_add_node(G, c, (uint32_t)G.hdr->coder[seq[i]]);
     if (curr < 0) return -2;
     if (prev >= 0) {
-      if (g_add_edge(G, (uint32_t)prev, (uint32_t)curr, w.at(i - 1) + w.at(i))) return -2;
+      // a new node has no out-edge yet: AddEdge always creates the edge
+      const int64_t e = g_new_edge(G, c, (uint32_t)prev, (uint32_t)curr, w.at(i - 1) + w.at(i));
+      if (e < 0 || g_add_label(G, c, (uint32_t)e)) return -2;
     }
     prev = curr;
   }
-  return (int64_t)G.hdr->n_nodes - (end - begin);
+  return (int64_t)c.nodes - (end - begin);
 }
 
 // Graph::TopologicalSort (graph.cpp:249-303): the reference's iterative DFS
@@ -557,11 +596,17 @@ static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32
       h->decoder[h->num_codes++] = ch;
     }
   }
+  GraphCounts c = g_counts(G);
+  // every exit leaves the counters in the header
+  auto done = [&](int32_t st) {
+    g_store_counts(G, c);
+    return st;
+  };
   if (n_pairs == 0) {
-    int64_t b = g_add_sequence(G, seq, w, 0, len);
-    if (b < -1) return kCapacity;
-    G.seq_begin[h->n_seqs++] = (uint32_t)b;
-    return kOk;  // the caller re-sorts (g_topo_sort_cta)
+    int64_t b = g_add_sequence(G, c, seq, w, 0, len);
+    if (b < -1) return done(kCapacity);
+    G.seq_begin[c.seqs++] = (uint32_t)b;
+    return done(kOk);  // the caller re-sorts (g_topo_sort_cta)
   }
   int32_t first_valid = -1, last_valid = -1;
   for (uint32_t k = 0; k < n_pairs; ++k) {
@@ -575,13 +620,13 @@ static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32
   if (first_valid == -1) return kMissingSequence;
   for (uint32_t k = 0; k < n_pairs; ++k) {
     int32_t nid = pairs[2 * k];
-    if (nid < -1 || nid >= (int32_t)h->n_nodes) return kInvalidAlignment;
+    if (nid < -1 || nid >= (int32_t)c.nodes) return kInvalidAlignment;
   }
-  int64_t begin = g_add_sequence(G, seq, w, 0, (uint32_t)first_valid);
-  if (begin < -1) return kCapacity;
-  int64_t prev = begin >= 0 ? (int64_t)h->n_nodes - 1 : -1;
-  int64_t last = g_add_sequence(G, seq, w, (uint32_t)last_valid + 1, len);
-  if (last < -1) return kCapacity;
+  int64_t begin = g_add_sequence(G, c, seq, w, 0, (uint32_t)first_valid);
+  if (begin < -1) return done(kCapacity);
+  int64_t prev = begin >= 0 ? (int64_t)c.nodes - 1 : -1;
+  int64_t last = g_add_sequence(G, c, seq, w, (uint32_t)last_valid + 1, len);
+  if (last < -1) return done(kCapacity);
   const uint32_t K = G.caps.aligned;
   bool prev_new = true;  // prev was created by this read (it has no edge to an old node)
   for (uint32_t k = 0; k < n_pairs; ++k) {
@@ -607,8 +652,8 @@ static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32
       }
     }
     if (curr < 0) {
-      curr = g_add_node(G, code);
-      if (curr < 0) return kCapacity;
+      curr = g_add_node(G, c, code);
+      if (curr < 0) return done(kCapacity);
       curr_new = true;
       if (nid != -1) {
         const uint32_t na = G.n_aligned[nid];
@@ -616,37 +661,37 @@ static __device__ __noinline__ int32_t g_add_alignment(GraphView& G, const int32
         for (uint32_t a = 0; a < na; ++a) {
           uint32_t kt = al[a];
           if (g_link_aligned(G, kt, (uint32_t)curr) || g_link_aligned(G, (uint32_t)curr, kt))
-            return kCapacity;
+            return done(kCapacity);
         }
         if (g_link_aligned(G, (uint32_t)nid, (uint32_t)curr) ||
             g_link_aligned(G, (uint32_t)curr, (uint32_t)nid))
-          return kCapacity;
+          return done(kCapacity);
       }
     }
     if (begin < 0) begin = curr;
     if (prev >= 0) {
       const uint32_t wt = w.at(pos - 1) + w.at(pos);
       if (!pre) {
-        if (g_add_edge(G, (uint32_t)prev, (uint32_t)curr, wt)) return kCapacity;
+        if (g_add_edge(G, c, (uint32_t)prev, (uint32_t)curr, wt)) return done(kCapacity);
       } else if (!prev_new && !curr_new && pre[2 * k + 1] != kNone) {
         // AddEdge on an existing edge: one more label and the weight
         const uint32_t e = pre[2 * k + 1];
-        if (g_add_label(G, e)) return kCapacity;
+        if (g_add_label(G, c, e)) return done(kCapacity);
         G.e_weight[e] += wt;
       } else {
-        const int64_t e = g_new_edge(G, (uint32_t)prev, (uint32_t)curr, wt);
-        if (e < 0 || g_add_label(G, (uint32_t)e)) return kCapacity;
+        const int64_t e = g_new_edge(G, c, (uint32_t)prev, (uint32_t)curr, wt);
+        if (e < 0 || g_add_label(G, c, (uint32_t)e)) return done(kCapacity);
       }
     }
     prev = curr;
     prev_new = curr_new;
   }
   if (last >= 0) {
-    if (g_add_edge(G, (uint32_t)prev, (uint32_t)last, w.at(last_valid) + w.at(last_valid + 1)))
-      return kCapacity;
+    if (g_add_edge(G, c, (uint32_t)prev, (uint32_t)last, w.at(last_valid) + w.at(last_valid + 1)))
+      return done(kCapacity);
   }
-  G.seq_begin[h->n_seqs++] = (uint32_t)begin;
-  return kOk;  // the caller re-sorts (g_topo_sort_cta)
+  G.seq_begin[c.seqs++] = (uint32_t)begin;
+  return done(kOk);  // the caller re-sorts (g_topo_sort_cta)
 }
 
 // ---------------------------------------------------------------------------
