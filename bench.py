@@ -82,6 +82,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--windows-per-cta", type=int, default=1, choices=[1, 2, 4],
                     help="windows in flight per CTA (16-bit windows)")
+    ap.add_argument("--cluster", type=int, default=0, choices=[0, 1],
+                    help="0: long 32-bit rows on thread-block clusters; 1: one CTA per window")
     ap.add_argument("--parity-windows", type=int, default=256,
                     help="windows rerun with alignments and checked against the oracle")
     ap.add_argument("--no-resident", action="store_true",
@@ -401,7 +403,8 @@ def main():
                                     window_strand=wstrand,
                                     autotune=args.workload == "batch_10k" and not args.tile,
                                     columns_per_thread=cpt, threads_per_window=nt,
-                                    windows_per_cta=args.windows_per_cta, device=device)
+                                    windows_per_cta=args.windows_per_cta, cluster=args.cluster,
+                                    device=device)
 
     batch = make_batch()
     for _ in range(args.warmup):
@@ -514,7 +517,7 @@ def main():
         "config": common_config(cfg, world),
         "tile": {"threads_per_window": res.threads_per_window,
                  "columns_per_thread": res.columns_per_thread, "ctas": res.ctas,
-                 "windows_per_cta": args.windows_per_cta},
+                 "windows_per_cta": args.windows_per_cta, "cluster": args.cluster},
         "gcups": gcups, "cells_per_step": cells * world,
         "e2e": e2e, "plain": plain,
         "gpu_launches": launches,

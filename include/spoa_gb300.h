@@ -217,6 +217,10 @@ typedef struct {
   int32_t windows_per_cta;         /* 2 or 4: windows of 16-bit width in flight
                                       per CTA, their graph updates on parallel
                                       lanes; otherwise 1 */
+  int32_t cluster;                 /* 0: windows of 32-bit scores whose rows pass
+                                      1,536 columns run on thread-block clusters
+                                      (2, 4 or 8 CTAs per window, each a column
+                                      range of every row); 1: never */
   int32_t device_set;              /* nonzero: the batch lives on `device`;
                                       0: on the calling thread's current device
                                       at batch_create.  Every later call on the

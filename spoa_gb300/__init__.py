@@ -80,8 +80,8 @@ class _BatchDesc(C.Structure):
                 ("columns_per_thread", C.c_int32), ("ctas", C.c_int32),
                 ("memory_budget", C.c_uint64), ("want_alignments", C.c_int32),
                 ("want_msa", C.c_int32), ("autotune", C.c_int32),
-                ("windows_per_cta", C.c_int32), ("device_set", C.c_int32),
-                ("device", C.c_int32)]
+                ("windows_per_cta", C.c_int32), ("cluster", C.c_int32),
+                ("device_set", C.c_int32), ("device", C.c_int32)]
 
 
 class _BatchResult(C.Structure):
@@ -509,7 +509,7 @@ class Batch:
     def _create(self, seqs, off, wro, type_, m, n, g, e, q, c, window_types, window_strand,
                 quals, want_alignments=False, want_msa=False, threads_per_window=0,
                 columns_per_thread=0, ctas=0, max_nodes=0, memory_budget=0, autotune=False,
-                windows_per_cta=1, device=None):
+                windows_per_cta=1, device=None, cluster=0):
         self._seqs = np.ascontiguousarray(seqs, np.uint8)
         self._off = np.ascontiguousarray(off, np.uint64)
         self._wro = np.ascontiguousarray(wro, np.uint32)
@@ -541,6 +541,7 @@ class Batch:
         d.want_msa = 1 if want_msa else 0
         d.autotune = 1 if autotune else 0
         d.windows_per_cta = windows_per_cta
+        d.cluster = cluster
         d.device_set = 1 if device is not None else 0
         d.device = int(device) if device is not None else 0
         self._desc = d

@@ -46,7 +46,71 @@ struct BlockScratch {
   int32_t wv2[32];
   int32_t edge[32];
   int32_t bcast[8];
+  int32_t cl[8];  // values this CTA publishes to the other CTAs of its cluster
 };
+
+// ---------------------------------------------------------------------------
+// thread-block clusters: one long window's row spread over CL CTAs
+// ---------------------------------------------------------------------------
+// CTA r of a cluster of CL owns virtual threads r * nt ... r * nt + nt - 1
+// of the row.  Scan carries, the left neighbour's column and the final
+// reductions cross CTAs through distributed shared memory, each exchange
+// behind one cluster barrier (every CTA of the cluster runs the same
+// sequence of barriers: the control flow is uniform over the cluster).
+template <int CL>
+__device__ __forceinline__ uint32_t cl_rank() {
+  if constexpr (CL == 1) {
+    return 0;
+  } else {
+#ifdef __CUDA_ARCH__
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+#elif defined(SPOA_GB300_SIMT_HOST)
+    return simt::cta_rank;
+#else
+    return 0;
+#endif
+  }
+}
+
+// Barrier of the whole cluster (of the CTA when CL == 1), ordering the
+// memory operations before it against those after it for all its threads.
+template <int CL>
+__device__ __forceinline__ void cl_sync() {
+  if constexpr (CL == 1) {
+    __syncthreads();
+  } else {
+#ifdef __CUDA_ARCH__
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+                 "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+#elif defined(SPOA_GB300_SIMT_HOST)
+    simt::cluster_sync();
+#endif
+  }
+}
+
+// A 32-bit shared variable of CTA `rank` of the cluster (the same variable
+// as `local` in this CTA).
+__device__ __forceinline__ int32_t cl_peek(const int32_t* local, uint32_t rank) {
+#ifdef __CUDA_ARCH__
+  const uint32_t sa = (uint32_t)__cvta_generic_to_shared(local);
+  uint32_t ra;
+  int32_t v;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(sa), "r"(rank));
+  asm volatile("ld.shared::cluster.b32 %0, [%1];" : "=r"(v) : "r"(ra) : "memory");
+  return v;
+#elif defined(SPOA_GB300_SIMT_HOST)
+  return *simt::peer(local, rank);
+#else
+  return local[0] + 0 * (int32_t)rank;
+#endif
+}
+
+// Slots of BlockScratch::cl: the in-row scans (the Q scan and the E / H
+// scan), the left neighbour's column, the final row maximum, minimum row
+// and minimum column.
+enum : int { kClScanA = 0, kClScanB = 1, kClLeft = 2, kClMax = 3, kClMin = 4, kClMinJ = 5 };
 
 // Exclusive prefix-max of v over the CTA's threads (kNegBig for thread 0).
 // NW: warps of the CTA when known at compile time (0: blockDim.x / 32).
@@ -74,6 +138,34 @@ __device__ __forceinline__ int32_t block_excl_max(int32_t v, BlockScratch& sh) {
 }
 
 template <int NW = 0>
+__device__ __forceinline__ int32_t block_max(int32_t v, BlockScratch& sh);
+template <int NW = 0>
+__device__ __forceinline__ int32_t block_min(int32_t v, BlockScratch& sh);
+
+// The maximum / minimum of v over every thread of the cluster (every
+// thread gets it); `slot` is the BlockScratch::cl entry the exchange uses.
+template <int NW, int CL>
+__device__ __forceinline__ int32_t cluster_max(int32_t v, BlockScratch& sh, int slot) {
+  v = block_max<NW>(v, sh);
+  if constexpr (CL > 1) {
+    if (threadIdx.x == 0) sh.cl[slot] = v;
+    cl_sync<CL>();
+    for (uint32_t r = 0; r < (uint32_t)CL; ++r) v = imax(v, cl_peek(&sh.cl[slot], r));
+  }
+  return v;
+}
+template <int NW, int CL>
+__device__ __forceinline__ int32_t cluster_min(int32_t v, BlockScratch& sh, int slot) {
+  v = block_min<NW>(v, sh);
+  if constexpr (CL > 1) {
+    if (threadIdx.x == 0) sh.cl[slot] = v;
+    cl_sync<CL>();
+    for (uint32_t r = 0; r < (uint32_t)CL; ++r) v = min(v, cl_peek(&sh.cl[slot], r));
+  }
+  return v;
+}
+
+template <int NW>
 __device__ __forceinline__ int32_t block_max(int32_t v, BlockScratch& sh) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t nw = NW ? NW : blockDim.x >> 5;
@@ -90,7 +182,7 @@ __device__ __forceinline__ int32_t block_max(int32_t v, BlockScratch& sh) {
   return v;
 }
 
-template <int NW = 0>
+template <int NW>
 __device__ __forceinline__ int32_t block_min(int32_t v, BlockScratch& sh) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t nw = NW ? NW : blockDim.x >> 5;
@@ -114,13 +206,23 @@ __device__ __forceinline__ int32_t block_min(int32_t v, BlockScratch& sh) {
 // With b_t = agg_t - t*CPT*pen this is a plain prefix-max.  Only thread 0
 // knows `init`; it folds it into its own aggregate (its strip end is then
 // exactly X[CPT-1]), so the other threads never need it.
-template <int CPT, int NW = 0>
+// With CL > 1, t is the thread's index in the cluster's row and the
+// exclusive prefix also takes the maximum over the CTAs before this one
+// (each publishes the maximum over its threads in slot `slot`).
+template <int CPT, int NW = 0, int CL = 1>
 __device__ __forceinline__ int32_t scan_carry(int32_t agg, int32_t init, int32_t pen,
-                                              BlockScratch& sh) {
-  const int32_t t = (int32_t)threadIdx.x;
+                                              BlockScratch& sh, int slot = kClScanA) {
+  const int32_t t = (int32_t)(cl_rank<CL>() * blockDim.x + threadIdx.x);
   const int32_t D = CPT * pen;
   int32_t v = t == 0 ? imax(agg, init + D) : agg;
-  int32_t ex = block_excl_max<NW>(v - t * D, sh);
+  const int32_t x = v - t * D;
+  int32_t ex = block_excl_max<NW>(x, sh);
+  if constexpr (CL > 1) {
+    if (threadIdx.x == blockDim.x - 1) sh.cl[slot] = imax(ex, x);
+    cl_sync<CL>();
+    const uint32_t rank = cl_rank<CL>();
+    for (uint32_t r = 0; r < rank; ++r) ex = imax(ex, cl_peek(&sh.cl[slot], r));
+  }
   return t == 0 ? init : ex + (t - 1) * D;
 }
 
@@ -355,7 +457,9 @@ __host__ __device__ __forceinline__ uint64_t colmap(uint64_t j, uint64_t nt) {
 }
 
 // Value of thread t-1 (thread 0 gets `fill`).
-template <int NW = 0>
+// With CL > 1, thread 0 of CTA r > 0 gets the last thread of CTA r - 1
+// and `fill` goes to the first thread of the cluster.
+template <int NW = 0, int CL = 1>
 __device__ __forceinline__ int32_t from_left(int32_t a, int32_t fill, BlockScratch& sh) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int32_t x = __shfl_up_sync(0xffffffffu, a, 1);
@@ -365,15 +469,22 @@ __device__ __forceinline__ int32_t from_left(int32_t a, int32_t fill, BlockScrat
     if (lane == 0 && warp > 0) x = sh.wv[warp - 1];
     __syncthreads();
   }
+  if constexpr (CL > 1) {
+    if (threadIdx.x == blockDim.x - 1) sh.cl[kClLeft] = a;
+    cl_sync<CL>();
+    const uint32_t rank = cl_rank<CL>();
+    if (threadIdx.x == 0 && rank > 0) x = cl_peek(&sh.cl[kClLeft], rank - 1);
+    return threadIdx.x == 0 && rank == 0 ? fill : x;
+  }
   return threadIdx.x == 0 ? fill : x;
 }
 
 // Strip scan of X[j] = max(a[j], X[j-1] + pen) over this thread's pairs with
 // the CTA carry.  On return x[k] holds X at the columns of pair k; returns
 // X[s-1], the value carried into the strip (init for thread 0).
-template <int CPT, typename Lx, int NW = 0>
+template <int CPT, typename Lx, int NW = 0, int CL = 1>
 __device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, int32_t pen,
-                                             BlockScratch& sh) {
+                                             BlockScratch& sh, int slot = kClScanA) {
   constexpr int HP = CPT / 2;
   static_assert(HP <= 16, "pair masks hold at most 16 pairs per strip");
   using P = typename Lx::P;
@@ -382,7 +493,7 @@ __device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, in
   for (int k = 1; k < HP; ++k) x[k] = Lx::addmax(x[k - 1], pen2, x[k]);
   const int32_t lo_agg = Lx::lo(x[HP - 1]), hi_agg = Lx::hi(x[HP - 1]);
   const int32_t agg = imax(hi_agg, lo_agg + HP * pen);
-  const int32_t c = scan_carry<CPT, NW>(agg, init, pen, sh);  // X[s-1]
+  const int32_t c = scan_carry<CPT, NW, CL>(agg, init, pen, sh, slot);  // X[s-1]
   const int32_t c_hi = imax(lo_agg, c + HP * pen);          // X[s+HP-1]
   const P carry = Lx::make(c, c_hi);
 #pragma unroll
@@ -396,7 +507,7 @@ __device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, in
 // NT: the CTA's threads when known at compile time (0: blockDim.x); with it
 // every row offset of a load or store is a constant of the instruction and
 // the scans of a one-warp CTA take no shared-memory path.
-template <int SUB, int CPT, typename T, int NT = 0>
+template <int SUB, int CPT, typename T, int NT = 0, int CL = 1>
 __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restrict__ seq,
                            uint32_t L, uint32_t V, int32_t lanes, BlockScratch& sh,
                            int64_t* out_max_i, int64_t* out_max_j, int32_t* out_score) {
@@ -405,7 +516,10 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
   using L16 = Lanes<int16_t>;
   constexpr int HP = CPT / 2;
   static_assert(HP <= 16, "pair masks hold at most 16 pairs per strip");
-  const uint32_t t = threadIdx.x;
+  // this thread's index in the row: in the cluster's row when CL > 1
+  const uint32_t ntc = NT ? NT : blockDim.x;  // threads of the CTA
+  const uint32_t ntv = ntc * CL;               // threads of the row
+  const uint32_t t = cl_rank<CL>() * ntc + threadIdx.x;
   const uint32_t s0 = t * CPT;
   const uint64_t ld = D.caps.ld;        // elements per row
   const uint64_t wrow = ld / 2;         // pair words per row
@@ -413,7 +527,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
   // and the next; the warp's accesses to them are contiguous
   const uint64_t w0 = 2 * (uint64_t)t;
   constexpr int NW = NT / 32;
-  const uint64_t st2 = 2 * (uint64_t)(NT ? NT : blockDim.x);
+  const uint64_t st2 = 2 * (uint64_t)ntv;
   const int32_t type = S.type;
   const int32_t m = S.m, n = S.n, g = S.g, e = S.e, q = S.q, c = S.c;
   const int32_t NEGW = lanes == 8 ? (INT32_MIN + 1024) : (INT16_MIN + 1024);
@@ -667,7 +781,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
     if (SUB == kLinear) {
 #pragma unroll
       for (int k = 0; k < HP; ++k) hs[k] = h[k];
-      pair_scan<CPT, Lx, NW>(hs, fci, g, sh);
+      pair_scan<CPT, Lx, NW, CL>(hs, fci, g, sh, kClScanA);
       if (type == kSW) {
         const P z = Lx::splat(0);
 #pragma unroll
@@ -679,7 +793,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
 #pragma unroll
         for (int k = 0; k < HP; ++k) x[k] = Lx::add(h[k], q2);
         // x = Q' (Q of the next column); Q[s0] = Q'[s0-1] is the carry
-        const int32_t qin = pair_scan<CPT, Lx, NW>(x, fci + q, c, sh);
+        const int32_t qin = pair_scan<CPT, Lx, NW, CL>(x, fci + q, c, sh, kClScanA);
         qq[0] = Lx::make(qin, Lx::lo(x[HP - 1]));
 #pragma unroll
         for (int k = 1; k < HP; ++k) qq[k] = x[k - 1];
@@ -697,7 +811,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
             x[k] = Lx::add(h[k], g2);
           }
         }
-        const int32_t ein = pair_scan<CPT, Lx, NW>(x, fci + g, e, sh);  // x = E'
+        const int32_t ein = pair_scan<CPT, Lx, NW, CL>(x, fci + g, e, sh, kClScanB);  // x = E'
         ee[0] = Lx::make(ein, Lx::lo(x[HP - 1]));
 #pragma unroll
         for (int k = 1; k < HP; ++k) ee[k] = x[k - 1];
@@ -711,7 +825,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
       }
     }
     // column s0-1 of this row (thread 0: the first column fc)
-    const int32_t lH = from_left<NW>(Lx::hi(hs[HP - 1]), fci, sh);
+    const int32_t lH = from_left<NW, CL>(Lx::hi(hs[HP - 1]), fci, sh);
     // the gap rows E and Q as the recurrences computed them: the traceback
     // re-derives its horizontal tests from them
     if (SUB >= kAffine) {
@@ -768,8 +882,8 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
   }
 
   // global selection: best value, then the earliest row reaching it
-  const int32_t B = block_max<NW>(bval, sh);
-  const int32_t R = block_min<NW>(bval == B && brow >= 0 ? brow : 0x7fffffff, sh);
+  const int32_t B = cluster_max<NW, CL>(bval, sh, kClMax);
+  const int32_t R = cluster_min<NW, CL>(bval == B && brow >= 0 ? brow : 0x7fffffff, sh, kClMin);
   int64_t max_i = -1;
   int32_t score = 0;
   if (type == kSW) {
@@ -802,9 +916,9 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
       int32_t jj = 0x7fffffff;
       for (int r = 0; r < CPT && jj == 0x7fffffff; ++r) {
         const uint32_t j = s0 + r;
-        if (j < L && Lx::elem(H, base + colmap<CPT>(j, NT ? NT : blockDim.x)) == score) jj = (int32_t)j;
+        if (j < L && Lx::elem(H, base + colmap<CPT>(j, ntv)) == score) jj = (int32_t)j;
       }
-      jj = block_min<NW>(jj, sh);
+      jj = cluster_min<NW, CL>(jj, sh, kClMinJ);
       max_j = jj == 0x7fffffff ? -1 : jj;
     }
   }

@@ -449,6 +449,94 @@ __global__ void __maxnreg__(kBatchMaxRegs<T>) k_serve(ServeArgs a) {
   }
 }
 
+// Long windows on thread-block clusters: a cluster of CL CTAs owns one
+// window at a time and spreads each row over its CTAs (window_read_cl);
+// the lead CTA takes windows from the work queue and runs the serial
+// phases.  The arena is per cluster.  Launched with cluster dimensions
+// (CL, 1, 1) by launch_batch_cl.
+template <int SUB, int CPT, typename T, int CL>
+__global__ void __maxnreg__(kBatchMaxRegs<T>) k_batch_cl(BatchArgs a) {
+  __shared__ BlockScratch sh;
+  __shared__ SharedState ss;
+  __shared__ int32_t s_w;
+  __shared__ uint32_t s_dims[2];
+  __shared__ const int32_t* s_pairs;
+  __shared__ int32_t s_score, s_rev;
+  __shared__ uint32_t s_np;
+  __shared__ GraphView G;
+  __shared__ DpView D;
+  const bool lead = cl_rank<CL>() == 0;
+  if (threadIdx.x == 0) {
+    uint8_t* base = a.arena + a.arena_stride * (blockIdx.x / CL);
+    const uint64_t gbytes = graph_layout(base, a.gcaps, &G);
+    dp_layout(base + gbytes, a.dcaps, &D);
+  }
+  __syncthreads();
+  Scoring S = a.base;
+  while (true) {
+    if (lead && threadIdx.x == 0) {
+      const uint32_t k = atomicAdd(a.queue, 1u);
+      s_w = (int32_t)(k < a.n_work ? a.work[k] : kNone);
+    }
+    cl_sync<CL>();
+    const uint32_t w = (uint32_t)cl_peek(&s_w, 0);
+    if (w == kNone) break;
+    if (lead && threadIdx.x == 0) g_reset(G);
+    S.type = a.win_type ? a.win_type[w] : a.base.type;
+    const bool strand = a.win_strand ? a.win_strand[w] != 0 : false;
+    cl_sync<CL>();
+    int32_t status = kOk;
+    unsigned long long cells = 0;
+    for (uint32_t r = a.win_read_off[w]; r < a.win_read_off[w + 1]; ++r) {
+      const uint64_t off = a.seq_off[r];
+      const uint32_t L = (uint32_t)(a.seq_off[r + 1] - off);
+      cells += (unsigned long long)G.hdr->n_nodes * L * (strand ? 2u : 1u);
+      const int32_t st = window_read_cl<SUB, CPT, T, CL>(
+          S, G, D, sh, ss, a.seqs + off, L, a.quals ? a.quals + off : nullptr, strand, &s_score,
+          &s_rev, &s_pairs, &s_np);
+      if (st != kOk) {
+        status = st;
+        break;
+      }
+      if (lead && threadIdx.x == 0) {
+        a.read_scores[r] = s_score;
+        a.read_rev[r] = (uint8_t)s_rev;
+        if (a.aln_out) {
+          const uint64_t cap = a.aln_off[r + 1] - a.aln_off[r];
+          const uint32_t np = (uint32_t)min((uint64_t)s_np, cap);
+          for (uint32_t k = 0; k < 2 * np; ++k) a.aln_out[2 * a.aln_off[r] + k] = s_pairs[k];
+          a.aln_len[r] = s_np;
+        }
+      }
+    }
+    if (lead) {
+      if (status == kOk) {
+        if (threadIdx.x == 0) {
+          const uint64_t cap = a.cons_off[w + 1] - a.cons_off[w];
+          write_consensus(G, a.cons + a.cons_off[w], cap, &a.cons_len[w]);
+          s_dims[0] = a.cons_len[w] > cap ? kCapacity : kOk;
+        }
+        __syncthreads();
+        if (s_dims[0] != kOk) status = kCapacity;
+        __syncthreads();
+        if (status == kOk && a.msa_out) {
+          const int32_t st = window_msa(G, false, a.msa_out + a.msa_off[w],
+                                        a.msa_off[w + 1] - a.msa_off[w], &a.msa_rows[w],
+                                        &a.msa_cols[w], s_dims);
+          if (st != kOk) status = st;
+        }
+      }
+      if (threadIdx.x == 0) {
+        a.win_status[w] = status;
+        if (a.cells) atomicAdd(a.cells, cells);
+      }
+    }
+    cl_sync<CL>();
+  }
+  // no CTA leaves while another may still read its shared memory
+  cl_sync<CL>();
+}
+
 // W windows per CTA (batch_cta_mw): the serial graph updates of the W
 // windows run on W lanes side by side.
 template <int SUB, int CPT, typename T, int W>
@@ -671,6 +759,71 @@ int32_t occupancy_serve(int cpt, int nt, int* blocks) {
   return kOk;
 }
 
+// Clusters of CL CTAs of nt threads (12 columns per thread, 32-bit
+// lanes), `clusters` of them.
+constexpr int kClCpt = 12;
+template <int SUB, int CL>
+int32_t launch_batch_cl_n(int nt, int clusters, const BatchArgs& a, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(clusters * CL), 1, 1);
+  cfg.blockDim = dim3((unsigned)nt, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, k_batch_cl<SUB, kClCpt, int32_t, CL>, a) != cudaSuccess) {
+    cudaGetLastError();
+    return kCuda;
+  }
+  return kOk;
+}
+
+template <int SUB>
+int32_t launch_batch_cl(int cl, int nt, int clusters, const BatchArgs& a, cudaStream_t s) {
+  switch (cl) {
+    case 2: return launch_batch_cl_n<SUB, 2>(nt, clusters, a, s);
+    case 4: return launch_batch_cl_n<SUB, 4>(nt, clusters, a, s);
+    case 8: return launch_batch_cl_n<SUB, 8>(nt, clusters, a, s);
+    default: return kInvalidArgument;
+  }
+}
+
+// Clusters of the kernel that can be resident at once.
+template <int SUB, int CL>
+int32_t occupancy_batch_cl_n(int nt, int* clusters) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(CL * 64), 1, 1);
+  cfg.blockDim = dim3((unsigned)nt, 1, 1);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaOccupancyMaxActiveClusters(clusters, k_batch_cl<SUB, kClCpt, int32_t, CL>, &cfg) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return kCuda;
+  }
+  return kOk;
+}
+
+template <int SUB>
+int32_t occupancy_batch_cl(int cl, int nt, int* clusters) {
+  switch (cl) {
+    case 2: return occupancy_batch_cl_n<SUB, 2>(nt, clusters);
+    case 4: return occupancy_batch_cl_n<SUB, 4>(nt, clusters);
+    case 8: return occupancy_batch_cl_n<SUB, 8>(nt, clusters);
+    default: return kInvalidArgument;
+  }
+}
+
 #define SPOA_GB300_INSTANTIATE(SUB, T)                                                          \
   template int32_t launch_align<SUB, T>(int, int, const Scoring&, const GraphView&,             \
                                         const DpView&, const uint8_t*, uint32_t, ReadOut*);     \
@@ -691,6 +844,8 @@ int32_t occupancy_serve(int cpt, int nt, int* blocks) {
 
 #define SPOA_GB300_INSTANTIATE_SEG(SUB)                                                         \
   template int32_t launch_batch_seg<SUB, int32_t>(int, int, int, const BatchArgs&, cudaStream_t); \
-  template int32_t occupancy_batch_seg<SUB, int32_t>(int, int, int*);
+  template int32_t occupancy_batch_seg<SUB, int32_t>(int, int, int*);                             \
+  template int32_t launch_batch_cl<SUB>(int, int, int, const BatchArgs&, cudaStream_t);           \
+  template int32_t occupancy_batch_cl<SUB>(int, int, int*);
 
 }  // namespace spoa_gb300

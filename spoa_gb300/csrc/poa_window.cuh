@@ -154,6 +154,96 @@ __device__ void window_read(const Scoring& S, GraphView& G, DpView& D, BlockScra
   }
 }
 
+// One read of a window on a cluster of CL CTAs (long rows): every CTA of
+// the cluster calls it.  The forward pass runs on all of them, each CTA a
+// column range of the row (dp_forward with CL); the prologue, the row
+// metadata, the traceback, the strand choice, AddAlignment and the sort run
+// on CTA 0 (the lead), and every decision is read back from the lead's
+// shared state after a cluster barrier, so each CTA takes the same path
+// and meets the same barriers.  Returns the status (the same in every
+// thread of the cluster); the lead's thread 0 gets the outputs.
+template <int SUB, int CPT, typename T, int CL>
+__device__ int32_t window_read_cl(const Scoring& S, GraphView& G, DpView& D, BlockScratch& sh,
+                                  SharedState& ss, const uint8_t* seq, uint32_t L,
+                                  const uint8_t* qual, bool strand, int32_t* out_score,
+                                  int32_t* out_rev, const int32_t** out_pairs, uint32_t* out_np) {
+  const bool lead = cl_rank<CL>() == 0;
+  const uint32_t ntv = blockDim.x * CL;
+  if (lead && threadIdx.x == 0) {
+    read_prologue(S, G, D, L, ntv * CPT, sizeof(T) == 4, ss);
+    ss.has_f = ss.has_r = 0;
+    ss.score_f = ss.score_r = 0;
+    ss.np_f = ss.np_r = 0;
+  }
+  cl_sync<CL>();
+  int32_t st = cl_peek(&ss.status, 0);
+  if (st != kOk) return st;
+  const bool dp = cl_peek(&ss.mode, 0) == 1;
+  const int32_t lanes = cl_peek(&ss.lanes, 0);
+  const uint32_t V = G.hdr->n_nodes;
+  auto align = [&](const uint8_t* sq, int32_t* pairs, int32_t* has, int32_t* score,
+                   uint32_t* np) {
+    int64_t mi, mj;
+    int32_t sc;
+    dp_forward<SUB, CPT, T, 0, CL>(S, D, sq, L, V, lanes, sh, &mi, &mj, &sc);
+    if (lead && threadIdx.x == 0) {
+      *np = 0;
+      *has = 0;
+      if (mi >= 0) {
+        *has = 1;
+        *score = sc;
+        const int32_t t = dp_traceback<SUB, CPT, T>(S, D, G, sq, L, V, mi, mj, pairs, np, ntv);
+        if (t != kOk) ss.status = t;
+      }
+    }
+    cl_sync<CL>();
+  };
+  if (dp) {
+    if (lead) dp_build_rows(G, D, sh);
+    cl_sync<CL>();
+    align(seq, D.aln_a, &ss.has_f, &ss.score_f, &ss.np_f);
+  }
+  if (strand) {
+    if (lead)
+      for (uint32_t j = threadIdx.x; j < L; j += blockDim.x)
+        D.seq_rc[j] = complement_base(seq[L - 1 - j]);
+    cl_sync<CL>();
+    st = cl_peek(&ss.status, 0);
+    if (dp && st == kOk) align(D.seq_rc, D.aln_b, &ss.has_r, &ss.score_r, &ss.np_r);
+  }
+  if (lead && cl_peek(&ss.status, 0) == kOk) {
+    // main.cpp:276-301: scores start at 0; keep forward if score >= score_rev
+    const int32_t sf = ss.has_f ? ss.score_f : 0;
+    const int32_t sr = ss.has_r ? ss.score_r : 0;
+    const bool rev = strand && !(sf >= sr);
+    const int32_t* pairs = rev ? D.aln_b : D.aln_a;
+    const uint32_t np = rev ? ss.np_r : ss.np_f;
+    const uint8_t* chosen = rev ? D.seq_rc : seq;
+    uint32_t* pre = reinterpret_cast<uint32_t*>(rev ? D.aln_a : D.aln_b);
+    g_add_prepass(G, pairs, np, chosen, L, pre);
+    if (threadIdx.x == 0) {
+      WeightSrc ws{nullptr, qual, L, rev ? 1u : 0u, 1u};
+      const int32_t a = g_add_alignment(G, pairs, np, chosen, L, ws, pre);
+      if (a != kOk) ss.status = a;
+      *out_score = rev ? sr : sf;
+      *out_rev = rev ? 1 : 0;
+      *out_pairs = pairs;
+      *out_np = np;
+    }
+    __syncthreads();
+    if (ss.status == kOk && L > 0) {
+      int* ret = &ss.pad;
+      if (g_topo_sort_cta(G, ret) != 0 && threadIdx.x == 0) ss.status = kCapacity;
+      __syncthreads();
+    }
+  }
+  cl_sync<CL>();
+  st = cl_peek(&ss.status, 0);
+  // the lead rewrites ss for the next read only after every CTA has read it
+  cl_sync<CL>();
+  return st;
+}
+
 __device__ inline void write_consensus(GraphView& G, uint8_t* out, uint64_t cap, uint32_t* len) {
   g_consensus(G);
   const uint32_t n = G.hdr->n_consensus;

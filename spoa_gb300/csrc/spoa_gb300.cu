@@ -60,7 +60,9 @@ SPOA_EXTERN(kConvex, int32_t)
 #define SPOA_EXTERN_SEG(SUB)                                                                     \
   extern template int32_t launch_batch_seg<SUB, int32_t>(int, int, int, const BatchArgs&,        \
                                                          cudaStream_t);                          \
-  extern template int32_t occupancy_batch_seg<SUB, int32_t>(int, int, int*);
+  extern template int32_t occupancy_batch_seg<SUB, int32_t>(int, int, int*);                     \
+  extern template int32_t launch_batch_cl<SUB>(int, int, int, const BatchArgs&, cudaStream_t);   \
+  extern template int32_t occupancy_batch_cl<SUB>(int, int, int*);
 SPOA_EXTERN_SEG(kLinear)
 SPOA_EXTERN_SEG(kAffine)
 SPOA_EXTERN_SEG(kConvex)
@@ -117,6 +119,9 @@ constexpr int kCpts32[] = {8, 12, 16, 24, 32};
    : (sub) == kAffine ? fn<kAffine>(__VA_ARGS__)                                         \
    : (sub) == kConvex ? fn<kConvex>(__VA_ARGS__)                                         \
                       : (int32_t)kInvalidArgument)
+
+// 32-bit rows wider than this run on thread-block clusters (k_batch_cl).
+constexpr uint32_t kClusterMinCols = 1536;
 
 // Latency tile: the smallest strip (most threads) that covers L.
 bool latency_tile(uint32_t L, bool wide, int* cpt, int* nt) {
@@ -1069,6 +1074,7 @@ struct Pass {
   int tuned_cpt = 0, tuned_nt = 0;  // tile chosen by the tuner (0: the default)
   int tuned_wpc = 0, tuned_regs = 0;  // windows per CTA and register cap chosen by the tuner
   int regs = 0;             // 128: the one-warp 16-bit kernel with 128 registers
+  int cl = 1;               // CTAs per window (k_batch_cl when > 1); ctas counts clusters
   int cls = 0;              // length class
   double work = 0;          // estimated DP work (sum of read lengths x longest read)
   uint64_t arena_off = 0;   // byte offset of this pass's arenas in the batch arena
@@ -1161,8 +1167,15 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
     wnodes = std::max(wnodes, wp[w].nodes);
     many_aligned = many_aligned || wp[w].many_aligned;
   }
-  int cpt = d.columns_per_thread, nt = d.threads_per_window, segs = 1;
-  if (p->tuned_cpt > 0 && (uint64_t)p->tuned_cpt * p->tuned_nt >= L) {
+  int cpt = d.columns_per_thread, nt = d.threads_per_window, segs = 1, cl = 1;
+  const bool forced = cpt > 0 && nt > 0;
+  if (p->wide && !forced && d.cluster != 1 && L > kClusterMinCols &&
+      L <= (uint32_t)kClCpt * 8 * 512) {
+    // a thread-block cluster per window: 2, 4 or 8 CTAs, 12 columns per thread
+    cl = L > 4u * 128 * kClCpt ? 8 : L > 2u * 128 * kClCpt ? 4 : 2;
+    cpt = kClCpt;
+    nt = (int)std::max<uint64_t>(32, ((uint64_t)(L + cl * kClCpt - 1) / (cl * kClCpt) + 31) / 32 * 32);
+  } else if (p->tuned_cpt > 0 && (uint64_t)p->tuned_cpt * p->tuned_nt >= L) {
     cpt = p->tuned_cpt;
     nt = p->tuned_nt;
   }
@@ -1175,19 +1188,19 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
     } else if (!throughput_tile(L, p->wide, &cpt, &nt)) {
       return kTooLarge;
     }
-  } else if ((uint64_t)cpt * nt < L) {
+  } else if ((uint64_t)cpt * nt * cl < L) {
     return kTooLarge;
   }
   uint64_t nodes = d.max_nodes ? std::max<uint64_t>(d.max_nodes, wnodes) : wnodes;
   GraphCaps gc;
   DpCaps dc;
   uint64_t stride =
-      arena_caps(b->base.sub, p->wide, cpt * segs, nt, nodes, maxsum, maxreads, many_aligned, &gc,
-                 &dc);
+      arena_caps(b->base.sub, p->wide, cpt * segs * cl, nt, nodes, maxsum, maxreads, many_aligned,
+                 &gc, &dc);
   // several windows per CTA: 16-bit lanes, single-strip tiles (the tuner's
   // choice for the class, else the descriptor's)
   const int want_wpc = p->tuned_wpc > 0 ? p->tuned_wpc : d.windows_per_cta;
-  const int wpc = (want_wpc == 2 || want_wpc == 4) && !p->wide && segs == 1 ? want_wpc : 1;
+  const int wpc = (want_wpc == 2 || want_wpc == 4) && !p->wide && segs == 1 && cl == 1 ? want_wpc : 1;
   if (wpc > 1) {
     DpView dv;
     stride = align_up(mw_layout(nullptr, wpc, gc, dc, &dv, nullptr, nullptr, nullptr), 256);
@@ -1195,6 +1208,25 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
   // 128 registers: one-warp 16-bit single-window tiles, when the tuner chose it
   const int regs = p->tuned_regs == 128 && !p->wide && segs == 1 && wpc == 1 && nt == 32 ? 128 : 0;
   int blocks = 1;
+  if (cl > 1) {
+    // clusters resident on the whole device, not per SM
+    int clusters = 1;
+    if (SPOA_BY_SUB16(b->base.sub, occupancy_batch_cl, cl, nt, &clusters)) return kCuda;
+    uint64_t n = std::max(clusters, 1);
+    n = std::min<uint64_t>(n, std::max<uint64_t>(1, b->budget / stride));
+    n = std::min<uint64_t>(n, p->windows.size());
+    p->gcaps = gc;
+    p->dcaps = dc;
+    p->cpt = cpt;
+    p->nt = nt;
+    p->segs = 1;
+    p->wpc = 1;
+    p->regs = 0;
+    p->cl = cl;
+    p->ctas = (int)std::max<uint64_t>(n, 1);
+    p->stride = stride;
+    return kOk;
+  }
   if (segs > 1 ? SPOA_BY_SUB32(b->base.sub, occupancy_batch_seg, segs, nt, &blocks)
       : wpc > 1 ? SPOA_BY_SUB16(b->base.sub, occupancy_batch_mw, cpt, nt, wpc, &blocks)
       : regs ? SPOA_BY_SUB16(b->base.sub, occupancy_batch_r128, cpt, &blocks)
@@ -1212,6 +1244,7 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
   p->segs = segs;
   p->wpc = wpc;
   p->regs = regs;
+  p->cl = 1;
   p->ctas = (int)std::max<uint64_t>(ctas, 1);
   p->stride = stride;
   return kOk;
@@ -1259,6 +1292,7 @@ BatchArgs make_args(spoa_gb300_batch* b, const Pass& p, uint8_t* cons, const uin
 int32_t launch_pass(spoa_gb300_batch* b, const Pass& p, int ctas, const BatchArgs& a,
                     cudaStream_t s) {
   ++b->launches;
+  if (p.cl > 1) return SPOA_BY_SUB16(b->base.sub, launch_batch_cl, p.cl, p.nt, ctas, a, s);
   if (p.segs > 1) return SPOA_BY_SUB32(b->base.sub, launch_batch_seg, p.segs, p.nt, ctas, a, s);
   if (p.wpc > 1)
     return SPOA_BY_SUB16(b->base.sub, launch_batch_mw, p.cpt, p.nt, p.wpc, ctas, a, s);
@@ -1454,7 +1488,7 @@ int32_t autotune(spoa_gb300_batch* b, cudaStream_t s) {
   CU(cudaEventCreate(&e1));
   for (const Pass& p : b->passes) {
     TileChoice known;
-    if (p.segs > 1 || tuned_tile(b->base.sub, p.wide, p.cls, &known)) continue;
+    if (p.segs > 1 || p.cl > 1 || tuned_tile(b->base.sub, p.wide, p.cls, &known)) continue;
     uint32_t L = 1;
     for (uint32_t w : p.windows) L = std::max(L, b->lmax[w]);
     std::vector<TileChoice> cands;

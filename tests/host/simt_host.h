@@ -24,6 +24,7 @@
 #include <cstdio>
 #endif
 
+#define SPOA_GB300_SIMT_HOST 1
 #define __host__
 #define __device__
 #define __forceinline__ inline
@@ -52,11 +53,15 @@ struct HostDim {
 
 namespace simt {
 
+// One CTA, or a cluster of `ncta` CTAs of `nt` threads each (the threads of
+// CTA r are ranks r * nt ... r * nt + nt - 1 of the launch).
 struct Cta {
-  unsigned nt = 1;
-  std::unique_ptr<std::barrier<>> all;
-  std::vector<std::unique_ptr<std::barrier<>>> warp;
-  std::vector<int32_t> slots;  // 32 per warp
+  unsigned nt = 1, ncta = 1;
+  std::vector<std::unique_ptr<std::barrier<>>> cta_bar;  // per CTA
+  std::unique_ptr<std::barrier<>> cluster_bar;           // all threads
+  std::vector<std::unique_ptr<std::barrier<>>> warp;     // per CTA and warp
+  std::vector<int32_t> slots;                            // 32 per warp
+  std::vector<char*> scratch;  // per CTA: its shared-memory stand-in
 };
 
 inline Cta*& cta() {
@@ -64,34 +69,62 @@ inline Cta*& cta() {
   return c;
 }
 inline thread_local HostDim tid{0};
+inline thread_local unsigned cta_rank = 0;
 
-// Runs body() on nt threads as one CTA; returns when all have finished.
-inline void launch(unsigned nt, const std::function<void()>& body) {
+// Runs body() on ncta CTAs of nt threads (a cluster when ncta > 1);
+// scratch[r] is CTA r's shared-memory stand-in (for the distributed shared
+// memory of a cluster).  Returns when all threads have finished.
+inline void launch_cluster(unsigned ncta, unsigned nt, const std::vector<char*>& scratch,
+                           const std::function<void()>& body) {
   Cta c;
   c.nt = nt;
-  c.all = std::make_unique<std::barrier<>>(nt);
-  for (unsigned w = 0; w < (nt + 31) / 32; ++w)
-    c.warp.push_back(std::make_unique<std::barrier<>>(std::min(32u, nt - 32 * w)));
-  c.slots.assign(32 * ((nt + 31) / 32), 0);
+  c.ncta = ncta;
+  c.scratch = scratch;
+  for (unsigned r = 0; r < ncta; ++r) c.cta_bar.push_back(std::make_unique<std::barrier<>>(nt));
+  c.cluster_bar = std::make_unique<std::barrier<>>(nt * ncta);
+  const unsigned nw = (nt + 31) / 32;
+  for (unsigned r = 0; r < ncta; ++r)
+    for (unsigned w = 0; w < nw; ++w)
+      c.warp.push_back(std::make_unique<std::barrier<>>(std::min(32u, nt - 32 * w)));
+  c.slots.assign(32 * nw * ncta, 0);
   cta() = &c;
   std::vector<std::thread> th;
-  for (unsigned t = 0; t < nt; ++t)
-    th.emplace_back([t, &body] {
-      tid.x = t;
-      body();
-    });
+  for (unsigned r = 0; r < ncta; ++r)
+    for (unsigned t = 0; t < nt; ++t)
+      th.emplace_back([r, t, &body] {
+        tid.x = t;
+        cta_rank = r;
+        body();
+      });
   for (auto& x : th) x.join();
   cta() = nullptr;
 }
 
+// Runs body() on nt threads as one CTA; returns when all have finished.
+inline void launch(unsigned nt, const std::function<void()>& body) {
+  launch_cluster(1, nt, {}, body);
+}
+
 inline int32_t exchange(int32_t v, unsigned src_lane) {
   Cta& c = *cta();
-  const unsigned w = tid.x / 32, lane = tid.x % 32;
+  const unsigned w = cta_rank * ((c.nt + 31) / 32) + tid.x / 32, lane = tid.x % 32;
   c.slots[32 * w + lane] = v;
   c.warp[w]->arrive_and_wait();
   const int32_t r = c.slots[32 * w + src_lane];
   c.warp[w]->arrive_and_wait();
   return r;
+}
+
+inline void cluster_sync() {
+  if (cta()) cta()->cluster_bar->arrive_and_wait();
+}
+
+// The copy of a shared variable of this CTA in CTA `rank` of the cluster.
+template <typename T>
+inline T* peer(T* local, unsigned rank) {
+  Cta& c = *cta();
+  const std::ptrdiff_t off = reinterpret_cast<const char*>(local) - c.scratch[cta_rank];
+  return reinterpret_cast<T*>(c.scratch[rank] + off);
 }
 
 }  // namespace simt
@@ -109,7 +142,7 @@ static inline void __syncthreads() {
   static std::atomic<long> n{0};
   if (threadIdx.x == 0) fprintf(stderr, "sync %ld\n", n++);
 #endif
-  if (simt::cta()) simt::cta()->all->arrive_and_wait();
+  if (simt::cta()) simt::cta()->cta_bar[simt::cta_rank]->arrive_and_wait();
 }
 
 template <typename T>
@@ -153,7 +186,10 @@ static inline unsigned __ballot_sync(unsigned, int pred) {
 static inline int __ffs(unsigned x) { return x ? __builtin_ctz(x) + 1 : 0; }
 
 static inline void __syncwarp(unsigned = 0xffffffffu) {
-  if (simt::cta()) simt::cta()->warp[threadIdx.x / 32]->arrive_and_wait();
+  if (simt::cta()) {
+    simt::Cta& c = *simt::cta();
+    c.warp[simt::cta_rank * ((c.nt + 31) / 32) + threadIdx.x / 32]->arrive_and_wait();
+  }
 }
 
 // ---- SIMD integer intrinsics, per their documented lane semantics ----

@@ -60,6 +60,59 @@ int32_t run(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t
   return kOk;
 }
 
+// One window through window_read_cl on a cluster of CL emulated CTAs of nt
+// threads each (every CTA its own shared state, the row spread over them).
+template <int SUB, int CPT, typename T, int CL>
+int32_t run_cl(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t* off,
+               const char* quals, int32_t strand, uint32_t nt, int32_t* scores, int32_t* rev,
+               int32_t* aln, uint64_t aln_cap, uint64_t* aln_off, char* cons, uint32_t cons_cap,
+               uint32_t* cons_len) {
+  uint64_t sum = 0;
+  for (uint32_t r = 0; r < n_reads; ++r) sum += off[r + 1] - off[r];
+  GraphCaps gc{(uint32_t)sum + 2, 2 * (uint32_t)sum + n_reads + 8, (uint32_t)sum + n_reads + 8,
+               n_reads + 1, 31};
+  GraphView G;
+  std::vector<uint8_t> gbuf(graph_layout(nullptr, gc, &G) + 256);
+  graph_layout(gbuf.data(), gc, &G);
+  DpCaps dc{gc.nodes + 1, CPT * nt * CL, gc.edges + gc.nodes + 2, S.sub, sizeof(T)};
+  DpView D;
+  std::vector<uint8_t> dbuf(dp_layout(nullptr, dc, &D) + 256);
+  dp_layout(dbuf.data(), dc, &D);
+  simt::launch(1, [&] { g_reset(G); });
+  struct CtaShared {
+    BlockScratch sh;
+    SharedState ss;
+  };
+  std::vector<CtaShared> cs(CL);
+  std::vector<char*> scratch;
+  for (auto& c : cs) scratch.push_back(reinterpret_cast<char*>(&c));
+  uint64_t na = 0;
+  aln_off[0] = 0;
+  for (uint32_t r = 0; r < n_reads; ++r) {
+    const uint32_t L = (uint32_t)(off[r + 1] - off[r]);
+    const uint8_t* seq = reinterpret_cast<const uint8_t*>(seqs) + off[r];
+    const uint8_t* qual = quals ? reinterpret_cast<const uint8_t*>(quals) + off[r] : nullptr;
+    int32_t score = 0, rv = 0, st = kOk;
+    const int32_t* pairs = nullptr;
+    uint32_t np = 0;
+    simt::launch_cluster(CL, nt, scratch, [&] {
+      CtaShared& me = cs[simt::cta_rank];
+      const int32_t s = window_read_cl<SUB, CPT, T, CL>(S, G, D, me.sh, me.ss, seq, L, qual,
+                                                        strand != 0, &score, &rv, &pairs, &np);
+      if (simt::cta_rank == 0 && threadIdx.x == 0) st = s;
+    });
+    if (st != kOk) return st;
+    scores[r] = score;
+    rev[r] = rv;
+    if (na + np > aln_cap) return kCapacity;
+    for (uint32_t k = 0; k < 2 * np; ++k) aln[2 * na + k] = pairs[k];
+    na += np;
+    aln_off[r + 1] = na;
+  }
+  simt::launch(1, [&] { write_consensus(G, reinterpret_cast<uint8_t*>(cons), cons_cap, cons_len); });
+  return kOk;
+}
+
 }  // namespace
 
 extern "C" int32_t wh_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t e, int32_t q,
@@ -107,4 +160,35 @@ extern "C" int32_t wh_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t
   if (wide) BY_SUB(16, int32_t) else BY_SUB(16, int16_t)
 #undef BY_SUB
 #undef RUN
+}
+
+// The cluster form (window_read_cl): cl CTAs of nt threads, 12 columns per
+// thread, 32-bit lanes.
+extern "C" int32_t wh_run_cl(int32_t type, int32_t m, int32_t n, int32_t g, int32_t e, int32_t q,
+                             int32_t c, int32_t cl, uint32_t nt, uint32_t n_reads,
+                             const char* seqs, const uint64_t* off, const char* quals,
+                             int32_t strand, int32_t* scores, int32_t* rev, int32_t* aln,
+                             uint64_t aln_cap, uint64_t* aln_off, char* cons, uint32_t cons_cap,
+                             uint32_t* cons_len) {
+  const int32_t sub = g >= e ? kLinear : ((g <= q || e >= c) ? kAffine : kConvex);
+  if (sub == kLinear) {
+    e = g;
+  } else if (sub == kAffine) {
+    q = g;
+    c = e;
+  }
+  const Scoring S{type, sub, m, n, g, e, q, c};
+#define RUNC(SUBV, CLV)                                                                     \
+  return run_cl<SUBV, 12, int32_t, CLV>(S, n_reads, seqs, off, quals, strand, nt, scores, rev, \
+                                        aln, aln_cap, aln_off, cons, cons_cap, cons_len)
+#define BY_SUBC(CLV)                     \
+  switch (sub) {                         \
+    case kLinear: RUNC(kLinear, CLV);    \
+    case kAffine: RUNC(kAffine, CLV);    \
+    default: RUNC(kConvex, CLV);         \
+  }
+  if (cl == 2) BY_SUBC(2)
+  BY_SUBC(4)
+#undef BY_SUBC
+#undef RUNC
 }

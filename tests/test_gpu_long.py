@@ -61,9 +61,34 @@ def test_segmented_rows_vs_oracle(gap):
     params = GAPS[gap]
     for typ in (0, 1, 2):
         ref = po.run_window(typ, *params, w.reads, with_msa=False)
-        res = sg.batch_poa([w.reads], typ, *params, want_alignments=True)
+        # cluster=1: one CTA per window, the segmented kernel
+        res = sg.batch_poa([w.reads], typ, *params, want_alignments=True, cluster=1)
         assert (res.status == 0).all()
         _check(res, ref)
+
+
+@pytest.mark.timeout(900)
+@pytest.mark.parametrize("gap", sorted(GAPS))
+def test_cluster_rows_vs_oracle(gap):
+    """Rows of 2-2.4k and 4.2-4.8k columns on the int32 width: clusters of
+    2 and 4 CTAs split each row; NW, SW and OV, both strands, two windows
+    per batch (two clusters side by side), every score, strand choice and
+    alignment and the consensus."""
+    params = GAPS[gap]
+    ws = [synth.long_10k(21, n_reads=3, tpl_len=2400, min_len=2000),
+          synth.long_10k(22, n_reads=3, tpl_len=4800, min_len=4200)]
+    reads = [[synth.revcomp(r) if j == 1 else r for j, r in enumerate(w.reads)] for w in ws]
+    for typ in (0, 1, 2):
+        strand = typ != 0
+        res = sg.batch_poa(reads, typ, *params, want_alignments=True,
+                           window_strand=[strand] * 2)
+        assert (res.status == 0).all()
+        r0 = 0
+        for k, rs in enumerate(reads):
+            ref = po.run_window(typ, *params, rs, strand_ambiguous=strand, with_msa=False)
+            _check(res, ref, k, r0)
+            assert res.reversed[r0:r0 + len(rs)].tolist() == [int(x) for x in ref.reversed]
+            r0 += len(rs)
 
 
 @pytest.mark.timeout(900)

@@ -35,6 +35,8 @@ def wh():
     I32, U32, P = C.c_int32, C.c_uint32, C.c_void_p
     L.wh_run.argtypes = [I32] * 9 + [U32, U32, C.c_char_p, P, C.c_char_p, I32, P, P, P,
                                      C.c_uint64, P, C.c_char_p, U32, P]
+    L.wh_run_cl.argtypes = [I32] * 8 + [U32, U32, C.c_char_p, P, C.c_char_p, I32, P, P, P,
+                                        C.c_uint64, P, C.c_char_p, U32, P]
     return L
 
 
@@ -139,3 +141,46 @@ def test_one_warp_build_of_the_forward(wh, ref_windows):
             assert _check_window(wh, rec, cpt=16) == 32
             done += 1
     assert done >= 8
+
+
+def run_host_cl(L, type_, params, reads, quals, strand, cl, nt):
+    nr = len(reads)
+    off = np.zeros(nr + 1, np.uint64)
+    off[1:] = np.cumsum([len(r) for r in reads])
+    cap = int(off[-1]) * 2 + 64 * nr + 64
+    aln = np.zeros(2 * cap, np.int32)
+    aoff = np.zeros(nr + 1, np.uint64)
+    cons = C.create_string_buffer(int(off[-1]) + 16)
+    clen = C.c_uint32()
+    scores = np.zeros(nr, np.int32)
+    rev = np.zeros(nr, np.int32)
+    qb = b"".join(quals) if quals is not None else None
+    st = L.wh_run_cl(type_, *params, cl, nt, nr, b"".join(reads), _ptr(off), qb,
+                     1 if strand else 0, _ptr(scores), _ptr(rev), _ptr(aln), cap, _ptr(aoff),
+                     cons, len(cons), C.byref(clen))
+    alns = [aln[2 * int(aoff[r]):2 * int(aoff[r + 1])].reshape(-1, 2) for r in range(nr)]
+    return st, scores.tolist(), rev.tolist(), alns, cons.raw[:clen.value].decode()
+
+
+def test_cluster_rows(wh):
+    """The cluster form of a window (window_read_cl: each row spread over 2
+    or 4 emulated CTAs, the scan carries, the left neighbour's column and
+    the final reductions crossing CTAs through their shared state behind
+    cluster barriers; the serial phases on the lead CTA) against the oracle
+    for every alignment type and gap model, both strands, 32-bit lanes."""
+    from spoa_gb300 import synth
+    w = synth.long_10k(12, n_reads=3, tpl_len=560, min_len=500)
+    reads = list(w.reads)
+    lin, aff, cvx = (5, -4, -8, -8, -8, -8), (5, -4, -8, -6, -8, -6), (5, -4, -8, -6, -10, -4)
+    cases = ((lin, 0, 2, False), (aff, 1, 4, True), (cvx, 2, 2, False), (cvx, 0, 4, True))
+    for params, typ, cl, strand in cases:
+        rs = reads if not strand else [synth.revcomp(r) if j % 2 else r
+                                      for j, r in enumerate(reads)]
+        st, scores, rev, alns, cons = run_host_cl(wh, typ, params, rs, None, strand, cl, 32)
+        assert st == 0, (params, typ, cl, st)
+        ref = po.run_window(typ, *params, rs, strand_ambiguous=strand, with_msa=False)
+        assert scores == ref.scores, (params, typ, cl)
+        assert rev == [int(x) for x in ref.reversed], (params, typ, cl)
+        for a, b in zip(alns, ref.alignments):
+            assert np.array_equal(a, b), (params, typ, cl)
+        assert cons == ref.consensus, (params, typ, cl)
