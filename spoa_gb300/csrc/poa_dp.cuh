@@ -46,7 +46,8 @@ struct BlockScratch {
   int32_t wv2[32];
   int32_t edge[32];
   int32_t bcast[8];
-  int32_t cl[8];  // values this CTA publishes to the other CTAs of its cluster
+  int32_t cl[8];      // values this CTA publishes to the other CTAs of its cluster
+  int32_t clx[2][8];  // its row tails (cluster_publish), by row parity
 };
 
 // ---------------------------------------------------------------------------
@@ -90,6 +91,27 @@ __device__ __forceinline__ void cl_sync() {
   }
 }
 
+// The split form of cl_sync (CL > 1): arrive, releasing this thread's
+// earlier memory operations to the cluster; other work; then wait for every
+// thread of the cluster to arrive, acquiring theirs.  Memory operations
+// between the two are not ordered by the barrier.
+template <int CL>
+__device__ __forceinline__ void cl_arrive() {
+#ifdef __CUDA_ARCH__
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+#elif defined(SPOA_GB300_SIMT_HOST)
+  simt::cluster_arrive();
+#endif
+}
+template <int CL>
+__device__ __forceinline__ void cl_wait() {
+#ifdef __CUDA_ARCH__
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+#elif defined(SPOA_GB300_SIMT_HOST)
+  simt::cluster_wait();
+#endif
+}
+
 // A 32-bit shared variable of CTA `rank` of the cluster (the same variable
 // as `local` in this CTA).
 __device__ __forceinline__ int32_t cl_peek(const int32_t* local, uint32_t rank) {
@@ -107,10 +129,9 @@ __device__ __forceinline__ int32_t cl_peek(const int32_t* local, uint32_t rank) 
 #endif
 }
 
-// Slots of BlockScratch::cl: the in-row scans (the Q scan and the E / H
-// scan), the left neighbour's column, the final row maximum, minimum row
-// and minimum column.
-enum : int { kClScanA = 0, kClScanB = 1, kClLeft = 2, kClMax = 3, kClMin = 4, kClMinJ = 5 };
+// Slots of BlockScratch::cl: the final row maximum, minimum row and minimum
+// column.
+enum : int { kClMax = 0, kClMin = 1, kClMinJ = 2 };
 
 // Exclusive prefix-max of v over the CTA's threads (kNegBig for thread 0).
 // NW: warps of the CTA when known at compile time (0: blockDim.x / 32).
@@ -206,23 +227,14 @@ __device__ __forceinline__ int32_t block_min(int32_t v, BlockScratch& sh) {
 // With b_t = agg_t - t*CPT*pen this is a plain prefix-max.  Only thread 0
 // knows `init`; it folds it into its own aggregate (its strip end is then
 // exactly X[CPT-1]), so the other threads never need it.
-// With CL > 1, t is the thread's index in the cluster's row and the
-// exclusive prefix also takes the maximum over the CTAs before this one
-// (each publishes the maximum over its threads in slot `slot`).
-template <int CPT, int NW = 0, int CL = 1>
+template <int CPT, int NW = 0>
 __device__ __forceinline__ int32_t scan_carry(int32_t agg, int32_t init, int32_t pen,
-                                              BlockScratch& sh, int slot = kClScanA) {
-  const int32_t t = (int32_t)(cl_rank<CL>() * blockDim.x + threadIdx.x);
+                                              BlockScratch& sh) {
+  const int32_t t = (int32_t)threadIdx.x;
   const int32_t D = CPT * pen;
   int32_t v = t == 0 ? imax(agg, init + D) : agg;
   const int32_t x = v - t * D;
-  int32_t ex = block_excl_max<NW>(x, sh);
-  if constexpr (CL > 1) {
-    if (threadIdx.x == blockDim.x - 1) sh.cl[slot] = imax(ex, x);
-    cl_sync<CL>();
-    const uint32_t rank = cl_rank<CL>();
-    for (uint32_t r = 0; r < rank; ++r) ex = imax(ex, cl_peek(&sh.cl[slot], r));
-  }
+  const int32_t ex = block_excl_max<NW>(x, sh);
   return t == 0 ? init : ex + (t - 1) * D;
 }
 
@@ -457,9 +469,7 @@ __host__ __device__ __forceinline__ uint64_t colmap(uint64_t j, uint64_t nt) {
 }
 
 // Value of thread t-1 (thread 0 gets `fill`).
-// With CL > 1, thread 0 of CTA r > 0 gets the last thread of CTA r - 1
-// and `fill` goes to the first thread of the cluster.
-template <int NW = 0, int CL = 1>
+template <int NW = 0>
 __device__ __forceinline__ int32_t from_left(int32_t a, int32_t fill, BlockScratch& sh) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int32_t x = __shfl_up_sync(0xffffffffu, a, 1);
@@ -469,22 +479,15 @@ __device__ __forceinline__ int32_t from_left(int32_t a, int32_t fill, BlockScrat
     if (lane == 0 && warp > 0) x = sh.wv[warp - 1];
     __syncthreads();
   }
-  if constexpr (CL > 1) {
-    if (threadIdx.x == blockDim.x - 1) sh.cl[kClLeft] = a;
-    cl_sync<CL>();
-    const uint32_t rank = cl_rank<CL>();
-    if (threadIdx.x == 0 && rank > 0) x = cl_peek(&sh.cl[kClLeft], rank - 1);
-    return threadIdx.x == 0 && rank == 0 ? fill : x;
-  }
   return threadIdx.x == 0 ? fill : x;
 }
 
 // Strip scan of X[j] = max(a[j], X[j-1] + pen) over this thread's pairs with
 // the CTA carry.  On return x[k] holds X at the columns of pair k; returns
 // X[s-1], the value carried into the strip (init for thread 0).
-template <int CPT, typename Lx, int NW = 0, int CL = 1>
+template <int CPT, typename Lx, int NW = 0>
 __device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, int32_t pen,
-                                             BlockScratch& sh, int slot = kClScanA) {
+                                             BlockScratch& sh) {
   constexpr int HP = CPT / 2;
   static_assert(HP <= 16, "pair masks hold at most 16 pairs per strip");
   using P = typename Lx::P;
@@ -493,12 +496,99 @@ __device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, in
   for (int k = 1; k < HP; ++k) x[k] = Lx::addmax(x[k - 1], pen2, x[k]);
   const int32_t lo_agg = Lx::lo(x[HP - 1]), hi_agg = Lx::hi(x[HP - 1]);
   const int32_t agg = imax(hi_agg, lo_agg + HP * pen);
-  const int32_t c = scan_carry<CPT, NW, CL>(agg, init, pen, sh, slot);  // X[s-1]
+  const int32_t c = scan_carry<CPT, NW>(agg, init, pen, sh);  // X[s-1]
   const int32_t c_hi = imax(lo_agg, c + HP * pen);          // X[s+HP-1]
   const P carry = Lx::make(c, c_hi);
 #pragma unroll
   for (int k = 0; k < HP; ++k) x[k] = Lx::addmax(carry, Lx::splat((k + 1) * pen), x[k]);
   return c;
+}
+
+// The best path of a Q' carry into E' at column u of a CTA's range (u
+// from 0): through a vector start u' <= u (u' + 1 a multiple of `lanes`,
+// where E' also takes Q), at u' * c + (u - u') * e; linear in u', so the
+// last vector start when c >= e, else the first.  -infinity before the
+// first vector start.
+__device__ __forceinline__ int32_t mq_path(int32_t u, int32_t c, int32_t e, int32_t lanes) {
+  if (u < lanes - 1) return kNegBig;
+  const int32_t up = c >= e ? ((u + 1) & ~(lanes - 1)) - 1 : lanes - 1;
+  return up * c + (u - up) * e;
+}
+
+// What a cluster row carries into a CTA's range: the scan (H' for linear
+// gaps, E' otherwise) and Q' (convex) at the column before the range, and H
+// there (the diagonal source of the range's first column in the next row).
+struct ClusterCarry {
+  int32_t x, q, left;
+};
+
+// The one exchange of a cluster row, in two halves around the barrier so
+// that work between them (the row's F/O stores) is not waited for.
+// cluster_publish: the CTA's last thread publishes the CTA-local scans at
+// the last two columns of its range (sa, sp; convex also Q': qa, qp) and h
+// at the last column (ha), and every thread arrives.  The buffer alternates
+// with the row parity: a CTA rewrites it two rows later, after a barrier
+// that every CTA reaches only when done reading it.
+template <int CL>
+__device__ __forceinline__ void cluster_publish(int32_t sa, int32_t sp, int32_t ha, int32_t qa,
+                                                int32_t qp, uint32_t row, BlockScratch& sh) {
+  int32_t* rec = sh.clx[row & 1];
+  if (threadIdx.x == blockDim.x - 1) {
+    rec[0] = sa;
+    rec[1] = sp;
+    rec[2] = ha;
+    rec[3] = qa;
+    rec[4] = qp;
+  }
+  cl_arrive<CL>();
+}
+
+// cluster_fold: waits for the cluster, then every warp folds the CTAs
+// before its own, lane k holding CTA k's values (X the carry into CTA k):
+//   X'   = max(sa_k, X + W*pen)
+//   E'   gains Q + g + mq_path(u)      (convex)
+//   Q''  = max(qa_k, Q + W*c)
+//   H    = max(ha_k, E'[W-2], Q'[W-2]) at CTA k's last column (relu for SW).
+template <int SUB, int CL>
+__device__ __forceinline__ ClusterCarry cluster_fold(uint32_t row, int32_t W, int32_t type,
+                                                     int32_t pen, int32_t g, int32_t c, int32_t e,
+                                                     int32_t lanes, BlockScratch& sh) {
+  cl_wait<CL>();
+  const int32_t* rec = sh.clx[row & 1];
+  const uint32_t rank = cl_rank<CL>(), lane = threadIdx.x & 31;
+  int32_t va = kNegBig, vp = kNegBig, vh = kNegBig, vqa = kNegBig, vqp = kNegBig;
+  if (lane < rank) {
+    va = cl_peek(rec + 0, lane);
+    vp = cl_peek(rec + 1, lane);
+    vh = cl_peek(rec + 2, lane);
+    if (SUB == kConvex) {
+      vqa = cl_peek(rec + 3, lane);
+      vqp = cl_peek(rec + 4, lane);
+    }
+  }
+  ClusterCarry r{kNegBig, kNegBig, 0};
+  const int32_t mq_last = mq_path(W - 1, c, e, lanes), mq_prev = mq_path(W - 2, c, e, lanes);
+  for (uint32_t k = 0; k < rank; ++k) {
+    const int32_t a = __shfl_sync(0xffffffffu, va, k);
+    const int32_t ap = __shfl_sync(0xffffffffu, vp, k);
+    const int32_t ah = __shfl_sync(0xffffffffu, vh, k);
+    int32_t xl = imax(a, r.x + W * pen), xp = imax(ap, r.x + (W - 1) * pen);
+    int32_t ql = kNegBig, qpl = kNegBig;
+    if (SUB == kConvex) {
+      const int32_t aq = __shfl_sync(0xffffffffu, vqa, k);
+      const int32_t aqp = __shfl_sync(0xffffffffu, vqp, k);
+      ql = imax(aq, r.q + W * c);
+      qpl = imax(aqp, r.q + (W - 1) * c);
+      xl = imax(xl, r.q + g + mq_last);
+      xp = imax(xp, r.q + g + mq_prev);
+    }
+    int32_t hl = SUB == kLinear ? xl : (SUB == kAffine ? imax(ah, xp) : imax(ah, imax(xp, qpl)));
+    if (type == kSW) hl = imax(hl, 0);
+    r.x = xl;
+    r.q = ql;
+    r.left = hl;
+  }
+  return r;
 }
 
 
@@ -766,66 +856,157 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
         }
       }
     }
-    if (SUB >= kAffine) {
+    // the row's F and O (a cluster stores them while its barrier completes)
+    auto store_fo = [&]() {
+      if (SUB >= kAffine) {
 #pragma unroll
-      for (int k = 0; k < HP; k += 2) {
-        Lx::store2(F, rw + (k / 2) * st2, f[k], f[k + 1]);
-        if (SUB == kConvex) Lx::store2(O, rw + (k / 2) * st2, o[k], o[k + 1]);
+        for (int k = 0; k < HP; k += 2) {
+          Lx::store2(F, rw + (k / 2) * st2, f[k], f[k + 1]);
+          if (SUB == kConvex) Lx::store2(O, rw + (k / 2) * st2, o[k], o[k + 1]);
+        }
       }
-    }
+    };
+    if constexpr (CL == 1) store_fo();
     // Columns past the read are computed like the others and never masked:
     // they only feed columns to their right (the in-row scans run left to
     // right, the diagonal reads column j-1), the row selection below masks
     // them, and the traceback never reaches them.
     P hs[HP], ee[HP], qq[HP];
-    if (SUB == kLinear) {
+    // column s0-1 of this row for the CTA's thread 0: the first column fc
+    // in the cluster's first CTA, else the last column of the CTA before
+    int32_t lfill = fci;
+    if constexpr (CL == 1) {
+      if (SUB == kLinear) {
 #pragma unroll
-      for (int k = 0; k < HP; ++k) hs[k] = h[k];
-      pair_scan<CPT, Lx, NW, CL>(hs, fci, g, sh, kClScanA);
-      if (type == kSW) {
-        const P z = Lx::splat(0);
+        for (int k = 0; k < HP; ++k) hs[k] = h[k];
+        pair_scan<CPT, Lx, NW>(hs, fci, g, sh);
+        if (type == kSW) {
+          const P z = Lx::splat(0);
 #pragma unroll
-        for (int k = 0; k < HP; ++k) hs[k] = Lx::max(hs[k], z, NZ);
-      }
-    } else {
-      if (SUB == kConvex) {
-        P x[HP];
+          for (int k = 0; k < HP; ++k) hs[k] = Lx::max(hs[k], z, NZ);
+        }
+      } else {
+        if (SUB == kConvex) {
+          P x[HP];
 #pragma unroll
-        for (int k = 0; k < HP; ++k) x[k] = Lx::add(h[k], q2);
-        // x = Q' (Q of the next column); Q[s0] = Q'[s0-1] is the carry
-        const int32_t qin = pair_scan<CPT, Lx, NW, CL>(x, fci + q, c, sh, kClScanA);
-        qq[0] = Lx::make(qin, Lx::lo(x[HP - 1]));
+          for (int k = 0; k < HP; ++k) x[k] = Lx::add(h[k], q2);
+          // x = Q' (Q of the next column); Q[s0] = Q'[s0-1] is the carry
+          const int32_t qin = pair_scan<CPT, Lx, NW>(x, fci + q, c, sh);
+          qq[0] = Lx::make(qin, Lx::lo(x[HP - 1]));
 #pragma unroll
-        for (int k = 1; k < HP; ++k) qq[k] = x[k - 1];
-      }
-      {
-        P x[HP];
+          for (int k = 1; k < HP; ++k) qq[k] = x[k - 1];
+        }
+        {
+          P x[HP];
+#pragma unroll
+          for (int k = 0; k < HP; ++k) {
+            if (SUB == kConvex) {
+              // max(H1, Q at vector starts) + g: bits k and 16 + k of bmap
+              // moved to bits 15 and 31 give the pair's lane masks
+              const uint32_t bm = sign_lanes(bmap << (15 - k));
+              x[k] = Lx::add(Lx::max(h[k], Lx::select(bm, qq[k], NEG2), NZ), g2);
+            } else {
+              x[k] = Lx::add(h[k], g2);
+            }
+          }
+          const int32_t ein = pair_scan<CPT, Lx, NW>(x, fci + g, e, sh);  // x = E'
+          ee[0] = Lx::make(ein, Lx::lo(x[HP - 1]));
+#pragma unroll
+          for (int k = 1; k < HP; ++k) ee[k] = x[k - 1];
+        }
 #pragma unroll
         for (int k = 0; k < HP; ++k) {
-          if (SUB == kConvex) {
-            // max(H1, Q at vector starts) + g: bits k and 16 + k of bmap
-            // moved to bits 15 and 31 give the pair's lane masks
-            const uint32_t bm = sign_lanes(bmap << (15 - k));
-            x[k] = Lx::add(Lx::max(h[k], Lx::select(bm, qq[k], NEG2), NZ), g2);
-          } else {
-            x[k] = Lx::add(h[k], g2);
-          }
+          if (SUB == kConvex)
+            hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], qq[k]) : Lx::max3(h[k], ee[k], qq[k]);
+          else
+            hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], ee[k]) : Lx::max(h[k], ee[k], NZ);
         }
-        const int32_t ein = pair_scan<CPT, Lx, NW, CL>(x, fci + g, e, sh, kClScanB);  // x = E'
-        ee[0] = Lx::make(ein, Lx::lo(x[HP - 1]));
+      }
+    } else {
+      // A cluster row: CTA r owns columns r*W ... r*W + W - 1.  Every in-row
+      // scan runs CTA-local, from the row's initial values in CTA 0 and from
+      // -infinity in the others; one exchange then gives each CTA the values
+      // carried into its range (cluster_fold).  The scans are max-plus
+      // linear, so a carry X of a scan with penalty pen adds
+      // X + (u + 1) * pen at column u of the range, and for convex gaps the
+      // Q carry also reaches E' through the vector starts (mq).
+      const uint32_t rank = cl_rank<CL>();
+      const int32_t u0 = (int32_t)(threadIdx.x * CPT);  // first column in the range
+      // linear: H'; affine, convex: E' (and Q' in xq)
+      P xs[HP], xq[HP];
+      int32_t qin = kNegBig, sc_in;
+      if (SUB == kConvex) {
 #pragma unroll
-        for (int k = 1; k < HP; ++k) ee[k] = x[k - 1];
+        for (int k = 0; k < HP; ++k) xq[k] = Lx::add(h[k], q2);
+        qin = pair_scan<CPT, Lx, NW>(xq, rank == 0 ? fci + q : kNegBig, c, sh);
+        qq[0] = Lx::make(qin, Lx::lo(xq[HP - 1]));
+#pragma unroll
+        for (int k = 1; k < HP; ++k) qq[k] = xq[k - 1];
       }
 #pragma unroll
       for (int k = 0; k < HP; ++k) {
-        if (SUB == kConvex)
-          hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], qq[k]) : Lx::max3(h[k], ee[k], qq[k]);
-        else
-          hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], ee[k]) : Lx::max(h[k], ee[k], NZ);
+        if (SUB == kLinear) {
+          xs[k] = h[k];
+        } else if (SUB == kConvex) {
+          const uint32_t bm = sign_lanes(bmap << (15 - k));
+          xs[k] = Lx::add(Lx::max(h[k], Lx::select(bm, qq[k], NEG2), NZ), g2);
+        } else {
+          xs[k] = Lx::add(h[k], g2);
+        }
+      }
+      const int32_t pen = SUB == kLinear ? g : e;
+      sc_in = pair_scan<CPT, Lx, NW>(xs, rank == 0 ? (SUB == kLinear ? fci : fci + g) : kNegBig,
+                                   pen, sh);
+      cluster_publish<CL>(Lx::hi(xs[HP - 1]), Lx::hi(xs[HP - 2]), Lx::hi(h[HP - 1]),
+                          SUB == kConvex ? Lx::hi(xq[HP - 1]) : kNegBig,
+                          SUB == kConvex ? Lx::hi(xq[HP - 2]) : kNegBig, i, sh);
+      store_fo();
+      const ClusterCarry cc =
+          cluster_fold<SUB, CL>(i, (int32_t)(ntc * CPT), type, pen, g, c, e, lanes, sh);
+      if (rank > 0) {
+        const P cs = Lx::make(cc.x + (u0 + 1) * pen, cc.x + (u0 + HP + 1) * pen);
+#pragma unroll
+        for (int k = 0; k < HP; ++k) xs[k] = Lx::addmax(cs, Lx::splat(k * pen), xs[k]);
+        sc_in = imax(sc_in, cc.x + u0 * pen);
+        if (SUB == kConvex) {
+          const P cq = Lx::make(cc.q + (u0 + 1) * c, cc.q + (u0 + HP + 1) * c);
+#pragma unroll
+          for (int k = 0; k < HP; ++k) xq[k] = Lx::addmax(cq, Lx::splat(k * c), xq[k]);
+          qin = imax(qin, cc.q + u0 * c);
+          qq[0] = Lx::make(qin, Lx::lo(xq[HP - 1]));
+#pragma unroll
+          for (int k = 1; k < HP; ++k) qq[k] = xq[k - 1];
+          const int32_t qg = cc.q + g;
+#pragma unroll
+          for (int k = 0; k < HP; ++k)
+            xs[k] = Lx::max(xs[k], Lx::make(qg + mq_path(u0 + k, c, e, lanes),
+                                            qg + mq_path(u0 + HP + k, c, e, lanes)), NZ);
+          sc_in = imax(sc_in, qg + mq_path(u0 - 1, c, e, lanes));
+        }
+        lfill = cc.left;
+      }
+      if (SUB == kLinear) {
+#pragma unroll
+        for (int k = 0; k < HP; ++k) hs[k] = xs[k];
+        if (type == kSW) {
+          const P z = Lx::splat(0);
+#pragma unroll
+          for (int k = 0; k < HP; ++k) hs[k] = Lx::max(hs[k], z, NZ);
+        }
+      } else {
+        ee[0] = Lx::make(sc_in, Lx::lo(xs[HP - 1]));
+#pragma unroll
+        for (int k = 1; k < HP; ++k) ee[k] = xs[k - 1];
+#pragma unroll
+        for (int k = 0; k < HP; ++k) {
+          if (SUB == kConvex)
+            hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], qq[k]) : Lx::max3(h[k], ee[k], qq[k]);
+          else
+            hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], ee[k]) : Lx::max(h[k], ee[k], NZ);
+        }
       }
     }
-    // column s0-1 of this row (thread 0: the first column fc)
-    const int32_t lH = from_left<NW, CL>(Lx::hi(hs[HP - 1]), fci, sh);
+    const int32_t lH = from_left<NW>(Lx::hi(hs[HP - 1]), lfill, sh);
     // the gap rows E and Q as the recurrences computed them: the traceback
     // re-derives its horizontal tests from them
     if (SUB >= kAffine) {

@@ -17,6 +17,7 @@
 #include <cstring>
 #include <functional>
 #include <memory>
+#include <optional>
 #include <thread>
 #include <vector>
 #ifdef SIMT_TRACE
@@ -117,6 +118,18 @@ inline int32_t exchange(int32_t v, unsigned src_lane) {
 
 inline void cluster_sync() {
   if (cta()) cta()->cluster_bar->arrive_and_wait();
+}
+
+// The split form: arrive, then (after other work) wait for the others.
+inline thread_local std::optional<std::barrier<>::arrival_token> cluster_token;
+inline void cluster_arrive() {
+  if (cta()) cluster_token.emplace(cta()->cluster_bar->arrive());
+}
+inline void cluster_wait() {
+  if (cta() && cluster_token) {
+    cta()->cluster_bar->wait(std::move(*cluster_token));
+    cluster_token.reset();
+  }
 }
 
 // The copy of a shared variable of this CTA in CTA `rank` of the cluster.
