@@ -76,6 +76,8 @@ def parse():
     ap.add_argument("--serve-windows", type=int, default=600,
                     help="serve: windows per offered load")
     ap.add_argument("--windows", type=int, default=0, help="override the window count")
+    ap.add_argument("--long-reads", type=int, default=0,
+                    help="long_10k: only the first N reads of the window (a small case)")
     ap.add_argument("--plain-sample", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
@@ -115,7 +117,7 @@ def common_config(cfg: dict, world: int) -> dict:
                 l2="inputs and per-CTA arenas larger than L2 (129 MB)")
 
 
-def workload(name: str, n_override: int, rank: int):
+def workload(name: str, n_override: int, rank: int, long_reads: int = 0):
     """Returns (windows, type, params, per-window types, strand flags, config)."""
     if name == "batch_10k":
         n = n_override or 10000
@@ -138,9 +140,12 @@ def workload(name: str, n_override: int, rank: int):
         return wins, typ, params, None, None, {"workload": "single_500: one 500-nt window, 30 "
                                                             "reads, NW affine", "windows": 1}
     wins = [synth.long_10k(2 + rank)]
+    cfg = {"workload": "long_10k: one 10-kb window, 40 reads 2-10 kb, SW convex", "windows": 1}
+    if long_reads:
+        wins[0].reads = wins[0].reads[:long_reads]
+        cfg["reads"] = long_reads
     typ, params = synth.SCORING["long_10k"]
-    return wins, typ, params, None, None, {"workload": "long_10k: one 10-kb window, 40 reads "
-                                                        "2-10 kb, SW convex", "windows": 1}
+    return wins, typ, params, None, None, cfg
 
 
 class Clocks:
@@ -392,7 +397,8 @@ def main():
     if args.workload == "serve":
         return serve(args, sg, rank, world, dist, device)
 
-    wins, typ, params, wtypes, wstrand, cfg = workload(args.workload, args.windows, rank)
+    wins, typ, params, wtypes, wstrand, cfg = workload(args.workload, args.windows, rank,
+                                                       args.long_reads)
     n_windows = len(wins)
     seqs, off, wro = flatten(wins, pinned=True)
 
@@ -644,7 +650,8 @@ def reference_arm(args):
     oracle.  Each step times a bounded sample of the same workload."""
     from oracle import pyoracle as po
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    wins, typ, params, wtypes, wstrand, cfg = workload(args.workload, args.windows, 0)
+    wins, typ, params, wtypes, wstrand, cfg = workload(args.workload, args.windows, 0,
+                                                       args.long_reads)
     threads = os.cpu_count() or 1
     types, strands = _types_strands(wins, typ, wtypes, wstrand)
     total_steps = args.steps + args.warmup

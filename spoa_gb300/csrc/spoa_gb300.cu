@@ -178,6 +178,19 @@ bool seg_tile(uint32_t L, int* cpt, int* nt, int* segs) {
   return false;
 }
 
+// Cluster tile for 32-bit rows wider than kClusterMinCols: 2, 4 or 8 CTAs
+// per window (more CTAs from 2 x 128 x 12 and 4 x 128 x 12 columns), 12
+// columns per thread, the fewest 32-thread multiples per CTA that cover L.
+// False when L is not in the clusters' range (up to 8 x 512 x 12 columns).
+bool cluster_tile(uint32_t L, int* cl, int* nt) {
+  if (L <= kClusterMinCols || L > (uint32_t)kClCpt * 8 * 512) return false;
+  const int c = L > 4u * 128 * kClCpt ? 8 : L > 2u * 128 * kClCpt ? 4 : 2;
+  const uint64_t per = (uint64_t)c * kClCpt;
+  *cl = c;
+  *nt = (int)std::max<uint64_t>(32, ((L + per - 1) / per + 31) / 32 * 32);
+  return true;
+}
+
 // Makes `dev` the calling thread's current device while the guard lives and
 // restores the previous current device afterwards.
 struct DeviceGuard {
@@ -1169,12 +1182,8 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
   }
   int cpt = d.columns_per_thread, nt = d.threads_per_window, segs = 1, cl = 1;
   const bool forced = cpt > 0 && nt > 0;
-  if (p->wide && !forced && d.cluster != 1 && L > kClusterMinCols &&
-      L <= (uint32_t)kClCpt * 8 * 512) {
-    // a thread-block cluster per window: 2, 4 or 8 CTAs, 12 columns per thread
-    cl = L > 4u * 128 * kClCpt ? 8 : L > 2u * 128 * kClCpt ? 4 : 2;
-    cpt = kClCpt;
-    nt = (int)std::max<uint64_t>(32, ((uint64_t)(L + cl * kClCpt - 1) / (cl * kClCpt) + 31) / 32 * 32);
+  if (p->wide && !forced && d.cluster != 1 && cluster_tile(L, &cl, &nt)) {
+    cpt = kClCpt;  // a thread-block cluster per window
   } else if (p->tuned_cpt > 0 && (uint64_t)p->tuned_cpt * p->tuned_nt >= L) {
     cpt = p->tuned_cpt;
     nt = p->tuned_nt;
@@ -2176,6 +2185,25 @@ struct ServedWindow {
   Clock::time_point finished;
 };
 
+// Pinned staging buffers are allocated when the server starts and grow
+// geometrically (from kPinnedMin), so serving rarely calls the page-locked
+// allocator, which is slow and an implicit synchronisation point.
+constexpr uint64_t kPinnedMin = 1ull << 20;
+bool grow_pinned(uint8_t*& p, uint64_t& cap, uint64_t need) {
+  if (p != nullptr && cap >= need) return true;
+  const uint64_t want = std::max(std::max(need, 2 * cap), kPinnedMin);
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+  if (cudaHostAlloc(&p, want, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    p = nullptr;
+    return false;
+  }
+  cap = want;
+  return true;
+}
+
 // One launch in flight: its windows, its block of the pool, its pinned
 // staging buffer and the offsets of the parts inside both.
 struct ServedLaunch {
@@ -2252,6 +2280,7 @@ struct spoa_gb300_server {
   spoa_gb300_server_desc desc{};
   Scoring base{};
   int device = 0;
+  int sm_count = 1;
   DevicePool pool;
   Resident res;
   std::vector<ServedLaunch> slots;
@@ -2292,6 +2321,7 @@ void finish_window(spoa_gb300_server* sv, const std::shared_ptr<ServedWindow>& w
 
 bool resident_eligible(const spoa_gb300_server* sv, const ServedWindow& w);
 
+
 // Takes arrived windows of the front window's class and width (in arrival
 // order) into a free slot while their footprint fits the pool; false when
 // nothing could be admitted.
@@ -2315,7 +2345,8 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
         take.push_back(*it);
   }
   const bool wide = take.front()->plan.wide;
-  // footprint of the first k windows; halve k until it fits the pool
+  // footprint of the first k windows (arenas for the CTAs or clusters that
+  // run them); halve k until it fits the pool
   size_t k = take.size();
   while (k > 0) {
     uint32_t lmax = 1, maxreads = 1;
@@ -2331,12 +2362,17 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
       R += w.off.size() - 1;
       S += w.sumlen;
     }
-    // the batched kernel's tiles: 32-bit rows past 12 x 512 columns go to
-    // the segmented forward
-    int cpt = 0, nt = 0, segs = 1;
-    const bool tiled = wide && lmax > (uint32_t)kSegCpt * 512
-                           ? seg_tile(lmax, &cpt, &nt, &segs)
-                           : throughput_tile(lmax, wide, &cpt, &nt);
+    // the batched kernel's tiles: long 32-bit rows on thread-block clusters,
+    // past their range the segmented forward
+    int cpt = 0, nt = 0, segs = 1, cl = 1;
+    bool tiled;
+    if (wide && cluster_tile(lmax, &cl, &nt)) {
+      cpt = kClCpt;
+      tiled = true;
+    } else {
+      tiled = wide && lmax > (uint32_t)kSegCpt * 512 ? seg_tile(lmax, &cpt, &nt, &segs)
+                                                      : throughput_tile(lmax, wide, &cpt, &nt);
+    }
     if (!tiled) {
       // a read longer than any tile: the window fails alone
       auto w = take.front();
@@ -2350,7 +2386,18 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
     GraphCaps gc;
     DpCaps dc;
     const uint64_t stride =
-        arena_caps(sv->base.sub, wide, cpt * segs, nt, nodes, maxsum, maxreads, many, &gc, &dc);
+        arena_caps(sv->base.sub, wide, cpt * segs * cl, nt, nodes, maxsum, maxreads, many, &gc,
+                   &dc);
+    // the kernels are persistent (every CTA, or cluster, takes windows from
+    // the work queue until it is empty): launch no more than can be
+    // resident at once
+    int resident = 0;
+    if ((cl > 1     ? SPOA_BY_SUB16(sv->base.sub, occupancy_batch_cl, cl, nt, &resident)
+         : segs > 1 ? SPOA_BY_SUB32(sv->base.sub, occupancy_batch_seg, segs, nt, &resident)
+                    : SPOA_BY_SUB(sv->base.sub, wide, occupancy_batch, cpt, nt, &resident)) != kOk)
+      resident = 1;
+    if (cl == 1) resident *= sv->sm_count;
+    const uint64_t grid = std::min<uint64_t>(k, (uint64_t)std::max(resident, 1));
     // inputs: work, queue, window read offsets, read offsets, types, strands,
     // consensus offsets, reads; outputs: scores, strands, lengths, status,
     // cell counters, consensus; then the arenas
@@ -2372,7 +2419,7 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
     const uint64_t o_cells = o; o = a16(o + 16);
     const uint64_t o_cons = o; o = a16(o + S + n);
     const uint64_t arena_off = align_up(o, 256);
-    const uint64_t total = arena_off + stride * n;
+    const uint64_t total = arena_off + stride * grid;
     if (total > sv->pool.size()) {
       if (k == 1) {  // can never fit: fail it
         auto w = take.front();
@@ -2393,16 +2440,9 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
       continue;
     }
     // admitted: stage the inputs in the slot's pinned buffer
-    if (L.pinned_cap < arena_off) {
-      if (L.pinned) cudaFreeHost(L.pinned);
-      L.pinned = nullptr;
-      L.pinned_cap = 0;
-      if (cudaHostAlloc(&L.pinned, arena_off, cudaHostAllocDefault) != cudaSuccess) {
-        cudaGetLastError();
-        sv->pool.release(off);
-        return false;
-      }
-      L.pinned_cap = arena_off;
+    if (!grow_pinned(L.pinned, L.pinned_cap, arena_off)) {
+      sv->pool.release(off);
+      return false;
     }
     uint8_t* h = L.pinned;
     auto* work = reinterpret_cast<uint32_t*>(h + i_work);
@@ -2457,8 +2497,10 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
     bool ok = cudaMemcpyAsync(d, h, in_bytes, cudaMemcpyHostToDevice, L.stream) == cudaSuccess &&
               cudaMemsetAsync(d + o_cells, 0, 16, L.stream) == cudaSuccess;
     if (ok)
-      ok = (segs > 1 ? SPOA_BY_SUB32(sv->base.sub, launch_batch_seg, segs, nt, (int)n, a, L.stream)
-                     : SPOA_BY_SUB(sv->base.sub, wide, launch_batch, cpt, nt, (int)n, a, L.stream))
+      ok = (cl > 1 ? SPOA_BY_SUB16(sv->base.sub, launch_batch_cl, cl, nt, (int)grid, a, L.stream)
+            : segs > 1
+                ? SPOA_BY_SUB32(sv->base.sub, launch_batch_seg, segs, nt, (int)grid, a, L.stream)
+                : SPOA_BY_SUB(sv->base.sub, wide, launch_batch, cpt, nt, (int)grid, a, L.stream))
            == kOk;
     if (ok)
       ok = cudaMemcpyAsync(h + o_scores, d + o_scores, arena_off - o_scores, cudaMemcpyDeviceToHost,
@@ -2591,6 +2633,20 @@ bool resident_setup_once(spoa_gb300_server* sv) {
     return false;
   }
   R.entries.resize(kResidentRing);
+  // staging batches ready before windows arrive (pinned allocations can
+  // wait for the device's work in flight)
+  for (int k = 0; k < 4; ++k) {
+    ResidentStage st;
+    const bool ok = cudaEventCreateWithFlags(&st.copied, cudaEventDisableTiming) == cudaSuccess &&
+                    grow_pinned(st.pinned, st.cap, kPinnedMin);
+    if (!ok) {
+      cudaGetLastError();
+      if (st.copied) cudaEventDestroy(st.copied);
+      if (st.pinned) cudaFreeHost(st.pinned);
+      return false;
+    }
+    R.spare.push_back(std::move(st));
+  }
   R.ready = true;
   return true;
 }
@@ -2640,18 +2696,10 @@ bool resident_admit(spoa_gb300_server* sv) {
     R.spare.push_back(std::move(st));
     return false;
   }
-  if (st.cap < total) {
-    if (st.pinned) cudaFreeHost(st.pinned);
-    st.pinned = nullptr;
-    st.cap = 0;
-    if (cudaHostAlloc(&st.pinned, total, cudaHostAllocDefault) != cudaSuccess) {
-      cudaGetLastError();
-      st.pinned = nullptr;
-      for (auto& p : parts) sv->pool.release(p.first);
-      R.spare.push_back(std::move(st));
-      return false;
-    }
-    st.cap = total;
+  if (!grow_pinned(st.pinned, st.cap, total)) {
+    for (auto& p : parts) sv->pool.release(p.first);
+    R.spare.push_back(std::move(st));
+    return false;
   }
   uint64_t o = 0;
   bool ok = true;
@@ -2870,6 +2918,12 @@ int32_t spoa_gb300_server_create(const spoa_gb300_server_desc* d, spoa_gb300_ser
     delete sv;
     return kCuda;
   }
+  if (cudaDeviceGetAttribute(&sv->sm_count, cudaDevAttrMultiProcessorCount, sv->device) !=
+          cudaSuccess ||
+      sv->sm_count < 1) {
+    cudaGetLastError();
+    sv->sm_count = 1;
+  }
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
     cudaGetLastError();
@@ -2884,7 +2938,8 @@ int32_t spoa_gb300_server_create(const spoa_gb300_server_desc* d, spoa_gb300_ser
   sv->slots.resize(sv->desc.max_streams);
   for (ServedLaunch& L : sv->slots) {
     if (cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming) != cudaSuccess ||
+        !grow_pinned(L.pinned, L.pinned_cap, kPinnedMin)) {
       cudaGetLastError();
       spoa_gb300_server_destroy(sv);
       return kCuda;

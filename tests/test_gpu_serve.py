@@ -83,14 +83,20 @@ def test_wait_timeout_and_unknown_ticket():
 
 @pytest.mark.gpu
 def test_long_window_served():
-    """A window of 6.5-7k-column int32 rows through the server (the
-    segmented kernel), against the oracle."""
-    w = synth.long_10k(11, n_reads=3, tpl_len=7200, min_len=6500)
+    """Windows of 2-2.4k, 4.2-4.8k and 6.5-7k-column int32 rows through the
+    server (thread-block clusters of 2, 4 and 8 CTAs; the two shorter ones
+    strand-ambiguous, submitted together), against the oracle."""
+    ws = [(synth.long_10k(11, n_reads=3, tpl_len=7200, min_len=6500).reads, False),
+          (synth.long_10k(21, n_reads=3, tpl_len=2400, min_len=2000).reads, True),
+          (synth.long_10k(22, n_reads=3, tpl_len=4800, min_len=4200).reads, True)]
+    ws[1] = ([synth.revcomp(r) if j == 1 else r for j, r in enumerate(ws[1][0])], True)
     with sg.Server(2, *PARAMS) as sv:
-        t = sv.submit(w.reads, 2, False)
-        st, cons, lat = sv.wait(t, timeout=600)
-    assert st == 0
-    assert cons == po.run_window(2, *PARAMS, w.reads, with_msa=False).consensus
+        tickets = [sv.submit(reads, 2, strand) for reads, strand in ws]
+        got = [sv.wait(t, timeout=600) for t in tickets]
+    for (reads, strand), (st, cons, lat) in zip(ws, got):
+        assert st == 0
+        assert cons == po.run_window(2, *PARAMS, reads, strand_ambiguous=strand,
+                                     with_msa=False).consensus
 
 
 @pytest.mark.gpu
