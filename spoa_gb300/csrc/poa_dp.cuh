@@ -42,9 +42,14 @@ __device__ __forceinline__ int32_t addmax(int32_t a, int32_t b, int32_t c) {
 }
 
 struct BlockScratch {
+  // per-warp slots of the in-row exchanges, one array per exchange of a
+  // row (the Q scan, the E / H scan, the left column): the next write to a
+  // slot comes after another exchange's barrier, so none needs a barrier
+  // after its reads.  wv2 takes the left column during the row loop and
+  // the block reductions after it (each of those starts with a barrier).
+  int32_t wq[32];
   int32_t wv[32];
   int32_t wv2[32];
-  int32_t edge[32];
   int32_t bcast[8];
   int32_t cl[8];      // values this CTA publishes to the other CTAs of its cluster
   int32_t clx[2][8];  // its row tails (cluster_publish), by row parity
@@ -135,8 +140,10 @@ enum : int { kClMax = 0, kClMin = 1, kClMinJ = 2 };
 
 // Exclusive prefix-max of v over the CTA's threads (kNegBig for thread 0).
 // NW: warps of the CTA when known at compile time (0: blockDim.x / 32).
+// `slots` (32 per-warp values) must not be written again before the CTA's
+// next barrier.
 template <int NW = 0>
-__device__ __forceinline__ int32_t block_excl_max(int32_t v, BlockScratch& sh) {
+__device__ __forceinline__ int32_t block_excl_max(int32_t v, int32_t* slots) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t nw = NW ? NW : blockDim.x >> 5;
   int32_t x = v;
@@ -148,11 +155,10 @@ __device__ __forceinline__ int32_t block_excl_max(int32_t v, BlockScratch& sh) {
   int32_t ex = __shfl_up_sync(0xffffffffu, x, 1);
   if (lane == 0) ex = kNegBig;
   if (nw > 1) {
-    if (lane == 31) sh.wv[warp] = x;
+    if (lane == 31) slots[warp] = x;
     __syncthreads();
     int32_t wp = kNegBig;
-    for (uint32_t w = 0; w < warp; ++w) wp = imax(wp, sh.wv[w]);
-    __syncthreads();
+    for (uint32_t w = 0; w < warp; ++w) wp = imax(wp, slots[w]);
     ex = imax(ex, wp);
   }
   return ex;
@@ -229,12 +235,12 @@ __device__ __forceinline__ int32_t block_min(int32_t v, BlockScratch& sh) {
 // exactly X[CPT-1]), so the other threads never need it.
 template <int CPT, int NW = 0>
 __device__ __forceinline__ int32_t scan_carry(int32_t agg, int32_t init, int32_t pen,
-                                              BlockScratch& sh) {
+                                              int32_t* slots) {
   const int32_t t = (int32_t)threadIdx.x;
   const int32_t D = CPT * pen;
   int32_t v = t == 0 ? imax(agg, init + D) : agg;
   const int32_t x = v - t * D;
-  const int32_t ex = block_excl_max<NW>(x, sh);
+  const int32_t ex = block_excl_max<NW>(x, slots);
   return t == 0 ? init : ex + (t - 1) * D;
 }
 
@@ -468,16 +474,16 @@ __host__ __device__ __forceinline__ uint64_t colmap(uint64_t j, uint64_t nt) {
   return 2 * ((k >> 1) * 2 * nt + 2 * t + (k & 1)) + r / (CPT / 2);
 }
 
-// Value of thread t-1 (thread 0 gets `fill`).
+// Value of thread t-1 (thread 0 gets `fill`); the slots of sh.wv2 must not
+// be written again before the CTA's next barrier.
 template <int NW = 0>
 __device__ __forceinline__ int32_t from_left(int32_t a, int32_t fill, BlockScratch& sh) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int32_t x = __shfl_up_sync(0xffffffffu, a, 1);
   if ((NW ? NW : blockDim.x >> 5) > 1) {
-    if (lane == 31) sh.wv[warp] = a;
+    if (lane == 31) sh.wv2[warp] = a;
     __syncthreads();
-    if (lane == 0 && warp > 0) x = sh.wv[warp - 1];
-    __syncthreads();
+    if (lane == 0 && warp > 0) x = sh.wv2[warp - 1];
   }
   return threadIdx.x == 0 ? fill : x;
 }
@@ -487,7 +493,7 @@ __device__ __forceinline__ int32_t from_left(int32_t a, int32_t fill, BlockScrat
 // X[s-1], the value carried into the strip (init for thread 0).
 template <int CPT, typename Lx, int NW = 0>
 __device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, int32_t pen,
-                                             BlockScratch& sh) {
+                                             int32_t* slots) {
   constexpr int HP = CPT / 2;
   static_assert(HP <= 16, "pair masks hold at most 16 pairs per strip");
   using P = typename Lx::P;
@@ -496,7 +502,7 @@ __device__ __forceinline__ int32_t pair_scan(typename Lx::P* x, int32_t init, in
   for (int k = 1; k < HP; ++k) x[k] = Lx::addmax(x[k - 1], pen2, x[k]);
   const int32_t lo_agg = Lx::lo(x[HP - 1]), hi_agg = Lx::hi(x[HP - 1]);
   const int32_t agg = imax(hi_agg, lo_agg + HP * pen);
-  const int32_t c = scan_carry<CPT, NW>(agg, init, pen, sh);  // X[s-1]
+  const int32_t c = scan_carry<CPT, NW>(agg, init, pen, slots);  // X[s-1]
   const int32_t c_hi = imax(lo_agg, c + HP * pen);          // X[s+HP-1]
   const P carry = Lx::make(c, c_hi);
 #pragma unroll
@@ -597,7 +603,7 @@ __device__ __forceinline__ ClusterCarry cluster_fold(uint32_t row, int32_t W, in
 // NT: the CTA's threads when known at compile time (0: blockDim.x); with it
 // every row offset of a load or store is a constant of the instruction and
 // the scans of a one-warp CTA take no shared-memory path.
-template <int SUB, int CPT, typename T, int NT = 0, int CL = 1>
+template <int SUB, int CPT, typename T, int NT = 0>
 __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8_t* __restrict__ seq,
                            uint32_t L, uint32_t V, int32_t lanes, BlockScratch& sh,
                            int64_t* out_max_i, int64_t* out_max_j, int32_t* out_score) {
@@ -606,7 +612,434 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
   using L16 = Lanes<int16_t>;
   constexpr int HP = CPT / 2;
   static_assert(HP <= 16, "pair masks hold at most 16 pairs per strip");
-  // this thread's index in the row: in the cluster's row when CL > 1
+  const uint32_t t = threadIdx.x;
+  const uint32_t s0 = t * CPT;
+  const uint64_t ld = D.caps.ld;        // elements per row
+  const uint64_t wrow = ld / 2;         // pair words per row
+  // pairs k and k+1 (k even) of this thread: pair words w0 + (k/2) * st2
+  // and the next; the warp's accesses to them are contiguous
+  const uint64_t w0 = 2 * (uint64_t)t;
+  constexpr int NW = NT / 32;
+  const uint64_t st2 = 2 * (uint64_t)(NT ? NT : blockDim.x);
+  const int32_t type = S.type;
+  const int32_t m = S.m, n = S.n, g = S.g, e = S.e, q = S.q, c = S.c;
+  const int32_t NEGW = lanes == 8 ? (INT32_MIN + 1024) : (INT16_MIN + 1024);
+  void* __restrict__ H = D.H;
+  void* __restrict__ F = D.F;
+  void* __restrict__ O = D.O;
+  void* __restrict__ E = D.E;
+  void* __restrict__ Q = D.Q;
+  const P NEG2 = Lx::splat(Lx::kNeg);
+  const uint32_t NZ = S.min16x2;  // neutral operand of Lx::max
+  const P m2 = Lx::splat(m), n2 = Lx::splat(n);
+  const P g2 = Lx::splat(g), e2 = Lx::splat(e), q2 = Lx::splat(q), c2 = Lx::splat(c);
+  const P ge2 = Lx::splat(g - e), qc2 = Lx::splat(q - c);
+  const bool edge_thread = s0 + CPT > L;  // strip reaches past the read
+
+  // read characters, 4 per register: byte b of sq8[k/4] is column s0+k of
+  // the low half-strip (k = 4*(k/4) + b), sqh8 the same for the high half;
+  // columns past the read hold 0xFF (whatever they match only feeds columns
+  // past the read)
+  uint32_t sq8[(HP + 3) / 4], sqh8[(HP + 3) / 4];
+#pragma unroll
+  for (int k4 = 0; k4 < (HP + 3) / 4; ++k4) {
+    uint32_t lo = 0, hi = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const uint32_t k = k4 * 4 + b;
+      const uint32_t jl = s0 + k, jh = s0 + HP + k;
+      lo |= (k < HP && jl < L ? (uint32_t)seq[jl] : 0xFFu) << (8 * b);
+      hi |= (k < HP && jh < L ? (uint32_t)seq[jh] : 0xFFu) << (8 * b);
+    }
+    sq8[k4] = lo;
+    sqh8[k4] = hi;
+  }
+  // the two characters of pair k as 16-bit lanes
+  auto sq = [&](int k) -> L16::P {
+    return L16::P{__byte_perm(sq8[k / 4], sqh8[k / 4], (uint32_t)(k % 4) | (0x4u + k % 4) << 8) &
+                  0x00FF00FFu};
+  };
+  // convex: columns whose E' input also takes Q (vector starts of the
+  // reference, (col + 1) % lanes == 0), as a bitmap (bit k low, 16+k high)
+  uint32_t bmap = 0;
+  if (SUB == kConvex) {
+#pragma unroll
+    for (int k = 0; k < HP; ++k) {
+      if ((s0 + k + 1) % (uint32_t)lanes == 0) bmap |= 1u << k;
+      if ((s0 + HP + k + 1) % (uint32_t)lanes == 0) bmap |= 1u << (16 + k);
+    }
+  }
+
+  // row 0 (implementation.hpp:555-694) and its registers
+  P ph[HP], pf[HP], po[HP];
+#pragma unroll
+  for (int k = 0; k < HP; ++k) {
+    int32_t v[2];
+#pragma unroll
+    for (int hf = 0; hf < 2; ++hf) {
+      const int32_t j = (int32_t)(s0 + hf * HP + k);
+      if (type == kSW) {
+        v[hf] = 0;
+      } else if (SUB == kConvex) {
+        v[hf] = imax(g + j * e, q + j * c);
+      } else if (SUB == kAffine) {
+        v[hf] = g + j * e;
+      } else {
+        v[hf] = g + j * g;
+      }
+    }
+    ph[k] = Lx::make(v[0], v[1]);
+    pf[k] = NEG2;
+    po[k] = NEG2;
+  }
+#pragma unroll
+  for (int k = 0; k < HP; k += 2) {
+    const uint64_t wk = w0 + (k / 2) * st2;
+    Lx::store2(H, wk, ph[k], ph[k + 1]);
+    if (SUB >= kAffine) Lx::store2(F, wk, pf[k], pf[k + 1]);
+    if (SUB == kConvex) Lx::store2(O, wk, po[k], po[k + 1]);
+  }
+  int32_t left_prev;  // row i-1 at column s0-1 (thread 0: its first column)
+  {
+    const int32_t j = (int32_t)s0 - 1;
+    int32_t v;
+    if (type == kSW) {
+      v = 0;
+    } else if (SUB == kConvex) {
+      v = imax(g + j * e, q + j * c);
+    } else if (SUB == kAffine) {
+      v = g + j * e;
+    } else {
+      v = g + j * g;
+    }
+    left_prev = t == 0 ? 0 : v;
+  }
+  if (t == 0) {
+    D.fc[0] = 0;
+    D.fcF[0] = 0;
+    D.fcO[0] = 0;
+  }
+  int32_t bval = type == kSW ? 0 : (type == kOV ? kNegBig : NEGW);
+  int32_t brow = -1;
+  int32_t first_sink = -1;
+  // the thread holding column L-1 (NW selection)
+  const uint32_t jl = L - 1;
+  const bool owns_last = jl >= s0 && jl < s0 + CPT;
+  const int32_t last_k = (int32_t)((jl - s0) % HP), last_hi = (int32_t)((jl - s0) / HP);
+  // first column of the previous row (thread 0), kept in registers
+  int32_t fc_prev = 0, fcF_prev = 0, fcO_prev = 0;
+  // the next row's record is loaded one row ahead, off the critical path
+  uint4 rec_next = D.rowrec[1];
+  __syncthreads();
+
+  for (uint32_t i = 1; i <= V; ++i) {
+    const uint4 rec = rec_next;
+    if (i < V) rec_next = D.rowrec[i + 1];
+    const uint32_t rflags = (rec.y >> 16) & 0xFFu;
+    const L16::P rc2 = L16::splat(rec.y >> 24);
+    // Over the predecessors only maxima are taken: the diagonal source
+    // max_p H_p[j-1] (hd), for linear gaps the vertical max_p H_p[j] (f),
+    // for affine/convex max_p max(H_p + g - e, F_p) (f) and
+    // max_p max(H_p + q - c, O_p) (o).  The substitution score and the gap
+    // extension are the same for every predecessor and are added once per
+    // row; max_p(x_p) + s = max_p(x_p + s) exactly (no value wraps: the width
+    // rule keeps every finite value and the -infinity margin in range).
+    P hd[HP], f[HP], o[HP];
+    int32_t fl = kNegBig, fa = kNegBig, fo = kNegBig;
+    // the predecessor order only matters to the traceback, which keeps the
+    // reference's order
+    auto accumulate = [&](const P* hp, const P* fp, const P* op, int32_t hleft, bool first) {
+#pragma unroll
+      for (int k = 0; k < HP; ++k) {
+        const P left = k == 0 ? Lx::make(hleft, Lx::lo(hp[HP - 1])) : hp[k - 1];
+        hd[k] = first ? left : Lx::max(hd[k], left, NZ);
+        if (SUB == kLinear) {
+          f[k] = first ? hp[k] : Lx::max(f[k], hp[k], NZ);
+        } else {
+          f[k] = first ? Lx::addmax(hp[k], ge2, fp[k]) : Lx::max3(f[k], Lx::add(hp[k], ge2), fp[k]);
+          if (SUB == kConvex)
+            o[k] = first ? Lx::addmax(hp[k], qc2, op[k]) : Lx::max3(o[k], Lx::add(hp[k], qc2), op[k]);
+        }
+      }
+    };
+    bool first = true;
+    if (rflags & kRowPrevPred) {
+      // the previous rank is a predecessor: its row is in registers
+      if (t == 0) {
+        fl = imax(fl, fc_prev);
+        if (SUB >= kAffine) fa = imax(fa, fcF_prev);
+        if (SUB == kConvex) fo = imax(fo, fcO_prev);
+      }
+      accumulate(ph, pf, po, t == 0 ? fc_prev : left_prev, true);
+      first = false;
+    }
+    // the other predecessors: two from the record, any further ones from the
+    // predecessor list (rows with more than two are rare)
+    uint32_t p = rec.z;
+    uint32_t visited = 0, skipped = 0;
+    uint32_t pi = rec.x;
+    const uint32_t pend = (rflags & kRowMore) ? D.pred_ptr[i + 1] : rec.x;
+    while (p != kNone) {
+      P hp[HP], fp[HP], op[HP];
+      const uint64_t rwp = (uint64_t)p * wrow + w0;
+#pragma unroll
+      for (int k = 0; k < HP; k += 2) {
+        const uint64_t wk = rwp + (k / 2) * st2;
+        Lx::load2(H, wk, hp[k], hp[k + 1]);
+        if (SUB >= kAffine) Lx::load2(F, wk, fp[k], fp[k + 1]);
+        if (SUB == kConvex) Lx::load2(O, wk, op[k], op[k + 1]);
+      }
+      // column s0-1: the high lane of the left thread's last pair (HP-1,
+      // odd), pair word (HP/2 - 1) * st2 + w0 - 1
+      int32_t hleft;
+      if (t == 0) {
+        hleft = D.fc[p];
+        fl = imax(fl, D.fc[p]);
+        if (SUB >= kAffine) fa = imax(fa, D.fcF[p]);
+        if (SUB == kConvex) fo = imax(fo, D.fcO[p]);
+      } else {
+        hleft = Lx::elem(H, (uint64_t)p * ld + 2 * ((HP / 2 - 1) * st2 + w0 - 1) + 1);
+      }
+      accumulate(hp, fp, op, hleft, first);
+      first = false;
+      if (++visited == 1) {
+        p = rec.w;
+      } else {
+        p = kNone;
+        while (pi < pend) {
+          const uint32_t q = D.preds[pi++];
+          if (q == i - 1) continue;
+          if (skipped < 2) {
+            ++skipped;
+            continue;
+          }
+          p = q;
+          break;
+        }
+      }
+    }
+    // NW first column (thread 0)
+    int32_t fci = 0;
+    if (t == 0) {
+      const bool source = (rflags & kRowSource) != 0;
+      if (type == kNW) {
+        if (SUB == kLinear) {
+          fci = (source ? 0 : fl) + g;
+        } else {
+          const int32_t vF = (source ? g - e : fa) + e;
+          D.fcF[i] = vF;
+          fcF_prev = vF;
+          if (SUB == kConvex) {
+            const int32_t vO = (source ? q - c : fo) + c;
+            D.fcO[i] = vO;
+            fcO_prev = vO;
+            fci = imax(vF, vO);
+          } else {
+            fci = vF;
+          }
+        }
+      }
+      D.fc[i] = fci;
+      fc_prev = fci;
+    }
+    const uint64_t rw = (uint64_t)i * wrow + w0;
+    P h[HP];
+#pragma unroll
+    for (int k = 0; k < HP; ++k) {
+      const P d = Lx::add(hd[k], Lx::profile(sq(k).v, rc2.v, m2, n2));
+      if (SUB == kLinear) {
+        h[k] = Lx::addmax(f[k], g2, d);
+      } else {
+        f[k] = Lx::add(f[k], e2);
+        if (SUB == kConvex) {
+          o[k] = Lx::add(o[k], c2);
+          h[k] = Lx::max3(d, f[k], o[k]);
+        } else {
+          h[k] = Lx::max(d, f[k], NZ);
+        }
+      }
+    }
+    if (SUB >= kAffine) {
+#pragma unroll
+      for (int k = 0; k < HP; k += 2) {
+        Lx::store2(F, rw + (k / 2) * st2, f[k], f[k + 1]);
+        if (SUB == kConvex) Lx::store2(O, rw + (k / 2) * st2, o[k], o[k + 1]);
+      }
+    }
+    // Columns past the read are computed like the others and never masked:
+    // they only feed columns to their right (the in-row scans run left to
+    // right, the diagonal reads column j-1), the row selection below masks
+    // them, and the traceback never reaches them.
+    P hs[HP], ee[HP], qq[HP];
+    if (SUB == kLinear) {
+#pragma unroll
+      for (int k = 0; k < HP; ++k) hs[k] = h[k];
+      pair_scan<CPT, Lx, NW>(hs, fci, g, sh.wv);
+      if (type == kSW) {
+        const P z = Lx::splat(0);
+#pragma unroll
+        for (int k = 0; k < HP; ++k) hs[k] = Lx::max(hs[k], z, NZ);
+      }
+    } else {
+      if (SUB == kConvex) {
+        P x[HP];
+#pragma unroll
+        for (int k = 0; k < HP; ++k) x[k] = Lx::add(h[k], q2);
+        // x = Q' (Q of the next column); Q[s0] = Q'[s0-1] is the carry
+        const int32_t qin = pair_scan<CPT, Lx, NW>(x, fci + q, c, sh.wq);
+        qq[0] = Lx::make(qin, Lx::lo(x[HP - 1]));
+#pragma unroll
+        for (int k = 1; k < HP; ++k) qq[k] = x[k - 1];
+      }
+      {
+        P x[HP];
+#pragma unroll
+        for (int k = 0; k < HP; ++k) {
+          if (SUB == kConvex) {
+            // max(H1, Q at vector starts) + g: bits k and 16 + k of bmap
+            // moved to bits 15 and 31 give the pair's lane masks
+            const uint32_t bm = sign_lanes(bmap << (15 - k));
+            x[k] = Lx::add(Lx::max(h[k], Lx::select(bm, qq[k], NEG2), NZ), g2);
+          } else {
+            x[k] = Lx::add(h[k], g2);
+          }
+        }
+        const int32_t ein = pair_scan<CPT, Lx, NW>(x, fci + g, e, sh.wv);  // x = E'
+        ee[0] = Lx::make(ein, Lx::lo(x[HP - 1]));
+#pragma unroll
+        for (int k = 1; k < HP; ++k) ee[k] = x[k - 1];
+      }
+#pragma unroll
+      for (int k = 0; k < HP; ++k) {
+        if (SUB == kConvex)
+          hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], qq[k]) : Lx::max3(h[k], ee[k], qq[k]);
+        else
+          hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], ee[k]) : Lx::max(h[k], ee[k], NZ);
+      }
+    }
+    // column s0-1 of this row (thread 0: the first column fc)
+    const int32_t lH = from_left<NW>(Lx::hi(hs[HP - 1]), fci, sh);
+    // the gap rows E and Q as the recurrences computed them: the traceback
+    // re-derives its horizontal tests from them
+    if (SUB >= kAffine) {
+#pragma unroll
+      for (int k = 0; k < HP; k += 2) {
+        Lx::store2cs(E, rw + (k / 2) * st2, ee[k], ee[k + 1]);
+        if (SUB == kConvex) Lx::store2cs(Q, rw + (k / 2) * st2, qq[k], qq[k + 1]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < HP; k += 2) Lx::store2(H, rw + (k / 2) * st2, hs[k], hs[k + 1]);
+
+    // row selection (strict <: the earliest row wins a tie)
+    if (type == kNW) {
+      if ((rflags & kRowSink) && owns_last) {
+        int32_t v = kNegBig;
+#pragma unroll
+        for (int k = 0; k < HP; ++k)
+          if (k == last_k) v = last_hi ? Lx::hi(hs[k]) : Lx::lo(hs[k]);
+        if (v > bval) {
+          bval = v;
+          brow = (int32_t)i;
+        }
+      }
+    } else if (type == kSW || (rflags & kRowSink)) {
+      P mx = hs[0];
+      if (edge_thread) {
+#pragma unroll
+        for (int k = 0; k < HP; ++k) {
+          const uint32_t vm = (s0 + k < L ? 0x0000FFFFu : 0u) | (s0 + HP + k < L ? 0xFFFF0000u : 0u);
+          const P x = Lx::select(vm, hs[k], NEG2);
+          mx = k == 0 ? x : Lx::max(mx, x, NZ);
+        }
+      } else {
+#pragma unroll
+        for (int k = 1; k < HP; ++k) mx = Lx::max(mx, hs[k], NZ);
+      }
+      const int32_t tm = s0 < L ? imax(Lx::lo(mx), Lx::hi(mx)) : kNegBig;
+      if (tm > bval) {
+        bval = tm;
+        brow = (int32_t)i;
+      }
+      if (type == kOV && first_sink < 0) first_sink = (int32_t)i;
+    }
+    // this row becomes the registers of row i-1
+#pragma unroll
+    for (int k = 0; k < HP; ++k) {
+      ph[k] = hs[k];
+      if (SUB >= kAffine) pf[k] = f[k];
+      if (SUB == kConvex) po[k] = o[k];
+    }
+    left_prev = t == 0 ? 0 : lH;
+    __syncthreads();
+  }
+
+  // global selection: best value, then the earliest row reaching it
+  const int32_t B = block_max<NW>(bval, sh);
+  const int32_t R = block_min<NW>(bval == B && brow >= 0 ? brow : 0x7fffffff, sh);
+  int64_t max_i = -1;
+  int32_t score = 0;
+  if (type == kSW) {
+    if (B > 0 && R != 0x7fffffff) {
+      max_i = R;
+      score = B;
+    }
+  } else if (type == kOV) {
+    // _mmxxx_max_value starts from 0: a sink row never scores below 0, and
+    // when no sink row is positive the first sink row wins with score 0
+    if (B > 0) {
+      max_i = R;
+      score = B;
+    } else {
+      max_i = first_sink;
+      score = 0;
+    }
+  } else {
+    if (R != 0x7fffffff && B > NEGW) {
+      max_i = R;
+      score = B;
+    }
+  }
+  int64_t max_j = -1;
+  if (max_i >= 0) {
+    if (type == kNW) {
+      max_j = (int64_t)L - 1;
+    } else {
+      const uint64_t base = (uint64_t)max_i * ld;
+      int32_t jj = 0x7fffffff;
+      for (int r = 0; r < CPT && jj == 0x7fffffff; ++r) {
+        const uint32_t j = s0 + r;
+        if (j < L && Lx::elem(H, base + colmap<CPT>(j, NT ? NT : blockDim.x)) == score) jj = (int32_t)j;
+      }
+      jj = block_min<NW>(jj, sh);
+      max_j = jj == 0x7fffffff ? -1 : jj;
+    }
+  }
+  *out_max_i = max_i;
+  *out_max_j = max_j;
+  *out_score = score;
+}
+
+// The forward pass of dp_forward over a thread-block cluster of CL CTAs
+// (long 32-bit rows): CTA r of the cluster owns virtual threads
+// r * nt ... r * nt + nt - 1 of the row, and the in-row scans cross the CTAs
+// through one exchange per row (cluster_publish / cluster_fold).  Its own
+// function, apart from dp_forward: the one-CTA forward is the polishing
+// batch's hot loop, and a shared template measurably changed its code.
+template <int SUB, int CPT, typename T, int CL>
+__device__ __noinline__ void dp_forward_cl(const Scoring& S, DpView& D,
+                                           const uint8_t* __restrict__ seq, uint32_t L,
+                                           uint32_t V, int32_t lanes, BlockScratch& sh,
+                                           int64_t* out_max_i, int64_t* out_max_j,
+                                           int32_t* out_score) {
+  static_assert(CL > 1, "one CTA runs dp_forward");
+  constexpr int NT = 0;
+  using Lx = Lanes<T>;
+  using P = typename Lx::P;
+  using L16 = Lanes<int16_t>;
+  constexpr int HP = CPT / 2;
+  static_assert(HP <= 16, "pair masks hold at most 16 pairs per strip");
+  // this thread's index in the cluster's row
   const uint32_t ntc = NT ? NT : blockDim.x;  // threads of the CTA
   const uint32_t ntv = ntc * CL;               // threads of the row
   const uint32_t t = cl_rank<CL>() * ntc + threadIdx.x;
@@ -866,7 +1299,6 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
         }
       }
     };
-    if constexpr (CL == 1) store_fo();
     // Columns past the read are computed like the others and never masked:
     // they only feed columns to their right (the in-row scans run left to
     // right, the diagonal reads column j-1), the row selection below masks
@@ -875,54 +1307,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
     // column s0-1 of this row for the CTA's thread 0: the first column fc
     // in the cluster's first CTA, else the last column of the CTA before
     int32_t lfill = fci;
-    if constexpr (CL == 1) {
-      if (SUB == kLinear) {
-#pragma unroll
-        for (int k = 0; k < HP; ++k) hs[k] = h[k];
-        pair_scan<CPT, Lx, NW>(hs, fci, g, sh);
-        if (type == kSW) {
-          const P z = Lx::splat(0);
-#pragma unroll
-          for (int k = 0; k < HP; ++k) hs[k] = Lx::max(hs[k], z, NZ);
-        }
-      } else {
-        if (SUB == kConvex) {
-          P x[HP];
-#pragma unroll
-          for (int k = 0; k < HP; ++k) x[k] = Lx::add(h[k], q2);
-          // x = Q' (Q of the next column); Q[s0] = Q'[s0-1] is the carry
-          const int32_t qin = pair_scan<CPT, Lx, NW>(x, fci + q, c, sh);
-          qq[0] = Lx::make(qin, Lx::lo(x[HP - 1]));
-#pragma unroll
-          for (int k = 1; k < HP; ++k) qq[k] = x[k - 1];
-        }
-        {
-          P x[HP];
-#pragma unroll
-          for (int k = 0; k < HP; ++k) {
-            if (SUB == kConvex) {
-              // max(H1, Q at vector starts) + g: bits k and 16 + k of bmap
-              // moved to bits 15 and 31 give the pair's lane masks
-              const uint32_t bm = sign_lanes(bmap << (15 - k));
-              x[k] = Lx::add(Lx::max(h[k], Lx::select(bm, qq[k], NEG2), NZ), g2);
-            } else {
-              x[k] = Lx::add(h[k], g2);
-            }
-          }
-          const int32_t ein = pair_scan<CPT, Lx, NW>(x, fci + g, e, sh);  // x = E'
-          ee[0] = Lx::make(ein, Lx::lo(x[HP - 1]));
-#pragma unroll
-          for (int k = 1; k < HP; ++k) ee[k] = x[k - 1];
-        }
-#pragma unroll
-        for (int k = 0; k < HP; ++k) {
-          if (SUB == kConvex)
-            hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], qq[k]) : Lx::max3(h[k], ee[k], qq[k]);
-          else
-            hs[k] = type == kSW ? Lx::max3_relu(h[k], ee[k], ee[k]) : Lx::max(h[k], ee[k], NZ);
-        }
-      }
-    } else {
+    {
       // A cluster row: CTA r owns columns r*W ... r*W + W - 1.  Every in-row
       // scan runs CTA-local, from the row's initial values in CTA 0 and from
       // -infinity in the others; one exchange then gives each CTA the values
@@ -938,7 +1323,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
       if (SUB == kConvex) {
 #pragma unroll
         for (int k = 0; k < HP; ++k) xq[k] = Lx::add(h[k], q2);
-        qin = pair_scan<CPT, Lx, NW>(xq, rank == 0 ? fci + q : kNegBig, c, sh);
+        qin = pair_scan<CPT, Lx, NW>(xq, rank == 0 ? fci + q : kNegBig, c, sh.wq);
         qq[0] = Lx::make(qin, Lx::lo(xq[HP - 1]));
 #pragma unroll
         for (int k = 1; k < HP; ++k) qq[k] = xq[k - 1];
@@ -956,7 +1341,7 @@ __device__ __noinline__ void dp_forward(const Scoring& S, DpView& D, const uint8
       }
       const int32_t pen = SUB == kLinear ? g : e;
       sc_in = pair_scan<CPT, Lx, NW>(xs, rank == 0 ? (SUB == kLinear ? fci : fci + g) : kNegBig,
-                                   pen, sh);
+                                     pen, sh.wv);
       cluster_publish<CL>(Lx::hi(xs[HP - 1]), Lx::hi(xs[HP - 2]), Lx::hi(h[HP - 1]),
                           SUB == kConvex ? Lx::hi(xq[HP - 1]) : kNegBig,
                           SUB == kConvex ? Lx::hi(xq[HP - 2]) : kNegBig, i, sh);
@@ -1293,7 +1678,7 @@ __device__ __noinline__ void dp_forward_seg(const Scoring& S, DpView& D,
       if (SUB == kLinear) {
 #pragma unroll
         for (int k = 0; k < HP; ++k) hs[k] = h[k];
-        pair_scan<CPT, Lx>(hs, sg == 0 ? fci : carry_h, g, sh);
+        pair_scan<CPT, Lx>(hs, sg == 0 ? fci : carry_h, g, sh.wv);
         out_h = Lx::hi(hs[HP - 1]);
         if (type == kSW) {
           const P z = Lx::splat(0);
@@ -1305,7 +1690,7 @@ __device__ __noinline__ void dp_forward_seg(const Scoring& S, DpView& D,
           P x[HP];
 #pragma unroll
           for (int k = 0; k < HP; ++k) x[k] = Lx::add(h[k], q2);
-          const int32_t qin = pair_scan<CPT, Lx>(x, sg == 0 ? fci + q : carry_q, c, sh);
+          const int32_t qin = pair_scan<CPT, Lx>(x, sg == 0 ? fci + q : carry_q, c, sh.wq);
           out_q = Lx::hi(x[HP - 1]);
           qq[0] = Lx::make(qin, Lx::lo(x[HP - 1]));
 #pragma unroll
@@ -1330,7 +1715,7 @@ __device__ __noinline__ void dp_forward_seg(const Scoring& S, DpView& D,
               x[k] = Lx::add(h[k], g2);
             }
           }
-          const int32_t ein = pair_scan<CPT, Lx>(x, sg == 0 ? fci + g : carry_e, e, sh);
+          const int32_t ein = pair_scan<CPT, Lx>(x, sg == 0 ? fci + g : carry_e, e, sh.wv);
           out_e = Lx::hi(x[HP - 1]);
           ee[0] = Lx::make(ein, Lx::lo(x[HP - 1]));
 #pragma unroll

@@ -185,7 +185,7 @@ __device__ int32_t window_read_cl(const Scoring& S, GraphView& G, DpView& D, Blo
                    uint32_t* np) {
     int64_t mi, mj;
     int32_t sc;
-    dp_forward<SUB, CPT, T, 0, CL>(S, D, sq, L, V, lanes, sh, &mi, &mj, &sc);
+    dp_forward_cl<SUB, CPT, T, CL>(S, D, sq, L, V, lanes, sh, &mi, &mj, &sc);
     if (lead && threadIdx.x == 0) {
       *np = 0;
       *has = 0;
