@@ -59,10 +59,12 @@ struct BlockScratch {
 // thread-block clusters: one long window's row spread over CL CTAs
 // ---------------------------------------------------------------------------
 // CTA r of a cluster of CL owns virtual threads r * nt ... r * nt + nt - 1
-// of the row.  Scan carries, the left neighbour's column and the final
-// reductions cross CTAs through distributed shared memory, each exchange
-// behind one cluster barrier (every CTA of the cluster runs the same
-// sequence of barriers: the control flow is uniform over the cluster).
+// of the row.  What a row carries across CTAs (its scans' tails and the
+// left column) crosses in one exchange per row (cluster_publish /
+// cluster_fold), the final reductions in one exchange each, all through
+// distributed shared memory behind a cluster barrier; every CTA of the
+// cluster runs the same sequence of barriers (the control flow is uniform
+// over the cluster).
 template <int CL>
 __device__ __forceinline__ uint32_t cl_rank() {
   if constexpr (CL == 1) {
@@ -129,8 +131,9 @@ __device__ __forceinline__ int32_t cl_peek(const int32_t* local, uint32_t rank) 
   return v;
 #elif defined(SPOA_GB300_SIMT_HOST)
   return *simt::peer(local, rank);
-#else
-  return local[0] + 0 * (int32_t)rank;
+#else  // the host pass of nvcc, which never runs device code
+  (void)rank;
+  return *local;
 #endif
 }
 
