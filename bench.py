@@ -84,8 +84,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--windows-per-cta", type=int, default=1, choices=[1, 2, 4],
                     help="windows in flight per CTA (16-bit windows)")
-    ap.add_argument("--cluster", type=int, default=0, choices=[0, 1],
-                    help="0: long 32-bit rows on thread-block clusters; 1: one CTA per window")
+    ap.add_argument("--cluster", type=int, default=0, choices=[0, 1, 2, 4, 8],
+                    help="0: long 32-bit rows on thread-block clusters; 1: one CTA per "
+                         "window; 2, 4, 8: CTAs per cluster")
     ap.add_argument("--parity-windows", type=int, default=256,
                     help="windows rerun with alignments and checked against the oracle")
     ap.add_argument("--no-resident", action="store_true",

@@ -220,7 +220,10 @@ typedef struct {
   int32_t cluster;                 /* 0: windows of 32-bit scores whose rows pass
                                       1,536 columns run on thread-block clusters
                                       (2, 4 or 8 CTAs per window, each a column
-                                      range of every row); 1: never */
+                                      range of every row; more CTAs per window
+                                      when few windows share the pass); 1:
+                                      never; 2, 4 or 8: that many CTAs per such
+                                      window (more when its rows need them) */
   int32_t device_set;              /* nonzero: the batch lives on `device`;
                                       0: on the calling thread's current device
                                       at batch_create.  Every later call on the

@@ -178,13 +178,24 @@ bool seg_tile(uint32_t L, int* cpt, int* nt, int* segs) {
   return false;
 }
 
-// Cluster tile for 32-bit rows wider than kClusterMinCols: 2, 4 or 8 CTAs
-// per window (more CTAs from 2 x 128 x 12 and 4 x 128 x 12 columns), 12
-// columns per thread, the fewest 32-thread multiples per CTA that cover L.
-// False when L is not in the clusters' range (up to 8 x 512 x 12 columns).
-bool cluster_tile(uint32_t L, int* cl, int* nt) {
+// Cluster tile for `windows` windows of 32-bit rows of up to L columns
+// (wider than kClusterMinCols): 2, 4 or 8 CTAs per window, 12 columns per
+// thread, the fewest 32-thread multiples per CTA that cover L.  The
+// smallest cluster that holds the row, doubled while the windows' clusters
+// still fit one CTA per SM: a lone window runs fastest on the most SMs (the
+// 10-kb window: 3.23 s on 8 CTAs, 3.56 s on 4, 4.42 s on 2), a batch of
+// many on the fewest per window (2,000 uneven windows: 111.8 windows/s on
+// 2 CTAs, 93.3 on 4).  `force` (2, 4 or 8) asks for that many CTAs, or
+// more when the row needs them.  False when L is not in the clusters' range
+// (up to 8 x 512 x 12 columns).
+bool cluster_tile(uint32_t L, uint64_t windows, int sm_count, int force, int* cl, int* nt) {
   if (L <= kClusterMinCols || L > (uint32_t)kClCpt * 8 * 512) return false;
-  const int c = L > 4u * 128 * kClCpt ? 8 : L > 2u * 128 * kClCpt ? 4 : 2;
+  int c = L > 4u * 512 * kClCpt ? 8 : L > 2u * 512 * kClCpt ? 4 : 2;
+  if (force == 2 || force == 4 || force == 8)
+    c = std::max(c, force);
+  else
+    while (c < 8 && std::max<uint64_t>(windows, 1) * (uint64_t)(2 * c) <= (uint64_t)sm_count)
+      c *= 2;
   const uint64_t per = (uint64_t)c * kClCpt;
   *cl = c;
   *nt = (int)std::max<uint64_t>(32, ((L + per - 1) / per + 31) / 32 * 32);
@@ -1182,7 +1193,8 @@ int32_t plan_pass(spoa_gb300_batch* b, Pass* p, const std::vector<WindowPlan>& w
   }
   int cpt = d.columns_per_thread, nt = d.threads_per_window, segs = 1, cl = 1;
   const bool forced = cpt > 0 && nt > 0;
-  if (p->wide && !forced && d.cluster != 1 && cluster_tile(L, &cl, &nt)) {
+  if (p->wide && !forced && d.cluster != 1 &&
+      cluster_tile(L, p->windows.size(), b->sm_count, d.cluster, &cl, &nt)) {
     cpt = kClCpt;  // a thread-block cluster per window
   } else if (p->tuned_cpt > 0 && (uint64_t)p->tuned_cpt * p->tuned_nt >= L) {
     cpt = p->tuned_cpt;
@@ -2366,7 +2378,7 @@ bool admit(spoa_gb300_server* sv, ServedLaunch& L) {
     // past their range the segmented forward
     int cpt = 0, nt = 0, segs = 1, cl = 1;
     bool tiled;
-    if (wide && cluster_tile(lmax, &cl, &nt)) {
+    if (wide && cluster_tile(lmax, k, sv->sm_count, 0, &cl, &nt)) {
       cpt = kClCpt;
       tiled = true;
     } else {

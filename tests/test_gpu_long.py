@@ -72,16 +72,16 @@ def test_segmented_rows_vs_oracle(gap):
 def test_cluster_rows_vs_oracle(gap):
     """Rows of 2-2.4k and 4.2-4.8k columns on the int32 width: clusters of
     2 and 4 CTAs split each row; NW, SW and OV, both strands, two windows
-    per batch (two clusters side by side), every score, strand choice and
-    alignment and the consensus."""
+    per batch, every score, strand choice and alignment and the consensus.
+    (Single windows take 8-CTA clusters in the other tests here.)"""
     params = GAPS[gap]
     ws = [synth.long_10k(21, n_reads=3, tpl_len=2400, min_len=2000),
           synth.long_10k(22, n_reads=3, tpl_len=4800, min_len=4200)]
     reads = [[synth.revcomp(r) if j == 1 else r for j, r in enumerate(w.reads)] for w in ws]
-    for typ in (0, 1, 2):
+    for typ, cl in ((0, 2), (1, 4), (2, 2), (2, 4)):
         strand = typ != 0
         res = sg.batch_poa(reads, typ, *params, want_alignments=True,
-                           window_strand=[strand] * 2)
+                           window_strand=[strand] * 2, cluster=cl)
         assert (res.status == 0).all()
         r0 = 0
         for k, rs in enumerate(reads):
