@@ -1317,7 +1317,7 @@ __device__ __noinline__ void dp_forward_cl(const Scoring& S, DpView& D,
       // carried into its range (cluster_fold).  The scans are max-plus
       // linear, so a carry X of a scan with penalty pen adds
       // X + (u + 1) * pen at column u of the range, and for convex gaps the
-      // Q carry also reaches E' through the vector starts (mq).
+      // Q carry also reaches E' through the vector starts (mq_path).
       const uint32_t rank = cl_rank<CL>();
       const int32_t u0 = (int32_t)(threadIdx.x * CPT);  // first column in the range
       // linear: H'; affine, convex: E' (and Q' in xq)

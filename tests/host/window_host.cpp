@@ -162,6 +162,12 @@ extern "C" int32_t wh_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t
 #undef RUN
 }
 
+// mq_path of the cluster forward (the best path of a Q' carry into E'),
+// for a unit test against the brute-force maximum.
+extern "C" int32_t wh_mq_path(int32_t u, int32_t c, int32_t e, int32_t lanes) {
+  return mq_path(u, c, e, lanes);
+}
+
 // The cluster form (window_read_cl): cl CTAs of nt threads, 12 columns per
 // thread, 32-bit lanes.
 extern "C" int32_t wh_run_cl(int32_t type, int32_t m, int32_t n, int32_t g, int32_t e, int32_t q,

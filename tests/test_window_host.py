@@ -184,3 +184,19 @@ def test_cluster_rows(wh):
         for a, b in zip(alns, ref.alignments):
             assert np.array_equal(a, b), (params, typ, cl)
         assert cons == ref.consensus, (params, typ, cl)
+
+
+def test_mq_path_is_the_best_vector_start(wh):
+    """The closed form the cluster forward uses for a Q' carry entering E':
+    max over vector starts u' <= u ((u' + 1) % lanes == 0) of
+    u' * c + (u - u') * e, -infinity before the first vector start."""
+    wh.wh_mq_path.restype = C.c_int32
+    wh.wh_mq_path.argtypes = [C.c_int32] * 4
+    neg = -(1 << 28)
+    rng = np.random.default_rng(5)
+    for lanes in (8, 16):
+        for c, e in [(-4, -6), (-6, -4), (-5, -5), (-1, -10), (-10, -1), (0, -3)]:
+            for u in list(range(0, 70)) + list(rng.integers(0, 6144, 40)):
+                starts = [v for v in range(0, u + 1) if (v + 1) % lanes == 0]
+                want = max(v * c + (u - v) * e for v in starts) if starts else neg
+                assert wh.wh_mq_path(int(u), c, e, lanes) == want, (u, c, e, lanes)
