@@ -164,19 +164,21 @@ def run_host_cl(L, type_, params, reads, quals, strand, cl, nt):
 
 def test_cluster_rows(wh):
     """The cluster form of a window (window_read_cl: each row spread over 2
-    or 4 emulated CTAs, the scan carries, the left neighbour's column and
-    the final reductions crossing CTAs through their shared state behind
-    cluster barriers; the serial phases on the lead CTA) against the oracle
-    for every alignment type and gap model, both strands, 32-bit lanes."""
+    or 4 emulated CTAs of one or two warps, one exchange of scan tails per
+    row and the final reductions crossing CTAs through their shared state
+    behind cluster barriers; the serial phases on the lead CTA) against the
+    oracle for every alignment type and gap model, both strands, 32-bit
+    lanes."""
     from spoa_gb300 import synth
-    w = synth.long_10k(12, n_reads=3, tpl_len=560, min_len=500)
+    w = synth.long_10k(12, n_reads=3, tpl_len=420, min_len=380)
     reads = list(w.reads)
     lin, aff, cvx = (5, -4, -8, -8, -8, -8), (5, -4, -8, -6, -8, -6), (5, -4, -8, -6, -10, -4)
-    cases = ((lin, 0, 2, False), (aff, 1, 4, True), (cvx, 2, 2, False), (cvx, 0, 4, True))
-    for params, typ, cl, strand in cases:
+    cases = ((lin, 0, 2, False, 32), (aff, 1, 4, True, 32), (cvx, 2, 2, False, 32),
+             (cvx, 0, 4, True, 32), (cvx, 1, 2, True, 64))
+    for params, typ, cl, strand, nt in cases:
         rs = reads if not strand else [synth.revcomp(r) if j % 2 else r
                                       for j, r in enumerate(reads)]
-        st, scores, rev, alns, cons = run_host_cl(wh, typ, params, rs, None, strand, cl, 32)
+        st, scores, rev, alns, cons = run_host_cl(wh, typ, params, rs, None, strand, cl, nt)
         assert st == 0, (params, typ, cl, st)
         ref = po.run_window(typ, *params, rs, strand_ambiguous=strand, with_msa=False)
         assert scores == ref.scores, (params, typ, cl)
