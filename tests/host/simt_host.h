@@ -1,29 +1,30 @@
 // simt_host.h - runs CUDA device code of this repository on the host, for
 // the CPU test suite.  TEST INFRASTRUCTURE ONLY.
 //
-// One CTA of `nt` threads is `nt` std::threads.  threadIdx is thread-local,
-// __syncthreads is a barrier of the CTA, a warp shuffle is an exchange
-// through a per-warp slot array between two barriers of the warp (every
-// shuffle of this code is executed by full warps), and __shared__ data is
-// the caller's.  The SIMD integer intrinsics the DP uses are written here
-// from their documented per-lane meaning: 16-bit lanes add with wrap-around,
-// maxima compare lanes as signed values.
+// One CTA of `nt` threads is `nt` fibers (ucontext) on the calling OS
+// thread.  A fiber runs until it waits at a barrier; threadIdx is set for
+// the fiber that runs.  __syncthreads is a barrier of the CTA, a warp
+// shuffle is an exchange through a per-warp slot array between two barriers
+// of the warp (every shuffle of this code is executed by full warps), and
+// __shared__ data is the caller's.  A barrier that can never complete
+// aborts the launch with the place each thread waits.  The SIMD integer
+// intrinsics the DP uses are written here from their documented per-lane
+// meaning: 16-bit lanes add with wrap-around, maxima compare lanes as
+// signed values.
 #pragma once
+
+#include <sys/mman.h>
+#include <ucontext.h>
 
 #include <algorithm>
 #include <atomic>
-#include <barrier>
 #include <cstdint>
-#include <cstring>
-#include <functional>
-#include <memory>
-#include <optional>
-#include <thread>
-#include <vector>
-#ifdef SIMT_TRACE
-#include <atomic>
 #include <cstdio>
-#endif
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <functional>
+#include <vector>
 
 #define SPOA_GB300_SIMT_HOST 1
 #define __host__
@@ -54,15 +55,38 @@ struct HostDim {
 
 namespace simt {
 
+// An emulated thread: a fiber with its own stack on the calling OS thread.
+struct Fiber {
+  ucontext_t ctx;
+  unsigned t = 0, r = 0;  // threadIdx.x and CTA rank
+  bool done = false;
+  bool has_token = false;  // between cluster_arrive and cluster_wait
+  uint64_t token = 0;      // the cluster barrier's phase at the arrive
+  const char* waits_on = nullptr;  // kind of barrier it is blocked on
+  uint64_t shuffles = 0;           // warp shuffles done (picks the slot array)
+};
+
+// A barrier of `expected` fibers; `phase` counts completed rounds.
+struct Barrier {
+  unsigned expected = 0, arrived = 0;
+  uint64_t phase = 0;
+  std::vector<unsigned> waiting;  // fibers blocked on the current phase
+};
+
 // One CTA, or a cluster of `ncta` CTAs of `nt` threads each (the threads of
-// CTA r are ranks r * nt ... r * nt + nt - 1 of the launch).
+// CTA r are fibers r * nt ... r * nt + nt - 1 of the launch).
 struct Cta {
   unsigned nt = 1, ncta = 1;
-  std::vector<std::unique_ptr<std::barrier<>>> cta_bar;  // per CTA
-  std::unique_ptr<std::barrier<>> cluster_bar;           // all threads
-  std::vector<std::unique_ptr<std::barrier<>>> warp;     // per CTA and warp
-  std::vector<int32_t> slots;                            // 32 per warp
-  std::vector<char*> scratch;  // per CTA: its shared-memory stand-in
+  std::vector<Barrier> cta_bar;  // per CTA
+  Barrier cluster_bar;           // all threads
+  std::vector<Barrier> warp;     // per CTA and warp
+  std::vector<int32_t> slots;    // 2 x 32 per warp (alternating shuffles)
+  std::vector<char*> scratch;    // per CTA: its shared-memory stand-in
+  std::vector<Fiber> fib;
+  std::deque<unsigned> runq;  // fibers ready to run, in order
+  unsigned cur = 0;           // the running fiber
+  ucontext_t sched;           // the launching code's context
+  const std::function<void()>* body = nullptr;
 };
 
 inline Cta*& cta() {
@@ -72,33 +96,146 @@ inline Cta*& cta() {
 inline thread_local HostDim tid{0};
 inline thread_local unsigned cta_rank = 0;
 
-// Runs body() on ncta CTAs of nt threads (a cluster when ncta > 1);
-// scratch[r] is CTA r's shared-memory stand-in (for the distributed shared
-// memory of a cluster).  Returns when all threads have finished.
+// Fiber stacks, kept for the process's lifetime and reused by every launch;
+// the lowest page of each is a guard page, so an overflow faults instead of
+// overwriting a neighbour.
+constexpr size_t kStackBytes = 1u << 20;
+inline std::vector<char*>& stack_pool() {
+  static std::vector<char*> pool;
+  return pool;
+}
+inline char* stack_at(size_t k) {
+  auto& pool = stack_pool();
+  while (pool.size() <= k) {
+    void* p = mmap(nullptr, kStackBytes, PROT_READ | PROT_WRITE,
+                   MAP_PRIVATE | MAP_ANONYMOUS | MAP_NORESERVE, -1, 0);
+    if (p == MAP_FAILED) {
+      std::fprintf(stderr, "simt: no memory for a fiber stack\n");
+      std::abort();
+    }
+    mprotect(p, 4096, PROT_NONE);
+    pool.push_back(static_cast<char*>(p));
+  }
+  return pool[k];
+}
+
+inline void fiber_entry() {
+  Cta& c = *cta();
+  (*c.body)();
+  c.fib[c.cur].done = true;  // returns to c.sched through uc_link
+}
+
+// The running fiber waits: the OS thread switches straight to the next
+// ready fiber (or back to the scheduler when none is ready); the fiber
+// resumes once a barrier release has queued it again.
+inline void block(const char* kind) {
+  Cta& c = *cta();
+  const unsigned me = c.cur;
+  c.fib[me].waits_on = kind;
+  if (c.runq.empty()) {
+    swapcontext(&c.fib[me].ctx, &c.sched);
+  } else {
+    const unsigned nx = c.runq.front();
+    c.runq.pop_front();
+    c.cur = nx;
+    c.fib[nx].waits_on = nullptr;
+    tid.x = c.fib[nx].t;
+    cta_rank = c.fib[nx].r;
+    swapcontext(&c.fib[me].ctx, &c.fib[nx].ctx);
+  }
+  // resumed: whoever switched here set c.cur, tid and cta_rank to this fiber
+}
+
+// Arrives at `b`; the last arrival of a phase releases the waiting fibers.
+// Released fibers are queued in arrival order on even phases and in reverse
+// order on odd ones, so that code between two barriers runs in both thread
+// orders over a launch (a missing barrier shows in one of them).
+inline uint64_t arrive(Barrier& b) {
+  Cta& c = *cta();
+  const uint64_t ph = b.phase;
+  if (++b.arrived == b.expected) {
+    b.arrived = 0;
+    ++b.phase;
+    if (ph & 1)
+      c.runq.insert(c.runq.end(), b.waiting.rbegin(), b.waiting.rend());
+    else
+      c.runq.insert(c.runq.end(), b.waiting.begin(), b.waiting.end());
+    b.waiting.clear();
+  }
+  return ph;
+}
+
+inline void wait(Barrier& b, uint64_t ph, const char* kind) {
+  Cta& c = *cta();
+  while (b.phase == ph) {
+    b.waiting.push_back(c.cur);
+    block(kind);
+  }
+}
+
+inline void arrive_and_wait(Barrier& b, const char* kind) { wait(b, arrive(b), kind); }
+
+// Runs body() on ncta CTAs of nt threads (a cluster when ncta > 1) as
+// fibers on the calling OS thread, each running until it waits at a barrier
+// (no preemption between barriers); scratch[r] is CTA r's shared-memory
+// stand-in (for the distributed shared memory of a cluster).  Returns when
+// all threads have finished.  If every unfinished thread waits at a barrier
+// that can no longer complete (a barrier one path of the code skips), the
+// launch reports where each thread waits and aborts the process instead of
+// hanging.
 inline void launch_cluster(unsigned ncta, unsigned nt, const std::vector<char*>& scratch,
                            const std::function<void()>& body) {
   Cta c;
   c.nt = nt;
   c.ncta = ncta;
   c.scratch = scratch;
-  for (unsigned r = 0; r < ncta; ++r) c.cta_bar.push_back(std::make_unique<std::barrier<>>(nt));
-  c.cluster_bar = std::make_unique<std::barrier<>>(nt * ncta);
+  c.body = &body;
+  c.cta_bar.resize(ncta);
+  for (auto& b : c.cta_bar) b.expected = nt;
+  c.cluster_bar.expected = nt * ncta;
   const unsigned nw = (nt + 31) / 32;
+  c.warp.resize(ncta * nw);
   for (unsigned r = 0; r < ncta; ++r)
-    for (unsigned w = 0; w < nw; ++w)
-      c.warp.push_back(std::make_unique<std::barrier<>>(std::min(32u, nt - 32 * w)));
-  c.slots.assign(32 * nw * ncta, 0);
+    for (unsigned w = 0; w < nw; ++w) c.warp[r * nw + w].expected = std::min(32u, nt - 32 * w);
+  c.slots.assign(2 * 32 * nw * ncta, 0);
+  const unsigned n = ncta * nt;
+  c.fib.resize(n);
+  Cta* outer = cta();
   cta() = &c;
-  std::vector<std::thread> th;
-  for (unsigned r = 0; r < ncta; ++r)
-    for (unsigned t = 0; t < nt; ++t)
-      th.emplace_back([r, t, &body] {
-        tid.x = t;
-        cta_rank = r;
-        body();
-      });
-  for (auto& x : th) x.join();
-  cta() = nullptr;
+  for (unsigned k = 0; k < n; ++k) {
+    Fiber& f = c.fib[k];
+    f.r = k / nt;
+    f.t = k % nt;
+    getcontext(&f.ctx);
+    f.ctx.uc_stack.ss_sp = stack_at(k) + 4096;
+    f.ctx.uc_stack.ss_size = kStackBytes - 4096;
+    f.ctx.uc_link = &c.sched;
+    makecontext(&f.ctx, fiber_entry, 0);
+    c.runq.push_back(k);
+  }
+  const HostDim tid0 = tid;
+  const unsigned rank0 = cta_rank;
+  while (!c.runq.empty()) {
+    c.cur = c.runq.front();
+    c.runq.pop_front();
+    Fiber& f = c.fib[c.cur];
+    f.waits_on = nullptr;
+    tid.x = f.t;
+    cta_rank = f.r;
+    swapcontext(&c.sched, &f.ctx);
+  }
+  for (const Fiber& f : c.fib)
+    if (!f.done) {
+      std::fprintf(stderr, "simt: barrier deadlock (%u CTAs of %u threads):\n", ncta, nt);
+      for (const Fiber& g : c.fib)
+        if (!g.done)
+          std::fprintf(stderr, "  CTA %u thread %u waits at a %s barrier\n", g.r, g.t,
+                       g.waits_on ? g.waits_on : "?");
+      std::abort();
+    }
+  tid = tid0;
+  cta_rank = rank0;
+  cta() = outer;
 }
 
 // Runs body() on nt threads as one CTA; returns when all have finished.
@@ -106,30 +243,38 @@ inline void launch(unsigned nt, const std::function<void()>& body) {
   launch_cluster(1, nt, {}, body);
 }
 
+// A warp shuffle: every lane writes its value, waits for the warp, reads
+// the source lane's.  Two slot arrays alternate between shuffles, so one
+// warp barrier suffices: a lane can write the array again only after the
+// next shuffle's barrier, which every lane reaches after its read.
 inline int32_t exchange(int32_t v, unsigned src_lane) {
   Cta& c = *cta();
+  const unsigned nw = c.ncta * ((c.nt + 31) / 32);
   const unsigned w = cta_rank * ((c.nt + 31) / 32) + tid.x / 32, lane = tid.x % 32;
-  c.slots[32 * w + lane] = v;
-  c.warp[w]->arrive_and_wait();
-  const int32_t r = c.slots[32 * w + src_lane];
-  c.warp[w]->arrive_and_wait();
-  return r;
+  Fiber& f = c.fib[c.cur];
+  int32_t* slots = c.slots.data() + 32 * (w + nw * (f.shuffles++ & 1));
+  slots[lane] = v;
+  arrive_and_wait(c.warp[w], "warp");
+  return slots[src_lane];
 }
 
 inline void cluster_sync() {
-  if (cta()) cta()->cluster_bar->arrive_and_wait();
+  if (cta()) arrive_and_wait(cta()->cluster_bar, "cluster");
 }
 
 // The split form: arrive, then (after other work) wait for the others.
-inline thread_local std::optional<std::barrier<>::arrival_token> cluster_token;
 inline void cluster_arrive() {
-  if (cta()) cluster_token.emplace(cta()->cluster_bar->arrive());
+  if (!cta()) return;
+  Fiber& f = cta()->fib[cta()->cur];
+  f.token = arrive(cta()->cluster_bar);
+  f.has_token = true;
 }
 inline void cluster_wait() {
-  if (cta() && cluster_token) {
-    cta()->cluster_bar->wait(std::move(*cluster_token));
-    cluster_token.reset();
-  }
+  if (!cta()) return;
+  Fiber& f = cta()->fib[cta()->cur];
+  if (!f.has_token) return;
+  f.has_token = false;
+  wait(cta()->cluster_bar, f.token, "cluster");
 }
 
 // The copy of a shared variable of this CTA in CTA `rank` of the cluster.
@@ -155,7 +300,7 @@ static inline void __syncthreads() {
   static std::atomic<long> n{0};
   if (threadIdx.x == 0) fprintf(stderr, "sync %ld\n", n++);
 #endif
-  if (simt::cta()) simt::cta()->cta_bar[simt::cta_rank]->arrive_and_wait();
+  if (simt::cta()) simt::arrive_and_wait(simt::cta()->cta_bar[simt::cta_rank], "CTA");
 }
 
 template <typename T>
@@ -201,7 +346,7 @@ static inline int __ffs(unsigned x) { return x ? __builtin_ctz(x) + 1 : 0; }
 static inline void __syncwarp(unsigned = 0xffffffffu) {
   if (simt::cta()) {
     simt::Cta& c = *simt::cta();
-    c.warp[simt::cta_rank * ((c.nt + 31) / 32) + threadIdx.x / 32]->arrive_and_wait();
+    simt::arrive_and_wait(c.warp[simt::cta_rank * ((c.nt + 31) / 32) + threadIdx.x / 32], "warp");
   }
 }
 

@@ -1,0 +1,71 @@
+// simt_selftest.cpp - checks of the SIMT emulation itself (simt_host.h).
+// TEST INFRASTRUCTURE ONLY: tests/test_window_host.py runs it.
+//   simt_selftest ok    - shuffles, CTA and split cluster barriers give the
+//                         values a GPU gives; exits 0
+//   simt_selftest skip  - one thread leaves before a __syncthreads that the
+//                         others wait at; the emulation must abort with a
+//                         barrier-deadlock report instead of hanging
+#include "simt_host.h"
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+int main(int argc, char** argv) {
+  const bool skip = argc > 1 && std::strcmp(argv[1], "skip") == 0;
+  if (skip) {
+    simt::launch(64, [] {
+      __syncthreads();
+      if (threadIdx.x == 37) return;
+      __syncthreads();
+    });
+    std::printf("no deadlock reported\n");
+    return 0;
+  }
+  // warp inclusive prefix sum by shuffles, then a CTA-wide exchange
+  std::vector<int> out(128), sh(128);
+  simt::launch(128, [&] {
+    int v = (int)threadIdx.x + 1;
+    for (unsigned d = 1; d < 32; d *= 2) {
+      const int u = __shfl_up_sync(0xffffffffu, v, d);
+      if (threadIdx.x % 32 >= d) v += u;
+    }
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    out[threadIdx.x] = sh[127 - threadIdx.x];
+  });
+  for (unsigned t = 0; t < 128; ++t) {
+    const unsigned src = 127 - t, w0 = src / 32 * 32;
+    int want = 0;
+    for (unsigned k = w0; k <= src; ++k) want += (int)k + 1;
+    if (out[t] != want) {
+      std::printf("prefix sum: thread %u has %d, want %d\n", t, out[t], want);
+      return 1;
+    }
+  }
+  // a cluster of 4 CTAs: each publishes a value, arrives, does other work,
+  // waits, then reads every peer's value through the distributed view
+  struct Shared {
+    int v;
+  };
+  std::vector<Shared> cs(4);
+  std::vector<char*> scratch;
+  for (auto& c : cs) scratch.push_back(reinterpret_cast<char*>(&c));
+  std::vector<int> sums(4 * 32);
+  simt::launch_cluster(4, 32, scratch, [&] {
+    Shared& me = cs[simt::cta_rank];
+    if (threadIdx.x == 0) me.v = 10 * ((int)simt::cta_rank + 1);
+    simt::cluster_arrive();
+    simt::cluster_wait();
+    int s = 0;
+    for (unsigned r = 0; r < 4; ++r) s += simt::peer(&me, r)->v;
+    sums[simt::cta_rank * 32 + threadIdx.x] = s;
+  });
+  for (int s : sums)
+    if (s != 100) {
+      std::printf("cluster exchange: %d, want 100\n", s);
+      return 1;
+    }
+  std::printf("ok\n");
+  return 0;
+}

@@ -194,6 +194,7 @@ extern "C" int32_t wh_run_cl(int32_t type, int32_t m, int32_t n, int32_t g, int3
     default: RUNC(kConvex, CLV);         \
   }
   if (cl == 2) BY_SUBC(2)
+  if (cl == 8) BY_SUBC(8)
   BY_SUBC(4)
 #undef BY_SUBC
 #undef RUNC

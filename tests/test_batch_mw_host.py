@@ -84,6 +84,25 @@ def test_windows_per_cta_match_the_oracle(mw, W, strand, with_quals):
         r0 += n
 
 
+@pytest.mark.parametrize("W,type_,params", [(2, 1, (5, -4, -8, -6, -8, -6)),
+                                             (4, 0, (5, -4, -8, -8, -8, -8)),
+                                             (4, 1, (5, -4, -8, -6, -10, -4))])
+def test_other_alignment_types_and_gap_models(mw, W, type_, params):
+    """NW affine, SW linear and NW convex windows of the polishing shape
+    (450-550 bases) on W slots, both strands, against the oracle."""
+    windows = [synth.batch_window(880 + k).reads[:5] for k in range(W + 1)]
+    status, scores, rev, cons = run_mw(mw, windows, type_, params, W, True)
+    assert status == [0] * len(windows)
+    r0 = 0
+    for w, win in enumerate(windows):
+        ref = po.run_window(type_, *params, win, strand_ambiguous=True, with_msa=False)
+        n = len(win)
+        assert scores[r0:r0 + n] == ref.scores, (W, type_, w)
+        assert rev[r0:r0 + n] == [int(x) for x in ref.reversed], (W, type_, w)
+        assert cons[w] == ref.consensus, (W, type_, w)
+        r0 += n
+
+
 def test_fewer_windows_than_slots(mw):
     """One window on a CTA of four slots: the empty slots stay idle."""
     rng = np.random.default_rng(5)

@@ -84,17 +84,18 @@ def _check_window(L, rec, cpt=8, wide=False):
 
 
 def test_window_device_code_matches_the_oracle(wh, ref_windows):
-    """Recorded windows of every shape the fixture holds (adversarial
-    lengths, N bases, qualities, both strands, long insertions) through the
-    emulated CTA; reads up to 256 columns take one warp, longer ones two."""
-    nts, strands = set(), 0
-    for i, rec in enumerate(ref_windows):
+    """Every recorded window of up to 12 reads of up to 512 bases (200 of
+    the fixture's 209: adversarial lengths, N bases, qualities, both
+    strands, long insertions) through the emulated CTA; reads up to 256
+    columns take one warp, longer ones two."""
+    nts, strands, done = set(), 0, 0
+    for rec in ref_windows:
         if max(len(r) for r in rec["reads"]) > 512 or len(rec["reads"]) > 12:
             continue
-        if i % 14 == 0 or (rec["strand_ambiguous"] and i % 12 == 1):
-            nts.add(_check_window(wh, rec))
-            strands += rec["strand_ambiguous"]
-    assert nts >= {32} and strands >= 4
+        nts.add(_check_window(wh, rec))
+        strands += rec["strand_ambiguous"]
+        done += 1
+    assert done == 200 and nts == {32, 64} and strands >= 40
 
 
 def test_two_warp_ctas_and_int32_rows(wh):
@@ -131,16 +132,16 @@ def test_segmented_rows(wh):
 def test_one_warp_build_of_the_forward(wh, ref_windows):
     """The forward pass built for exactly 32 threads (row offsets fixed at
     compile time, scans without the cross-warp path), as the batched kernel
-    runs every polishing-sized window, on recorded windows of up to 512
-    columns (16 columns per thread), both strands included."""
+    runs every polishing-sized window, on every recorded window of up to 12
+    reads of up to 512 columns (16 columns per thread), both strands
+    included."""
     done = 0
-    for i, rec in enumerate(ref_windows):
+    for rec in ref_windows:
         if max(len(r) for r in rec["reads"]) > 512 or len(rec["reads"]) > 12:
             continue
-        if i % 9 == 0 or (rec["strand_ambiguous"] and i % 10 == 3):
-            assert _check_window(wh, rec, cpt=16) == 32
-            done += 1
-    assert done >= 8
+        assert _check_window(wh, rec, cpt=16) == 32
+        done += 1
+    assert done == 200
 
 
 def run_host_cl(L, type_, params, reads, quals, strand, cl, nt):
@@ -163,29 +164,38 @@ def run_host_cl(L, type_, params, reads, quals, strand, cl, nt):
 
 
 def test_cluster_rows(wh):
-    """The cluster form of a window (window_read_cl: each row spread over 2
-    or 4 emulated CTAs of one or two warps, one exchange of scan tails per
+    """The cluster form of a window (window_read_cl: each row spread over 2,
+    4 or 8 emulated CTAs of one or two warps, one exchange of scan tails per
     row and the final reductions crossing CTAs through their shared state
     behind cluster barriers; the serial phases on the lead CTA) against the
-    oracle for every alignment type and gap model, both strands, 32-bit
-    lanes."""
+    oracle for every alignment type and gap model, both strands, quality
+    weights, 32-bit lanes.  The 8-CTA cases leave the last CTAs columns
+    beyond the reads (a row narrower than the cluster)."""
     from spoa_gb300 import synth
-    w = synth.long_10k(12, n_reads=3, tpl_len=420, min_len=380)
-    reads = list(w.reads)
+    short = list(synth.long_10k(12, n_reads=3, tpl_len=420, min_len=380).reads)
+    long_ = list(synth.long_10k(13, n_reads=3, tpl_len=860, min_len=800).reads)
+    rng = np.random.Generator(np.random.PCG64(12))
     lin, aff, cvx = (5, -4, -8, -8, -8, -8), (5, -4, -8, -6, -8, -6), (5, -4, -8, -6, -10, -4)
-    cases = ((lin, 0, 2, False, 32), (aff, 1, 4, True, 32), (cvx, 2, 2, False, 32),
-             (cvx, 0, 4, True, 32), (cvx, 1, 2, True, 64))
-    for params, typ, cl, strand, nt in cases:
+    # (scoring, type, CTAs, strand-ambiguous, threads per CTA, qualities, reads):
+    # a cluster holds 12 columns per thread, so 2 x 32 threads take 768
+    cases = ((lin, 0, 2, False, 32, False, short), (aff, 1, 4, True, 32, False, long_),
+             (cvx, 2, 2, False, 32, True, short), (cvx, 0, 4, True, 32, False, short),
+             (cvx, 1, 2, True, 64, True, long_), (cvx, 2, 8, True, 32, False, short),
+             (aff, 0, 8, False, 32, True, long_))
+    for params, typ, cl, strand, nt, with_q, reads in cases:
         rs = reads if not strand else [synth.revcomp(r) if j % 2 else r
                                       for j, r in enumerate(reads)]
-        st, scores, rev, alns, cons = run_host_cl(wh, typ, params, rs, None, strand, cl, nt)
-        assert st == 0, (params, typ, cl, st)
-        ref = po.run_window(typ, *params, rs, strand_ambiguous=strand, with_msa=False)
-        assert scores == ref.scores, (params, typ, cl)
-        assert rev == [int(x) for x in ref.reversed], (params, typ, cl)
+        qs = ([bytes((rng.integers(0, 41, size=len(r)) + 33).astype(np.uint8)) for r in rs]
+              if with_q else None)
+        st, scores, rev, alns, cons = run_host_cl(wh, typ, params, rs, qs, strand, cl, nt)
+        case = (params, typ, cl, strand, nt, with_q, len(reads))
+        assert st == 0, (case, st)
+        ref = po.run_window(typ, *params, rs, qs, strand_ambiguous=strand, with_msa=False)
+        assert scores == ref.scores, case
+        assert rev == [int(x) for x in ref.reversed], case
         for a, b in zip(alns, ref.alignments):
-            assert np.array_equal(a, b), (params, typ, cl)
-        assert cons == ref.consensus, (params, typ, cl)
+            assert np.array_equal(a, b), case
+        assert cons == ref.consensus, case
 
 
 def test_mq_path_is_the_best_vector_start(wh):
@@ -202,3 +212,22 @@ def test_mq_path_is_the_best_vector_start(wh):
                 starts = [v for v in range(0, u + 1) if (v + 1) % lanes == 0]
                 want = max(v * c + (u - v) * e for v in starts) if starts else neg
                 assert wh.wh_mq_path(int(u), c, e, lanes) == want, (u, c, e, lanes)
+
+
+def test_emulation_reports_a_skipped_barrier():
+    """The SIMT emulation itself: shuffles, CTA barriers and the split
+    cluster barrier give a GPU's values, and a thread that leaves before a
+    __syncthreads the others wait at (a hang on a GPU) ends the emulated
+    launch with a barrier-deadlock report instead of hanging the suite."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    src = os.path.join(ROOT, "tests", "host", "simt_selftest.cpp")
+    exe = os.path.join(ROOT, "tests", "host", "_build", "simt_selftest")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    subprocess.run(["g++", "-std=c++20", "-O1", src, "-o", exe], check=True)
+    ok = subprocess.run([exe, "ok"], capture_output=True, text=True, timeout=60)
+    assert ok.returncode == 0 and ok.stdout.strip() == "ok", ok.stdout
+    bad = subprocess.run([exe, "skip"], capture_output=True, text=True, timeout=60)
+    assert bad.returncode != 0
+    assert "barrier deadlock" in bad.stderr
+    assert "thread 0 waits at a CTA barrier" in bad.stderr
