@@ -180,7 +180,10 @@ __device__ int32_t window_read_cl(const Scoring& S, GraphView& G, DpView& D, Blo
   if (st != kOk) return st;
   const bool dp = cl_peek(&ss.mode, 0) == 1;
   const int32_t lanes = cl_peek(&ss.lanes, 0);
-  const uint32_t V = G.hdr->n_nodes;
+  // Read only when this read is aligned: a read that is only added (the
+  // first one, without strands) reaches the lead's AddAlignment, which
+  // rewrites the count, with no cluster barrier after this point.
+  const uint32_t V = dp ? G.hdr->n_nodes : 0u;
   auto align = [&](const uint8_t* sq, int32_t* pairs, int32_t* has, int32_t* score,
                    uint32_t* np) {
     int64_t mi, mj;

@@ -26,6 +26,21 @@
 #include <functional>
 #include <vector>
 
+// Built with -fsanitize=thread, the emulation is a race detector for the
+// device code: fibers switch without ordering each other, and the only
+// happens-before edges are the ones a GPU gives (barrier arrive -> barrier
+// completion, launch -> threads -> launch end, atomics), so two threads that
+// touch the same shared or global bytes between barriers, one of them
+// writing, are reported with both stacks.
+#if defined(__SANITIZE_THREAD__)
+#include <sanitizer/tsan_interface.h>
+#define SIMT_RACECHECK 1
+extern "C" void AnnotateIgnoreReadsBegin(const char* file, int line);
+extern "C" void AnnotateIgnoreReadsEnd(const char* file, int line);
+extern "C" void AnnotateIgnoreWritesBegin(const char* file, int line);
+extern "C" void AnnotateIgnoreWritesEnd(const char* file, int line);
+#endif
+
 #define SPOA_GB300_SIMT_HOST 1
 #define __host__
 #define __device__
@@ -64,6 +79,7 @@ struct Fiber {
   uint64_t token = 0;      // the cluster barrier's phase at the arrive
   const char* waits_on = nullptr;  // kind of barrier it is blocked on
   uint64_t shuffles = 0;           // warp shuffles done (picks the slot array)
+  void* race_ctx = nullptr;        // the race detector's fiber (racecheck builds)
 };
 
 // A barrier of `expected` fibers; `phase` counts completed rounds.
@@ -71,6 +87,7 @@ struct Barrier {
   unsigned expected = 0, arrived = 0;
   uint64_t phase = 0;
   std::vector<unsigned> waiting;  // fibers blocked on the current phase
+  char order[2] = {0, 0};  // happens-before keys of even and odd phases (racecheck)
 };
 
 // One CTA, or a cluster of `ncta` CTAs of `nt` threads each (the threads of
@@ -87,6 +104,8 @@ struct Cta {
   unsigned cur = 0;           // the running fiber
   ucontext_t sched;           // the launching code's context
   const std::function<void()>* body = nullptr;
+  void* race_sched = nullptr;  // the launching code's race-detector context
+  char order_start = 0, order_end = 0;  // launch -> threads -> launch end
 };
 
 inline Cta*& cta() {
@@ -119,20 +138,85 @@ inline char* stack_at(size_t k) {
   return pool[k];
 }
 
-inline void fiber_entry() {
+// The emulator's own bookkeeping (run queue, barrier counters, shuffle
+// slots, threadIdx): kept out of the race detector's view for the scope of
+// one of these, since it stands for hardware state, not device-code data.
+struct Internal {
+#ifdef SIMT_RACECHECK
+  Internal() {
+    AnnotateIgnoreReadsBegin(__FILE__, __LINE__);
+    AnnotateIgnoreWritesBegin(__FILE__, __LINE__);
+  }
+  ~Internal() {
+    AnnotateIgnoreWritesEnd(__FILE__, __LINE__);
+    AnnotateIgnoreReadsEnd(__FILE__, __LINE__);
+  }
+#endif
+};
+
+// Happens-before edges for the race detector (no-ops in other builds).
+inline void order_release(void* key) {
+#ifdef SIMT_RACECHECK
+  __tsan_release(key);
+#else
+  (void)key;
+#endif
+}
+inline void order_acquire(void* key) {
+#ifdef SIMT_RACECHECK
+  __tsan_acquire(key);
+#else
+  (void)key;
+#endif
+}
+// Tells the race detector which fiber runs next, without ordering the two.
+// A macro, and the functions that use it are not instrumented: the
+// detector keeps a call stack per fiber, so no instrumented function may
+// return between this and the switch of stacks that follows it.
+#ifdef SIMT_RACECHECK
+#define SIMT_RACE_SWITCH(ctx) __tsan_switch_to_fiber((ctx), __tsan_switch_to_fiber_no_sync)
+#define SIMT_SWITCHES __attribute__((no_sanitize_thread))
+#else
+#define SIMT_RACE_SWITCH(ctx) ((void)(ctx))
+#define SIMT_SWITCHES
+#endif
+
+// The race detector's context for fiber k, like the stacks kept and reused
+// by every launch (a destroyed detector fiber whose stack is reused did not
+// survive the next launch).
+inline void* race_ctx_at(size_t k) {
+#ifdef SIMT_RACECHECK
+  static std::vector<void*> pool;
+  while (pool.size() <= k) pool.push_back(__tsan_create_fiber(0));
+  return pool[k];
+#else
+  (void)k;
+  return nullptr;
+#endif
+}
+
+SIMT_SWITCHES inline void fiber_entry() {
   Cta& c = *cta();
+  order_acquire(&c.order_start);
   (*c.body)();
-  c.fib[c.cur].done = true;  // returns to c.sched through uc_link
+  order_release(&c.order_end);
+  {
+    Internal in;  // ends before the switch: it counts in this fiber's detector state
+    c.fib[c.cur].done = true;
+  }
+  SIMT_RACE_SWITCH(c.race_sched);  // returns to c.sched through uc_link
 }
 
 // The running fiber waits: the OS thread switches straight to the next
 // ready fiber (or back to the scheduler when none is ready); the fiber
 // resumes once a barrier release has queued it again.
-inline void block(const char* kind) {
+SIMT_SWITCHES inline void block(const char* kind) {
+  Internal in;
   Cta& c = *cta();
   const unsigned me = c.cur;
   c.fib[me].waits_on = kind;
   if (c.runq.empty()) {
+    SIMT_RACE_SWITCH(c.race_sched);
     swapcontext(&c.fib[me].ctx, &c.sched);
   } else {
     const unsigned nx = c.runq.front();
@@ -141,6 +225,7 @@ inline void block(const char* kind) {
     c.fib[nx].waits_on = nullptr;
     tid.x = c.fib[nx].t;
     cta_rank = c.fib[nx].r;
+    SIMT_RACE_SWITCH(c.fib[nx].race_ctx);
     swapcontext(&c.fib[me].ctx, &c.fib[nx].ctx);
   }
   // resumed: whoever switched here set c.cur, tid and cta_rank to this fiber
@@ -151,8 +236,10 @@ inline void block(const char* kind) {
 // order on odd ones, so that code between two barriers runs in both thread
 // orders over a launch (a missing barrier shows in one of them).
 inline uint64_t arrive(Barrier& b) {
+  Internal in;
   Cta& c = *cta();
   const uint64_t ph = b.phase;
+  order_release(&b.order[ph & 1]);
   if (++b.arrived == b.expected) {
     b.arrived = 0;
     ++b.phase;
@@ -165,12 +252,18 @@ inline uint64_t arrive(Barrier& b) {
   return ph;
 }
 
+// Waits until the phase that began as `ph` has completed.  The keys of
+// even and odd phases alternate: a thread can release phase ph + 2 only
+// after every thread has arrived at ph + 1, that is after every thread has
+// acquired ph.
 inline void wait(Barrier& b, uint64_t ph, const char* kind) {
+  Internal in;
   Cta& c = *cta();
   while (b.phase == ph) {
     b.waiting.push_back(c.cur);
     block(kind);
   }
+  order_acquire(&b.order[ph & 1]);
 }
 
 inline void arrive_and_wait(Barrier& b, const char* kind) { wait(b, arrive(b), kind); }
@@ -185,6 +278,7 @@ inline void arrive_and_wait(Barrier& b, const char* kind) { wait(b, arrive(b), k
 // hanging.
 inline void launch_cluster(unsigned ncta, unsigned nt, const std::vector<char*>& scratch,
                            const std::function<void()>& body) {
+  Internal in;
   Cta c;
   c.nt = nt;
   c.ncta = ncta;
@@ -211,8 +305,13 @@ inline void launch_cluster(unsigned ncta, unsigned nt, const std::vector<char*>&
     f.ctx.uc_stack.ss_size = kStackBytes - 4096;
     f.ctx.uc_link = &c.sched;
     makecontext(&f.ctx, fiber_entry, 0);
+    f.race_ctx = race_ctx_at(k);
     c.runq.push_back(k);
   }
+#ifdef SIMT_RACECHECK
+  c.race_sched = __tsan_get_current_fiber();
+#endif
+  order_release(&c.order_start);
   const HostDim tid0 = tid;
   const unsigned rank0 = cta_rank;
   while (!c.runq.empty()) {
@@ -222,6 +321,7 @@ inline void launch_cluster(unsigned ncta, unsigned nt, const std::vector<char*>&
     f.waits_on = nullptr;
     tid.x = f.t;
     cta_rank = f.r;
+    SIMT_RACE_SWITCH(f.race_ctx);
     swapcontext(&c.sched, &f.ctx);
   }
   for (const Fiber& f : c.fib)
@@ -233,6 +333,7 @@ inline void launch_cluster(unsigned ncta, unsigned nt, const std::vector<char*>&
                        g.waits_on ? g.waits_on : "?");
       std::abort();
     }
+  order_acquire(&c.order_end);
   tid = tid0;
   cta_rank = rank0;
   cta() = outer;
@@ -248,6 +349,7 @@ inline void launch(unsigned nt, const std::function<void()>& body) {
 // warp barrier suffices: a lane can write the array again only after the
 // next shuffle's barrier, which every lane reaches after its read.
 inline int32_t exchange(int32_t v, unsigned src_lane) {
+  Internal in;
   Cta& c = *cta();
   const unsigned nw = c.ncta * ((c.nt + 31) / 32);
   const unsigned w = cta_rank * ((c.nt + 31) / 32) + tid.x / 32, lane = tid.x % 32;
@@ -264,12 +366,14 @@ inline void cluster_sync() {
 
 // The split form: arrive, then (after other work) wait for the others.
 inline void cluster_arrive() {
+  Internal in;
   if (!cta()) return;
   Fiber& f = cta()->fib[cta()->cur];
   f.token = arrive(cta()->cluster_bar);
   f.has_token = true;
 }
 inline void cluster_wait() {
+  Internal in;
   if (!cta()) return;
   Fiber& f = cta()->fib[cta()->cur];
   if (!f.has_token) return;
@@ -280,6 +384,7 @@ inline void cluster_wait() {
 // The copy of a shared variable of this CTA in CTA `rank` of the cluster.
 template <typename T>
 inline T* peer(T* local, unsigned rank) {
+  Internal in;
   Cta& c = *cta();
   const std::ptrdiff_t off = reinterpret_cast<const char*>(local) - c.scratch[cta_rank];
   return reinterpret_cast<T*>(c.scratch[rank] + off);

@@ -5,6 +5,10 @@
 //   simt_selftest skip  - one thread leaves before a __syncthreads that the
 //                         others wait at; the emulation must abort with a
 //                         barrier-deadlock report instead of hanging
+//   simt_selftest race  - thread 0 writes a shared value that thread 33
+//                         reads with no barrier between them (a data race
+//                         on a GPU); a -fsanitize=thread build must report
+//                         it, while "ok" must run without a report
 #include "simt_host.h"
 
 #include <cstdio>
@@ -13,6 +17,17 @@
 
 int main(int argc, char** argv) {
   const bool skip = argc > 1 && std::strcmp(argv[1], "skip") == 0;
+  const bool race = argc > 1 && std::strcmp(argv[1], "race") == 0;
+  if (race) {
+    int shared_value = 0, seen = 0;
+    simt::launch(64, [&] {
+      if (threadIdx.x == 0) shared_value = 7;
+      if (threadIdx.x == 33) seen = shared_value;  // no barrier: a race
+      __syncthreads();
+    });
+    std::printf("read %d\n", seen);
+    return 0;
+  }
   if (skip) {
     simt::launch(64, [] {
       __syncthreads();

@@ -1,0 +1,79 @@
+"""Race and undefined-behaviour check of the device code on the CPU.
+
+compute-sanitizer's racecheck does not run where the GPU tests run, so the
+SIMT emulation (tests/host/simt_host.h) stands in for it: built with
+-fsanitize=thread, its emulated threads are fibers that the race detector
+sees as threads ordered only by what orders them on a GPU (barrier
+arrive -> barrier completion, launch -> threads -> launch end, atomics).
+tests/host/racecheck_main.cpp drives the window code (one-warp and two-warp
+CTAs, both widths, the one-warp build, the segmented forward, clusters of
+2, 4 and 8 CTAs) and the W-windows-per-CTA loop over every alignment type
+and gap model, strands and qualities; any pair of threads that touch the
+same shared or global bytes between barriers with one of them writing, and
+any undefined behaviour (-fsanitize=undefined: signed overflow, shifts,
+misaligned access), fails the test.  A planted race in
+tests/host/simt_selftest.cpp shows that the detector sees one.
+"""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+HOST = os.path.join(ROOT, "tests", "host")
+BUILD = os.path.join(HOST, "_build")
+FLAGS = ["g++", "-std=c++20", "-O1", "-g", "-fsanitize=thread,undefined",
+         "-fno-sanitize-recover=undefined"]
+
+
+def _sanitizers_available():
+    if shutil.which("g++") is None:
+        return False
+    os.makedirs(BUILD, exist_ok=True)
+    probe = os.path.join(BUILD, "tsan_probe")
+    r = subprocess.run(FLAGS + ["-x", "c++", "-", "-o", probe], input="int main() {}",
+                       text=True, capture_output=True)
+    return r.returncode == 0 and subprocess.run([probe]).returncode == 0
+
+
+pytestmark = pytest.mark.skipif(not _sanitizers_available(),
+                                reason="g++ with ThreadSanitizer not available")
+
+
+def _build_all(targets):
+    procs = [subprocess.Popen(FLAGS + extra + [src, "-o", out], stderr=subprocess.PIPE,
+                              text=True) for src, out, extra in targets]
+    for p in procs:
+        _, err = p.communicate()
+        assert p.returncode == 0, err
+
+
+def _report(r):
+    return (r.stdout + r.stderr)[-4000:]
+
+
+def test_detector_sees_a_planted_race():
+    exe = os.path.join(BUILD, "simt_selftest_tsan")
+    _build_all([(os.path.join(HOST, "simt_selftest.cpp"), exe, [])])
+    ok = subprocess.run([exe, "ok"], capture_output=True, text=True, timeout=120)
+    assert ok.returncode == 0 and "ThreadSanitizer" not in ok.stderr, _report(ok)
+    bad = subprocess.run([exe, "race"], capture_output=True, text=True, timeout=120)
+    assert bad.returncode != 0
+    assert "WARNING: ThreadSanitizer: data race" in bad.stderr
+    assert "simt_selftest.cpp" in bad.stderr
+
+
+def test_device_code_has_no_races_or_undefined_behaviour():
+    src = os.path.join(HOST, "racecheck_main.cpp")
+    win, mw = os.path.join(BUILD, "racecheck_window"), os.path.join(BUILD, "racecheck_mw")
+    _build_all([(src, win, []), (src, mw, ["-DRACECHECK_MW"])])
+    procs = [subprocess.Popen([exe], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+             for exe in (win, mw)]
+    for p in procs:
+        out, err = p.communicate(timeout=900)
+        r = subprocess.CompletedProcess(p.args, p.returncode, out, err)
+        assert "WARNING: ThreadSanitizer" not in err, _report(r)
+        assert "runtime error" not in err, _report(r)
+        assert p.returncode == 0 and out.strip().endswith("statuses ok"), _report(r)
