@@ -316,7 +316,7 @@ int32_t graph_reserve(spoa_gb300_graph* g, uint64_t len, uint64_t reads = 1) {
     const uint32_t K = need.aligned;
     CU(cudaMemcpy(nv.hdr, o.hdr, sizeof(GraphHeader), cudaMemcpyDeviceToDevice));
 #define CP(field, count, esz) \
-  if (count) CU(cudaMemcpy(nv.field, o.field, (count) * (esz), cudaMemcpyDeviceToDevice))
+  if ((count) != 0) CU(cudaMemcpy(nv.field, o.field, (count) * (esz), cudaMemcpyDeviceToDevice))
     CP(code, N, 1);
     CP(nlink, N, 16);
     CP(in_deg, N, 4);

@@ -28,18 +28,18 @@ FLAGS = ["g++", "-std=c++20", "-O1", "-g", "-fsanitize=thread,undefined",
          "-fno-sanitize-recover=undefined"]
 
 
-def _sanitizers_available():
+@pytest.fixture(scope="module")
+def sanitizers():
+    """Skips unless g++ builds and runs a -fsanitize=thread,undefined program
+    (probed when the first test of this file runs, not at collection)."""
     if shutil.which("g++") is None:
-        return False
+        pytest.skip("g++ not available")
     os.makedirs(BUILD, exist_ok=True)
     probe = os.path.join(BUILD, "tsan_probe")
     r = subprocess.run(FLAGS + ["-x", "c++", "-", "-o", probe], input="int main() {}",
                        text=True, capture_output=True)
-    return r.returncode == 0 and subprocess.run([probe]).returncode == 0
-
-
-pytestmark = pytest.mark.skipif(not _sanitizers_available(),
-                                reason="g++ with ThreadSanitizer not available")
+    if r.returncode != 0 or subprocess.run([probe]).returncode != 0:
+        pytest.skip("g++ with ThreadSanitizer not available")
 
 
 def _build_all(targets):
@@ -54,7 +54,7 @@ def _report(r):
     return (r.stdout + r.stderr)[-4000:]
 
 
-def test_detector_sees_a_planted_race():
+def test_detector_sees_a_planted_race(sanitizers):
     exe = os.path.join(BUILD, "simt_selftest_tsan")
     _build_all([(os.path.join(HOST, "simt_selftest.cpp"), exe, [])])
     ok = subprocess.run([exe, "ok"], capture_output=True, text=True, timeout=120)
@@ -65,7 +65,7 @@ def test_detector_sees_a_planted_race():
     assert "simt_selftest.cpp" in bad.stderr
 
 
-def test_device_code_has_no_races_or_undefined_behaviour():
+def test_device_code_has_no_races_or_undefined_behaviour(sanitizers):
     src = os.path.join(HOST, "racecheck_main.cpp")
     win, mw = os.path.join(BUILD, "racecheck_window"), os.path.join(BUILD, "racecheck_mw")
     _build_all([(src, win, []), (src, mw, ["-DRACECHECK_MW"])])
