@@ -251,7 +251,10 @@ typedef struct {
   int32_t threads_per_window, columns_per_thread, ctas, launches;
 } spoa_gb300_batch_result;
 
-/* Uploads a batch and sizes the device arenas. */
+/* Uploads a batch and sizes the device arenas.  Before any CUDA call it
+ * returns SPOA_GB300_ERR_INVALID_ARGUMENT for a null descriptor, output or
+ * offset array, an unknown type (default or per window), a positive
+ * penalty, window_read_off[0] != 0 or decreasing window offsets. */
 int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* desc, spoa_gb300_batch** out);
 /* Runs the persistent kernel on device-resident inputs (stream may be 0).
  * Windows that outgrow their arena are rerun with a larger one. */

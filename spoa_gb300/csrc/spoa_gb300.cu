@@ -1733,7 +1733,18 @@ int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* d, spoa_gb300_batch
   if (!d || !out || !d->window_read_off || !d->seq_off || (!d->seqs && d->n_windows))
     return kInvalidArgument;
   *out = nullptr;
+  // what the descriptor alone decides is checked before any CUDA call:
+  // types, penalties (AlignmentEngine::Create), the window offsets
   if (d->type != kSW && d->type != kNW && d->type != kOV) return kInvalidArgument;
+  if (d->g > 0 || d->q > 0 || d->e > 0 || d->c > 0) return kInvalidArgument;
+  if (d->window_read_off[0] != 0) return kInvalidArgument;
+  for (uint32_t w = 0; w < d->n_windows; ++w) {
+    if (d->window_read_off[w + 1] < d->window_read_off[w]) return kInvalidArgument;
+    if (d->window_type) {
+      const int8_t t = d->window_type[w];
+      if (t != kSW && t != kNW && t != kOV) return kInvalidArgument;
+    }
+  }
   const int dev = resolve_device(d->device_set, d->device);
   if (dev < 0) return d->device_set ? kInvalidArgument : kCuda;
   DeviceGuard guard(dev);
@@ -1750,24 +1761,13 @@ int32_t spoa_gb300_batch_create(const spoa_gb300_batch_desc* d, spoa_gb300_batch
   b->base = base;
   b->n_windows = d->n_windows;
   b->wro.assign(d->window_read_off, d->window_read_off + d->n_windows + 1);
-  b->n_reads = b->wro[d->n_windows] - b->wro[0];
-  if (b->wro[0] != 0) {
-    delete b;
-    return kInvalidArgument;
-  }
+  b->n_reads = b->wro[d->n_windows];
   b->seq_off.assign(d->seq_off, d->seq_off + b->n_reads + 1);
   cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
   b->lmax.assign(b->n_windows, 1);
   b->sumlen.assign(b->n_windows, 0);
   b->nreads.assign(b->n_windows, 0);
   for (uint32_t w = 0; w < b->n_windows; ++w) {
-    if (d->window_type) {
-      int8_t t = d->window_type[w];
-      if (t != kSW && t != kNW && t != kOV) {
-        delete b;
-        return kInvalidArgument;
-      }
-    }
     for (uint32_t r = b->wro[w]; r < b->wro[w + 1]; ++r) {
       uint64_t L = b->seq_off[r + 1] - b->seq_off[r];
       if (L > (uint64_t)INT32_MAX) {
