@@ -5,8 +5,8 @@
 // behaviour (signed overflow, bad shifts, misaligned access) of the device
 // code.  TEST INFRASTRUCTURE ONLY (tests/test_window_host.py builds and runs
 // it).  Built with RACECHECK_MW it drives the W-windows-per-CTA loop, else
-// the one-window loop (window_read), the cluster form (window_read_cl) and
-// the segmented forward.  Correctness against the oracle is checked by the
+// the one-window loop (window_read) with the MSA of the window, the cluster
+// form (window_read_cl) and the segmented forward.  Correctness against the oracle is checked by the
 // other host tests; this program checks only statuses.
 #ifdef RACECHECK_MW
 #include "batch_mw_host.cpp"
@@ -117,7 +117,8 @@ int main() {
     std::vector<int32_t> aln(2 * cap);
     std::vector<uint64_t> aoff(nr + 1);
     std::vector<char> cons(f.seqs.size() + 16);
-    uint32_t clen = 0;
+    uint32_t clen = 0, dims[2] = {0, 0};
+    std::vector<char> msa((nr + 1) * (f.seqs.size() + 1));  // rows x at most every base
     const int32_t* G = kGaps[gap];
     const int32_t st =
         cl ? wh_run_cl(type, 5, -4, G[0], G[1], G[2], G[3], cl, nt, nr, f.seqs.data(),
@@ -127,7 +128,7 @@ int main() {
            : wh_run(type, 5, -4, G[0], G[1], G[2], G[3], wide, cpt, nt, nr, f.seqs.data(),
                     f.off.data(), quals ? f.quals.data() : nullptr, strand, scores.data(),
                     rev.data(), aln.data(), cap, aoff.data(), cons.data(),
-                    (uint32_t)cons.size(), &clen);
+                    (uint32_t)cons.size(), &clen, msa.data(), msa.size(), dims);
     check(what, st, type, gap);
   };
   // every variant on three (type, gap model) pairs that cover each type and

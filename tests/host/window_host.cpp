@@ -16,7 +16,7 @@ template <int SUB, int CPT, typename T, int SEGS = 1, int NT = 0>
 int32_t run(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t* off,
             const char* quals, int32_t strand, uint32_t nt, int32_t* scores, int32_t* rev,
             int32_t* aln, uint64_t aln_cap, uint64_t* aln_off, char* cons, uint32_t cons_cap,
-            uint32_t* cons_len) {
+            uint32_t* cons_len, char* msa, uint64_t msa_cap, uint32_t* msa_dims) {
   uint64_t sum = 0;
   uint32_t lmax = 1;
   for (uint32_t r = 0; r < n_reads; ++r) {
@@ -57,6 +57,17 @@ int32_t run(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t
     aln_off[r + 1] = na;
   }
   simt::launch(1, [&] { write_consensus(G, reinterpret_cast<uint8_t*>(cons), cons_cap, cons_len); });
+  if (msa) {
+    // the MSA as the batched kernel writes it: rows spread over the CTA
+    uint32_t s_dims[2];
+    int32_t st = kOk;
+    simt::launch(nt, [&] {
+      const int32_t r = window_msa(G, false, reinterpret_cast<uint8_t*>(msa), msa_cap,
+                                   &msa_dims[0], &msa_dims[1], s_dims);
+      if (threadIdx.x == 0) st = r;
+    });
+    if (st != kOk) return st;
+  }
   return kOk;
 }
 
@@ -120,7 +131,7 @@ extern "C" int32_t wh_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t
                           const char* seqs, const uint64_t* off, const char* quals,
                           int32_t strand, int32_t* scores, int32_t* rev, int32_t* aln,
                           uint64_t aln_cap, uint64_t* aln_off, char* cons, uint32_t cons_cap,
-                          uint32_t* cons_len) {
+                          uint32_t* cons_len, char* msa, uint64_t msa_cap, uint32_t* msa_dims) {
   // AlignmentEngine::Create's subtype and canonical penalties
   // (alignment_engine.cpp:57-66)
   const int32_t sub = g >= e ? kLinear : ((g <= q || e >= c) ? kAffine : kConvex);
@@ -133,7 +144,8 @@ extern "C" int32_t wh_run(int32_t type, int32_t m, int32_t n, int32_t g, int32_t
   const Scoring S{type, sub, m, n, g, e, q, c};
 #define RUN(SUBV, C, TT, ...)                                                              \
   return run<SUBV, C, TT, ##__VA_ARGS__>(S, n_reads, seqs, off, quals, strand, nt, scores, rev, \
-                                         aln, aln_cap, aln_off, cons, cons_cap, cons_len)
+                                         aln, aln_cap, aln_off, cons, cons_cap, cons_len, msa, \
+                                         msa_cap, msa_dims)
 #define BY_SUB(C, TT)                   \
   switch (sub) {                        \
     case kLinear: RUN(kLinear, C, TT);  \

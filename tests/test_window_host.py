@@ -34,7 +34,8 @@ def wh():
     L = C.CDLL(OUT)
     I32, U32, P = C.c_int32, C.c_uint32, C.c_void_p
     L.wh_run.argtypes = [I32] * 9 + [U32, U32, C.c_char_p, P, C.c_char_p, I32, P, P, P,
-                                     C.c_uint64, P, C.c_char_p, U32, P]
+                                     C.c_uint64, P, C.c_char_p, U32, P, C.c_char_p,
+                                     C.c_uint64, P]
     L.wh_run_cl.argtypes = [I32] * 8 + [U32, U32, C.c_char_p, P, C.c_char_p, I32, P, P, P,
                                         C.c_uint64, P, C.c_char_p, U32, P]
     return L
@@ -44,7 +45,9 @@ def _ptr(a):
     return a.ctypes.data_as(C.c_void_p)
 
 
-def run_host(L, type_, params, reads, quals, strand, cpt, nt, wide):
+def run_host(L, type_, params, reads, quals, strand, cpt, nt, wide, msa=None):
+    """One window through the emulated CTA; with msa=[] the window's MSA
+    rows (the batched kernel's window_msa) are appended to that list."""
     off = np.zeros(len(reads) + 1, np.uint64)
     off[1:] = np.cumsum([len(r) for r in reads])
     nr = len(reads)
@@ -54,27 +57,37 @@ def run_host(L, type_, params, reads, quals, strand, cpt, nt, wide):
     aoff = np.zeros(nr + 1, np.uint64)
     cons = C.create_string_buffer(int(off[-1]) + 16)
     clen = C.c_uint32()
+    mcap = (nr + 1) * (int(off[-1]) + 1)
+    mbuf = C.create_string_buffer(mcap) if msa is not None else None
+    dims = (C.c_uint32 * 2)()
     st = L.wh_run(type_, *params, 1 if wide else 0, cpt, nt, nr, b"".join(reads), _ptr(off),
                   b"".join(quals) if quals else None, 1 if strand else 0, _ptr(scores), _ptr(rev),
-                  _ptr(aln), cap, _ptr(aoff), cons, len(cons), C.byref(clen))
+                  _ptr(aln), cap, _ptr(aoff), cons, len(cons), C.byref(clen), mbuf, mcap, dims)
     alns = [aln[2 * int(aoff[r]):2 * int(aoff[r + 1])].reshape(-1, 2) for r in range(nr)]
+    if msa is not None and st == 0:
+        rows, cols = dims[0], dims[1]
+        msa.extend(mbuf.raw[k * cols:(k + 1) * cols].decode() for k in range(rows))
     return st, scores.tolist(), rev.tolist(), alns, cons.raw[:clen.value].decode()
 
 
-def _check_window(L, rec, cpt=8, wide=False):
+def _check_window(L, rec, cpt=8, wide=False, with_msa=False):
     reads = [r.encode() for r in rec["reads"]]
     quals = [q.encode() for q in rec["quals"]] if rec["quals"] else None
     lmax = max(len(r) for r in reads)
     nt = 32 * max(1, -(-lmax // (cpt * 32)))
     strand = rec["strand_ambiguous"]
+    msa = [] if with_msa else None
     st, scores, rev, alns, cons = run_host(L, rec["type"], rec["params"], reads, quals, strand,
-                                           cpt, nt, wide)
+                                           cpt, nt, wide, msa)
     if st == NEEDS_WIDE:
+        msa = [] if with_msa else None
         st, scores, rev, alns, cons = run_host(L, rec["type"], rec["params"], reads, quals,
-                                               strand, cpt, nt, True)
+                                               strand, cpt, nt, True, msa)
     assert st == 0, (rec.get("name"), st)
     ref = po.run_window(rec["type"], *rec["params"], reads, quals, strand_ambiguous=strand,
-                        with_msa=False)
+                        with_msa=with_msa)
+    if with_msa:
+        assert msa == ref.msa, rec.get("name")
     assert scores == ref.scores, rec.get("name")
     assert rev == [int(x) for x in ref.reversed], rec.get("name")
     for a, b in zip(alns, ref.alignments):
@@ -86,13 +99,13 @@ def _check_window(L, rec, cpt=8, wide=False):
 def test_window_device_code_matches_the_oracle(wh, ref_windows):
     """Every recorded window of up to 12 reads of up to 512 bases (200 of
     the fixture's 209: adversarial lengths, N bases, qualities, both
-    strands, long insertions) through the emulated CTA; reads up to 256
-    columns take one warp, longer ones two."""
+    strands, long insertions) through the emulated CTA, its MSA included;
+    reads up to 256 columns take one warp, longer ones two."""
     nts, strands, done = set(), 0, 0
     for rec in ref_windows:
         if max(len(r) for r in rec["reads"]) > 512 or len(rec["reads"]) > 12:
             continue
-        nts.add(_check_window(wh, rec))
+        nts.add(_check_window(wh, rec, with_msa=True))
         strands += rec["strand_ambiguous"]
         done += 1
     assert done == 200 and nts == {32, 64} and strands >= 40
