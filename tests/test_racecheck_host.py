@@ -1,7 +1,7 @@
 """Race and undefined-behaviour check of the device code on the CPU.
 
-compute-sanitizer's racecheck does not run where the GPU tests run, so the
-SIMT emulation (tests/host/simt_host.h) stands in for it: built with
+The SIMT emulation (tests/host/simt_host.h) does the work of a GPU race
+checker on the host, with no GPU: built with
 -fsanitize=thread, its emulated threads are fibers that the race detector
 sees as threads ordered only by what orders them on a GPU (barrier
 arrive -> barrier completion, launch -> threads -> launch end, atomics).
