@@ -12,6 +12,27 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 
+def host_library(src: str, out: str, deps, std: str, opt: str) -> str:
+    """Builds a host test library from `src` (rebuilt when a dependency is
+    newer) and returns its path.  With SPOA_HOST_UBSAN=1 in the environment
+    it is built with -fsanitize=undefined and no recovery, into a file of
+    its own, so that undefined behaviour of the product code it compiles
+    ends the process with a report."""
+    import shutil
+    import subprocess
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    flags = ["g++", f"-std={std}", opt, "-shared", "-fPIC", "-pthread"]
+    if os.environ.get("SPOA_HOST_UBSAN") == "1":
+        flags += ["-g", "-fsanitize=undefined", "-fno-sanitize-recover=undefined"]
+        out = out.replace(".so", "_ubsan.so")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    if not os.path.exists(out) or any(os.path.getmtime(d) > os.path.getmtime(out)
+                                      for d in [src] + list(deps)):
+        subprocess.run(flags + [src, "-o", out], check=True)
+    return out
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 

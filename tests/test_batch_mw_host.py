@@ -6,13 +6,11 @@ scores, strand choices and consensus must equal the oracle's, for W = 2
 the batched kernel; tests/test_window_host.py covers its device code.)"""
 import ctypes as C
 import os
-import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import ROOT, host_library
 from oracle import pyoracle as po
 from spoa_gb300 import synth
 
@@ -23,16 +21,10 @@ CSRC = os.path.join(ROOT, "spoa_gb300", "csrc")
 
 @pytest.fixture(scope="module")
 def mw():
-    if shutil.which("g++") is None:
-        pytest.skip("g++ not available")
-    os.makedirs(os.path.dirname(OUT), exist_ok=True)
-    deps = [SRC, os.path.join(ROOT, "tests", "host", "simt_host.h")] + [
+    deps = [os.path.join(ROOT, "tests", "host", "simt_host.h")] + [
         os.path.join(CSRC, f) for f in ("poa_device.cuh", "poa_dp.cuh", "poa_window.cuh",
                                         "poa_batch_mw.cuh")]
-    if not os.path.exists(OUT) or any(os.path.getmtime(d) > os.path.getmtime(OUT) for d in deps):
-        subprocess.run(["g++", "-std=c++20", "-O1", "-shared", "-fPIC", "-pthread", SRC, "-o",
-                        OUT], check=True)
-    L = C.CDLL(OUT)
+    L = C.CDLL(host_library(SRC, OUT, deps, "c++20", "-O1"))
     I32, U32, P = C.c_int32, C.c_uint32, C.c_void_p
     L.mw_run.argtypes = [I32] * 8 + [U32, P, C.c_char_p, P, P, P, P, C.c_char_p, P, P, P,
                                      C.c_char_p]

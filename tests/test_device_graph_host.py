@@ -5,13 +5,11 @@ read by read: node characters, rank order, every edge (tail, head, weight,
 labels), aligned lists, sequence starts and the consensus."""
 import ctypes as C
 import os
-import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import ROOT, host_library
 from oracle import pyoracle as po
 from spoa_gb300 import synth
 
@@ -22,13 +20,8 @@ P, U32 = C.c_void_p, C.c_uint32
 
 @pytest.fixture(scope="module")
 def dg():
-    if shutil.which("g++") is None:
-        pytest.skip("g++ not available")
-    os.makedirs(os.path.dirname(OUT), exist_ok=True)
-    deps = [SRC, os.path.join(ROOT, "spoa_gb300", "csrc", "poa_device.cuh")]
-    if not os.path.exists(OUT) or any(os.path.getmtime(d) > os.path.getmtime(OUT) for d in deps):
-        subprocess.run(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", SRC, "-o", OUT], check=True)
-    L = C.CDLL(OUT)
+    deps = [os.path.join(ROOT, "spoa_gb300", "csrc", "poa_device.cuh")]
+    L = C.CDLL(host_library(SRC, OUT, deps, "c++17", "-O2"))
     L.dg_create.restype = P
     L.dg_create.argtypes = [U32] * 5
     L.dg_destroy.argtypes = [P]

@@ -3,13 +3,11 @@ spoa_gb300_graph_gfa) on the oracle's graphs of recorded windows, byte for
 byte against the oracle's GFA text (which the recorded reference GFA pins)."""
 import ctypes as C
 import os
-import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import ROOT, host_library
 from oracle import pyoracle as po
 from spoa_gb300.gfa import gfa_lines
 
@@ -19,14 +17,8 @@ OUT = os.path.join(ROOT, "tests", "host", "_build", "libgfa_host.so")
 
 @pytest.fixture(scope="module")
 def gh():
-    if shutil.which("g++") is None:
-        pytest.skip("g++ not available")
-    os.makedirs(os.path.dirname(OUT), exist_ok=True)
-    deps = [SRC, os.path.join(ROOT, "spoa_gb300", "csrc", "gfa_text.h")]
-    if not os.path.exists(OUT) or any(os.path.getmtime(d) > os.path.getmtime(OUT) for d in deps):
-        subprocess.run(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", SRC, "-o", OUT],
-                       check=True)
-    L = C.CDLL(OUT)
+    deps = [os.path.join(ROOT, "spoa_gb300", "csrc", "gfa_text.h")]
+    L = C.CDLL(host_library(SRC, OUT, deps, "c++17", "-O2"))
     P = C.c_void_p
     L.gh_gfa.argtypes = [C.c_uint32] * 3 + [P] * 11 + [C.c_int32, C.c_char_p, C.c_uint64]
     L.gh_gfa.restype = C.c_uint64

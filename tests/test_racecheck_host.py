@@ -77,3 +77,20 @@ def test_device_code_has_no_races_or_undefined_behaviour(sanitizers):
         assert "WARNING: ThreadSanitizer" not in err, _report(r)
         assert "runtime error" not in err, _report(r)
         assert p.returncode == 0 and out.strip().endswith("statuses ok"), _report(r)
+
+
+def test_graph_code_and_gfa_writer_under_ubsan():
+    """The parts of the product's code the race check does not drive --
+    the device graph code's Subgraph and graph loading, and the GFA writer
+    -- rebuilt for the host with -fsanitize=undefined and run through their
+    CPU tests in a child process: undefined behaviour ends it with a
+    report.  (The race check's build already runs the window code, its MSA
+    and the W-windows loop under the same sanitizer.)"""
+    import sys
+    env = dict(os.environ, SPOA_HOST_UBSAN="1")
+    r = subprocess.run(
+        [sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider", "-m", "not gpu",
+         "tests/test_device_graph_host.py", "tests/test_gfa_text.py"],
+        cwd=ROOT, env=env, capture_output=True, text=True, timeout=900)
+    assert "runtime error" not in r.stdout + r.stderr, _report(r)
+    assert r.returncode == 0 and " passed" in r.stdout, _report(r)

@@ -12,7 +12,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import ROOT
+from conftest import ROOT, host_library
 from oracle import pyoracle as po
 
 SRC = os.path.join(ROOT, "tests", "host", "window_host.cpp")
@@ -23,15 +23,9 @@ NEEDS_WIDE = 11
 
 @pytest.fixture(scope="module")
 def wh():
-    if shutil.which("g++") is None:
-        pytest.skip("g++ not available")
-    os.makedirs(os.path.dirname(OUT), exist_ok=True)
-    deps = [SRC, os.path.join(ROOT, "tests", "host", "simt_host.h")] + [
+    deps = [os.path.join(ROOT, "tests", "host", "simt_host.h")] + [
         os.path.join(CSRC, f) for f in ("poa_device.cuh", "poa_dp.cuh", "poa_window.cuh")]
-    if not os.path.exists(OUT) or any(os.path.getmtime(d) > os.path.getmtime(OUT) for d in deps):
-        subprocess.run(["g++", "-std=c++20", "-O1", "-shared", "-fPIC", "-pthread", SRC, "-o",
-                        OUT], check=True)
-    L = C.CDLL(OUT)
+    L = C.CDLL(host_library(SRC, OUT, deps, "c++20", "-O1"))
     I32, U32, P = C.c_int32, C.c_uint32, C.c_void_p
     L.wh_run.argtypes = [I32] * 9 + [U32, U32, C.c_char_p, P, C.c_char_p, I32, P, P, P,
                                      C.c_uint64, P, C.c_char_p, U32, P, C.c_char_p,
