@@ -79,7 +79,7 @@ def test_device_code_has_no_races_or_undefined_behaviour(sanitizers):
         assert p.returncode == 0 and out.strip().endswith("statuses ok"), _report(r)
 
 
-def test_graph_code_and_gfa_writer_under_ubsan():
+def test_graph_code_and_gfa_writer_under_ubsan(sanitizers):
     """The parts of the product's code the race check does not drive --
     the device graph code's Subgraph and graph loading, and the GFA writer
     -- rebuilt for the host with -fsanitize=undefined and run through their
