@@ -24,6 +24,7 @@
 #include <cstring>
 #include <deque>
 #include <functional>
+#include <source_location>
 #include <vector>
 
 // Built with -fsanitize=thread, the emulation is a race detector for the
@@ -88,6 +89,8 @@ struct Barrier {
   uint64_t phase = 0;
   std::vector<unsigned> waiting;  // fibers blocked on the current phase
   char order[2] = {0, 0};  // happens-before keys of even and odd phases (racecheck)
+  const char* site_file = nullptr;  // where the current phase's first thread
+  unsigned site_line = 0;           // called __syncthreads
 };
 
 // One CTA, or a cluster of `ncta` CTAs of `nt` threads each (the threads of
@@ -400,12 +403,32 @@ static struct BlockDimProxy {
 } blockDim;
 static const HostDim blockIdx{0};
 
-static inline void __syncthreads() {
+// __syncthreads is an aligned barrier: every thread of the CTA must reach
+// the same one (the same call in the source) in each phase, or the GPU's
+// behaviour is undefined.  The emulation checks that and aborts with both
+// places when two threads of a CTA meet at different __syncthreads.
+static inline void __syncthreads(
+    const std::source_location site = std::source_location::current()) {
 #ifdef SIMT_TRACE
   static std::atomic<long> n{0};
   if (threadIdx.x == 0) fprintf(stderr, "sync %ld\n", n++);
 #endif
-  if (simt::cta()) simt::arrive_and_wait(simt::cta()->cta_bar[simt::cta_rank], "CTA");
+  if (!simt::cta()) return;
+  simt::Barrier& b = simt::cta()->cta_bar[simt::cta_rank];
+  {
+    simt::Internal in;
+    if (b.arrived == 0) {
+      b.site_file = site.file_name();
+      b.site_line = site.line();
+    } else if (b.site_line != site.line() || std::strcmp(b.site_file, site.file_name()) != 0) {
+      std::fprintf(stderr,
+                   "simt: threads of CTA %u meet at different __syncthreads: %s:%u and %s:%u\n",
+                   simt::cta_rank, b.site_file, b.site_line, site.file_name(),
+                   (unsigned)site.line());
+      std::abort();
+    }
+  }
+  simt::arrive_and_wait(b, "CTA");
 }
 
 template <typename T>

@@ -5,6 +5,9 @@
 //   simt_selftest skip  - one thread leaves before a __syncthreads that the
 //                         others wait at; the emulation must abort with a
 //                         barrier-deadlock report instead of hanging
+//   simt_selftest split - threads of one CTA wait at two different
+//                         __syncthreads (undefined on a GPU); the emulation
+//                         must abort naming both
 //   simt_selftest race  - thread 0 writes a shared value that thread 33
 //                         reads with no barrier between them (a data race
 //                         on a GPU); a -fsanitize=thread build must report
@@ -18,6 +21,16 @@
 int main(int argc, char** argv) {
   const bool skip = argc > 1 && std::strcmp(argv[1], "skip") == 0;
   const bool race = argc > 1 && std::strcmp(argv[1], "race") == 0;
+  if (argc > 1 && std::strcmp(argv[1], "split") == 0) {
+    simt::launch(64, [] {
+      if (threadIdx.x < 32)
+        __syncthreads();
+      else
+        __syncthreads();
+    });
+    std::printf("no split barrier reported\n");
+    return 0;
+  }
   if (race) {
     int shared_value = 0, seen = 0;
     simt::launch(64, [&] {

@@ -223,9 +223,11 @@ def test_mq_path_is_the_best_vector_start(wh):
 
 def test_emulation_reports_a_skipped_barrier():
     """The SIMT emulation itself: shuffles, CTA barriers and the split
-    cluster barrier give a GPU's values, and a thread that leaves before a
+    cluster barrier give a GPU's values; a thread that leaves before a
     __syncthreads the others wait at (a hang on a GPU) ends the emulated
-    launch with a barrier-deadlock report instead of hanging the suite."""
+    launch with a barrier-deadlock report instead of hanging the suite, and
+    threads of a CTA that wait at two different __syncthreads (undefined on
+    a GPU) end it with both places named."""
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
     src = os.path.join(ROOT, "tests", "host", "simt_selftest.cpp")
@@ -238,3 +240,6 @@ def test_emulation_reports_a_skipped_barrier():
     assert bad.returncode != 0
     assert "barrier deadlock" in bad.stderr
     assert "thread 0 waits at a CTA barrier" in bad.stderr
+    split = subprocess.run([exe, "split"], capture_output=True, text=True, timeout=60)
+    assert split.returncode != 0
+    assert "meet at different __syncthreads" in split.stderr
