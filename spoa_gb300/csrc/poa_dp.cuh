@@ -82,18 +82,31 @@ __device__ __forceinline__ uint32_t cl_rank() {
   }
 }
 
+// In the host emulation of the device code (tests only), the cluster
+// barriers take the place they are called from, so that the emulation can
+// check that every thread meets the same (aligned) barrier.
+#ifdef SPOA_GB300_SIMT_HOST
+#define SPOA_GB300_BARRIER_SITE const simt::Site site = simt::Site::current()
+#else
+#define SPOA_GB300_BARRIER_SITE
+#endif
+
 // Barrier of the whole cluster (of the CTA when CL == 1), ordering the
 // memory operations before it against those after it for all its threads.
 template <int CL>
-__device__ __forceinline__ void cl_sync() {
+__device__ __forceinline__ void cl_sync(SPOA_GB300_BARRIER_SITE) {
   if constexpr (CL == 1) {
+#ifdef SPOA_GB300_SIMT_HOST
+    __syncthreads(site);
+#else
     __syncthreads();
+#endif
   } else {
 #ifdef __CUDA_ARCH__
     asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
                  "barrier.cluster.wait.acquire.aligned;" ::: "memory");
 #elif defined(SPOA_GB300_SIMT_HOST)
-    simt::cluster_sync();
+    simt::cluster_sync(site);
 #endif
   }
 }
@@ -103,11 +116,11 @@ __device__ __forceinline__ void cl_sync() {
 // thread of the cluster to arrive, acquiring theirs.  Memory operations
 // between the two are not ordered by the barrier.
 template <int CL>
-__device__ __forceinline__ void cl_arrive() {
+__device__ __forceinline__ void cl_arrive(SPOA_GB300_BARRIER_SITE) {
 #ifdef __CUDA_ARCH__
   asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
 #elif defined(SPOA_GB300_SIMT_HOST)
-  simt::cluster_arrive();
+  simt::cluster_arrive(site);
 #endif
 }
 template <int CL>

@@ -71,6 +71,8 @@ struct HostDim {
 
 namespace simt {
 
+using Site = std::source_location;
+
 // An emulated thread: a fiber with its own stack on the calling OS thread.
 struct Fiber {
   ucontext_t ctx;
@@ -271,6 +273,23 @@ inline void wait(Barrier& b, uint64_t ph, const char* kind) {
 
 inline void arrive_and_wait(Barrier& b, const char* kind) { wait(b, arrive(b), kind); }
 
+// Aligned barriers (__syncthreads, the cluster barrier): every thread must
+// arrive through the same call in each phase; the first arrival of a phase
+// records its place, and a thread arriving from another place aborts the
+// launch with both.
+inline void check_site(Barrier& b, const Site& site, const char* kind) {
+  Internal in;
+  if (b.arrived == 0) {
+    b.site_file = site.file_name();
+    b.site_line = site.line();
+  } else if (b.site_line != site.line() || std::strcmp(b.site_file, site.file_name()) != 0) {
+    std::fprintf(stderr, "simt: threads of CTA %u meet at different %s barriers: %s:%u and %s:%u\n",
+                 cta_rank, kind, b.site_file, b.site_line, site.file_name(),
+                 (unsigned)site.line());
+    std::abort();
+  }
+}
+
 // Runs body() on ncta CTAs of nt threads (a cluster when ncta > 1) as
 // fibers on the calling OS thread, each running until it waits at a barrier
 // (no preemption between barriers); scratch[r] is CTA r's shared-memory
@@ -363,14 +382,17 @@ inline int32_t exchange(int32_t v, unsigned src_lane) {
   return slots[src_lane];
 }
 
-inline void cluster_sync() {
-  if (cta()) arrive_and_wait(cta()->cluster_bar, "cluster");
+inline void cluster_sync(const Site& site = Site::current()) {
+  if (!cta()) return;
+  check_site(cta()->cluster_bar, site, "cluster");
+  arrive_and_wait(cta()->cluster_bar, "cluster");
 }
 
 // The split form: arrive, then (after other work) wait for the others.
-inline void cluster_arrive() {
-  Internal in;
+inline void cluster_arrive(const Site& site = Site::current()) {
   if (!cta()) return;
+  check_site(cta()->cluster_bar, site, "cluster");
+  Internal in;
   Fiber& f = cta()->fib[cta()->cur];
   f.token = arrive(cta()->cluster_bar);
   f.has_token = true;
@@ -407,27 +429,14 @@ static const HostDim blockIdx{0};
 // the same one (the same call in the source) in each phase, or the GPU's
 // behaviour is undefined.  The emulation checks that and aborts with both
 // places when two threads of a CTA meet at different __syncthreads.
-static inline void __syncthreads(
-    const std::source_location site = std::source_location::current()) {
+static inline void __syncthreads(const simt::Site site = simt::Site::current()) {
 #ifdef SIMT_TRACE
   static std::atomic<long> n{0};
   if (threadIdx.x == 0) fprintf(stderr, "sync %ld\n", n++);
 #endif
   if (!simt::cta()) return;
   simt::Barrier& b = simt::cta()->cta_bar[simt::cta_rank];
-  {
-    simt::Internal in;
-    if (b.arrived == 0) {
-      b.site_file = site.file_name();
-      b.site_line = site.line();
-    } else if (b.site_line != site.line() || std::strcmp(b.site_file, site.file_name()) != 0) {
-      std::fprintf(stderr,
-                   "simt: threads of CTA %u meet at different __syncthreads: %s:%u and %s:%u\n",
-                   simt::cta_rank, b.site_file, b.site_line, site.file_name(),
-                   (unsigned)site.line());
-      std::abort();
-    }
-  }
+  simt::check_site(b, site, "__syncthreads");
   simt::arrive_and_wait(b, "CTA");
 }
 

@@ -242,4 +242,4 @@ def test_emulation_reports_a_skipped_barrier():
     assert "thread 0 waits at a CTA barrier" in bad.stderr
     split = subprocess.run([exe, "split"], capture_output=True, text=True, timeout=60)
     assert split.returncode != 0
-    assert "meet at different __syncthreads" in split.stderr
+    assert "meet at different __syncthreads barriers" in split.stderr
