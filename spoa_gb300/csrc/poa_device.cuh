@@ -61,6 +61,21 @@ __host__ __device__ inline uint64_t align_up(uint64_t x, uint64_t a) {
   return (x + a - 1) / a * a;
 }
 
+// Host builds of the device code for the tests may define
+// SPOA_GB300_HOST_REDZONE (with AddressSanitizer): every region of an arena
+// is then followed by a poisoned red zone, so that an access past the end
+// of a region is reported.  Device builds never define it.
+#if defined(SPOA_GB300_HOST_REDZONE) && !defined(__CUDA_ARCH__)
+#include <sanitizer/asan_interface.h>
+#define SPOA_GB300_REDZONE(base, p, bytes, off)                                       \
+  do {                                                                                \
+    (off) += 256;                                                                     \
+    if (base) ASAN_POISON_MEMORY_REGION((p) + (bytes), (base) + (off) - ((p) + (bytes))); \
+  } while (0)
+#else
+#define SPOA_GB300_REDZONE(base, p, bytes, off) ((void)0)
+#endif
+
 // ---------------------------------------------------------------------------
 // graph arena
 // ---------------------------------------------------------------------------
@@ -114,6 +129,7 @@ __host__ __device__ inline uint64_t graph_layout(uint8_t* base, const GraphCaps&
   auto take = [&](uint64_t bytes) -> uint8_t* {
     uint8_t* p = base ? base + off : nullptr;
     off = align_up(off + bytes, 256);
+    SPOA_GB300_REDZONE(base, p, bytes, off);
     return p;
   };
   const uint64_t N = c.nodes, E = c.edges;
@@ -186,6 +202,7 @@ __host__ __device__ inline uint64_t dp_layout(uint8_t* base, const DpCaps& c, Dp
   auto take = [&](uint64_t bytes) -> uint8_t* {
     uint8_t* p = base ? base + off : nullptr;
     off = align_up(off + bytes, 256);
+    SPOA_GB300_REDZONE(base, p, bytes, off);
     return p;
   };
   const uint64_t cells = (uint64_t)c.rows * c.ld;

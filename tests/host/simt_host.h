@@ -42,6 +42,17 @@ extern "C" void AnnotateIgnoreWritesBegin(const char* file, int line);
 extern "C" void AnnotateIgnoreWritesEnd(const char* file, int line);
 #endif
 
+// Built with -fsanitize=address, the fiber switches are announced to
+// AddressSanitizer (the stack each switch lands on), so that it keeps
+// checking the emulated threads' stacks; with SPOA_GB300_HOST_REDZONE the
+// device arenas of the code under test carry poisoned red zones between
+// their regions (poa_device.cuh), so an access past a region is reported.
+#if defined(__SANITIZE_ADDRESS__)
+#include <pthread.h>
+#include <sanitizer/common_interface_defs.h>
+#define SIMT_ASAN 1
+#endif
+
 #define SPOA_GB300_SIMT_HOST 1
 #define __host__
 #define __device__
@@ -83,6 +94,7 @@ struct Fiber {
   const char* waits_on = nullptr;  // kind of barrier it is blocked on
   uint64_t shuffles = 0;           // warp shuffles done (picks the slot array)
   void* race_ctx = nullptr;        // the race detector's fiber (racecheck builds)
+  void* asan_fake = nullptr;       // AddressSanitizer's state of this stack
 };
 
 // A barrier of `expected` fibers; `phase` counts completed rounds.
@@ -110,6 +122,9 @@ struct Cta {
   ucontext_t sched;           // the launching code's context
   const std::function<void()>* body = nullptr;
   void* race_sched = nullptr;  // the launching code's race-detector context
+  const void* sched_stack = nullptr;  // the launching thread's stack (AddressSanitizer)
+  size_t sched_stack_size = 0;
+  void* sched_asan_fake = nullptr;
   char order_start = 0, order_end = 0;  // launch -> threads -> launch end
 };
 
@@ -123,7 +138,13 @@ inline thread_local unsigned cta_rank = 0;
 // Fiber stacks, kept for the process's lifetime and reused by every launch;
 // the lowest page of each is a guard page, so an overflow faults instead of
 // overwriting a neighbour.
+#ifdef SIMT_ASAN
+// AddressSanitizer clears the shadow of the stack a switch lands on, so
+// its builds keep the stacks small
+constexpr size_t kStackBytes = 128u << 10;
+#else
 constexpr size_t kStackBytes = 1u << 20;
+#endif
 inline std::vector<char*>& stack_pool() {
   static std::vector<char*> pool;
   return pool;
@@ -181,10 +202,30 @@ inline void order_acquire(void* key) {
 #ifdef SIMT_RACECHECK
 #define SIMT_RACE_SWITCH(ctx) __tsan_switch_to_fiber((ctx), __tsan_switch_to_fiber_no_sync)
 #define SIMT_SWITCHES __attribute__((no_sanitize_thread))
+#elif defined(SIMT_ASAN)
+#define SIMT_RACE_SWITCH(ctx) ((void)(ctx))
+#define SIMT_SWITCHES __attribute__((no_sanitize_address))
 #else
 #define SIMT_RACE_SWITCH(ctx) ((void)(ctx))
 #define SIMT_SWITCHES
 #endif
+
+// AddressSanitizer's view of a switch: before it, the stack it lands on
+// (fake = nullptr when the leaving fiber ends); after landing, done.
+inline void asan_leave(void** fake, const void* bottom, size_t size) {
+#ifdef SIMT_ASAN
+  __sanitizer_start_switch_fiber(fake, bottom, size);
+#else
+  (void)fake, (void)bottom, (void)size;
+#endif
+}
+inline void asan_landed(void* fake) {
+#ifdef SIMT_ASAN
+  __sanitizer_finish_switch_fiber(fake, nullptr, nullptr);
+#else
+  (void)fake;
+#endif
+}
 
 // The race detector's context for fiber k, like the stacks kept and reused
 // by every launch (a destroyed detector fiber whose stack is reused did not
@@ -202,6 +243,7 @@ inline void* race_ctx_at(size_t k) {
 
 SIMT_SWITCHES inline void fiber_entry() {
   Cta& c = *cta();
+  asan_landed(nullptr);
   order_acquire(&c.order_start);
   (*c.body)();
   order_release(&c.order_end);
@@ -209,8 +251,9 @@ SIMT_SWITCHES inline void fiber_entry() {
     Internal in;  // ends before the switch: it counts in this fiber's detector state
     c.fib[c.cur].done = true;
   }
-  SIMT_RACE_SWITCH(c.race_sched);  // returns to c.sched through uc_link
-}
+  SIMT_RACE_SWITCH(c.race_sched);
+  asan_leave(nullptr, c.sched_stack, c.sched_stack_size);
+}  // returns to c.sched through uc_link
 
 // The running fiber waits: the OS thread switches straight to the next
 // ready fiber (or back to the scheduler when none is ready); the fiber
@@ -222,6 +265,7 @@ SIMT_SWITCHES inline void block(const char* kind) {
   c.fib[me].waits_on = kind;
   if (c.runq.empty()) {
     SIMT_RACE_SWITCH(c.race_sched);
+    asan_leave(&c.fib[me].asan_fake, c.sched_stack, c.sched_stack_size);
     swapcontext(&c.fib[me].ctx, &c.sched);
   } else {
     const unsigned nx = c.runq.front();
@@ -231,9 +275,11 @@ SIMT_SWITCHES inline void block(const char* kind) {
     tid.x = c.fib[nx].t;
     cta_rank = c.fib[nx].r;
     SIMT_RACE_SWITCH(c.fib[nx].race_ctx);
+    asan_leave(&c.fib[me].asan_fake, stack_at(nx) + 4096, kStackBytes - 4096);
     swapcontext(&c.fib[me].ctx, &c.fib[nx].ctx);
   }
   // resumed: whoever switched here set c.cur, tid and cta_rank to this fiber
+  asan_landed(c.fib[me].asan_fake);
 }
 
 // Arrives at `b`; the last arrival of a phase releases the waiting fibers.
@@ -333,6 +379,19 @@ inline void launch_cluster(unsigned ncta, unsigned nt, const std::vector<char*>&
 #ifdef SIMT_RACECHECK
   c.race_sched = __tsan_get_current_fiber();
 #endif
+#ifdef SIMT_ASAN
+  {
+    pthread_attr_t at;
+    void* addr = nullptr;
+    size_t size = 0;
+    if (pthread_getattr_np(pthread_self(), &at) == 0) {
+      pthread_attr_getstack(&at, &addr, &size);
+      pthread_attr_destroy(&at);
+    }
+    c.sched_stack = addr;
+    c.sched_stack_size = size;
+  }
+#endif
   order_release(&c.order_start);
   const HostDim tid0 = tid;
   const unsigned rank0 = cta_rank;
@@ -344,7 +403,9 @@ inline void launch_cluster(unsigned ncta, unsigned nt, const std::vector<char*>&
     tid.x = f.t;
     cta_rank = f.r;
     SIMT_RACE_SWITCH(f.race_ctx);
+    asan_leave(&c.sched_asan_fake, stack_at(c.cur) + 4096, kStackBytes - 4096);
     swapcontext(&c.sched, &f.ctx);
+    asan_landed(c.sched_asan_fake);
   }
   for (const Fiber& f : c.fib)
     if (!f.done) {

@@ -8,11 +8,16 @@
 //   simt_selftest split - threads of one CTA wait at two different
 //                         __syncthreads (undefined on a GPU); the emulation
 //                         must abort naming both
+//   simt_selftest redzone - writes one element past the end of a graph
+//                         arena's node-code region; a -fsanitize=address
+//                         build with SPOA_GB300_HOST_REDZONE must report it
 //   simt_selftest race  - thread 0 writes a shared value that thread 33
 //                         reads with no barrier between them (a data race
 //                         on a GPU); a -fsanitize=thread build must report
 //                         it, while "ok" must run without a report
 #include "simt_host.h"
+
+#include "../../spoa_gb300/csrc/poa_device.cuh"
 
 #include <cstdio>
 #include <cstring>
@@ -21,6 +26,17 @@
 int main(int argc, char** argv) {
   const bool skip = argc > 1 && std::strcmp(argv[1], "skip") == 0;
   const bool race = argc > 1 && std::strcmp(argv[1], "race") == 0;
+  if (argc > 1 && std::strcmp(argv[1], "redzone") == 0) {
+    spoa_gb300::GraphCaps gc{100, 300, 300, 5, 4};
+    spoa_gb300::GraphView G;
+    std::vector<uint8_t> arena(spoa_gb300::graph_layout(nullptr, gc, &G));
+    spoa_gb300::graph_layout(arena.data(), gc, &G);
+    simt::launch(32, [&] {
+      if (threadIdx.x == 0) G.code[gc.nodes] = 1;  // one past the region
+    });
+    std::printf("no red-zone access reported\n");
+    return 0;
+  }
   if (argc > 1 && std::strcmp(argv[1], "split") == 0) {
     simt::launch(64, [] {
       if (threadIdx.x < 32)

@@ -11,8 +11,12 @@ CTAs, both widths, the one-warp build, the segmented forward, clusters of
 and gap model, strands and qualities; any pair of threads that touch the
 same shared or global bytes between barriers with one of them writing, and
 any undefined behaviour (-fsanitize=undefined: signed overflow, shifts,
-misaligned access), fails the test.  A planted race in
-tests/host/simt_selftest.cpp shows that the detector sees one.
+misaligned access), fails the test.  The same driver built with
+-fsanitize=address and SPOA_GB300_HOST_REDZONE puts a poisoned red zone
+after every region of the device arenas (poa_device.cuh), so an access
+past a region (a write that on the GPU would land in the next region of
+the arena, unnoticed) fails it too.  Planted mistakes in
+tests/host/simt_selftest.cpp show that both detectors see one.
 """
 import os
 import shutil
@@ -26,6 +30,8 @@ HOST = os.path.join(ROOT, "tests", "host")
 BUILD = os.path.join(HOST, "_build")
 FLAGS = ["g++", "-std=c++20", "-O1", "-g", "-fsanitize=thread,undefined",
          "-fno-sanitize-recover=undefined"]
+ASAN = ["g++", "-std=c++20", "-O1", "-g", "-fsanitize=address,undefined",
+        "-fno-sanitize-recover=undefined", "-DSPOA_GB300_HOST_REDZONE"]
 
 
 @pytest.fixture(scope="module")
@@ -40,11 +46,16 @@ def sanitizers():
                        text=True, capture_output=True)
     if r.returncode != 0 or subprocess.run([probe]).returncode != 0:
         pytest.skip("g++ with ThreadSanitizer not available")
+    r = subprocess.run(ASAN + ["-x", "c++", "-", "-o", probe], input="int main() {}",
+                       text=True, capture_output=True)
+    if r.returncode != 0 or subprocess.run([probe]).returncode != 0:
+        pytest.skip("g++ with AddressSanitizer not available")
 
 
 def _build_all(targets):
-    procs = [subprocess.Popen(FLAGS + extra + [src, "-o", out], stderr=subprocess.PIPE,
-                              text=True) for src, out, extra in targets]
+    """targets: (source, output, extra flags, base flags) built in parallel."""
+    procs = [subprocess.Popen(base + extra + [src, "-o", out], stderr=subprocess.PIPE,
+                              text=True) for src, out, extra, base in targets]
     for p in procs:
         _, err = p.communicate()
         assert p.returncode == 0, err
@@ -54,27 +65,39 @@ def _report(r):
     return (r.stdout + r.stderr)[-4000:]
 
 
-def test_detector_sees_a_planted_race(sanitizers):
-    exe = os.path.join(BUILD, "simt_selftest_tsan")
-    _build_all([(os.path.join(HOST, "simt_selftest.cpp"), exe, [])])
-    ok = subprocess.run([exe, "ok"], capture_output=True, text=True, timeout=120)
-    assert ok.returncode == 0 and "ThreadSanitizer" not in ok.stderr, _report(ok)
-    bad = subprocess.run([exe, "race"], capture_output=True, text=True, timeout=120)
+def test_detectors_see_planted_mistakes(sanitizers):
+    src = os.path.join(HOST, "simt_selftest.cpp")
+    tsan, asan = os.path.join(BUILD, "simt_selftest_tsan"), os.path.join(BUILD, "simt_selftest_asan")
+    _build_all([(src, tsan, [], FLAGS), (src, asan, [], ASAN)])
+    for exe in (tsan, asan):
+        ok = subprocess.run([exe, "ok"], capture_output=True, text=True, timeout=120)
+        assert ok.returncode == 0 and "ERROR" not in ok.stderr, _report(ok)
+        assert "WARNING: ThreadSanitizer" not in ok.stderr, _report(ok)
+    bad = subprocess.run([tsan, "race"], capture_output=True, text=True, timeout=120)
     assert bad.returncode != 0
     assert "WARNING: ThreadSanitizer: data race" in bad.stderr
     assert "simt_selftest.cpp" in bad.stderr
+    bad = subprocess.run([asan, "redzone"], capture_output=True, text=True, timeout=120)
+    assert bad.returncode != 0
+    assert "AddressSanitizer: use-after-poison" in bad.stderr
+    assert "simt_selftest.cpp" in bad.stderr
 
 
-def test_device_code_has_no_races_or_undefined_behaviour(sanitizers):
+def test_device_code_has_no_races_overruns_or_undefined_behaviour(sanitizers):
     src = os.path.join(HOST, "racecheck_main.cpp")
-    win, mw = os.path.join(BUILD, "racecheck_window"), os.path.join(BUILD, "racecheck_mw")
-    _build_all([(src, win, []), (src, mw, ["-DRACECHECK_MW"])])
+    exes = {name: os.path.join(BUILD, name) for name in
+            ("racecheck_window", "racecheck_mw", "redzone_window", "redzone_mw")}
+    _build_all([(src, exes["racecheck_window"], [], FLAGS),
+                (src, exes["racecheck_mw"], ["-DRACECHECK_MW"], FLAGS),
+                (src, exes["redzone_window"], [], ASAN),
+                (src, exes["redzone_mw"], ["-DRACECHECK_MW"], ASAN)])
     procs = [subprocess.Popen([exe], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
-             for exe in (win, mw)]
+             for exe in exes.values()]
     for p in procs:
         out, err = p.communicate(timeout=900)
         r = subprocess.CompletedProcess(p.args, p.returncode, out, err)
         assert "WARNING: ThreadSanitizer" not in err, _report(r)
+        assert "ERROR: AddressSanitizer" not in err, _report(r)
         assert "runtime error" not in err, _report(r)
         assert p.returncode == 0 and out.strip().endswith("statuses ok"), _report(r)
 
