@@ -14,18 +14,21 @@ if ROOT not in sys.path:
 
 def host_library(src: str, out: str, deps, std: str, opt: str) -> str:
     """Builds a host test library from `src` (rebuilt when a dependency is
-    newer) and returns its path.  With SPOA_HOST_UBSAN=1 in the environment
-    it is built with -fsanitize=undefined and no recovery, into a file of
-    its own, so that undefined behaviour of the product code it compiles
-    ends the process with a report."""
+    newer) and returns its path.  With SPOA_HOST_SANITIZE=1 in the
+    environment it is built with AddressSanitizer (arena red zones:
+    SPOA_GB300_HOST_REDZONE) and UndefinedBehaviorSanitizer, no recovery,
+    into a file of its own, for a process that preloads the ASan runtime:
+    an overrun or undefined behaviour of the product code it compiles ends
+    the process with a report."""
     import shutil
     import subprocess
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
     flags = ["g++", f"-std={std}", opt, "-shared", "-fPIC", "-pthread"]
-    if os.environ.get("SPOA_HOST_UBSAN") == "1":
-        flags += ["-g", "-fsanitize=undefined", "-fno-sanitize-recover=undefined"]
-        out = out.replace(".so", "_ubsan.so")
+    if os.environ.get("SPOA_HOST_SANITIZE") == "1":
+        flags += ["-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=undefined",
+                  "-DSPOA_GB300_HOST_REDZONE"]
+        out = out.replace(".so", "_asan.so")
     os.makedirs(os.path.dirname(out), exist_ok=True)
     if not os.path.exists(out) or any(os.path.getmtime(d) > os.path.getmtime(out)
                                       for d in [src] + list(deps)):

@@ -102,18 +102,24 @@ def test_device_code_has_no_races_overruns_or_undefined_behaviour(sanitizers):
         assert p.returncode == 0 and out.strip().endswith("statuses ok"), _report(r)
 
 
-def test_graph_code_and_gfa_writer_under_ubsan(sanitizers):
-    """The parts of the product's code the race check does not drive --
-    the device graph code's Subgraph and graph loading, and the GFA writer
-    -- rebuilt for the host with -fsanitize=undefined and run through their
-    CPU tests in a child process: undefined behaviour ends it with a
-    report.  (The race check's build already runs the window code, its MSA
-    and the W-windows loop under the same sanitizer.)"""
+def test_graph_code_and_gfa_writer_under_asan_and_ubsan(sanitizers):
+    """The parts of the product's code the driver above does not run -- the
+    device graph code's Subgraph and graph loading, and the GFA writer --
+    rebuilt for the host with AddressSanitizer (arena red zones) and
+    UndefinedBehaviorSanitizer and run through their CPU tests in a child
+    process that preloads the ASan runtime: an overrun or undefined
+    behaviour ends it with a report."""
     import sys
-    env = dict(os.environ, SPOA_HOST_UBSAN="1")
+    libasan = subprocess.run(["g++", "-print-file-name=libasan.so"], capture_output=True,
+                             text=True).stdout.strip()
+    if not os.path.isabs(libasan) or not os.path.exists(libasan):
+        pytest.skip("no shared ASan runtime to preload")
+    env = dict(os.environ, SPOA_HOST_SANITIZE="1", LD_PRELOAD=libasan,
+               ASAN_OPTIONS="detect_leaks=0")
     r = subprocess.run(
         [sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider", "-m", "not gpu",
          "tests/test_device_graph_host.py", "tests/test_gfa_text.py"],
         cwd=ROOT, env=env, capture_output=True, text=True, timeout=900)
-    assert "runtime error" not in r.stdout + r.stderr, _report(r)
+    out = r.stdout + r.stderr
+    assert "ERROR: AddressSanitizer" not in out and "runtime error" not in out, _report(r)
     assert r.returncode == 0 and " passed" in r.stdout, _report(r)
