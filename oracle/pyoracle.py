@@ -106,11 +106,30 @@ class WindowParams(C.Structure):
                 ("c", C.c_int8), ("strand_ambiguous", C.c_int8)]
 
 
+def _sanitized_build() -> str:
+    """liboracle built with AddressSanitizer and UndefinedBehaviorSanitizer
+    (no recovery), for a process that preloads the ASan runtime; selected
+    by SPOA_ORACLE_SANITIZE=1 so that the oracle's own tests can run under
+    the sanitizers."""
+    out = os.path.join(_HERE, "_build", "liboracle_asan.so")
+    src = os.path.join(_HERE, "spoa_oracle.c")
+    if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
+        os.makedirs(os.path.dirname(out), exist_ok=True)
+        subprocess.run(["gcc", "-std=c11", "-O1", "-g", "-fPIC", "-shared",
+                        "-fsanitize=address,undefined", "-fno-sanitize-recover=undefined",
+                        "-o", out, src, "-lpthread"], check=True)
+    return out
+
+
 def lib():
     global _lib
     if _lib is None:
-        build()
-        L = C.CDLL(_LIB_PATH)
+        if os.environ.get("SPOA_ORACLE_SANITIZE") == "1":
+            path = _sanitized_build()
+        else:
+            build()
+            path = _LIB_PATH
+        L = C.CDLL(path)
         P = C.c_void_p
         L.oracle_graph_create.restype = P
         L.oracle_graph_destroy.argtypes = [P]

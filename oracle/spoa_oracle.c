@@ -532,12 +532,13 @@ void oracle_graph_export(const oracle_graph* g, uint8_t* chars,
       if (edge_weight) edge_weight[e] = ed->weight;
     }
   }
-  if (rank_to_node)
+  /* memcpy wants valid pointers even for 0 bytes: empty lists copy nothing */
+  if (rank_to_node && g->rank_to_node.n)
     memcpy(rank_to_node, g->rank_to_node.a,
            (size_t)g->rank_to_node.n * sizeof(uint32_t));
-  if (seq_begin)
+  if (seq_begin && g->sequences.n)
     memcpy(seq_begin, g->sequences.a, (size_t)g->sequences.n * sizeof(uint32_t));
-  if (consensus)
+  if (consensus && g->consensus.n)
     memcpy(consensus, g->consensus.a, (size_t)g->consensus.n * sizeof(uint32_t));
 }
 
@@ -1326,7 +1327,7 @@ static int32_t window_run_impl(const oracle_window_params* p,
     if (reversed) reversed[r] = rev;
     if (aln_pairs) {
       if (used + 2ull * nuse > aln_cap) { st = ORACLE_ERR_CAPACITY; goto out; }
-      memcpy(aln_pairs + used, use, (size_t)nuse * 2 * sizeof(int32_t));
+      if (nuse) memcpy(aln_pairs + used, use, (size_t)nuse * 2 * sizeof(int32_t));
     }
     used += 2ull * nuse;
     if (aln_off) aln_off[r + 1] = used / 2;

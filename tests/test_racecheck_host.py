@@ -123,3 +123,25 @@ def test_graph_code_and_gfa_writer_under_asan_and_ubsan(sanitizers):
     out = r.stdout + r.stderr
     assert "ERROR: AddressSanitizer" not in out and "runtime error" not in out, _report(r)
     assert r.returncode == 0 and " passed" in r.stdout, _report(r)
+
+
+def test_oracle_under_asan_and_ubsan(sanitizers):
+    """The oracle itself (the C restatement every parity test trusts),
+    built with AddressSanitizer and UndefinedBehaviorSanitizer
+    (SPOA_ORACLE_SANITIZE=1) and run through its tests against the recorded
+    reference windows, slices and saved graphs in a child process that
+    preloads the ASan runtime."""
+    import sys
+    libasan = subprocess.run(["g++", "-print-file-name=libasan.so"], capture_output=True,
+                             text=True).stdout.strip()
+    if not os.path.isabs(libasan) or not os.path.exists(libasan):
+        pytest.skip("no shared ASan runtime to preload")
+    env = dict(os.environ, SPOA_ORACLE_SANITIZE="1", LD_PRELOAD=libasan,
+               ASAN_OPTIONS="detect_leaks=0")
+    r = subprocess.run(
+        [sys.executable, "-m", "pytest", "-q", "-s", "-x", "-p", "no:cacheprovider",
+         "tests/test_oracle.py", "-k", "not spoa_test"],
+        cwd=ROOT, env=env, capture_output=True, text=True, timeout=900)
+    out = r.stdout + r.stderr
+    assert "ERROR: AddressSanitizer" not in out and "runtime error" not in out, _report(r)
+    assert r.returncode == 0 and " passed" in r.stdout, _report(r)
