@@ -4,13 +4,14 @@
 // One CTA of `nt` threads is `nt` fibers (ucontext) on the calling OS
 // thread.  A fiber runs until it waits at a barrier; threadIdx is set for
 // the fiber that runs.  __syncthreads is a barrier of the CTA, a warp
-// shuffle is an exchange through a per-warp slot array between two barriers
-// of the warp (every shuffle of this code is executed by full warps), and
+// shuffle is an exchange through per-warp slot arrays behind one barrier of
+// the warp (every shuffle of this code is executed by full warps), and
 // __shared__ data is the caller's.  A barrier that can never complete
-// aborts the launch with the place each thread waits.  The SIMD integer
-// intrinsics the DP uses are written here from their documented per-lane
-// meaning: 16-bit lanes add with wrap-around, maxima compare lanes as
-// signed values.
+// aborts the launch with the place each thread waits, and so do threads
+// that meet at two different calls of an aligned barrier (__syncthreads,
+// the cluster barrier).  The SIMD integer intrinsics the DP uses are
+// written here from their documented per-lane meaning: 16-bit lanes add
+// with wrap-around, maxima compare lanes as signed values.
 #pragma once
 
 #include <sys/mman.h>
@@ -104,7 +105,7 @@ struct Barrier {
   std::vector<unsigned> waiting;  // fibers blocked on the current phase
   char order[2] = {0, 0};  // happens-before keys of even and odd phases (racecheck)
   const char* site_file = nullptr;  // where the current phase's first thread
-  unsigned site_line = 0;           // called __syncthreads
+  unsigned site_line = 0;           // called the barrier (aligned barriers)
 };
 
 // One CTA, or a cluster of `ncta` CTAs of `nt` threads each (the threads of
