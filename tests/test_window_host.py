@@ -243,3 +243,36 @@ def test_emulation_reports_a_skipped_barrier():
     split = subprocess.run([exe, "split"], capture_output=True, text=True, timeout=60)
     assert split.returncode != 0
     assert "meet at different __syncthreads barriers" in split.stderr
+
+
+def test_recorded_windows_on_32_bit_lanes_and_clusters(wh, ref_windows):
+    """The 200 recorded windows of the tests above (N bases, qualities, both
+    strands, long insertions) on the 32-bit width of the one-CTA kernel, and
+    every second one on a cluster of 2 or 4 CTAs (window_read_cl), each
+    against the oracle."""
+    done_wide = done_cl = 0
+    k = 0
+    for rec in ref_windows:
+        if max(len(r) for r in rec["reads"]) > 512 or len(rec["reads"]) > 12:
+            continue
+        k += 1
+        _check_window(wh, rec, wide=True)
+        done_wide += 1
+        if k % 2:
+            continue
+        reads = [r.encode() for r in rec["reads"]]
+        quals = [q.encode() for q in rec["quals"]] if rec["quals"] else None
+        strand = rec["strand_ambiguous"]
+        cl = 2 if k % 4 else 4
+        st, scores, rev, alns, cons = run_host_cl(wh, rec["type"], rec["params"], reads, quals,
+                                                  strand, cl, 32)
+        assert st == 0, (rec.get("name"), cl, st)
+        ref = po.run_window(rec["type"], *rec["params"], reads, quals, strand_ambiguous=strand,
+                            with_msa=False)
+        assert scores == ref.scores, (rec.get("name"), cl)
+        assert rev == [int(x) for x in ref.reversed], (rec.get("name"), cl)
+        for a, b in zip(alns, ref.alignments):
+            assert np.array_equal(a, b), (rec.get("name"), cl)
+        assert cons == ref.consensus, (rec.get("name"), cl)
+        done_cl += 1
+    assert done_wide == 200 and done_cl == 100
