@@ -247,10 +247,10 @@ def test_emulation_reports_a_skipped_barrier():
 
 def test_recorded_windows_on_32_bit_lanes_and_clusters(wh, ref_windows):
     """The 200 recorded windows of the tests above (N bases, qualities, both
-    strands, long insertions) on the 32-bit width of the one-CTA kernel, and
-    every second one on a cluster of 2 or 4 CTAs (window_read_cl), each
-    against the oracle."""
-    done_wide = done_cl = 0
+    strands, long insertions) on the 32-bit width of the one-CTA kernel,
+    every fourth one through the segmented forward and every second one on a
+    cluster of 2 or 4 CTAs (window_read_cl), each against the oracle."""
+    done_wide = done_cl = done_seg = 0
     k = 0
     for rec in ref_windows:
         if max(len(r) for r in rec["reads"]) > 512 or len(rec["reads"]) > 12:
@@ -258,6 +258,17 @@ def test_recorded_windows_on_32_bit_lanes_and_clusters(wh, ref_windows):
         k += 1
         _check_window(wh, rec, wide=True)
         done_wide += 1
+        if k % 4 == 1:  # the segmented forward: two 12-column strips per thread
+            reads = [r.encode() for r in rec["reads"]]
+            quals = [q.encode() for q in rec["quals"]] if rec["quals"] else None
+            st, scores, rev, alns, cons = run_host(wh, rec["type"], rec["params"], reads, quals,
+                                                   rec["strand_ambiguous"], -12, 32, True)
+            ref = po.run_window(rec["type"], *rec["params"], reads, quals,
+                                strand_ambiguous=rec["strand_ambiguous"], with_msa=False)
+            assert st == 0 and scores == ref.scores and cons == ref.consensus, rec.get("name")
+            for a, b in zip(alns, ref.alignments):
+                assert np.array_equal(a, b), rec.get("name")
+            done_seg += 1
         if k % 2:
             continue
         reads = [r.encode() for r in rec["reads"]]
@@ -275,4 +286,4 @@ def test_recorded_windows_on_32_bit_lanes_and_clusters(wh, ref_windows):
             assert np.array_equal(a, b), (rec.get("name"), cl)
         assert cons == ref.consensus, (rec.get("name"), cl)
         done_cl += 1
-    assert done_wide == 200 and done_cl == 100
+    assert done_wide == 200 and done_cl == 100 and done_seg == 50
