@@ -103,3 +103,34 @@ def test_fewer_windows_than_slots(mw):
     status, scores, rev, cons = run_mw(mw, windows, 2, params, 4, False)
     ref = po.run_window(2, *params, windows[0], with_msa=False)
     assert status == [0] and scores == ref.scores and cons == [ref.consensus]
+
+
+def test_recorded_windows_through_the_w_windows_loop(mw, ref_windows):
+    """The 200 recorded windows of up to 12 reads of up to 512 bases (N
+    bases, qualities, both strands, long insertions), grouped by scoring,
+    type, strand mode and qualities into batches that run with 2 or 4
+    windows per CTA, against the oracle window by window."""
+    groups = {}
+    for rec in ref_windows:
+        if max(len(r) for r in rec["reads"]) > 512 or len(rec["reads"]) > 12:
+            continue
+        key = (tuple(rec["params"]), rec["type"], bool(rec["quals"]), rec["strand_ambiguous"])
+        groups.setdefault(key, []).append(rec)
+    done = 0
+    for g, ((params, type_, has_q, strand), recs) in enumerate(sorted(groups.items())):
+        W = 2 if g % 2 else 4
+        windows = [[r.encode() for r in rec["reads"]] for rec in recs]
+        quals = ([[q.encode() for q in rec["quals"]] for rec in recs] if has_q else None)
+        status, scores, rev, cons = run_mw(mw, windows, type_, params, W, strand, quals)
+        assert status == [0] * len(windows), (params, type_, W)
+        r0 = 0
+        for w, win in enumerate(windows):
+            ref = po.run_window(type_, *params, win, quals[w] if quals else None,
+                                strand_ambiguous=strand, with_msa=False)
+            n = len(win)
+            assert scores[r0:r0 + n] == ref.scores, (recs[w].get("name"), W)
+            assert rev[r0:r0 + n] == [int(x) for x in ref.reversed], (recs[w].get("name"), W)
+            assert cons[w] == ref.consensus, (recs[w].get("name"), W)
+            r0 += n
+            done += 1
+    assert done == 200
