@@ -139,25 +139,25 @@ int main() {
       const bool strand = (type + v) % 2 == 1, quals = (gap + v) % 2 == 0;
       switch (v) {
         case 0:  // one warp, 8 columns per thread
-          one("window_read 32x8", type, gap, 0, 8, 32, window(rng, 3, 180), strand, quals, 0);
+          one("window_read 32x8", type, gap, 0, 8, 32, window(rng, 3, 140), strand, quals, 0);
           break;
         case 1:  // the same on the 32-bit width
-          one("window_read 32x8 int32", type, gap, 1, 8, 32, window(rng, 3, 180), strand,
+          one("window_read 32x8 int32", type, gap, 1, 8, 32, window(rng, 3, 140), strand,
               quals, 0);
           break;
         case 2:  // the one-warp build (compile-time tile)
-          one("window_read one-warp 32x16", type, gap, 0, 16, 32, window(rng, 3, 300), strand,
+          one("window_read one-warp 32x16", type, gap, 0, 16, 32, window(rng, 3, 280), strand,
               quals, 0);
           break;
         case 3:  // a two-warp CTA (cross-warp scan carries)
-          one("window_read 64x8", type, gap, 0, 8, 64, window(rng, 3, 300), strand, quals, 0);
+          one("window_read 64x8", type, gap, 0, 8, 64, window(rng, 3, 280), strand, quals, 0);
           break;
         case 4:  // the segmented forward: two 12-column strips per thread
           one("window_read segmented", type, gap, 1, -12, 32, window(rng, 3, 450), strand,
               quals, 0);
           break;
         default:  // clusters of 2, 4 and 8 CTAs (32 threads x 12 columns each)
-          one("window_read_cl", type, gap, 1, 12, 32, window(rng, 3, 250), strand, quals,
+          one("window_read_cl", type, gap, 1, 12, 32, window(rng, 3, 200), strand, quals,
               v == 5 ? 2 : v == 6 ? 4 : 8);
       }
     }
