@@ -52,8 +52,20 @@ def sanitizers():
         pytest.skip("g++ with AddressSanitizer not available")
 
 
+def _sources_mtime():
+    """Newest change of the files these programs compile: the host test
+    sources and the device code's headers."""
+    import glob
+    files = glob.glob(os.path.join(HOST, "*.cpp")) + glob.glob(os.path.join(HOST, "*.h")) + \
+        glob.glob(os.path.join(ROOT, "spoa_gb300", "csrc", "*.cuh"))
+    return max(os.path.getmtime(f) for f in files)
+
+
 def _build_all(targets):
-    """targets: (source, output, extra flags, base flags) built in parallel."""
+    """targets: (source, output, extra flags, base flags) built in parallel
+    (those older than their sources)."""
+    newest = _sources_mtime()
+    targets = [t for t in targets if not os.path.exists(t[1]) or os.path.getmtime(t[1]) < newest]
     procs = [subprocess.Popen(base + extra + [src, "-o", out], stderr=subprocess.PIPE,
                               text=True) for src, out, extra, base in targets]
     for p in procs:
