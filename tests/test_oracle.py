@@ -136,3 +136,43 @@ def test_live_differential_against_reference():
         assert res.scores == ref["scores"]
         assert all(np.array_equal(a, b) for a, b in zip(res.alignments, ref["alignments"]))
         assert res.consensus == ref["consensus"] and res.msa == ref["msa"]
+
+
+@pytest.mark.skipif(po.build_reference() is None, reason="reference tree not present")
+def test_live_differential_random_scoring():
+    """Seeded random windows with random scoring through the compiled
+    reference and the oracle: alphabets of 2 to 20 letters, reads of 1-150
+    bases at error rates up to 60 %, match 0-10, mismatch -10-0, every gap
+    model with penalties 0 to -12 (equal ones included), every alignment
+    type, strands and qualities.  Pins the oracle where the recorded
+    fixtures do not reach."""
+    rng = np.random.default_rng(11)
+    alphabets = (b"ACGT", b"ACGTN", b"AC", b"ACDEFGHIKLMNPQRSTVWY")
+    specs = []
+    for k in range(150):
+        alpha = list(alphabets[int(rng.integers(len(alphabets)))])
+        tpl = rng.choice(alpha, size=int(rng.integers(1, 150)))
+        err = float(rng.choice([0.0, 0.05, 0.15, 0.6]))
+        reads = []
+        for _ in range(int(rng.integers(1, 8))):
+            out = []
+            for b in tpl:
+                u = rng.random()
+                if u < err / 3:
+                    continue
+                if u < 2 * err / 3:
+                    out.append(int(rng.choice(alpha)))
+                out.append(int(rng.choice(alpha)) if u < err else int(b))
+            reads.append(bytes(out) or bytes([alpha[0]]))
+        par = (int(rng.integers(0, 11)), int(rng.integers(-10, 1)),
+               *(int(x) for x in -rng.integers(0, 13, size=4)))
+        quals = ([bytes((rng.integers(0, 41, size=len(r)) + 33).astype(np.uint8)) for r in reads]
+                 if rng.random() < 0.3 else None)
+        specs.append((int(rng.integers(0, 3)), par, reads, quals, bool(rng.random() < 0.3)))
+    outs = po.parse_reference_output(po.run_reference(po.format_windows(specs)))
+    assert len(outs) == len(specs)
+    for (typ, par, reads, quals, strand), ref in zip(specs, outs):
+        res = po.run_window(typ, *par, reads, quals, strand)
+        assert res.scores == ref["scores"], (typ, par)
+        assert all(np.array_equal(a, b) for a, b in zip(res.alignments, ref["alignments"]))
+        assert res.consensus == ref["consensus"] and res.msa == ref["msa"], (typ, par)
