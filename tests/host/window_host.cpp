@@ -32,43 +32,55 @@ int32_t run(const Scoring& S, uint32_t n_reads, const char* seqs, const uint64_t
   DpView D;
   std::vector<uint8_t> dbuf(dp_layout(nullptr, dc, &D) + 256);
   dp_layout(dbuf.data(), dc, &D);
-  simt::launch(1, [&] { g_reset(G); });
   BlockScratch sh;
   SharedState ss;
+  // the whole window in one launch, read after read, as the batched kernel
+  // (k_batch) runs it: a CTA barrier after each read's outputs, nothing
+  // else between the reads
   uint64_t na = 0;
+  int32_t status = kOk;
+  int32_t score = 0, rv = 0;
+  const int32_t* pairs = nullptr;
+  uint32_t np = 0, s_dims[2];
   aln_off[0] = 0;
-  for (uint32_t r = 0; r < n_reads; ++r) {
-    const uint32_t L = (uint32_t)(off[r + 1] - off[r]);
-    const uint8_t* seq = reinterpret_cast<const uint8_t*>(seqs) + off[r];
-    const uint8_t* qual = quals ? reinterpret_cast<const uint8_t*>(quals) + off[r] : nullptr;
-    int32_t score = 0, rv = 0;
-    const int32_t* pairs = nullptr;
-    uint32_t np = 0;
-    simt::launch(nt, [&] {
+  simt::launch(nt, [&] {
+    if (threadIdx.x == 0) g_reset(G);
+    __syncthreads();
+    for (uint32_t r = 0; r < n_reads; ++r) {
+      const uint32_t L = (uint32_t)(off[r + 1] - off[r]);
+      const uint8_t* seq = reinterpret_cast<const uint8_t*>(seqs) + off[r];
+      const uint8_t* qual = quals ? reinterpret_cast<const uint8_t*>(quals) + off[r] : nullptr;
       window_read<SUB, CPT, T, SEGS, NT>(S, G, D, sh, ss, seq, L, qual, strand != 0, &score,
                                          &rv, &pairs, &np);
-    });
-    if (ss.status != kOk) return ss.status;
-    scores[r] = score;
-    rev[r] = rv;
-    if (na + np > aln_cap) return kCapacity;
-    for (uint32_t k = 0; k < 2 * np; ++k) aln[2 * na + k] = pairs[k];
-    na += np;
-    aln_off[r + 1] = na;
-  }
-  simt::launch(1, [&] { write_consensus(G, reinterpret_cast<uint8_t*>(cons), cons_cap, cons_len); });
-  if (msa) {
-    // the MSA as the batched kernel writes it: rows spread over the CTA
-    uint32_t s_dims[2];
-    int32_t st = kOk;
-    simt::launch(nt, [&] {
-      const int32_t r = window_msa(G, false, reinterpret_cast<uint8_t*>(msa), msa_cap,
-                                   &msa_dims[0], &msa_dims[1], s_dims);
-      if (threadIdx.x == 0) st = r;
-    });
-    if (st != kOk) return st;
-  }
-  return kOk;
+      if (ss.status != kOk) {
+        if (threadIdx.x == 0) status = ss.status;
+        return;
+      }
+      if (threadIdx.x == 0) {
+        scores[r] = score;
+        rev[r] = rv;
+        if (na + np > aln_cap) {
+          status = kCapacity;
+        } else {
+          for (uint32_t k = 0; k < 2 * np; ++k) aln[2 * na + k] = pairs[k];
+          na += np;
+          aln_off[r + 1] = na;
+        }
+      }
+      __syncthreads();
+      if (status != kOk) return;
+    }
+    if (threadIdx.x == 0)
+      write_consensus(G, reinterpret_cast<uint8_t*>(cons), cons_cap, cons_len);
+    __syncthreads();
+    if (msa) {
+      // the MSA as the batched kernel writes it: rows spread over the CTA
+      const int32_t st = window_msa(G, false, reinterpret_cast<uint8_t*>(msa), msa_cap,
+                                    &msa_dims[0], &msa_dims[1], s_dims);
+      if (threadIdx.x == 0 && st != kOk) status = st;
+    }
+  });
+  return status;
 }
 
 // One window through window_read_cl on a cluster of CL emulated CTAs of nt
@@ -89,7 +101,6 @@ int32_t run_cl(const Scoring& S, uint32_t n_reads, const char* seqs, const uint6
   DpView D;
   std::vector<uint8_t> dbuf(dp_layout(nullptr, dc, &D) + 256);
   dp_layout(dbuf.data(), dc, &D);
-  simt::launch(1, [&] { g_reset(G); });
   struct CtaShared {
     BlockScratch sh;
     SharedState ss;
@@ -97,31 +108,46 @@ int32_t run_cl(const Scoring& S, uint32_t n_reads, const char* seqs, const uint6
   std::vector<CtaShared> cs(CL);
   std::vector<char*> scratch;
   for (auto& c : cs) scratch.push_back(reinterpret_cast<char*>(&c));
+  // the whole window in one launch, as k_batch_cl runs it: the lead CTA's
+  // thread 0 takes each read's outputs, no other barrier between reads
   uint64_t na = 0;
+  int32_t status = kOk;
+  int32_t score = 0, rv = 0;
+  const int32_t* pairs = nullptr;
+  uint32_t np = 0;
   aln_off[0] = 0;
-  for (uint32_t r = 0; r < n_reads; ++r) {
-    const uint32_t L = (uint32_t)(off[r + 1] - off[r]);
-    const uint8_t* seq = reinterpret_cast<const uint8_t*>(seqs) + off[r];
-    const uint8_t* qual = quals ? reinterpret_cast<const uint8_t*>(quals) + off[r] : nullptr;
-    int32_t score = 0, rv = 0, st = kOk;
-    const int32_t* pairs = nullptr;
-    uint32_t np = 0;
-    simt::launch_cluster(CL, nt, scratch, [&] {
-      CtaShared& me = cs[simt::cta_rank];
-      const int32_t s = window_read_cl<SUB, CPT, T, CL>(S, G, D, me.sh, me.ss, seq, L, qual,
-                                                        strand != 0, &score, &rv, &pairs, &np);
-      if (simt::cta_rank == 0 && threadIdx.x == 0) st = s;
-    });
-    if (st != kOk) return st;
-    scores[r] = score;
-    rev[r] = rv;
-    if (na + np > aln_cap) return kCapacity;
-    for (uint32_t k = 0; k < 2 * np; ++k) aln[2 * na + k] = pairs[k];
-    na += np;
-    aln_off[r + 1] = na;
-  }
-  simt::launch(1, [&] { write_consensus(G, reinterpret_cast<uint8_t*>(cons), cons_cap, cons_len); });
-  return kOk;
+  simt::launch_cluster(CL, nt, scratch, [&] {
+    CtaShared& me = cs[simt::cta_rank];
+    const bool lead = simt::cta_rank == 0;
+    if (lead && threadIdx.x == 0) g_reset(G);
+    cl_sync<CL>();
+    for (uint32_t r = 0; r < n_reads; ++r) {
+      const uint32_t L = (uint32_t)(off[r + 1] - off[r]);
+      const uint8_t* seq = reinterpret_cast<const uint8_t*>(seqs) + off[r];
+      const uint8_t* qual = quals ? reinterpret_cast<const uint8_t*>(quals) + off[r] : nullptr;
+      const int32_t st = window_read_cl<SUB, CPT, T, CL>(S, G, D, me.sh, me.ss, seq, L, qual,
+                                                         strand != 0, &score, &rv, &pairs, &np);
+      if (st != kOk) {
+        if (lead && threadIdx.x == 0) status = st;
+        break;
+      }
+      if (lead && threadIdx.x == 0) {
+        scores[r] = score;
+        rev[r] = rv;
+        if (na + np > aln_cap) {
+          status = kCapacity;
+        } else {
+          for (uint32_t k = 0; k < 2 * np; ++k) aln[2 * na + k] = pairs[k];
+          na += np;
+          aln_off[r + 1] = na;
+        }
+      }
+    }
+    if (lead && threadIdx.x == 0 && status == kOk)
+      write_consensus(G, reinterpret_cast<uint8_t*>(cons), cons_cap, cons_len);
+    cl_sync<CL>();
+  });
+  return status;
 }
 
 }  // namespace
