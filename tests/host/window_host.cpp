@@ -1,9 +1,11 @@
 // window_host.cpp - one window through the device code of the batched
 // kernel (spoa_gb300/csrc/poa_window.cuh: forward pass with its CTA scans,
-// traceback, strand choice, AddAlignment, topological sort, consensus), run
-// on the host by the SIMT emulation of simt_host.h, one CTA of `nt` threads
-// per read.  TEST INFRASTRUCTURE ONLY (tests/test_window_host.py compares
-// it with the oracle); the product runs the same functions on the GPU.
+// traceback, strand choice, AddAlignment, topological sort, consensus, MSA),
+// run on the host by the SIMT emulation of simt_host.h: one emulated CTA
+// (or cluster of CTAs) of `nt` threads runs all reads of the window in one
+// launch, as the batched kernels do.  TEST INFRASTRUCTURE ONLY
+// (tests/test_window_host.py compares it with the oracle); the product runs
+// the same functions on the GPU.
 #include "simt_host.h"
 
 #include "../../spoa_gb300/csrc/poa_window.cuh"
