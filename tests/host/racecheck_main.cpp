@@ -133,7 +133,7 @@ int main() {
   };
   // every variant on three (type, gap model) pairs that cover each type and
   // each gap model once; strands and qualities vary with the pair
-  for (int v = 0; v < 8; ++v)
+  for (int v = 0; v < 9; ++v)
     for (int type = 0; type < 3; ++type) {
       const int gap = (3 + v - type) % 3;
       const bool strand = (type + v) % 2 == 1, quals = (gap + v) % 2 == 0;
@@ -155,6 +155,9 @@ int main() {
         case 4:  // the segmented forward: two 12-column strips per thread
           one("window_read segmented", type, gap, 1, -12, 32, window(rng, 3, 450), strand,
               quals, 0);
+          break;
+        case 8:  // nine warps: the scans' carries across many warps
+          one("window_read 288x8", type, gap, 0, 8, 288, window(rng, 2, 300), strand, quals, 0);
           break;
         default:  // clusters of 2, 4 and 8 CTAs (32 threads x 12 columns each)
           one("window_read_cl", type, gap, 1, 12, 32, window(rng, 3, 200), strand, quals,

@@ -5,9 +5,9 @@ checker on the host, with no GPU: built with
 -fsanitize=thread, its emulated threads are fibers that the race detector
 sees as threads ordered only by what orders them on a GPU (barrier
 arrive -> barrier completion, launch -> threads -> launch end, atomics).
-tests/host/racecheck_main.cpp drives the window code (one-warp and two-warp
-CTAs, both widths, the one-warp build, the segmented forward, clusters of
-2, 4 and 8 CTAs) and the W-windows-per-CTA loop over every alignment type
+tests/host/racecheck_main.cpp drives the window code (one-, two- and
+nine-warp CTAs, both widths, the one-warp build, the segmented forward,
+clusters of 2, 4 and 8 CTAs, the MSA) and the W-windows-per-CTA loop over every alignment type
 and gap model, strands and qualities; any pair of threads that touch the
 same shared or global bytes between barriers with one of them writing, and
 any undefined behaviour (-fsanitize=undefined: signed overflow, shifts,

@@ -346,3 +346,30 @@ def test_random_windows_and_scoring_against_the_oracle(wh):
         _check_window(wh, rec, with_msa=True)
         done += 1
     assert done >= N_RANDOM * 7 // 8
+
+
+def test_many_warp_ctas(wh):
+    """CTAs of 9, 16 and 32 warps, as the per-call form's latency tiles use
+    for long reads (the scans' carries across many warps, rows much wider
+    than the reads), against the oracle."""
+    from spoa_gb300 import synth
+    cases = ((288, 2, (5, -4, -8, -6, -10, -4), 2, 2100, False),
+             (512, 1, (5, -4, -8, -8, -8, -8), 3, 900, True),
+             (1024, 0, (5, -4, -8, -6, -8, -6), 3, 300, False))
+    for nt, typ, params, n_reads, length, strand in cases:
+        w = synth.long_10k(nt, n_reads=n_reads, tpl_len=length, min_len=length * 9 // 10)
+        reads = list(w.reads)
+        if strand:
+            reads = [synth.revcomp(r) if j % 2 else r for j, r in enumerate(reads)]
+        st, scores, rev, alns, cons = run_host(wh, typ, params, reads, None, strand, 8, nt,
+                                               False)
+        if st == NEEDS_WIDE:
+            st, scores, rev, alns, cons = run_host(wh, typ, params, reads, None, strand, 8, nt,
+                                                   True)
+        assert st == 0, (nt, st)
+        ref = po.run_window(typ, *params, reads, strand_ambiguous=strand, with_msa=False)
+        assert scores == ref.scores, nt
+        assert rev == [int(x) for x in ref.reversed], nt
+        for a, b in zip(alns, ref.alignments):
+            assert np.array_equal(a, b), nt
+        assert cons == ref.consensus, nt
