@@ -161,3 +161,56 @@ def test_subgraph_and_reload_match_the_oracle(dg):
         O.oracle_graph_destroy(x)
     for x in (g, grl):
         dg.dg_destroy(x)
+
+
+def test_random_windows_with_subgraphs_and_reloads(dg):
+    """Seeded random windows (alphabets of 2 to 20 letters, so up to 19
+    nodes aligned to one another; error rates up to 60 %; qualities; random
+    scoring and type): the graph after every read, then a few subgraphs and
+    a save-then-load, each against the oracle."""
+    O = po.lib()
+    rng = np.random.Generator(np.random.PCG64(31))
+    alphabets = (b"ACGT", b"AC", b"ACDEFGHIKLMNPQRSTVWY")
+    for k in range(40):
+        alpha = list(alphabets[k % 3])
+        tpl = rng.choice(alpha, size=int(rng.integers(5, 120)))
+        err = float(rng.choice([0.05, 0.2, 0.6]))
+        reads = []
+        for _ in range(int(rng.integers(2, 8))):
+            out = []
+            for b in tpl:
+                u = rng.random()
+                if u < err / 3:
+                    continue
+                if u < 2 * err / 3:
+                    out.append(int(rng.choice(alpha)))
+                out.append(int(rng.choice(alpha)) if u < err else int(b))
+            reads.append(bytes(out) or bytes([alpha[0]]))
+        quals = ([bytes((rng.integers(0, 41, size=len(r)) + 33).astype(np.uint8)) for r in reads]
+                 if k % 2 else None)
+        params = (int(rng.integers(1, 11)), int(rng.integers(-10, 0)),
+                  *(int(x) for x in -rng.integers(1, 13, size=4)))
+        og, g = _window(dg, int(rng.integers(0, 3)), params, reads, quals, prepass=k % 2 == 0)
+        n = O.oracle_graph_num_nodes(og)
+        nb = C.create_string_buffer(n + 1)
+        assert O.oracle_consensus(og, nb, n + 1) == dg.dg_consensus(g, nb, n + 1)
+        assert dg_state(dg, g) == oracle_state(og), k
+        for _ in range(3):
+            b, e = (int(x) for x in rng.integers(0, n, size=2))
+            osub, gsub = O.oracle_graph_create(), _new(dg, n)
+            m1, m2 = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
+            assert O.oracle_subgraph(og, b, e, osub, _ptr(m1)) == 0
+            assert dg.dg_subgraph(g, b, e, gsub, _ptr(m2)) == 0
+            ns = O.oracle_graph_num_nodes(osub)
+            assert m1[:ns].tolist() == m2[:ns].tolist()
+            assert dg_state(dg, gsub) == oracle_state(osub), (k, b, e)
+            O.oracle_graph_destroy(osub)
+            dg.dg_destroy(gsub)
+        orl, grl = O.oracle_graph_create(), _new(dg, sum(len(r) for r in reads))
+        assert O.oracle_graph_reload(og, orl) == 0
+        assert dg.dg_reload(g, grl) == 0
+        assert dg_state(dg, grl) == oracle_state(orl), k
+        for x in (og, orl):
+            O.oracle_graph_destroy(x)
+        for x in (g, grl):
+            dg.dg_destroy(x)
