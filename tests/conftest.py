@@ -36,6 +36,34 @@ def host_library(src: str, out: str, deps, std: str, opt: str) -> str:
     return out
 
 
+def random_test_window(rng):
+    """A window whose corners the recorded ones may not reach: 1-20 letter
+    alphabets, reads of 0-200 bases (empty ones included), depth 1-8, error
+    rates up to 60 %, random qualities."""
+    alphabets = (b"ACGT", b"ACGTN", b"AC", b"ACDEFGHIKLMNPQRSTVWY")
+    alpha = alphabets[int(rng.integers(len(alphabets)))]
+    tpl = rng.choice(list(alpha), size=int(rng.integers(1, 200)))
+    err = float(rng.choice([0.0, 0.05, 0.15, 0.6]))
+    reads = []
+    for _ in range(int(rng.integers(1, 9))):
+        if rng.random() < 0.05:
+            reads.append(b"")
+            continue
+        out = []
+        for b in tpl:
+            u = rng.random()
+            if u < err / 3:
+                continue
+            if u < 2 * err / 3:
+                out.append(int(rng.choice(list(alpha))))
+            out.append(int(rng.choice(list(alpha))) if u < err else int(b))
+        s = bytes(out[:200])
+        if rng.random() < 0.2 and len(s) > 4:
+            s = s[int(rng.integers(0, len(s) // 2)):]
+        reads.append(s)
+    return reads
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 

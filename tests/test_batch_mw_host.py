@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import ROOT, host_library
+from conftest import ROOT, host_library, random_test_window
 from oracle import pyoracle as po
 from spoa_gb300 import synth
 
@@ -134,3 +134,41 @@ def test_recorded_windows_through_the_w_windows_loop(mw, ref_windows):
             r0 += n
             done += 1
     assert done == 200
+
+
+def test_random_windows_through_the_w_windows_loop(mw):
+    """Seeded random windows (alphabets of 2 to 20 letters, empty reads,
+    error rates up to 60 %, qualities) with random scoring and type, in
+    batches of W + 1 windows on W = 2 and 4 slots, against the oracle; a
+    window that needs 32-bit scores reports it (this loop is 16-bit only)
+    and is left out of the comparison."""
+    rng = np.random.Generator(np.random.PCG64(404))
+    done = 0
+    for b in range(24):
+        W = 2 if b % 2 else 4
+        params = (int(rng.integers(0, 11)), int(rng.integers(-10, 1)),
+                  *(int(x) for x in -rng.integers(0, 13, size=4)))
+        type_, strand = int(rng.integers(0, 3)), bool(b % 3 == 0)
+        windows = []
+        while len(windows) < W + 1:
+            reads = random_test_window(rng)
+            if any(reads):
+                windows.append(reads)
+        quals = ([[bytes((rng.integers(0, 41, size=len(r)) + 33).astype(np.uint8)) for r in w]
+                  for w in windows] if b % 4 == 1 else None)
+        status, scores, rev, cons = run_mw(mw, windows, type_, params, W, strand, quals)
+        r0 = 0
+        for w, win in enumerate(windows):
+            n = len(win)
+            if status[w] == 11:  # needs the 32-bit kernel
+                r0 += n
+                continue
+            assert status[w] == 0, (b, w, status[w])
+            ref = po.run_window(type_, *params, win, quals[w] if quals else None,
+                                strand_ambiguous=strand, with_msa=False)
+            assert scores[r0:r0 + n] == ref.scores, (b, w)
+            assert rev[r0:r0 + n] == [int(x) for x in ref.reversed], (b, w)
+            assert cons[w] == ref.consensus, (b, w)
+            r0 += n
+            done += 1
+    assert done >= 60

@@ -12,7 +12,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import ROOT, host_library
+from conftest import ROOT, host_library, random_test_window
 from oracle import pyoracle as po
 
 SRC = os.path.join(ROOT, "tests", "host", "window_host.cpp")
@@ -289,34 +289,6 @@ def test_recorded_windows_on_32_bit_lanes_and_clusters(wh, ref_windows):
     assert done_wide == 200 and done_cl == 100 and done_seg == 50
 
 
-def _random_window(rng):
-    """A window whose corners the recorded ones may not reach: 1-20 letter
-    alphabets, reads of 0-200 bases (empty ones included), depth 1-8, error
-    rates up to 60 %, random qualities."""
-    alphabets = (b"ACGT", b"ACGTN", b"AC", b"ACDEFGHIKLMNPQRSTVWY")
-    alpha = alphabets[int(rng.integers(len(alphabets)))]
-    tpl = rng.choice(list(alpha), size=int(rng.integers(1, 200)))
-    err = float(rng.choice([0.0, 0.05, 0.15, 0.6]))
-    reads = []
-    for _ in range(int(rng.integers(1, 9))):
-        if rng.random() < 0.05:
-            reads.append(b"")
-            continue
-        out = []
-        for b in tpl:
-            u = rng.random()
-            if u < err / 3:
-                continue
-            if u < 2 * err / 3:
-                out.append(int(rng.choice(list(alpha))))
-            out.append(int(rng.choice(list(alpha))) if u < err else int(b))
-        s = bytes(out[:200])
-        if rng.random() < 0.2 and len(s) > 4:
-            s = s[int(rng.integers(0, len(s) // 2)):]
-        reads.append(s)
-    return reads
-
-
 N_RANDOM = int(os.environ.get("SPOA_RANDOM_WINDOWS", "300"))
 
 
@@ -329,7 +301,7 @@ def test_random_windows_and_scoring_against_the_oracle(wh):
     rng = np.random.Generator(np.random.PCG64(2024))
     done = 0
     for k in range(N_RANDOM):
-        reads = _random_window(rng)
+        reads = random_test_window(rng)
         m = int(rng.integers(0, 11))
         n = int(rng.integers(-10, 1)) if rng.random() < 0.9 else int(rng.integers(1, 4))
         g, e, q, c = (int(x) for x in -rng.integers(0, 13, size=4))
