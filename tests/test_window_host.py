@@ -297,7 +297,8 @@ def test_random_windows_and_scoring_against_the_oracle(wh):
     -10-0 and sometimes positive, gap penalties 0 to -12 in all three gap
     models, equal penalties included), every alignment type, strands and
     qualities, through the emulated CTA (the 32-bit width when the
-    reference's width rule asks for it) against the oracle, MSA included."""
+    reference's width rule asks for it) against the oracle, MSA included;
+    every fifth one also on a 2-CTA cluster."""
     rng = np.random.Generator(np.random.PCG64(2024))
     done = 0
     for k in range(N_RANDOM):
@@ -317,6 +318,16 @@ def test_random_windows_and_scoring_against_the_oracle(wh):
             continue
         _check_window(wh, rec, with_msa=True)
         done += 1
+        if k % 5 == 0:  # the same window on a 2-CTA cluster (32-bit lanes)
+            quals = [q.encode() for q in rec["quals"]] if rec["quals"] else None
+            st, scores, rev, alns, cons = run_host_cl(wh, rec["type"], rec["params"], reads,
+                                                      quals, rec["strand_ambiguous"], 2, 32)
+            ref = po.run_window(rec["type"], *rec["params"], reads, quals,
+                                strand_ambiguous=rec["strand_ambiguous"], with_msa=False)
+            assert st == 0 and scores == ref.scores and cons == ref.consensus, rec["name"]
+            assert rev == [int(x) for x in ref.reversed], rec["name"]
+            for a, b in zip(alns, ref.alignments):
+                assert np.array_equal(a, b), rec["name"]
     assert done >= N_RANDOM * 7 // 8
 
 
