@@ -298,7 +298,8 @@ def test_random_windows_and_scoring_against_the_oracle(wh):
     models, equal penalties included), every alignment type, strands and
     qualities, through the emulated CTA (the 32-bit width when the
     reference's width rule asks for it) against the oracle, MSA included;
-    every fifth one also on a 2-CTA cluster."""
+    every fifth one also on a 2-CTA cluster and another fifth through the
+    one-warp build."""
     rng = np.random.Generator(np.random.PCG64(2024))
     done = 0
     for k in range(N_RANDOM):
@@ -318,6 +319,8 @@ def test_random_windows_and_scoring_against_the_oracle(wh):
             continue
         _check_window(wh, rec, with_msa=True)
         done += 1
+        if k % 5 == 1:  # the one-warp build of the forward pass
+            _check_window(wh, rec, cpt=16)
         if k % 5 == 0:  # the same window on a 2-CTA cluster (32-bit lanes)
             quals = [q.encode() for q in rec["quals"]] if rec["quals"] else None
             st, scores, rev, alns, cons = run_host_cl(wh, rec["type"], rec["params"], reads,
